@@ -1,0 +1,251 @@
+"""Seeded synthetic genomes, reads and assembly graphs for the five workloads.
+
+No public dataset is used: every input is generated here from a seed, with
+the shapes the workloads name (genome size, repeat content, coverage, read
+length distribution, error profile, k).  Generation is host-side numpy and
+sits outside every timed region.
+
+Reads are sampled at uniform random start positions on a random strand and
+carry uniform substitution / insertion / deletion errors.  Read ids are Flye
+signed ids ``+1 .. +N``; a read's sequence is the forward strand as sampled.
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+BASES = np.frombuffer(b"ACGT", dtype=np.uint8)
+COMP = np.zeros(256, dtype=np.uint8)
+for _a, _b in zip(b"ACGTacgtN", b"TGCAtgcaN"):
+    COMP[_a] = _b
+
+
+def revcomp(seq: np.ndarray) -> np.ndarray:
+    return COMP[seq[::-1]]
+
+
+def random_genome(rng: np.random.Generator, length: int) -> np.ndarray:
+    return BASES[rng.integers(0, 4, size=length, dtype=np.uint8)]
+
+
+def mutate(rng: np.random.Generator, seq: np.ndarray, sub: float, ins: float = 0.0,
+           dele: float = 0.0) -> np.ndarray:
+    """Apply uniform substitution / insertion / deletion errors."""
+    n = len(seq)
+    out = seq.copy()
+    if sub > 0:
+        m = rng.random(n) < sub
+        shift = rng.integers(1, 4, size=int(m.sum()), dtype=np.uint8)
+        code = np.searchsorted(BASES, out[m])
+        out[m] = BASES[(code + shift) % 4]
+    if ins <= 0 and dele <= 0:
+        return out
+    r = rng.random(n)
+    keep = r >= dele
+    insert = (r >= dele) & (r < dele + ins)
+    reps = keep.astype(np.int64) + insert.astype(np.int64)
+    res = np.repeat(out, reps)
+    # the inserted base follows its anchor: positions of anchors after repeat
+    ends = np.cumsum(reps)
+    ins_pos = ends[insert] - 1
+    res[ins_pos] = BASES[rng.integers(0, 4, size=len(ins_pos), dtype=np.uint8)]
+    return res
+
+
+def lognormal_lengths(rng, n, mean, sd, lo, hi):
+    sigma2 = np.log(1.0 + (sd * sd) / (mean * mean))
+    mu = np.log(mean) - sigma2 / 2.0
+    v = rng.lognormal(mu, np.sqrt(sigma2), size=n)
+    return np.clip(v, lo, hi).astype(np.int64)
+
+
+@dataclass
+class ReadSet:
+    ids: np.ndarray  # int64 signed ids
+    offsets: np.ndarray  # int64, n+1
+    bases: np.ndarray  # uint8 ASCII, concatenated
+
+    @property
+    def n(self) -> int:
+        return len(self.ids)
+
+    @property
+    def total_bases(self) -> int:
+        return int(self.offsets[-1])
+
+    def seq(self, i: int) -> bytes:
+        return self.bases[self.offsets[i]:self.offsets[i + 1]].tobytes()
+
+    def subset(self, idx) -> "ReadSet":
+        idx = np.asarray(idx)
+        parts = [self.bases[self.offsets[i]:self.offsets[i + 1]] for i in idx]
+        lens = np.array([len(p) for p in parts], dtype=np.int64)
+        offs = np.zeros(len(idx) + 1, dtype=np.int64)
+        offs[1:] = np.cumsum(lens)
+        return ReadSet(self.ids[idx].copy(), offs,
+                       np.concatenate(parts) if parts else np.zeros(0, np.uint8))
+
+    @classmethod
+    def from_strings(cls, ids, seqs) -> "ReadSet":
+        arrs = [np.frombuffer(s.encode() if isinstance(s, str) else s, dtype=np.uint8)
+                for s in seqs]
+        offs = np.zeros(len(arrs) + 1, dtype=np.int64)
+        offs[1:] = np.cumsum([len(a) for a in arrs])
+        return cls(np.asarray(ids, dtype=np.int64), offs,
+                   np.concatenate(arrs) if arrs else np.zeros(0, np.uint8))
+
+
+def sample_reads(rng, genome: np.ndarray, coverage: float, lengths_fn, sub, ins, dele,
+                 max_reads: int | None = None) -> ReadSet:
+    glen = len(genome)
+    target = coverage * glen
+    lens: list[np.ndarray] = []
+    total = 0
+    while total < target:
+        chunk = lengths_fn(4096)
+        chunk = np.minimum(chunk, glen)
+        lens.append(chunk)
+        total += int(chunk.sum())
+    L = np.concatenate(lens)
+    L = L[np.cumsum(L) <= target + L[0]]
+    if max_reads is not None:
+        L = L[:max_reads]
+    n = len(L)
+    starts = rng.integers(0, glen - L + 1)
+    strand = rng.random(n) < 0.5
+    seqs = []
+    for i in range(n):
+        s = genome[starts[i]:starts[i] + L[i]]
+        if strand[i]:
+            s = revcomp(s)
+        seqs.append(mutate(rng, s, sub, ins, dele))
+    offs = np.zeros(n + 1, dtype=np.int64)
+    offs[1:] = np.cumsum([len(s) for s in seqs])
+    return ReadSet(np.arange(1, n + 1, dtype=np.int64), offs, np.concatenate(seqs))
+
+
+@dataclass
+class Workload:
+    name: str
+    k: int
+    reads: ReadSet
+    min_freq: int
+    max_freq: int
+    params: dict = field(default_factory=dict)
+    graph: "Graph | None" = None
+    seed: int = 0
+
+
+@dataclass
+class Graph:
+    edge_ids: np.ndarray  # int64 (> 0)
+    seq_ids: np.ndarray  # int64 (> 0) edge-sequence id of each forward edge
+    left: np.ndarray  # int32 node ids (complement node = id ^ 1)
+    right: np.ndarray
+    seqs: ReadSet  # edge sequences, ids = seq_ids
+
+
+OVERLAP_PARAMS = dict(min_overlap=1000, max_jump=1500, max_gap=500, gap_jump_threshold=100,
+                      max_overhang=1500, check_overhang=1, force_local=0, only_max_ext=1,
+                      max_overlaps=0, large_gap_penalty=2.0, small_gap_penalty=0.5,
+                      min_kmer_survival_rate=0.01, max_divergence=1.0, sample_rate=1.0)
+
+
+def plain_overlap(seed: int = 1, genome_len: int = 1_000_000, coverage: float = 20.0,
+                  max_reads: int | None = None) -> Workload:
+    """1 Mb uniform genome, 20x, lognormal(10 kb, 5 kb) in 1-50 kb, 1/0.5/0.5 % errors, k=15."""
+    rng = np.random.default_rng(seed)
+    genome = random_genome(rng, genome_len)
+    reads = sample_reads(rng, genome, coverage,
+                         lambda n: lognormal_lengths(rng, n, 10_000, 5_000, 1_000, 50_000),
+                         0.01, 0.005, 0.005, max_reads)
+    return Workload("plain-1Mb-20x-k15", 15, reads, min_freq=2,
+                    max_freq=int(5 * coverage), params=dict(OVERLAP_PARAMS, kmer_size=15),
+                    seed=seed)
+
+
+def repeat_genome(rng, genome_len: int, repeat_len: int, copies: int, repeat_div: float,
+                  at_fraction: float) -> np.ndarray:
+    genome = random_genome(rng, genome_len)
+    rep = random_genome(rng, repeat_len)
+    for _ in range(copies):
+        pos = int(rng.integers(0, genome_len - repeat_len))
+        genome[pos:pos + repeat_len] = mutate(rng, rep, repeat_div)
+    at_total = int(at_fraction * genome_len)
+    placed = 0
+    while placed < at_total:
+        ln = int(rng.integers(200, 2001)) & ~1
+        pos = int(rng.integers(0, genome_len - ln))
+        genome[pos:pos + ln] = np.resize(np.frombuffer(b"AT", dtype=np.uint8), ln)
+        placed += ln
+    return genome
+
+
+def batched_repeats(seed: int = 2, genome_len: int = 5_000_000, coverage: float = 40.0,
+                    max_reads: int | None = None) -> Workload:
+    """5 Mb genome, 30 x 5 kb repeat at 1 % divergence, 2 % (AT)n; HiFi 40x, k=17."""
+    rng = np.random.default_rng(seed)
+    genome = repeat_genome(rng, genome_len, 5_000, 30, 0.01, 0.02)
+    reads = sample_reads(rng, genome, coverage,
+                         lambda n: lognormal_lengths(rng, n, 15_000, 3_000, 1_000, 100_000),
+                         0.001, 0.0005, 0.0005, max_reads)
+    return Workload("batched-5Mb-repeats-40x-k17", 17, reads, min_freq=2,
+                    max_freq=int(5 * coverage), params=dict(OVERLAP_PARAMS, kmer_size=17),
+                    seed=seed)
+
+
+def read_to_graph(seed: int = 3, genome_len: int = 20_000_000, n_edges: int = 400,
+                  coverage: float = 30.0, max_reads: int | None = None) -> Workload:
+    """20 Mb genome cut into 400 edges (log-uniform 5-500 kb), 10 % duplicated at
+    0.5 % divergence; ONT 30x lognormal(20 kb, 12 kb) in 1-150 kb, 8 % error, k=15."""
+    rng = np.random.default_rng(seed)
+    genome = random_genome(rng, genome_len)
+    lo, hi = 5_000, 500_000
+    raw = np.exp(rng.uniform(np.log(lo), np.log(hi), size=n_edges))
+    lens = np.maximum((raw / raw.sum() * genome_len).astype(np.int64), 1000)
+    lens[-1] = genome_len - lens[:-1].sum()
+    cuts = np.concatenate([[0], np.cumsum(lens)])
+    seqs = [genome[cuts[i]:cuts[i + 1]] for i in range(n_edges)]
+    left = list(range(0, 2 * n_edges, 2))
+    right = list(range(2, 2 * n_edges + 2, 2))
+    dup = rng.choice(n_edges, size=max(1, n_edges // 10), replace=False)
+    for d in sorted(dup):
+        seqs.append(mutate(rng, seqs[d], 0.005))
+        left.append(left[d])
+        right.append(right[d])
+    ne = len(seqs)
+    offs = np.zeros(ne + 1, dtype=np.int64)
+    offs[1:] = np.cumsum([len(s) for s in seqs])
+    edge_seqs = ReadSet(np.arange(1, ne + 1, dtype=np.int64), offs, np.concatenate(seqs))
+    graph = Graph(np.arange(1, ne + 1, dtype=np.int64), np.arange(1, ne + 1, dtype=np.int64),
+                  np.array(left, dtype=np.int32), np.array(right, dtype=np.int32), edge_seqs)
+    reads = sample_reads(rng, genome, coverage,
+                         lambda n: lognormal_lengths(rng, n, 20_000, 12_000, 1_000, 150_000),
+                         0.03, 0.025, 0.025, max_reads)
+    params = dict(OVERLAP_PARAMS, kmer_size=15, min_overlap=100, check_overhang=0,
+                  max_overhang=0, only_max_ext=0)
+    return Workload("read-to-graph-20Mb-400edges-ont30x-k15", 15, reads, min_freq=1,
+                    max_freq=64, params=params, graph=graph, seed=seed)
+
+
+R2G_PARAMS = dict(max_jump=1500, max_read_overlap=50, min_overlap=1000, max_separation=500,
+                  long_edge=900, big_aln=500, max_chain_divergence=0.25)
+
+
+def small_overlap_case(seed: int, genome_len: int = 60_000, coverage: float = 8.0,
+                       mean_len: int = 6_000, k: int = 15, sub=0.01, ins=0.005,
+                       dele=0.005, repeat=False) -> Workload:
+    """A small seeded overlap workload for parity tests (seconds on the oracle)."""
+    rng = np.random.default_rng(seed)
+    if repeat:
+        genome = repeat_genome(rng, genome_len, 1_500, 6, 0.01, 0.01)
+    else:
+        genome = random_genome(rng, genome_len)
+    reads = sample_reads(rng, genome, coverage,
+                         lambda n: lognormal_lengths(rng, n, mean_len, mean_len // 2,
+                                                     1_000, 4 * mean_len),
+                         sub, ins, dele)
+    return Workload(f"small-{seed}", k, reads, min_freq=2, max_freq=int(5 * coverage),
+                    params=dict(OVERLAP_PARAMS, kmer_size=k), seed=seed)
