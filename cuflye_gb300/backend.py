@@ -1,0 +1,342 @@
+"""Host-side mirror of the reference's candidate-backend seam over the C ABI.
+
+The reference selects the candidate backend from ``CUFLYE_CANDIDATE_BACKEND``
+(``patches/flye/2.9.6/0002-cuflye-candidate-backend-seam.patch:29-43``), opens
+the CUDA device named by ``CUFLYE_CUDA_DEVICE`` under
+``CUFLYE_CUDA_MEMORY_BUDGET_BYTES`` and fails fast with the stub's message
+when the CUDA path cannot serve a request
+(``patches/flye/2.9.6/0003-cuflye-cuda-backend-stub.patch:37-46``).  This
+module keeps those names, meanings and errors and calls
+``libcuflye_gb300.so`` through ``include/cuflye.h``.  There is no CPU path
+here: if the library is missing, or a call is unsupported, it raises.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass, field
+from pathlib import Path
+
+import numpy as np
+
+from . import abi
+
+LIB_PATH = Path(__file__).resolve().parent / "_build" / "libcuflye_gb300.so"
+
+STATUS = {0: "CUFLYE_OK", 1: "CUFLYE_ERR_INVALID", 2: "CUFLYE_ERR_UNSUPPORTED",
+          3: "CUFLYE_ERR_BUDGET", 4: "CUFLYE_ERR_CUDA", 5: "CUFLYE_ERR_CAPACITY",
+          6: "CUFLYE_ERR_TIMEOUT", 7: "CUFLYE_ERR_NO_INDEX"}
+ERR_CAPACITY = 5
+
+
+class CuflyeError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+class OverlapParams(ctypes.Structure):
+    """cuflye_overlap_params; defaults are the chaining constants recorded by
+    the reference's Flye fixtures (maximum_jump 1500, max_jump_gap 500,
+    penalties 2 / 0.5 above / below 100, survival rate 0.01, ...)."""
+
+    _fields_ = [(n, ctypes.c_int32) for n in (
+        "kmer_size", "min_overlap", "max_jump", "max_gap", "gap_jump_threshold", "max_overhang",
+        "check_overhang", "force_local", "only_max_ext", "max_overlaps")] + [
+        (n, ctypes.c_float) for n in ("large_gap_penalty", "small_gap_penalty",
+                                      "min_kmer_survival_rate", "max_divergence", "sample_rate")]
+
+    @classmethod
+    def make(cls, **kw) -> "OverlapParams":
+        p = cls(kmer_size=15, min_overlap=1000, max_jump=1500, max_gap=500,
+                gap_jump_threshold=100, max_overhang=1500, check_overhang=1, force_local=0,
+                only_max_ext=1, max_overlaps=0, large_gap_penalty=2.0, small_gap_penalty=0.5,
+                min_kmer_survival_rate=0.01, max_divergence=1.0, sample_rate=1.0)
+        for k, v in kw.items():
+            setattr(p, k, v)
+        return p
+
+
+class R2GParams(ctypes.Structure):
+    """cuflye_r2g_params (ReadAligner constants: SMALL_ALN/BIG_ALN/LONG_EDGE at
+    patches/flye/2.9.6/0025-cuflye-read-alignment-dump.patch:94-96)."""
+
+    _fields_ = [(n, ctypes.c_int32) for n in (
+        "max_jump", "max_read_overlap", "min_overlap", "max_separation", "long_edge",
+        "big_aln")] + [("max_chain_divergence", ctypes.c_float)]
+
+    @classmethod
+    def make(cls, **kw) -> "R2GParams":
+        p = cls(max_jump=1500, max_read_overlap=50, min_overlap=1000, max_separation=500,
+                long_edge=900, big_aln=500, max_chain_divergence=0.25)
+        for k, v in kw.items():
+            setattr(p, k, v)
+        return p
+
+
+_LIB = None
+_vp = ctypes.c_void_p
+_i64p = ctypes.POINTER(ctypes.c_int64)
+_i32p = ctypes.POINTER(ctypes.c_int32)
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+_u32p = ctypes.POINTER(ctypes.c_uint32)
+_szp = ctypes.POINTER(ctypes.c_size_t)
+
+
+def load_library(path: Path | None = None) -> ctypes.CDLL:
+    """Loads the CUDA library; raises if it has not been built."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    p = Path(path or os.environ.get("CUFLYE_GB300_LIB", LIB_PATH))
+    if not p.exists():
+        raise RuntimeError(f"libcuflye_gb300.so not built ({p}); run cuflye_gb300.build.build()")
+    L = ctypes.CDLL(str(p))
+    S = ctypes.c_int
+    L.cuflye_candidate_backend.restype = ctypes.c_int
+    L.cuflye_candidate_backend.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+    L.cuflye_open.restype = S
+    L.cuflye_open.argtypes = [ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(_vp)]
+    L.cuflye_open_from_env.restype = S
+    L.cuflye_open_from_env.argtypes = [ctypes.POINTER(_vp)]
+    L.cuflye_close.argtypes = [_vp]
+    L.cuflye_last_error.restype = ctypes.c_char_p
+    L.cuflye_last_error.argtypes = [_vp]
+    L.cuflye_memory_stats.restype = S
+    L.cuflye_memory_stats.argtypes = [_vp, _u64p, _u64p]
+    L.cuflye_index_build.restype = S
+    L.cuflye_index_build.argtypes = [_vp, ctypes.c_int, ctypes.c_size_t, _i64p, _i64p,
+                                     ctypes.c_char_p, ctypes.c_uint32, ctypes.c_uint32]
+    L.cuflye_index_from_entries.restype = S
+    L.cuflye_index_from_entries.argtypes = [_vp, ctypes.c_int, ctypes.c_size_t, _i64p, _i64p,
+                                            _u64p, ctypes.c_size_t, _u64p]
+    L.cuflye_index_stats.restype = S
+    L.cuflye_index_stats.argtypes = [_vp, _u64p, _u64p, _u64p]
+    L.cuflye_candidates.restype = S
+    L.cuflye_candidates.argtypes = [_vp, ctypes.c_size_t, _i64p, _i64p, ctypes.c_char_p, _vp,
+                                    ctypes.c_size_t, _szp, _vp, ctypes.c_size_t, _szp]
+    L.cuflye_overlaps.restype = S
+    L.cuflye_overlaps.argtypes = [_vp, ctypes.c_size_t, _i64p, _i64p, ctypes.c_char_p,
+                                  ctypes.POINTER(OverlapParams), _vp, ctypes.c_size_t, _szp]
+    L.cuflye_set_batch_queries.restype = S
+    L.cuflye_set_batch_queries.argtypes = [_vp, ctypes.c_size_t]
+    L.cuflye_graph_set.restype = S
+    L.cuflye_graph_set.argtypes = [_vp, ctypes.c_size_t, _i64p, _i64p, _i32p, _i32p]
+    L.cuflye_read_to_graph.restype = S
+    L.cuflye_read_to_graph.argtypes = [_vp, ctypes.c_size_t, _i64p, _i64p, ctypes.c_char_p,
+                                       ctypes.POINTER(OverlapParams), ctypes.POINTER(R2GParams),
+                                       _vp, ctypes.c_size_t, _szp]
+    L.cuflye_std_sort_segments.restype = S
+    L.cuflye_std_sort_segments.argtypes = [_vp, _u64p, _u32p, _u64p, ctypes.c_size_t]
+    L.cuflye_last_timing.restype = S
+    L.cuflye_last_timing.argtypes = [_vp, ctypes.POINTER(ctypes.c_double), _u64p, ctypes.c_size_t]
+    _LIB = L
+    return L
+
+
+def candidate_backend() -> str:
+    """'cpu' or 'cuda' from CUFLYE_CANDIDATE_BACKEND; anything else raises
+    ``Unsupported CUFLYE_CANDIDATE_BACKEND: <value>`` like the reference."""
+    buf = ctypes.create_string_buffer(256)
+    r = load_library().cuflye_candidate_backend(buf, 256)
+    if r < 0:
+        raise RuntimeError(buf.value.decode())
+    return "cuda" if r == 1 else "cpu"
+
+
+def stub_message(device: str | None = None, budget: str | None = None) -> str:
+    """The fail-fast text of the reference stub for an unsupported request."""
+    device = device if device is not None else (os.environ.get("CUFLYE_CUDA_DEVICE") or "0")
+    budget = budget if budget is not None else (
+        os.environ.get("CUFLYE_CUDA_MEMORY_BUDGET_BYTES") or "unbounded")
+    return ("cuFlye CUDA candidate backend selected; adapter=gb300; "
+            f"CUFLYE_CUDA_DEVICE={device}; CUFLYE_CUDA_MEMORY_BUDGET_BYTES={budget}; ")
+
+
+def _ptr(a: np.ndarray, t):
+    return a.ctypes.data_as(t)
+
+
+@dataclass
+class Sequences:
+    """Flye-style records: signed ids and concatenated ASCII bases."""
+
+    ids: np.ndarray
+    offsets: np.ndarray
+    bases: np.ndarray  # uint8
+
+    @classmethod
+    def of(cls, reads) -> "Sequences":
+        if isinstance(reads, Sequences):
+            return reads
+        return cls(np.ascontiguousarray(reads.ids, dtype=np.int64),
+                   np.ascontiguousarray(reads.offsets, dtype=np.int64),
+                   np.ascontiguousarray(reads.bases, dtype=np.uint8))
+
+    @property
+    def n(self) -> int:
+        return len(self.ids)
+
+
+class CudaBackend:
+    """One device context: resident index, optional graph, device arena."""
+
+    def __init__(self, device: int | None = None, memory_budget_bytes: int | None = None):
+        L = load_library()
+        h = _vp()
+        if device is None and memory_budget_bytes is None:
+            st = L.cuflye_open_from_env(ctypes.byref(h))
+        else:
+            st = L.cuflye_open(int(device or 0), int(memory_budget_bytes or 0), ctypes.byref(h))
+        if st != 0:
+            raise CuflyeError(st, stub_message() + "cuflye_open failed (see stderr)")
+        self._h = h
+        self._L = L
+        self.k = None
+
+    # -- plumbing
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._L.cuflye_close(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st: int) -> None:
+        if st != 0:
+            raise CuflyeError(st, self._L.cuflye_last_error(self._h).decode())
+
+    def memory_stats(self) -> tuple[int, int]:
+        a, b = ctypes.c_uint64(), ctypes.c_uint64()
+        self._check(self._L.cuflye_memory_stats(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def set_batch_queries(self, n: int) -> None:
+        self._check(self._L.cuflye_set_batch_queries(self._h, int(n)))
+
+    def last_timing(self) -> tuple[list[float], list[int]]:
+        ms = (ctypes.c_double * 5)()
+        by = (ctypes.c_uint64 * 5)()
+        self._check(self._L.cuflye_last_timing(self._h, ms, by, 5))
+        return list(ms), list(by)
+
+    # -- index
+    def build_index(self, targets, k: int, min_freq: int, max_freq: int) -> dict:
+        t = Sequences.of(targets)
+        self._check(self._L.cuflye_index_build(self._h, int(k), t.n, _ptr(t.ids, _i64p),
+                                               _ptr(t.offsets, _i64p),
+                                               t.bases.ctypes.data_as(ctypes.c_char_p),
+                                               int(min_freq), int(max_freq)))
+        self.k = k
+        return self.index_stats()
+
+    def index_from_entries(self, k, target_ids, positions, keys, repetitive_keys=()) -> dict:
+        t = np.ascontiguousarray(target_ids, dtype=np.int64)
+        p = np.ascontiguousarray(positions, dtype=np.int64)
+        kk = np.ascontiguousarray(keys, dtype=np.uint64)
+        r = np.ascontiguousarray(repetitive_keys, dtype=np.uint64)
+        self._check(self._L.cuflye_index_from_entries(self._h, int(k), len(t), _ptr(t, _i64p),
+                                                      _ptr(p, _i64p), _ptr(kk, _u64p), len(r),
+                                                      _ptr(r, _u64p)))
+        self.k = k
+        return self.index_stats()
+
+    def index_stats(self) -> dict:
+        a, b, c = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        self._check(self._L.cuflye_index_stats(self._h, ctypes.byref(a), ctypes.byref(b),
+                                               ctypes.byref(c)))
+        return {"keys": a.value, "positions": b.value, "repetitive": c.value}
+
+    # -- candidate loop (collectCandidateMatches)
+    def candidates(self, queries, capacity: int | None = None) -> tuple[np.ndarray, np.ndarray]:
+        q = Sequences.of(queries)
+        cap = capacity if capacity is not None else max(1024, int(q.offsets[-1]) * 8)
+        fcap = max(1024, int(q.offsets[-1]) + 1)
+        while True:
+            out = np.empty(cap, dtype=abi.CANDIDATE_DTYPE)
+            fout = np.empty(fcap, dtype=abi.FILTERED_DTYPE)
+            n, nf = ctypes.c_size_t(), ctypes.c_size_t()
+            st = self._L.cuflye_candidates(self._h, q.n, _ptr(q.ids, _i64p),
+                                           _ptr(q.offsets, _i64p),
+                                           q.bases.ctypes.data_as(ctypes.c_char_p),
+                                           out.ctypes.data, cap, ctypes.byref(n),
+                                           fout.ctypes.data, fcap, ctypes.byref(nf))
+            if st == ERR_CAPACITY:
+                cap, fcap = max(cap, n.value), max(fcap, nf.value)
+                continue
+            self._check(st)
+            return out[:n.value].copy(), fout[:nf.value].copy()
+
+    # -- OverlapDetector::getSeqOverlaps
+    def overlaps(self, queries, params: OverlapParams, capacity: int | None = None) -> np.ndarray:
+        q = Sequences.of(queries)
+        cap = capacity if capacity is not None else max(1024, 64 * q.n)
+        while True:
+            out = np.empty(cap, dtype=abi.OVERLAP_DTYPE)
+            n = ctypes.c_size_t()
+            st = self._L.cuflye_overlaps(self._h, q.n, _ptr(q.ids, _i64p), _ptr(q.offsets, _i64p),
+                                         q.bases.ctypes.data_as(ctypes.c_char_p),
+                                         ctypes.byref(params), out.ctypes.data, cap,
+                                         ctypes.byref(n))
+            if st == ERR_CAPACITY:
+                cap = n.value
+                continue
+            self._check(st)
+            return out[:n.value].copy()
+
+    # -- ReadAligner::alignReads per-read body
+    def set_graph(self, edge_ids, seq_ids, left, right) -> None:
+        e = np.ascontiguousarray(edge_ids, dtype=np.int64)
+        s = np.ascontiguousarray(seq_ids, dtype=np.int64)
+        lft = np.ascontiguousarray(left, dtype=np.int32)
+        rgt = np.ascontiguousarray(right, dtype=np.int32)
+        self._check(self._L.cuflye_graph_set(self._h, len(e), _ptr(e, _i64p), _ptr(s, _i64p),
+                                             _ptr(lft, _i32p), _ptr(rgt, _i32p)))
+
+    def read_to_graph(self, reads, params: OverlapParams, r2g: R2GParams,
+                      capacity: int | None = None) -> np.ndarray:
+        q = Sequences.of(reads)
+        cap = capacity if capacity is not None else max(1024, 64 * q.n)
+        while True:
+            out = np.empty(cap, dtype=abi.READ_ALIGNMENT_DTYPE)
+            n = ctypes.c_size_t()
+            st = self._L.cuflye_read_to_graph(self._h, q.n, _ptr(q.ids, _i64p),
+                                              _ptr(q.offsets, _i64p),
+                                              q.bases.ctypes.data_as(ctypes.c_char_p),
+                                              ctypes.byref(params), ctypes.byref(r2g),
+                                              out.ctypes.data, cap, ctypes.byref(n))
+            if st == ERR_CAPACITY:
+                cap = n.value
+                continue
+            self._check(st)
+            return out[:n.value].copy()
+
+    # -- the device sort behind every Flye sort point
+    def std_sort_segments(self, keys, values, seg_offsets) -> tuple[np.ndarray, np.ndarray]:
+        k = np.array(keys, dtype=np.uint64)
+        v = np.array(values, dtype=np.uint32)
+        o = np.ascontiguousarray(seg_offsets, dtype=np.uint64)
+        self._check(self._L.cuflye_std_sort_segments(self._h, _ptr(k, _u64p), _ptr(v, _u32p),
+                                                     _ptr(o, _u64p), len(o) - 1))
+        return k, v
+
+
+def collect_candidate_matches_cuda(backend: CudaBackend, query_id: int, sequence: bytes):
+    """collectCandidateMatchesCuda*: candidate records and filtered positions of
+    one query, in Flye's generation order (the callee of
+    patches/flye/2.9.6/0005-cuflye-real-data-pack-dump.patch:246-250)."""
+    seq = np.frombuffer(sequence, dtype=np.uint8)
+    q = Sequences(np.array([query_id], dtype=np.int64),
+                  np.array([0, len(seq)], dtype=np.int64), seq.copy())
+    return backend.candidates(q)

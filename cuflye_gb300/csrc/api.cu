@@ -1,0 +1,1101 @@
+// api.cu — host orchestration behind the C ABI (include/cuflye.h).
+//
+// One context = one device, one stream, one device arena (named buffers that
+// grow and are reused across calls, like the reference's DeviceBuffer
+// ensureCapacity arena in cuda/cuflye_cuda_raii.hpp:27-114), a resident
+// k-mer index and an optional assembly graph.  Queries are processed in
+// passes: every pass runs hit counting, an exclusive scan and hit emission
+// for a contiguous run of queries, then the libstdc++-order match sort and
+// the chaining stages, all on the context's stream; the host only reads back
+// the sizes it needs to size the next stage's buffers.  A pass that would
+// exceed the memory budget is split in half; a single query that does not
+// fit fails with CUFLYE_ERR_BUDGET (records are never truncated,
+// docs/abi/candidate-record-v1.md:105-118).
+#include <dlfcn.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/cuflye.h"
+#include "kernels.h"
+#include "r2g.h"
+
+namespace cuflye {
+
+struct Error : std::runtime_error {
+  cuflye_status code;
+  Error(cuflye_status c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define CUFLYE_CHECK(call)                                                                \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      throw Error(CUFLYE_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));  \
+  } while (0)
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+};
+
+}  // namespace cuflye
+
+using namespace cuflye;
+
+struct cuflye_ctx {
+  int device = 0;
+  uint64_t budget = 0;  // 0 = unbounded
+  cudaStream_t stream = nullptr;
+  int num_sms = 0;
+  std::mutex mu;
+  std::string err;
+  std::map<std::string, DevBuf> bufs;
+  uint64_t in_use = 0, peak = 0;
+  DeviceStatus* status = nullptr;
+  // index
+  bool has_index = false;
+  DeviceIndex idx;
+  std::unordered_map<int64_t, uint32_t> slot_of;  // |signed id| -> slot
+  std::vector<int64_t> slot_signed_h;
+  // graph
+  bool has_graph = false;
+  // logf exception table
+  LogfTable logt{};
+  size_t queries_per_pass = 0;
+  // timing
+  cudaEvent_t ev[8]{};
+  double stage_ms[5]{};
+  uint64_t stage_bytes[5]{};
+};
+
+namespace {
+
+template <typename T>
+T* buf(cuflye_ctx* c, const std::string& name, uint64_t count) {
+  const size_t bytes = std::max<size_t>(static_cast<size_t>(count) * sizeof(T), 16);
+  DevBuf& b = c->bufs[name];
+  if (b.cap >= bytes) return static_cast<T*>(b.p);
+  const size_t want = std::max(bytes, b.cap + b.cap / 2);
+  if (c->budget && c->in_use - b.cap + want > c->budget) {
+    if (c->in_use - b.cap + bytes > c->budget)
+      throw Error(CUFLYE_ERR_BUDGET,
+                  "device memory budget exceeded: buffer '" + name + "' needs " +
+                      std::to_string(bytes) + " bytes; in use " + std::to_string(c->in_use) +
+                      " of CUFLYE_CUDA_MEMORY_BUDGET_BYTES=" + std::to_string(c->budget));
+  }
+  const size_t alloc = (c->budget && c->in_use - b.cap + want > c->budget) ? bytes : want;
+  if (b.p) CUFLYE_CHECK(cudaFree(b.p));
+  c->in_use -= b.cap;
+  b.p = nullptr;
+  b.cap = 0;
+  cudaError_t e = cudaMalloc(&b.p, alloc);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    throw Error(CUFLYE_ERR_BUDGET, "cudaMalloc of " + std::to_string(alloc) + " bytes for '" +
+                                       name + "' failed: " + cudaGetErrorString(e));
+  }
+  b.cap = alloc;
+  c->in_use += alloc;
+  c->peak = std::max(c->peak, c->in_use);
+  return static_cast<T*>(b.p);
+}
+
+void release(cuflye_ctx* c, const std::string& name) {
+  auto it = c->bufs.find(name);
+  if (it == c->bufs.end()) return;
+  if (it->second.p) cudaFree(it->second.p);
+  c->in_use -= it->second.cap;
+  c->bufs.erase(it);
+}
+
+void sync(cuflye_ctx* c) { CUFLYE_CHECK(cudaStreamSynchronize(c->stream)); }
+
+template <typename T>
+T read_scalar(cuflye_ctx* c, const T* dev) {
+  T v;
+  CUFLYE_CHECK(cudaMemcpyAsync(&v, dev, sizeof(T), cudaMemcpyDeviceToHost, c->stream));
+  sync(c);
+  return v;
+}
+
+void check_device_status(cuflye_ctx* c) {
+  DeviceStatus st;
+  CUFLYE_CHECK(cudaMemcpyAsync(&st, c->status, sizeof(st), cudaMemcpyDeviceToHost, c->stream));
+  sync(c);
+  if (st.code == kDevOk) return;
+  CUFLYE_CHECK(cudaMemsetAsync(c->status, 0, sizeof(DeviceStatus), c->stream));
+  switch (st.code) {
+    case kDevProposalOverflow:
+      throw Error(CUFLYE_ERR_UNSUPPORTED,
+                  "unsupported shape: a target group produced more than 64 overlap proposals "
+                  "(group " + std::to_string(st.detail) + ")");
+    case kDevLogDomain:
+      throw Error(CUFLYE_ERR_UNSUPPORTED,
+                  "unsupported shape: divergence argument outside [1, 2^24)");
+    case kDevTableFull:
+      throw Error(CUFLYE_ERR_CUDA, "k-mer table insertion failed (table full)");
+    default:
+      throw Error(CUFLYE_ERR_CUDA, "device status " + std::to_string(st.code));
+  }
+}
+
+uint64_t scan_u32(cuflye_ctx* c, const uint32_t* in, uint64_t* out, uint64_t n,
+                  const char* temp_name) {
+  uint64_t* temp = buf<uint64_t>(c, temp_name, scan_temp_words(n));
+  CUFLYE_CHECK(exclusive_scan_u32_to_u64(in, out, n, temp, c->stream));
+  // out[n] = total
+  const uint64_t ntiles = scan_temp_words(n) - 1;
+  CUFLYE_CHECK(cudaMemcpyAsync(out + n, temp + (n ? ntiles : 0), sizeof(uint64_t),
+                               cudaMemcpyDeviceToDevice, c->stream));
+  return read_scalar(c, out + n);
+}
+
+std::string lib_dir() {
+  Dl_info info;
+  if (dladdr(reinterpret_cast<void*>(&lib_dir), &info) && info.dli_fname) {
+    std::string p = info.dli_fname;
+    const size_t s = p.rfind('/');
+    return s == std::string::npos ? "." : p.substr(0, s);
+  }
+  return ".";
+}
+
+void load_logf_table(cuflye_ctx* c) {
+  const std::string path = lib_dir() + "/logf_exceptions.bin";
+  std::ifstream in(path, std::ios::binary);
+  if (!in)
+    throw Error(CUFLYE_ERR_INVALID,
+                "logf exception table missing: " + path + " (built by the package build step)");
+  uint32_t n = 0;
+  in.read(reinterpret_cast<char*>(&n), sizeof(n));
+  std::vector<uint32_t> xy(2 * static_cast<size_t>(n));
+  in.read(reinterpret_cast<char*>(xy.data()), static_cast<std::streamsize>(xy.size() * 4));
+  if (!in) throw Error(CUFLYE_ERR_INVALID, "logf exception table truncated: " + path);
+  std::vector<uint32_t> xs(n), ys(n);
+  for (uint32_t i = 0; i < n; ++i) {
+    xs[i] = xy[2 * i];
+    ys[i] = xy[2 * i + 1];
+  }
+  uint32_t* dx = buf<uint32_t>(c, "logf_x", n);
+  uint32_t* dy = buf<uint32_t>(c, "logf_y", n);
+  CUFLYE_CHECK(cudaMemcpy(dx, xs.data(), n * 4ull, cudaMemcpyHostToDevice));
+  CUFLYE_CHECK(cudaMemcpy(dy, ys.data(), n * 4ull, cudaMemcpyHostToDevice));
+  c->logt = LogfTable{dx, dy, n};
+}
+
+int bits_for(uint64_t v) {
+  int b = 0;
+  while (b < 64 && (v >> b) != 0) ++b;
+  return b;
+}
+
+// ---------------------------------------------------------------- index build
+
+void build_index(cuflye_ctx* c, int k, size_t n, const int64_t* ids, const int64_t* offsets,
+                 const char* bases, uint32_t min_freq, uint32_t max_freq) {
+  if (k < 1 || k > 31) throw Error(CUFLYE_ERR_UNSUPPORTED, "k must be in [1, 31]");
+  if (n == 0) throw Error(CUFLYE_ERR_INVALID, "index needs at least one target");
+  if (max_freq >= (1u << kCountBits) - 1)
+    throw Error(CUFLYE_ERR_UNSUPPORTED, "max_freq must be below 2^23 - 1");
+  std::vector<size_t> order(n);
+  for (size_t i = 0; i < n; ++i) {
+    if (ids[i] <= 0) throw Error(CUFLYE_ERR_INVALID, "index target ids must be > 0");
+    if (offsets[i + 1] < offsets[i]) throw Error(CUFLYE_ERR_INVALID, "offsets must not decrease");
+    if (offsets[i + 1] - offsets[i] >= (1ll << 31))
+      throw Error(CUFLYE_ERR_UNSUPPORTED, "target longer than 2^31");
+    order[i] = i;
+  }
+  std::sort(order.begin(), order.end(), [&](size_t a, size_t b) { return ids[a] < ids[b]; });
+  for (size_t i = 1; i < n; ++i)
+    if (ids[order[i]] == ids[order[i - 1]])
+      throw Error(CUFLYE_ERR_INVALID, "duplicate target id " + std::to_string(ids[order[i]]));
+  if (2 * n >= (1ull << 31)) throw Error(CUFLYE_ERR_UNSUPPORTED, "too many targets");
+  c->has_index = false;
+  c->slot_of.clear();
+  c->slot_signed_h.assign(n, 0);
+  std::vector<int32_t> slot_len(n);
+  std::vector<uint64_t> base_off(n), win_off(n + 1);
+  win_off[0] = 0;
+  int64_t maxlen = 0;
+  for (size_t s = 0; s < n; ++s) {
+    const size_t i = order[s];
+    c->slot_of[ids[i]] = static_cast<uint32_t>(s);
+    c->slot_signed_h[s] = ids[i];
+    const int64_t len = offsets[i + 1] - offsets[i];
+    slot_len[s] = static_cast<int32_t>(len);
+    maxlen = std::max(maxlen, len);
+    base_off[s] = static_cast<uint64_t>(offsets[i] - offsets[0]);
+    win_off[s + 1] = win_off[s] + (len >= k ? static_cast<uint64_t>(len - k + 1) : 0);
+  }
+  const uint64_t nbases = static_cast<uint64_t>(offsets[n] - offsets[0]);
+  const uint64_t nwin = win_off[n];
+  cudaStream_t st = c->stream;
+  uint8_t* d_ascii = buf<uint8_t>(c, "ib_ascii", nbases + 16);
+  CUFLYE_CHECK(cudaMemcpyAsync(d_ascii, bases + offsets[0], nbases, cudaMemcpyHostToDevice, st));
+  uint64_t* words = buf<uint64_t>(c, "ib_words", (nbases + 31) / 32 + 2);
+  CUFLYE_CHECK(pack_bases(d_ascii, nbases, words, st));
+  uint64_t* d_base = buf<uint64_t>(c, "ib_base", n);
+  uint64_t* d_win = buf<uint64_t>(c, "ib_win", n + 1);
+  int32_t* d_len = buf<int32_t>(c, "ix_slot_len", n);
+  int64_t* d_signed = buf<int64_t>(c, "ix_slot_signed", n);
+  CUFLYE_CHECK(cudaMemcpyAsync(d_base, base_off.data(), n * 8, cudaMemcpyHostToDevice, st));
+  CUFLYE_CHECK(cudaMemcpyAsync(d_win, win_off.data(), (n + 1) * 8, cudaMemcpyHostToDevice, st));
+  CUFLYE_CHECK(cudaMemcpyAsync(d_len, slot_len.data(), n * 4, cudaMemcpyHostToDevice, st));
+  CUFLYE_CHECK(cudaMemcpyAsync(d_signed, c->slot_signed_h.data(), n * 8, cudaMemcpyHostToDevice,
+                               st));
+  uint64_t* keys = buf<uint64_t>(c, "ib_keys", nwin);
+  uint64_t* vals = buf<uint64_t>(c, "ib_vals", nwin);
+  uint64_t* keys2 = buf<uint64_t>(c, "ib_keys2", nwin);
+  uint64_t* vals2 = buf<uint64_t>(c, "ib_vals2", nwin);
+  CUFLYE_CHECK(index_enumerate(words, d_base, d_win, d_len, static_cast<uint32_t>(n), nwin, k,
+                               keys, vals, st));
+  // LSD digits: position bytes, stored-id bytes, key bytes
+  std::vector<int> digits;
+  const int pbytes = (bits_for(static_cast<uint64_t>(maxlen)) + 7) / 8;
+  const int dbytes = (bits_for(2 * n) + 7) / 8;
+  const int kbytes = (2 * k + 7) / 8;
+  for (int d = 0; d < pbytes; ++d) digits.push_back(d);
+  for (int d = 0; d < dbytes; ++d) digits.push_back(4 + d);
+  for (int d = 0; d < kbytes; ++d) digits.push_back(8 + d);
+  uint32_t* hist = buf<uint32_t>(c, "ib_hist", radix_hist_words(nwin));
+  int in_alt = 0;
+  if (nwin)
+    CUFLYE_CHECK(radix_sort_pairs(keys, vals, keys2, vals2, nwin, digits.data(),
+                                  static_cast<int>(digits.size()), hist, &in_alt, st));
+  if (in_alt) {
+    std::swap(keys, keys2);
+    std::swap(vals, vals2);
+  }
+  // runs
+  uint32_t* flags = buf<uint32_t>(c, "ib_flags", nwin);
+  uint64_t* run_id = buf<uint64_t>(c, "ib_runid", nwin + 1);
+  CUFLYE_CHECK(index_mark_runs(keys, nwin, flags, st));
+  const uint64_t nruns = scan_u32(c, flags, run_id, nwin, "ib_scan");
+  uint64_t* run_start = buf<uint64_t>(c, "ib_runstart", nruns + 1);
+  CUFLYE_CHECK(index_run_starts(flags, run_id, nwin, nruns, run_start, st));
+  uint32_t* kept = buf<uint32_t>(c, "ib_kept", nruns);
+  uint8_t* cls = buf<uint8_t>(c, "ib_cls", nruns);
+  CUFLYE_CHECK(index_classify_runs(run_start, nruns, min_freq, max_freq, kept, cls, st));
+  uint64_t* kept_off = buf<uint64_t>(c, "ib_keptoff", nruns + 1);
+  const uint64_t npos = scan_u32(c, kept, kept_off, nruns, "ib_scan");
+  if (npos >= (1ull << 40)) throw Error(CUFLYE_ERR_UNSUPPORTED, "index larger than 2^40 entries");
+  uint64_t* pos = buf<uint64_t>(c, "ix_pos", npos);
+  CUFLYE_CHECK(index_copy_positions(vals, run_id, run_start, cls, kept_off, nwin, pos, st));
+  // table sized for every run (solid + repetitive + absent) at load <= 1/2
+  uint64_t cap = 16;
+  while (cap < 2 * nruns) cap <<= 1;
+  TableEntry* table = buf<TableEntry>(c, "ix_table", cap);
+  CUFLYE_CHECK(cudaMemsetAsync(table, 0xff, cap * sizeof(TableEntry), st));
+  CUFLYE_CHECK(index_insert(keys, run_start, cls, kept_off, nruns, table, cap - 1, c->status, st));
+  check_device_status(c);
+  // statistics
+  std::vector<uint8_t> h_cls(nruns);
+  if (nruns)
+    CUFLYE_CHECK(cudaMemcpyAsync(h_cls.data(), cls, nruns, cudaMemcpyDeviceToHost, st));
+  sync(c);
+  uint64_t nsolid = 0, nrep = 0;
+  for (uint8_t v : h_cls) {
+    nsolid += v == 1;
+    nrep += v == 2;
+  }
+  for (const char* t : {"ib_ascii", "ib_words", "ib_base", "ib_win", "ib_keys", "ib_vals",
+                        "ib_keys2", "ib_vals2", "ib_hist", "ib_flags", "ib_runid", "ib_runstart",
+                        "ib_kept", "ib_cls", "ib_keptoff", "ib_scan"})
+    release(c, t);
+  c->idx.k = k;
+  c->idx.transform = true;
+  c->idx.table = table;
+  c->idx.mask = cap - 1;
+  c->idx.pos = pos;
+  c->idx.npos = npos;
+  c->idx.slot_len = d_len;
+  c->idx.nslots = static_cast<uint32_t>(n);
+  c->idx.nkeys = nsolid + nrep;
+  c->idx.nrep = nrep;
+  c->has_index = true;
+}
+
+void build_index_entries(cuflye_ctx* c, int k, size_t n, const int64_t* tids, const int64_t* tpos,
+                         const uint64_t* keys_h, size_t nrep, const uint64_t* rep_h) {
+  if (k < 1 || k > 31) throw Error(CUFLYE_ERR_UNSUPPORTED, "k must be in [1, 31]");
+  c->has_index = false;
+  std::vector<int64_t> absids;
+  for (size_t i = 0; i < n; ++i) {
+    if (tids[i] == 0) throw Error(CUFLYE_ERR_INVALID, "target id must not be zero");
+    if (tpos[i] < 0 || tpos[i] >= (1ll << 31)) throw Error(CUFLYE_ERR_INVALID, "bad position");
+    absids.push_back(tids[i] < 0 ? -tids[i] : tids[i]);
+  }
+  std::sort(absids.begin(), absids.end());
+  absids.erase(std::unique(absids.begin(), absids.end()), absids.end());
+  c->slot_of.clear();
+  c->slot_signed_h = absids;
+  for (size_t s = 0; s < absids.size(); ++s) c->slot_of[absids[s]] = static_cast<uint32_t>(s);
+  const uint32_t nslots = static_cast<uint32_t>(std::max<size_t>(absids.size(), 1));
+  std::vector<uint64_t> vals_h(n);
+  for (size_t i = 0; i < n; ++i) {
+    const int64_t a = tids[i] < 0 ? -tids[i] : tids[i];
+    const uint32_t di = 2u * c->slot_of[a] + (tids[i] < 0 ? 1u : 0u);
+    vals_h[i] = (static_cast<uint64_t>(di) << 32) | static_cast<uint32_t>(tpos[i]);
+  }
+  cudaStream_t st = c->stream;
+  std::vector<int32_t> zero_len(nslots, 0);
+  std::vector<int64_t> signed_h(nslots, 1);
+  for (size_t s = 0; s < absids.size(); ++s) signed_h[s] = absids[s];
+  int32_t* d_len = buf<int32_t>(c, "ix_slot_len", nslots);
+  int64_t* d_signed = buf<int64_t>(c, "ix_slot_signed", nslots);
+  CUFLYE_CHECK(cudaMemcpyAsync(d_len, zero_len.data(), nslots * 4ull, cudaMemcpyHostToDevice, st));
+  CUFLYE_CHECK(cudaMemcpyAsync(d_signed, signed_h.data(), nslots * 8ull, cudaMemcpyHostToDevice, st));
+  const uint64_t nn = n;
+  uint64_t* keys = buf<uint64_t>(c, "ib_keys", nn);
+  uint64_t* vals = buf<uint64_t>(c, "ib_vals", nn);
+  uint64_t* keys2 = buf<uint64_t>(c, "ib_keys2", nn);
+  uint64_t* vals2 = buf<uint64_t>(c, "ib_vals2", nn);
+  if (nn) {
+    CUFLYE_CHECK(cudaMemcpyAsync(keys, keys_h, nn * 8, cudaMemcpyHostToDevice, st));
+    CUFLYE_CHECK(cudaMemcpyAsync(vals, vals_h.data(), nn * 8, cudaMemcpyHostToDevice, st));
+  }
+  std::vector<int> digits;
+  for (int d = 0; d < (2 * k + 7) / 8; ++d) digits.push_back(8 + d);
+  uint32_t* hist = buf<uint32_t>(c, "ib_hist", radix_hist_words(nn));
+  int in_alt = 0;
+  if (nn)
+    CUFLYE_CHECK(radix_sort_pairs(keys, vals, keys2, vals2, nn, digits.data(),
+                                  static_cast<int>(digits.size()), hist, &in_alt, st));
+  if (in_alt) {
+    std::swap(keys, keys2);
+    std::swap(vals, vals2);
+  }
+  uint32_t* flags = buf<uint32_t>(c, "ib_flags", nn);
+  uint64_t* run_id = buf<uint64_t>(c, "ib_runid", nn + 1);
+  CUFLYE_CHECK(index_mark_runs(keys, nn, flags, st));
+  const uint64_t nruns = scan_u32(c, flags, run_id, nn, "ib_scan");
+  uint64_t* run_start = buf<uint64_t>(c, "ib_runstart", nruns + 1);
+  CUFLYE_CHECK(index_run_starts(flags, run_id, nn, nruns, run_start, st));
+  uint32_t* kept = buf<uint32_t>(c, "ib_kept", nruns);
+  uint8_t* cls = buf<uint8_t>(c, "ib_cls", nruns);
+  CUFLYE_CHECK(index_classify_runs(run_start, nruns, 1, (1u << kCountBits) - 2, kept, cls, st));
+  uint64_t* kept_off = buf<uint64_t>(c, "ib_keptoff", nruns + 1);
+  const uint64_t npos = scan_u32(c, kept, kept_off, nruns, "ib_scan");
+  uint64_t* pos = buf<uint64_t>(c, "ix_pos", npos);
+  CUFLYE_CHECK(index_copy_positions(vals, run_id, run_start, cls, kept_off, nn, pos, st));
+  uint64_t cap = 16;
+  while (cap < 2 * (nruns + nrep)) cap <<= 1;
+  TableEntry* table = buf<TableEntry>(c, "ix_table", cap);
+  CUFLYE_CHECK(cudaMemsetAsync(table, 0xff, cap * sizeof(TableEntry), st));
+  CUFLYE_CHECK(index_insert(keys, run_start, cls, kept_off, nruns, table, cap - 1, c->status, st));
+  if (nrep) {
+    uint64_t* d_rep = buf<uint64_t>(c, "ib_rep", nrep);
+    CUFLYE_CHECK(cudaMemcpyAsync(d_rep, rep_h, nrep * 8, cudaMemcpyHostToDevice, st));
+    CUFLYE_CHECK(index_insert_repetitive(d_rep, nrep, table, cap - 1, c->status, st));
+  }
+  check_device_status(c);
+  for (const char* t : {"ib_keys", "ib_vals", "ib_keys2", "ib_vals2", "ib_hist", "ib_flags",
+                        "ib_runid", "ib_runstart", "ib_kept", "ib_cls", "ib_keptoff", "ib_scan",
+                        "ib_rep"})
+    release(c, t);
+  c->idx.k = k;
+  c->idx.transform = false;
+  c->idx.table = table;
+  c->idx.mask = cap - 1;
+  c->idx.pos = pos;
+  c->idx.npos = npos;
+  c->idx.slot_len = d_len;
+  c->idx.nslots = nslots;
+  c->idx.nkeys = nruns + nrep;
+  c->idx.nrep = nrep;
+  c->has_index = true;
+}
+
+// ---------------------------------------------------------------- passes
+
+struct Queries {
+  size_t n;
+  const int64_t* ids;
+  const int64_t* offsets;
+  const char* bases;
+};
+
+struct PassState {
+  uint32_t nq = 0;
+  uint64_t nwin = 0, nhits = 0, nfilt = 0;
+  uint64_t* keys = nullptr;
+  uint32_t* vals = nullptr;
+  uint64_t* kmers = nullptr;
+  int32_t* fpos = nullptr;
+  uint64_t* q_off = nullptr;  // nq + 1 hit offsets
+  uint64_t* f_off = nullptr;  // nq + 1 filtered offsets
+  QueryInfo* qinfo = nullptr;
+};
+
+// Upload one pass of queries and produce its hits in generation order.
+// Returns false (and leaves nothing allocated beyond the arena) when the
+// pass's hits would not fit the memory budget and the pass can be split.
+bool run_hits(cuflye_ctx* c, const Queries& Q, size_t q0, size_t q1, bool want_kmers,
+              uint64_t bytes_per_hit, PassState& ps) {
+  const int k = c->idx.k;
+  const uint32_t nq = static_cast<uint32_t>(q1 - q0);
+  ps.nq = nq;
+  std::vector<uint64_t> base_off(nq + 1), win_off(nq + 1);
+  std::vector<int32_t> qdi(nq);
+  std::vector<QueryInfo> qinfo(nq);
+  base_off[0] = 0;
+  win_off[0] = 0;
+  for (uint32_t i = 0; i < nq; ++i) {
+    const int64_t id = Q.ids[q0 + i];
+    if (id == 0) throw Error(CUFLYE_ERR_INVALID, "query id must not be zero");
+    const int64_t len = Q.offsets[q0 + i + 1] - Q.offsets[q0 + i];
+    if (len < 0) throw Error(CUFLYE_ERR_INVALID, "offsets must not decrease");
+    if (len >= (1ll << 31)) throw Error(CUFLYE_ERR_UNSUPPORTED, "query longer than 2^31");
+    base_off[i + 1] = base_off[i] + static_cast<uint64_t>(len);
+    win_off[i + 1] = win_off[i] + (len >= k ? static_cast<uint64_t>(len - k + 1) : 0);
+    const int64_t a = id < 0 ? -id : id;
+    auto it = c->slot_of.find(a);
+    qdi[i] = it == c->slot_of.end() ? -1 : static_cast<int32_t>(2u * it->second + (id < 0 ? 1u : 0u));
+    qinfo[i] = QueryInfo{id, static_cast<int32_t>(len), 0};
+  }
+  const uint64_t nbases = base_off[nq];
+  const uint64_t nwin = win_off[nq];
+  ps.nwin = nwin;
+  cudaStream_t st = c->stream;
+  uint8_t* d_ascii = buf<uint8_t>(c, "q_ascii", nbases + 16);
+  if (nbases)
+    CUFLYE_CHECK(cudaMemcpyAsync(d_ascii, Q.bases + Q.offsets[q0], nbases, cudaMemcpyHostToDevice,
+                                 st));
+  uint64_t* words = buf<uint64_t>(c, "q_words", (nbases + 31) / 32 + 2);
+  CUFLYE_CHECK(pack_bases(d_ascii, nbases, words, st));
+  uint64_t* d_base = buf<uint64_t>(c, "q_base", nq + 1);
+  uint64_t* d_win = buf<uint64_t>(c, "q_win", nq + 1);
+  int32_t* d_qdi = buf<int32_t>(c, "q_qdi", nq);
+  ps.qinfo = buf<QueryInfo>(c, "q_info", nq);
+  CUFLYE_CHECK(cudaMemcpyAsync(d_base, base_off.data(), (nq + 1) * 8ull, cudaMemcpyHostToDevice, st));
+  CUFLYE_CHECK(cudaMemcpyAsync(d_win, win_off.data(), (nq + 1) * 8ull, cudaMemcpyHostToDevice, st));
+  CUFLYE_CHECK(cudaMemcpyAsync(d_qdi, qdi.data(), nq * 4ull, cudaMemcpyHostToDevice, st));
+  CUFLYE_CHECK(cudaMemcpyAsync(ps.qinfo, qinfo.data(), nq * sizeof(QueryInfo),
+                               cudaMemcpyHostToDevice, st));
+  QueryBatch qb;
+  qb.words = words;
+  qb.base_off = d_base;
+  qb.win_off = d_win;
+  qb.qdi = d_qdi;
+  qb.nq = nq;
+  qb.nwin = nwin;
+  uint32_t* cnt = buf<uint32_t>(c, "w_cnt", nwin);
+  uint32_t* filt = buf<uint32_t>(c, "w_filt", nwin);
+  uint64_t* wmeta = buf<uint64_t>(c, "w_meta", nwin);
+  uint8_t* wflags = buf<uint8_t>(c, "w_flags", nwin);
+  CUFLYE_CHECK(hits_count(c->idx, qb, cnt, filt, wmeta, wflags, st));
+  uint64_t* hit_off = buf<uint64_t>(c, "w_hitoff", nwin + 1);
+  uint64_t* filt_off = buf<uint64_t>(c, "w_filtoff", nwin + 1);
+  ps.nhits = scan_u32(c, cnt, hit_off, nwin, "w_scan");
+  ps.nfilt = scan_u32(c, filt, filt_off, nwin, "w_scan");
+  if (c->budget) {
+    const uint64_t need = ps.nhits * bytes_per_hit;
+    if (c->in_use + need > c->budget && nq > 1) return false;
+  }
+  ps.q_off = buf<uint64_t>(c, "q_hitoff", nq + 1);
+  ps.f_off = buf<uint64_t>(c, "q_filtoff", nq + 1);
+  CUFLYE_CHECK(gather_query_offsets(d_win, hit_off, nq, ps.q_off, st));
+  CUFLYE_CHECK(gather_query_offsets(d_win, filt_off, nq, ps.f_off, st));
+  ps.keys = buf<uint64_t>(c, "h_keys", ps.nhits);
+  ps.vals = buf<uint32_t>(c, "h_vals", ps.nhits);
+  ps.kmers = want_kmers ? buf<uint64_t>(c, "h_kmers", ps.nhits) : nullptr;
+  ps.fpos = buf<int32_t>(c, "h_fpos", ps.nfilt);
+  CUFLYE_CHECK(hits_emit(c->idx, qb, hit_off, filt_off, wmeta, wflags, ps.keys, ps.vals, ps.kmers,
+                         ps.fpos, st));
+  return true;
+}
+
+ChainParams to_chain_params(const cuflye_overlap_params* p) {
+  ChainParams cp;
+  cp.k = p->kmer_size;
+  cp.min_overlap = p->min_overlap;
+  cp.max_jump = p->max_jump;
+  cp.max_gap = p->max_gap;
+  cp.gap_jump_threshold = p->gap_jump_threshold;
+  cp.max_overhang = p->max_overhang;
+  cp.check_overhang = p->check_overhang;
+  cp.force_local = p->force_local;
+  cp.only_max_ext = p->only_max_ext;
+  cp.max_overlaps = p->max_overlaps;
+  cp.large_gap_penalty = p->large_gap_penalty;
+  cp.small_gap_penalty = p->small_gap_penalty;
+  cp.min_kmer_survival_rate = p->min_kmer_survival_rate;
+  cp.max_divergence = p->max_divergence;
+  cp.sample_rate = p->sample_rate;
+  return cp;
+}
+
+// Sort + chaining of the pass's hits; returns the number of overlap rows left
+// on the device in "o_rows" (OverlapRow, query order, Flye emission order).
+uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
+  cudaStream_t st = c->stream;
+  const uint64_t H = ps.nhits;
+  const uint32_t nq = ps.nq;
+  uint32_t* lscr = buf<uint32_t>(c, "s_l", H + 1);
+  uint32_t* rscr = buf<uint32_t>(c, "s_r", H + 1);
+  uint32_t* lists = buf<uint32_t>(c, "s_lists", 3ull * std::max<uint64_t>(nq, 1));
+  uint32_t* scounts = buf<uint32_t>(c, "s_counts", 4);
+  // 1. KmerMatch sort per query: (ext id, cur pos) with libstdc++ order
+  uint64_t* qb = buf<uint64_t>(c, "s_qb", nq + 1);
+  CUFLYE_CHECK(cudaMemcpyAsync(qb, ps.q_off, (nq + 1) * 8ull, cudaMemcpyDeviceToDevice, st));
+  CUFLYE_CHECK(cudaEventRecord(c->ev[1], st));
+  CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, qb, qb + 1, nq, nullptr, lists,
+                                  scounts, c->num_sms, st));
+  CUFLYE_CHECK(cudaEventRecord(c->ev[2], st));
+  // 2. groups
+  uint32_t* gflags = buf<uint32_t>(c, "g_flags", H);
+  uint64_t* gid = buf<uint64_t>(c, "g_id", H + 1);
+  CUFLYE_CHECK(groups_mark(ps.keys, ps.q_off, nq, H, gflags, st));
+  const uint64_t G = scan_u32(c, gflags, gid, H, "g_scan");
+  if (G >= (1ull << 32)) throw Error(CUFLYE_ERR_UNSUPPORTED, "more than 2^32 target groups");
+  GroupInfo* groups = buf<GroupInfo>(c, "g_info", G);
+  CUFLYE_CHECK(groups_build(ps.keys, gflags, gid, ps.q_off, nq, H, G, groups, st));
+  uint32_t* ext_list = buf<uint32_t>(c, "g_extlist", G);
+  uint32_t* dp_list = buf<uint32_t>(c, "g_dplist", G);
+  uint32_t* gcounts = buf<uint32_t>(c, "g_counts", 4);
+  const int* slot_len = c->idx.slot_len;
+  CUFLYE_CHECK(groups_prefilter_n(ps.keys, ps.vals, groups, G, H, ps.qinfo, slot_len, cp,
+                                  ext_list, dp_list, gcounts, st));
+  uint64_t* sb = buf<uint64_t>(c, "g_sb", G);
+  uint64_t* se = buf<uint64_t>(c, "g_se", G);
+  uint32_t* glists = buf<uint32_t>(c, "g_lists", 3 * std::max<uint64_t>(G, 1));
+  const uint32_t G32 = static_cast<uint32_t>(G);
+  // 3. ext-sorted groups: re-sort by ext pos
+  CUFLYE_CHECK(groups_prepare_ext_sort(ps.keys, ps.vals, groups, ext_list, gcounts, sb, se, st));
+  CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, sb, se, G32, gcounts + 0, glists,
+                                  scounts, c->num_sms, st));
+  int32_t* cur = buf<int32_t>(c, "c_cur", H);
+  int32_t* ext = buf<int32_t>(c, "c_ext", H);
+  CUFLYE_CHECK(groups_split(ps.keys, ps.vals, groups, dp_list, gcounts, cur, ext, st));
+  // 4. DP
+  int32_t* score = buf<int32_t>(c, "c_score", H);
+  int32_t* bt = buf<int32_t>(c, "c_bt", H);
+  CUFLYE_CHECK(chain_dp(cur, ext, score, bt, groups, dp_list, gcounts, cp, c->num_sms, st));
+  // 5. score order (libstdc++ order of indices by score descending)
+  CUFLYE_CHECK(chain_prepare_order(score, ps.keys, ps.vals, groups, dp_list, gcounts, sb, se, st));
+  CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, sb, se, G32, gcounts + 1, glists,
+                                  scounts, c->num_sms, st));
+  // 6. backtrack, proposals, primary selection
+  const uint64_t pool_cap = 8 * G + 1024;
+  OverlapRow* pool = buf<OverlapRow>(c, "o_pool", pool_cap);
+  uint32_t* pool_count = buf<uint32_t>(c, "o_poolcount", 1);
+  uint32_t* group_rows = buf<uint32_t>(c, "o_grows", G);
+  CUFLYE_CHECK(cudaMemsetAsync(pool_count, 0, 4, st));
+  CUFLYE_CHECK(cudaMemsetAsync(group_rows, 0, std::max<uint64_t>(G, 1) * 4, st));
+  CUFLYE_CHECK(chain_backtrack(cur, ext, score, bt, ps.vals, groups, dp_list, gcounts, ps.qinfo,
+                               ps.f_off, ps.fpos, buf<int64_t>(c, "ix_slot_signed", 1), c->logt,
+                               cp, pool, pool_cap, pool_count, group_rows, c->status, G32, st));
+  check_device_status(c);
+  // 7. max_overlaps + compaction in group order
+  uint64_t* qg = buf<uint64_t>(c, "o_qg", nq + 1);
+  CUFLYE_CHECK(query_group_offsets(groups, G, nq, qg, st));
+  uint32_t* kept = buf<uint32_t>(c, "o_kept", G);
+  if (cp.max_overlaps > 0) {
+    CUFLYE_CHECK(rows_limit(group_rows, qg, nq, cp.max_overlaps, kept, st));
+  } else {
+    kept = group_rows;
+  }
+  uint64_t* kept_off = buf<uint64_t>(c, "o_keptoff", G + 1);
+  const uint64_t R = scan_u32(c, kept, kept_off, G, "o_scan");
+  const uint32_t npool = read_scalar(c, pool_count);
+  OverlapRow* rows = buf<OverlapRow>(c, "o_rows", R);
+  CUFLYE_CHECK(rows_scatter(pool, npool, kept, kept_off, rows, st));
+  CUFLYE_CHECK(cudaEventRecord(c->ev[3], st));
+  return R;
+}
+
+float elapsed(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0;
+  if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return ms;
+}
+
+void reset_timing(cuflye_ctx* c) {
+  for (int i = 0; i < 5; ++i) {
+    c->stage_ms[i] = 0;
+    c->stage_bytes[i] = 0;
+  }
+}
+
+void accumulate_timing(cuflye_ctx* c, bool chained) {
+  sync(c);
+  c->stage_ms[0] += elapsed(c->ev[0], c->ev[1]);
+  if (chained) {
+    c->stage_ms[1] += elapsed(c->ev[1], c->ev[2]);
+    c->stage_ms[2] += elapsed(c->ev[2], c->ev[3]);
+    c->stage_ms[3] += elapsed(c->ev[3], c->ev[4]);
+  }
+}
+
+size_t pass_size(cuflye_ctx* c, size_t n) {
+  if (c->queries_per_pass) return std::min(n, c->queries_per_pass);
+  return n;
+}
+
+// Runs passes over [0, n): `body(q0, q1, ps)` consumes each pass.
+template <typename Body>
+void for_each_pass(cuflye_ctx* c, const Queries& Q, bool kmers, uint64_t bytes_per_hit,
+                   Body body) {
+  size_t q0 = 0;
+  size_t step = std::max<size_t>(pass_size(c, Q.n), 1);
+  while (q0 < Q.n) {
+    size_t q1 = std::min(Q.n, q0 + step);
+    PassState ps;
+    CUFLYE_CHECK(cudaEventRecord(c->ev[0], c->stream));
+    if (!run_hits(c, Q, q0, q1, kmers, bytes_per_hit, ps)) {
+      step = std::max<size_t>((q1 - q0) / 2, 1);
+      continue;
+    }
+    CUFLYE_CHECK(cudaEventRecord(c->ev[1], c->stream));
+    body(q0, q1, ps);
+    q0 = q1;
+  }
+}
+
+constexpr uint64_t kChainBytesPerHit = 8 + 4 + 4 + 4 + 4 + 4 + 4 + 4 + 8;
+
+void require_index(cuflye_ctx* c) {
+  if (!c->has_index) throw Error(CUFLYE_ERR_NO_INDEX, "no k-mer index: call cuflye_index_build");
+}
+
+void check_params(cuflye_ctx* c, const cuflye_overlap_params* p) {
+  if (!p) throw Error(CUFLYE_ERR_INVALID, "params must not be null");
+  if (p->kmer_size != c->idx.k)
+    throw Error(CUFLYE_ERR_INVALID, "params.kmer_size differs from the index k");
+  if (p->max_jump <= 0 || p->min_overlap < 0)
+    throw Error(CUFLYE_ERR_INVALID, "max_jump must be > 0 and min_overlap >= 0");
+}
+
+// Device buffers for graph tables.
+struct GraphDev {
+  int64_t* edge_of_slot;
+  int32_t* left;
+  int32_t* right;
+};
+
+}  // namespace
+
+// ================================================================ C ABI
+
+#define CUFLYE_API_BEGIN(ctx)                   \
+  if (!(ctx)) return CUFLYE_ERR_INVALID;        \
+  std::lock_guard<std::mutex> lock_((ctx)->mu); \
+  try {
+#define CUFLYE_API_END(ctx)           \
+  }                                   \
+  catch (const Error& e) {            \
+    (ctx)->err = e.what();            \
+    return e.code;                    \
+  }                                   \
+  catch (const std::exception& e) {   \
+    (ctx)->err = e.what();            \
+    return CUFLYE_ERR_CUDA;           \
+  }                                   \
+  (ctx)->err.clear();                 \
+  return CUFLYE_OK;
+
+extern "C" {
+
+int cuflye_candidate_backend(char* msg, size_t msg_cap) {
+  const char* v = std::getenv("CUFLYE_CANDIDATE_BACKEND");
+  if (!v || !v[0] || std::strcmp(v, "cpu") == 0) return 0;
+  if (std::strcmp(v, "cuda") == 0) return 1;
+  if (msg && msg_cap) std::snprintf(msg, msg_cap, "Unsupported CUFLYE_CANDIDATE_BACKEND: %s", v);
+  return -1;
+}
+
+cuflye_status cuflye_open(int device, uint64_t memory_budget_bytes, cuflye_ctx** out) {
+  if (!out) return CUFLYE_ERR_INVALID;
+  *out = nullptr;
+  cuflye_ctx* c = new cuflye_ctx();
+  try {
+    int ndev = 0;
+    CUFLYE_CHECK(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev)
+      throw Error(CUFLYE_ERR_INVALID, "CUFLYE_CUDA_DEVICE=" + std::to_string(device) +
+                                          " is not a visible device (" + std::to_string(ndev) +
+                                          " visible)");
+    c->device = device;
+    c->budget = memory_budget_bytes;
+    CUFLYE_CHECK(cudaSetDevice(device));
+    CUFLYE_CHECK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    CUFLYE_CHECK(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device));
+    for (auto& e : c->ev) CUFLYE_CHECK(cudaEventCreate(&e));
+    c->status = buf<DeviceStatus>(c, "status", 1);
+    CUFLYE_CHECK(cudaMemset(c->status, 0, sizeof(DeviceStatus)));
+    load_logf_table(c);
+  } catch (const Error& e) {
+    std::fprintf(stderr, "cuflye_open: %s\n", e.what());
+    cuflye_close(c);
+    return e.code;
+  }
+  *out = c;
+  return CUFLYE_OK;
+}
+
+cuflye_status cuflye_open_from_env(cuflye_ctx** out) {
+  const char* dev = std::getenv("CUFLYE_CUDA_DEVICE");
+  const char* bud = std::getenv("CUFLYE_CUDA_MEMORY_BUDGET_BYTES");
+  int d = 0;
+  uint64_t b = 0;
+  if (dev && dev[0]) {
+    char* end = nullptr;
+    long v = std::strtol(dev, &end, 10);
+    if (!end || *end) return CUFLYE_ERR_INVALID;
+    d = static_cast<int>(v);
+  }
+  if (bud && bud[0] && std::strcmp(bud, "unbounded") != 0) {
+    char* end = nullptr;
+    unsigned long long v = std::strtoull(bud, &end, 10);
+    if (!end || *end) return CUFLYE_ERR_INVALID;
+    b = v;
+  }
+  return cuflye_open(d, b, out);
+}
+
+void cuflye_close(cuflye_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (auto& kv : c->bufs)
+    if (kv.second.p) cudaFree(kv.second.p);
+  for (auto& e : c->ev)
+    if (e) cudaEventDestroy(e);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+const char* cuflye_last_error(const cuflye_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+cuflye_status cuflye_memory_stats(const cuflye_ctx* c, uint64_t* in_use, uint64_t* peak) {
+  if (!c) return CUFLYE_ERR_INVALID;
+  if (in_use) *in_use = c->in_use;
+  if (peak) *peak = c->peak;
+  return CUFLYE_OK;
+}
+
+cuflye_status cuflye_index_build(cuflye_ctx* c, int k, size_t n, const int64_t* ids,
+                                 const int64_t* offsets, const char* bases, uint32_t min_freq,
+                                 uint32_t max_freq) {
+  CUFLYE_API_BEGIN(c)
+  CUFLYE_CHECK(cudaSetDevice(c->device));
+  if (!ids || !offsets || (!bases && n)) throw Error(CUFLYE_ERR_INVALID, "null input");
+  build_index(c, k, n, ids, offsets, bases, min_freq, max_freq);
+  CUFLYE_API_END(c)
+}
+
+cuflye_status cuflye_index_from_entries(cuflye_ctx* c, int k, size_t n, const int64_t* tids,
+                                        const int64_t* positions, const uint64_t* keys,
+                                        size_t n_rep, const uint64_t* rep_keys) {
+  CUFLYE_API_BEGIN(c)
+  CUFLYE_CHECK(cudaSetDevice(c->device));
+  build_index_entries(c, k, n, tids, positions, keys, n_rep, rep_keys);
+  CUFLYE_API_END(c)
+}
+
+cuflye_status cuflye_index_stats(const cuflye_ctx* c, uint64_t* keys, uint64_t* positions,
+                                 uint64_t* repetitive) {
+  if (!c) return CUFLYE_ERR_INVALID;
+  if (!c->has_index) return CUFLYE_ERR_NO_INDEX;
+  if (keys) *keys = c->idx.nkeys;
+  if (positions) *positions = c->idx.npos;
+  if (repetitive) *repetitive = c->idx.nrep;
+  return CUFLYE_OK;
+}
+
+cuflye_status cuflye_set_batch_queries(cuflye_ctx* c, size_t q) {
+  if (!c) return CUFLYE_ERR_INVALID;
+  c->queries_per_pass = q;
+  return CUFLYE_OK;
+}
+
+cuflye_status cuflye_candidates(cuflye_ctx* c, size_t n, const int64_t* ids,
+                                const int64_t* offsets, const char* bases, cuflye_candidate* out,
+                                size_t out_cap, size_t* n_out, cuflye_filtered_pos* filtered,
+                                size_t filtered_cap, size_t* n_filtered) {
+  CUFLYE_API_BEGIN(c)
+  CUFLYE_CHECK(cudaSetDevice(c->device));
+  require_index(c);
+  if (!ids || !offsets || (!bases && n)) throw Error(CUFLYE_ERR_INVALID, "null input");
+  reset_timing(c);
+  Queries Q{n, ids, offsets, bases};
+  size_t total = 0, ftotal = 0;
+  bool overflow = false;
+  for_each_pass(c, Q, true, 8 + 4 + 8 + 32, [&](size_t, size_t, PassState& ps) {
+    if (!overflow && total + ps.nhits <= out_cap && ftotal + ps.nfilt <= filtered_cap) {
+      cuflye_candidate* d_out = buf<cuflye_candidate>(c, "a_cand", ps.nhits);
+      cuflye_filtered_pos* d_f = buf<cuflye_filtered_pos>(c, "a_filt", ps.nfilt);
+      CUFLYE_CHECK(hits_to_abi(ps.keys, ps.vals, ps.kmers, ps.nhits, ps.q_off, ps.nq, ps.qinfo,
+                               buf<int64_t>(c, "ix_slot_signed", 1), d_out, c->stream));
+      CUFLYE_CHECK(filtered_to_abi(ps.fpos, ps.nfilt, ps.f_off, ps.nq, ps.qinfo, d_f, c->stream));
+      if (ps.nhits)
+        CUFLYE_CHECK(cudaMemcpyAsync(out + total, d_out, ps.nhits * sizeof(cuflye_candidate),
+                                     cudaMemcpyDeviceToHost, c->stream));
+      if (ps.nfilt)
+        CUFLYE_CHECK(cudaMemcpyAsync(filtered + ftotal, d_f,
+                                     ps.nfilt * sizeof(cuflye_filtered_pos),
+                                     cudaMemcpyDeviceToHost, c->stream));
+      sync(c);
+    } else {
+      overflow = true;
+    }
+    total += ps.nhits;
+    ftotal += ps.nfilt;
+    accumulate_timing(c, false);
+  });
+  if (n_out) *n_out = total;
+  if (n_filtered) *n_filtered = ftotal;
+  if (overflow)
+    throw Error(CUFLYE_ERR_CAPACITY, "output capacity too small: need " + std::to_string(total) +
+                                         " candidates and " + std::to_string(ftotal) +
+                                         " filtered positions");
+  CUFLYE_API_END(c)
+}
+
+cuflye_status cuflye_overlaps(cuflye_ctx* c, size_t n, const int64_t* ids, const int64_t* offsets,
+                              const char* bases, const cuflye_overlap_params* params,
+                              cuflye_overlap_range* out, size_t out_cap, size_t* n_out) {
+  CUFLYE_API_BEGIN(c)
+  CUFLYE_CHECK(cudaSetDevice(c->device));
+  require_index(c);
+  check_params(c, params);
+  if (!ids || !offsets || (!bases && n)) throw Error(CUFLYE_ERR_INVALID, "null input");
+  reset_timing(c);
+  const ChainParams cp = to_chain_params(params);
+  Queries Q{n, ids, offsets, bases};
+  size_t total = 0;
+  bool overflow = false;
+  uint64_t hits_total = 0, windows_total = 0;
+  for_each_pass(c, Q, false, kChainBytesPerHit, [&](size_t, size_t, PassState& ps) {
+    hits_total += ps.nhits;
+    windows_total += ps.nwin;
+    const uint64_t R = run_chain(c, ps, cp);
+    if (!overflow && total + R <= out_cap) {
+      cuflye_overlap_range* d_out = buf<cuflye_overlap_range>(c, "a_ovl", R);
+      CUFLYE_CHECK(rows_to_abi(buf<OverlapRow>(c, "o_rows", R), R, ps.qinfo,
+                               buf<int64_t>(c, "ix_slot_signed", 1), d_out, c->stream));
+      if (R)
+        CUFLYE_CHECK(cudaMemcpyAsync(out + total, d_out, R * sizeof(cuflye_overlap_range),
+                                     cudaMemcpyDeviceToHost, c->stream));
+    } else {
+      overflow = true;
+    }
+    CUFLYE_CHECK(cudaEventRecord(c->ev[4], c->stream));
+    total += R;
+    accumulate_timing(c, true);
+  });
+  c->stage_bytes[0] = windows_total * 32 + hits_total * 12;
+  c->stage_bytes[1] = hits_total * 24;
+  c->stage_bytes[2] = hits_total * 36;
+  if (n_out) *n_out = total;
+  if (overflow)
+    throw Error(CUFLYE_ERR_CAPACITY,
+                "output capacity too small: need " + std::to_string(total) + " overlap rows");
+  CUFLYE_API_END(c)
+}
+
+cuflye_status cuflye_graph_set(cuflye_ctx* c, size_t ne, const int64_t* edge_ids,
+                               const int64_t* seq_ids, const int32_t* left,
+                               const int32_t* right) {
+  CUFLYE_API_BEGIN(c)
+  CUFLYE_CHECK(cudaSetDevice(c->device));
+  require_index(c);
+  if (!c->idx.transform)
+    throw Error(CUFLYE_ERR_UNSUPPORTED, "read-to-graph needs an index built from edge sequences");
+  const uint32_t ns = c->idx.nslots;
+  std::vector<int64_t> eos(ns, 0);
+  std::vector<int32_t> l(ns, -1), r(ns, -1);
+  for (size_t e = 0; e < ne; ++e) {
+    if (edge_ids[e] <= 0 || seq_ids[e] <= 0)
+      throw Error(CUFLYE_ERR_INVALID, "edge ids and sequence ids must be > 0");
+    auto it = c->slot_of.find(seq_ids[e]);
+    if (it == c->slot_of.end())
+      throw Error(CUFLYE_ERR_INVALID,
+                  "edge sequence " + std::to_string(seq_ids[e]) + " is not in the index");
+    eos[it->second] = edge_ids[e];
+    l[it->second] = left[e];
+    r[it->second] = right[e];
+  }
+  for (uint32_t s = 0; s < ns; ++s)
+    if (eos[s] == 0)
+      throw Error(CUFLYE_ERR_INVALID, "indexed sequence " + std::to_string(c->slot_signed_h[s]) +
+                                          " has no graph edge");
+  int64_t* de = buf<int64_t>(c, "gr_edge", ns);
+  int32_t* dl = buf<int32_t>(c, "gr_left", ns);
+  int32_t* dr = buf<int32_t>(c, "gr_right", ns);
+  CUFLYE_CHECK(cudaMemcpy(de, eos.data(), ns * 8ull, cudaMemcpyHostToDevice));
+  CUFLYE_CHECK(cudaMemcpy(dl, l.data(), ns * 4ull, cudaMemcpyHostToDevice));
+  CUFLYE_CHECK(cudaMemcpy(dr, r.data(), ns * 4ull, cudaMemcpyHostToDevice));
+  c->has_graph = true;
+  CUFLYE_API_END(c)
+}
+
+cuflye_status cuflye_read_to_graph(cuflye_ctx* c, size_t n, const int64_t* ids,
+                                   const int64_t* offsets, const char* bases,
+                                   const cuflye_overlap_params* params,
+                                   const cuflye_r2g_params* r2g, cuflye_read_alignment* out,
+                                   size_t out_cap, size_t* n_out) {
+  CUFLYE_API_BEGIN(c)
+  CUFLYE_CHECK(cudaSetDevice(c->device));
+  require_index(c);
+  check_params(c, params);
+  if (!c->has_graph) throw Error(CUFLYE_ERR_INVALID, "no graph: call cuflye_graph_set");
+  if (!r2g) throw Error(CUFLYE_ERR_INVALID, "r2g params must not be null");
+  reset_timing(c);
+  const ChainParams cp = to_chain_params(params);
+  R2GParams rp{r2g->max_jump,       r2g->max_read_overlap, r2g->min_overlap,
+               r2g->max_separation, r2g->long_edge,        r2g->big_aln,
+               r2g->max_chain_divergence};
+  const uint32_t ns = c->idx.nslots;
+  R2GGraph g{buf<int64_t>(c, "gr_edge", ns), buf<int32_t>(c, "gr_left", ns),
+             buf<int32_t>(c, "gr_right", ns), buf<int64_t>(c, "ix_slot_signed", ns)};
+  Queries Q{n, ids, offsets, bases};
+  size_t total = 0;
+  uint64_t chain_base = 0;
+  bool overflow = false;
+  for_each_pass(c, Q, false, kChainBytesPerHit, [&](size_t, size_t, PassState& ps) {
+    cudaStream_t st = c->stream;
+    const uint64_t R = run_chain(c, ps, cp);
+    const uint32_t nq = ps.nq;
+    OverlapRow* rows = buf<OverlapRow>(c, "o_rows", R);
+    uint32_t* keep = buf<uint32_t>(c, "r_keep", R);
+    uint64_t* kpos = buf<uint64_t>(c, "r_kpos", R + 1);
+    CUFLYE_CHECK(r2g_filter(rows, R, rp, keep, st));
+    const uint64_t A = scan_u32(c, keep, kpos, R, "r_scan");
+    OverlapRow* aln = buf<OverlapRow>(c, "r_aln", A);
+    CUFLYE_CHECK(r2g_compact(rows, R, keep, kpos, aln, st));
+    // per-read alignment offsets: rows are in read order
+    {
+      std::vector<OverlapRow> tmp(R);
+      if (R) CUFLYE_CHECK(cudaMemcpyAsync(tmp.data(), rows, R * sizeof(OverlapRow),
+                                          cudaMemcpyDeviceToHost, st));
+      std::vector<uint32_t> hkeep(R);
+      if (R) CUFLYE_CHECK(cudaMemcpyAsync(hkeep.data(), keep, R * 4ull, cudaMemcpyDeviceToHost, st));
+      sync(c);
+      std::vector<uint64_t> a_off(nq + 1, 0);
+      for (uint64_t i = 0; i < R; ++i)
+        if (hkeep[i]) a_off[tmp[i].query + 1] += 1;
+      for (uint32_t q = 0; q < nq; ++q) a_off[q + 1] += a_off[q];
+      uint64_t* d_aoff = buf<uint64_t>(c, "r_aoff", nq + 1);
+      CUFLYE_CHECK(cudaMemcpyAsync(d_aoff, a_off.data(), (nq + 1) * 8ull, cudaMemcpyHostToDevice,
+                                   st));
+    }
+    uint64_t* d_aoff = buf<uint64_t>(c, "r_aoff", nq + 1);
+    uint64_t* skeys = buf<uint64_t>(c, "r_skeys", A);
+    uint32_t* svals = buf<uint32_t>(c, "r_svals", A);
+    CUFLYE_CHECK(r2g_sort_keys(aln, d_aoff, nq, skeys, svals, st));
+    uint32_t* sl = buf<uint32_t>(c, "r_sl", A + 1);
+    uint32_t* sr = buf<uint32_t>(c, "r_sr", A + 1);
+    uint32_t* slists = buf<uint32_t>(c, "r_slists", 3ull * nq);
+    uint32_t* scounts = buf<uint32_t>(c, "r_scounts", 4);
+    CUFLYE_CHECK(segmented_std_sort(skeys, svals, sl, sr, d_aoff, d_aoff + 1, nq, nullptr, slists,
+                                    scounts, c->num_sms, st));
+    OverlapRow* sorted = buf<OverlapRow>(c, "r_sorted", A);
+    CUFLYE_CHECK(r2g_permute(aln, d_aoff, nq, svals, sorted, st));
+    void* recs = buf<uint8_t>(c, "r_recs", A * r2g_rec_bytes());
+    int32_t* act = buf<int32_t>(c, "r_act", A);
+    int32_t* frz = buf<int32_t>(c, "r_frz", A);
+    int32_t* good = buf<int32_t>(c, "r_good", A);
+    uint32_t* n_good = buf<uint32_t>(c, "r_ngood", nq);
+    uint32_t* n_rows = buf<uint32_t>(c, "r_nrows", nq);
+    CUFLYE_CHECK(r2g_chain(sorted, d_aoff, nq, g, rp, recs, act, frz, good, n_good, n_rows, st));
+    uint64_t* row_off = buf<uint64_t>(c, "r_rowoff", nq + 1);
+    const uint64_t nrows = scan_u32(c, n_rows, row_off, nq, "r_scan");
+    // chain ids: 2 * good chains per read
+    std::vector<uint32_t> hg(nq);
+    if (nq) CUFLYE_CHECK(cudaMemcpyAsync(hg.data(), n_good, nq * 4ull, cudaMemcpyDeviceToHost, st));
+    sync(c);
+    std::vector<uint64_t> coff(nq + 1);
+    coff[0] = chain_base;
+    for (uint32_t q = 0; q < nq; ++q) coff[q + 1] = coff[q] + 2ull * hg[q];
+    uint64_t* d_coff = buf<uint64_t>(c, "r_coff", nq + 1);
+    CUFLYE_CHECK(cudaMemcpyAsync(d_coff, coff.data(), (nq + 1) * 8ull, cudaMemcpyHostToDevice, st));
+    cuflye_read_alignment* d_out = buf<cuflye_read_alignment>(c, "r_out", nrows);
+    int32_t* tmp = buf<int32_t>(c, "r_tmp", A);
+    CUFLYE_CHECK(r2g_emit(sorted, d_aoff, nq, g, ps.qinfo, recs, good, n_good, d_coff, row_off,
+                          tmp, d_out, st));
+    if (!overflow && total + nrows <= out_cap) {
+      if (nrows)
+        CUFLYE_CHECK(cudaMemcpyAsync(out + total, d_out, nrows * sizeof(cuflye_read_alignment),
+                                     cudaMemcpyDeviceToHost, st));
+    } else {
+      overflow = true;
+    }
+    CUFLYE_CHECK(cudaEventRecord(c->ev[4], st));
+    total += nrows;
+    chain_base = coff[nq];
+    accumulate_timing(c, true);
+  });
+  if (n_out) *n_out = total;
+  if (overflow)
+    throw Error(CUFLYE_ERR_CAPACITY,
+                "output capacity too small: need " + std::to_string(total) + " alignment rows");
+  CUFLYE_API_END(c)
+}
+
+cuflye_status cuflye_std_sort_segments(cuflye_ctx* c, uint64_t* keys, uint32_t* values,
+                                       const uint64_t* seg_offsets, size_t n_segments) {
+  CUFLYE_API_BEGIN(c)
+  CUFLYE_CHECK(cudaSetDevice(c->device));
+  if (!seg_offsets) throw Error(CUFLYE_ERR_INVALID, "null segment offsets");
+  if (n_segments >= (1ull << 32)) throw Error(CUFLYE_ERR_UNSUPPORTED, "too many segments");
+  const uint64_t n = seg_offsets[n_segments];
+  for (size_t s = 0; s < n_segments; ++s) {
+    if (seg_offsets[s + 1] < seg_offsets[s]) throw Error(CUFLYE_ERR_INVALID, "offsets decrease");
+    if (seg_offsets[s + 1] - seg_offsets[s] >= (1ull << 32))
+      throw Error(CUFLYE_ERR_UNSUPPORTED, "segment longer than 2^32 - 1");
+  }
+  if (n && (!keys || !values)) throw Error(CUFLYE_ERR_INVALID, "null keys or values");
+  if (n_segments == 0 || n == seg_offsets[0]) {
+    c->err.clear();
+    return CUFLYE_OK;
+  }
+  cudaStream_t st = c->stream;
+  const uint64_t base = seg_offsets[0];
+  const uint64_t m = n - base;
+  uint64_t* dk = buf<uint64_t>(c, "t_keys", m);
+  uint32_t* dv = buf<uint32_t>(c, "t_vals", m);
+  uint32_t* dl = buf<uint32_t>(c, "t_l", m + 1);
+  uint32_t* dr = buf<uint32_t>(c, "t_r", m + 1);
+  uint64_t* off = buf<uint64_t>(c, "t_off", n_segments + 1);
+  uint32_t* lists = buf<uint32_t>(c, "t_lists", 3 * n_segments);
+  uint32_t* counts = buf<uint32_t>(c, "t_counts", 4);
+  std::vector<uint64_t> rel(n_segments + 1);
+  for (size_t s = 0; s <= n_segments; ++s) rel[s] = seg_offsets[s] - base;
+  CUFLYE_CHECK(cudaMemcpyAsync(dk, keys + base, m * 8, cudaMemcpyHostToDevice, st));
+  CUFLYE_CHECK(cudaMemcpyAsync(dv, values + base, m * 4, cudaMemcpyHostToDevice, st));
+  CUFLYE_CHECK(cudaMemcpyAsync(off, rel.data(), rel.size() * 8, cudaMemcpyHostToDevice, st));
+  CUFLYE_CHECK(segmented_std_sort(dk, dv, dl, dr, off, off + 1,
+                                  static_cast<uint32_t>(n_segments), nullptr, lists, counts,
+                                  c->num_sms, st));
+  CUFLYE_CHECK(cudaMemcpyAsync(keys + base, dk, m * 8, cudaMemcpyDeviceToHost, st));
+  CUFLYE_CHECK(cudaMemcpyAsync(values + base, dv, m * 4, cudaMemcpyDeviceToHost, st));
+  sync(c);
+  CUFLYE_API_END(c)
+}
+
+cuflye_status cuflye_last_timing(const cuflye_ctx* c, double* stage_ms, uint64_t* stage_bytes,
+                                 size_t n_stages) {
+  if (!c) return CUFLYE_ERR_INVALID;
+  for (size_t i = 0; i < n_stages && i < 5; ++i) {
+    if (stage_ms) stage_ms[i] = c->stage_ms[i];
+    if (stage_bytes) stage_bytes[i] = c->stage_bytes[i];
+  }
+  return CUFLYE_OK;
+}
+
+}  // extern "C"

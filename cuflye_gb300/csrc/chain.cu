@@ -1,0 +1,652 @@
+// chain.cu — per-target chaining of sorted KmerMatches (getSeqOverlaps after
+// the candidate loop), following tools/replay_overlap_chains.py:228-422 and
+// cuda/cuflye_cuda_overlap_chain_replay.cu:977-1015, 1493-1719.
+//
+// A group is a run of equal ext ids inside one query's sorted matches.
+//   groups_*       : group bounds, the survival / span / overhang prefilter,
+//                    and the ext-sorted re-sort (via the libstdc++-order sort);
+//   chain_dp       : the O(n * window) DP, one warp per group (see dp_kernel);
+//   chain_backtrack: score-ordered backtrack (order from the libstdc++-order
+//                    sort of the scores), overlapTest, k-mer divergence,
+//                    proposal sort, primary selection and the divergence
+//                    filter, one thread per group;
+//   rows_*         : max_overlaps cutoff per query and order-preserving
+//                    compaction of the rows.
+#include <climits>
+#include <cstdint>
+
+#include "common.cuh"
+#include "introsort.cuh"
+#include "kernels.h"
+
+namespace cuflye {
+namespace {
+
+inline unsigned grid(uint64_t n, int b) {
+  return static_cast<unsigned>((n + b - 1) / b > 0 ? (n + b - 1) / b : 1);
+}
+
+__device__ __forceinline__ uint32_t upper_query(const uint64_t* __restrict__ q_off, uint32_t nq,
+                                                uint64_t i) {
+  // query q with q_off[q] <= i < q_off[q + 1]
+  uint32_t lo = 0, hi = nq - 1;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi + 1) >> 1;
+    if (q_off[mid] <= i)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void mark_ext_changes(const uint64_t* __restrict__ keys, uint64_t n,
+                                 uint32_t* __restrict__ flags) {
+  const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  flags[i] = (i == 0 || (keys[i] >> 32) != (keys[i - 1] >> 32)) ? 1u : 0u;
+}
+
+__global__ void mark_query_starts(const uint64_t* __restrict__ q_off, uint32_t nq,
+                                  uint32_t* __restrict__ flags) {
+  const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq) return;
+  if (q_off[q] < q_off[q + 1]) flags[q_off[q]] = 1u;
+}
+
+__global__ void build_groups(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ flags,
+                             const uint64_t* __restrict__ gid, const uint64_t* __restrict__ q_off,
+                             uint32_t nq, uint64_t n, GroupInfo* __restrict__ groups) {
+  const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n || !flags[i]) return;
+  GroupInfo g{};
+  g.start = i;
+  g.ext_di = static_cast<uint32_t>(keys[i] >> 32);
+  g.query = upper_query(q_off, nq, i);
+  groups[gid[i]] = g;
+}
+
+__global__ void prefilter_kernel(const uint64_t* __restrict__ keys,
+                                 const uint32_t* __restrict__ vals, GroupInfo* __restrict__ groups,
+                                 uint64_t ngroups, uint64_t nhits,
+                                 const QueryInfo* __restrict__ qinfo,
+                                 const int32_t* __restrict__ slot_len, ChainParams p,
+                                 uint32_t* __restrict__ ext_list, uint32_t* __restrict__ dp_list,
+                                 uint32_t* __restrict__ counts) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t g = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  if (g >= ngroups) return;
+  GroupInfo gi = groups[g];
+  const uint64_t end = g + 1 < ngroups ? groups[g + 1].start : nhits;
+  const uint32_t n = static_cast<uint32_t>(end - gi.start);
+  // unique query positions (changes of curPos, starting from prevPos = 0)
+  uint32_t uniq = 0;
+  int32_t mn = INT_MAX, mx = INT_MIN;
+  for (uint32_t j = lane; j < n; j += 32) {
+    const uint64_t i = gi.start + j;
+    const int32_t c = static_cast<int32_t>(keys[i] & 0xffffffffu);
+    const int32_t prev = j == 0 ? 0 : static_cast<int32_t>(keys[i - 1] & 0xffffffffu);
+    uniq += c != prev;
+    const int32_t e = static_cast<int32_t>(vals[i]);
+    mn = min(mn, e);
+    mx = max(mx, e);
+  }
+  for (int d = 16; d > 0; d >>= 1) {
+    uniq += __shfl_down_sync(0xffffffffu, uniq, d);
+    mn = min(mn, __shfl_down_sync(0xffffffffu, mn, d));
+    mx = max(mx, __shfl_down_sync(0xffffffffu, mx, d));
+  }
+  if (lane != 0) return;
+  const int32_t cur_len = qinfo[gi.query].len;
+  const int32_t ext_len = slot_len[gi.ext_di >> 1];
+  const int32_t min_cur = static_cast<int32_t>(keys[gi.start] & 0xffffffffu);
+  const int32_t max_cur = static_cast<int32_t>(keys[end - 1] & 0xffffffffu);
+  gi.n = n;
+  gi.ext_len = ext_len;
+  gi.ext_sorted = ext_len > cur_len;
+  bool ok = !(static_cast<float>(uniq) <
+              fmul(p.min_kmer_survival_rate, static_cast<float>(p.min_overlap)));
+  if (ok && (max_cur - min_cur < p.min_overlap || mx - mn < p.min_overlap)) ok = false;
+  if (ok && p.check_overhang && !p.force_local) {
+    if (min(min_cur, mn) > p.max_overhang) ok = false;
+    if (min(cur_len - max_cur, ext_len - mx) > p.max_overhang) ok = false;
+  }
+  gi.survive = ok;
+  groups[g] = gi;
+  if (ok) {
+    dp_list[atomicAdd(&counts[1], 1u)] = static_cast<uint32_t>(g);
+    if (gi.ext_sorted) ext_list[atomicAdd(&counts[0], 1u)] = static_cast<uint32_t>(g);
+  }
+}
+
+__global__ void prepare_ext_sort_kernel(uint64_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                                        const GroupInfo* __restrict__ groups,
+                                        const uint32_t* __restrict__ ext_list,
+                                        const uint32_t* __restrict__ counts,
+                                        uint64_t* __restrict__ sb, uint64_t* __restrict__ se) {
+  const uint32_t cnt = counts[0];
+  const int lane = threadIdx.x & 31;
+  const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t li = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; li < cnt; li += nwarps) {
+    const GroupInfo g = groups[ext_list[li]];
+    for (uint32_t j = lane; j < g.n; j += 32) {
+      const uint64_t i = g.start + j;
+      const uint64_t k = keys[i];
+      keys[i] = static_cast<uint64_t>(vals[i]);
+      vals[i] = static_cast<uint32_t>(k & 0xffffffffu);
+    }
+    if (lane == 0) {
+      sb[li] = g.start;
+      se[li] = g.start + g.n;
+    }
+  }
+}
+
+__global__ void split_kernel(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ vals,
+                             const GroupInfo* __restrict__ groups,
+                             const uint32_t* __restrict__ dp_list,
+                             const uint32_t* __restrict__ counts, int32_t* __restrict__ cur,
+                             int32_t* __restrict__ ext) {
+  const uint32_t cnt = counts[1];
+  const int lane = threadIdx.x & 31;
+  const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t li = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; li < cnt; li += nwarps) {
+    const GroupInfo g = groups[dp_list[li]];
+    for (uint32_t j = lane; j < g.n; j += 32) {
+      const uint64_t i = g.start + j;
+      if (g.ext_sorted) {
+        cur[i] = static_cast<int32_t>(vals[i]);
+        ext[i] = static_cast<int32_t>(keys[i] & 0xffffffffu);
+      } else {
+        cur[i] = static_cast<int32_t>(keys[i] & 0xffffffffu);
+        ext[i] = static_cast<int32_t>(vals[i]);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------- DP
+//
+// Flye's DP visits predecessors j = i-1, i-2, ... and keeps the first j (in
+// visit order) that strictly beats the running maximum, which starts at 0; it
+// stops right after an update with jumpDiv == 0 && curDelta < k, and right
+// after the first j whose sort-axis delta exceeds maxJump.  A warp evaluates
+// 32 predecessors at once (lane L <-> j = i-1-32c-L): an inclusive prefix
+// max over lanes gives each lane the running maximum before it, a ballot
+// finds the first lane that ends the scan, and the winner is the first lane
+// at or before it that attains the maximum (later equal scores do not update).
+// The 32 most recent elements live in a per-warp ring in shared memory; a
+// one-step fast path handles the common case where j = i-1 itself updates
+// and breaks.
+
+constexpr int kDpWarps = 8;
+
+struct DpRing {
+  int32_t c[32], e[32], s[32];
+};
+
+__device__ __forceinline__ void eval_chunk(bool valid, int32_t cj, int32_t ej, int32_t sj,
+                                           int32_t j, int32_t ci, int32_t ei, bool es,
+                                           const ChainParams& p, int32_t& best, int32_t& bestj,
+                                           bool& done) {
+  const int lane = threadIdx.x & 31;
+  const int32_t cd = ci - cj, ed = ei - ej;
+  const int32_t jd = abs(cd - ed);
+  const bool acc = valid && cd > 0 && cd < p.max_jump && ed > 0 && ed < p.max_jump &&
+                   jd <= p.max_gap;
+  int32_t sc = INT_MIN;
+  if (acc) {
+    const int32_t ms = min(min(cd, ed), p.k);
+    const float pen = jd > p.gap_jump_threshold ? p.large_gap_penalty : p.small_gap_penalty;
+    const int32_t gc = __float2int_rz(__fmul_rn(pen, static_cast<float>(jd)));
+    sc = sj + ms - gc;
+  }
+  const bool stop = !valid || (es ? ed > p.max_jump : cd > p.max_jump);
+  int32_t incl = sc;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int32_t o = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl = max(incl, o);
+  }
+  int32_t excl = __shfl_up_sync(0xffffffffu, incl, 1);
+  if (lane == 0) excl = INT_MIN;
+  const bool upd = acc && sc > max(best, excl);
+  const bool brk = (upd && jd == 0 && cd < p.k) || stop;
+  const unsigned bm = __ballot_sync(0xffffffffu, brk);
+  const int bl = bm ? __ffs(bm) - 1 : 31;
+  const int32_t nb = max(best, __shfl_sync(0xffffffffu, incl, bl));
+  if (nb > best) {
+    const unsigned um = __ballot_sync(0xffffffffu, upd && lane <= bl && sc == nb);
+    bestj = __shfl_sync(0xffffffffu, j, __ffs(um) - 1);
+    best = nb;
+  }
+  done = bm != 0;
+}
+
+__global__ void __launch_bounds__(kDpWarps * 32) dp_kernel(
+    const int32_t* __restrict__ cur, const int32_t* __restrict__ ext, int32_t* score,
+    int32_t* bt, const GroupInfo* __restrict__ groups, const uint32_t* __restrict__ list,
+    const uint32_t* __restrict__ counts, ChainParams p) {
+  __shared__ DpRing rings[kDpWarps];
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  DpRing& ring = rings[wib];
+  const uint32_t cnt = counts[1];
+  const uint32_t nwarps = gridDim.x * kDpWarps;
+  for (uint32_t li = blockIdx.x * kDpWarps + wib; li < cnt; li += nwarps) {
+    const GroupInfo g = groups[list[li]];
+    const uint64_t b = g.start;
+    const uint32_t n = g.n;
+    const bool es = g.ext_sorted != 0;
+    // prefetched block of 32 consecutive elements: lane L holds element i0 + L
+    uint32_t i0 = 0;
+    int32_t bc = 0, be = 0;
+    if (lane < static_cast<int>(n)) {
+      bc = __ldg(cur + b + lane);
+      be = __ldg(ext + b + lane);
+    }
+    int32_t pc = __shfl_sync(0xffffffffu, bc, 0), pe = __shfl_sync(0xffffffffu, be, 0);
+    int32_t pscore = 0;
+    if (lane == 0) {
+      ring.c[0] = pc;
+      ring.e[0] = pe;
+      ring.s[0] = 0;
+      score[b] = 0;
+      bt[b] = -1;
+    }
+    __syncwarp();
+    for (uint32_t i = 1; i < n; ++i) {
+      if (i - i0 == 32) {
+        i0 = i;
+        if (i0 + lane < n) {
+          bc = __ldg(cur + b + i0 + lane);
+          be = __ldg(ext + b + i0 + lane);
+        }
+      }
+      const int32_t ci = __shfl_sync(0xffffffffu, bc, i - i0);
+      const int32_t ei = __shfl_sync(0xffffffffu, be, i - i0);
+      int32_t best = 0, bestj = 0;
+      // fast path: j = i - 1 updates and breaks
+      {
+        const int32_t cd = ci - pc, ed = ei - pe;
+        const int32_t jd = abs(cd - ed);
+        bool fast = false;
+        if (cd > 0 && cd < p.max_jump && ed > 0 && ed < p.max_jump && jd == 0 && cd < p.k) {
+          const int32_t sc = pscore + min(min(cd, ed), p.k);
+          if (sc > 0) {
+            best = sc;
+            bestj = static_cast<int32_t>(i) - 1;
+            fast = true;
+          }
+        }
+        if (!fast) {
+          bool done = false;
+          // chunk 0 from the ring
+          {
+            const int32_t j = static_cast<int32_t>(i) - 1 - lane;
+            const bool valid = j >= 0;
+            int32_t cj = 0, ej = 0, sj = 0;
+            if (valid) {
+              const int r = j & 31;
+              cj = ring.c[r];
+              ej = ring.e[r];
+              sj = ring.s[r];
+            }
+            eval_chunk(valid, cj, ej, sj, j, ci, ei, es, p, best, bestj, done);
+          }
+          for (int32_t c0 = static_cast<int32_t>(i) - 33; !done && c0 >= 0; c0 -= 32) {
+            const int32_t j = c0 - lane;
+            const bool valid = j >= 0;
+            int32_t cj = 0, ej = 0, sj = 0;
+            if (valid) {
+              cj = __ldg(cur + b + j);
+              ej = __ldg(ext + b + j);
+              sj = __ldcg(score + b + j);
+            }
+            eval_chunk(valid, cj, ej, sj, j, ci, ei, es, p, best, bestj, done);
+          }
+        }
+      }
+      const int32_t si = max(best, p.k);
+      if (lane == 0) {
+        const int r = i & 31;
+        ring.c[r] = ci;
+        ring.e[r] = ei;
+        ring.s[r] = si;
+        score[b + i] = si;
+        bt[b + i] = best > p.k ? bestj : -1;
+      }
+      __syncwarp();
+      pc = ci;
+      pe = ei;
+      pscore = si;
+    }
+    __syncwarp();
+  }
+}
+
+__global__ void prepare_order_kernel(const int32_t* __restrict__ score, uint64_t* __restrict__ keys,
+                                     uint32_t* __restrict__ vals,
+                                     const GroupInfo* __restrict__ groups,
+                                     const uint32_t* __restrict__ dp_list,
+                                     const uint32_t* __restrict__ counts,
+                                     uint64_t* __restrict__ sb, uint64_t* __restrict__ se) {
+  const uint32_t cnt = counts[1];
+  const int lane = threadIdx.x & 31;
+  const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t li = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; li < cnt; li += nwarps) {
+    const GroupInfo g = groups[dp_list[li]];
+    for (uint32_t j = lane; j < g.n; j += 32) {
+      const uint64_t i = g.start + j;
+      keys[i] = static_cast<uint64_t>(static_cast<uint32_t>(INT_MAX - score[i]));
+      vals[i] = j;
+    }
+    if (lane == 0) {
+      sb[li] = g.start;
+      se[li] = g.start + g.n;
+    }
+  }
+}
+
+// ---------------------------------------------------------------- backtrack
+
+constexpr int kMaxProposals = 64;
+
+struct Prop {
+  int32_t cb, ce, eb, ee, score, clen;
+  float div;
+};
+
+__device__ __forceinline__ bool overlap_test(const Prop& o, int64_t cur_id, int64_t ext_id,
+                                             int32_t cur_len, int32_t ext_len,
+                                             const ChainParams& p) {
+  const int32_t cr = o.ce - o.cb, er = o.ee - o.eb;
+  if (cr < p.min_overlap || er < p.min_overlap) return false;
+  const int32_t diff = abs(cr - er);
+  if (static_cast<float>(diff) > fmul(0.5f, static_cast<float>(min(cr, er)))) return false;
+  if (cur_id == ext_id) {
+    const int32_t inter = min(o.ce, o.ee) - max(o.cb, o.eb);
+    if (static_cast<float>(inter) > fdiv(static_cast<float>(cr), 2.0f)) return false;
+  }
+  if (cur_id == -ext_id) {
+    const int32_t inter = min(o.ce, ext_len - o.eb) - max(o.cb, ext_len - o.ee);
+    if (static_cast<float>(inter) > fdiv(static_cast<float>(cr), 2.0f)) return false;
+  }
+  if (!p.force_local && p.check_overhang) {
+    const int32_t lr = max(min(o.cb, o.eb), min(cur_len - o.ce, ext_len - o.ee));
+    if (lr > p.max_overhang) return false;
+  }
+  return true;
+}
+
+__device__ __forceinline__ uint32_t lower_bound_i32(const int32_t* a, uint32_t n, int32_t x) {
+  uint32_t lo = 0, hi = n;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (a[mid] < x)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+__global__ void backtrack_kernel(const int32_t* __restrict__ cur, const int32_t* __restrict__ ext,
+                                 const int32_t* __restrict__ score, int32_t* __restrict__ bt,
+                                 const uint32_t* __restrict__ order,
+                                 const GroupInfo* __restrict__ groups,
+                                 const uint32_t* __restrict__ dp_list,
+                                 const uint32_t* __restrict__ counts,
+                                 const QueryInfo* __restrict__ qinfo,
+                                 const uint64_t* __restrict__ f_off,
+                                 const int32_t* __restrict__ fpos,
+                                 const int64_t* __restrict__ slot_signed, LogfTable logt,
+                                 ChainParams p, OverlapRow* __restrict__ pool, uint64_t pool_cap,
+                                 uint32_t* __restrict__ pool_count,
+                                 uint32_t* __restrict__ group_rows, DeviceStatus* st) {
+  const uint32_t li = blockIdx.x * blockDim.x + threadIdx.x;
+  if (li >= counts[1]) return;
+  const uint32_t gidx = dp_list[li];
+  const GroupInfo g = groups[gidx];
+  const uint64_t b = g.start;
+  const int32_t k = p.k;
+  const QueryInfo qi = qinfo[g.query];
+  const int64_t ext_signed = (g.ext_di & 1u) ? -slot_signed[g.ext_di >> 1]
+                                             : slot_signed[g.ext_di >> 1];
+  const int32_t* fq = fpos + f_off[g.query];
+  const uint32_t nf = static_cast<uint32_t>(f_off[g.query + 1] - f_off[g.query]);
+  Prop props[kMaxProposals];
+  int np = 0;
+  for (uint32_t oi = 0; oi < g.n; ++oi) {
+    const uint32_t start = order[b + oi];
+    if (bt[b + start] == -1) continue;
+    int32_t pos = static_cast<int32_t>(start), first = 0, clen = 0;
+    while (pos != -1) {
+      first = pos;
+      ++clen;
+      const int32_t nx = bt[b + pos];
+      bt[b + pos] = -1;
+      pos = nx;
+    }
+    Prop o;
+    o.cb = cur[b + first];
+    o.ce = cur[b + start] + k - 1;
+    o.eb = ext[b + first];
+    o.ee = ext[b + start] + k - 1;
+    o.score = score[b + start] - score[b + first] + k - 1;
+    o.clen = clen;
+    if (!overlap_test(o, qi.signed_id, ext_signed, qi.len, g.ext_len, p)) continue;
+    const uint32_t lo = lower_bound_i32(fq, nf, o.cb);
+    const uint32_t hi = lower_bound_i32(fq, nf, o.ce + 1);
+    const int32_t norm = max(o.ce - o.cb, o.ee - o.eb) - static_cast<int32_t>(hi - lo);
+    if (norm <= 0) continue;
+    float rate = fdiv(fmul(static_cast<float>(clen), p.sample_rate), static_cast<float>(norm));
+    rate = rate < 1.0f ? rate : 1.0f;
+    const float x = fdiv(1.0f, rate);
+    if (!(x < 16777216.0f)) raise_status(st, kDevLogDomain, 0, static_cast<int64_t>(gidx));
+    o.div = fdiv(flye_logf(x, logt), static_cast<float>(k));
+    if (np == kMaxProposals) {
+      raise_status(st, kDevProposalOverflow, 0, static_cast<int64_t>(gidx));
+      group_rows[gidx] = 0;
+      return;
+    }
+    props[np++] = o;
+  }
+  // proposals by score descending, libstdc++ order
+  uint64_t K[kMaxProposals];
+  uint32_t V[kMaxProposals];
+  for (int i = 0; i < np; ++i) {
+    K[i] = static_cast<uint64_t>(static_cast<uint32_t>(INT_MAX - props[i].score));
+    V[i] = static_cast<uint32_t>(i);
+  }
+  isort::serial_introsort(K, V, 0, static_cast<uint32_t>(np),
+                          isort::depth_limit(static_cast<uint32_t>(np)));
+  int prim[kMaxProposals];
+  int nprim = 0;
+  if (p.only_max_ext) {
+    if (np > 0) prim[nprim++] = static_cast<int>(V[0]);
+  } else {
+    for (int s = 0; s < np; ++s) {
+      const Prop& o = props[V[s]];
+      bool contained = false;
+      for (int t = 0; t < nprim && !contained; ++t) {
+        const Prop& pr = props[prim[t]];
+        contained = pr.cb <= o.cb && o.ce <= pr.ce && pr.eb <= o.eb && o.ee <= pr.ee &&
+                    pr.score > o.score;
+      }
+      if (!contained) prim[nprim++] = static_cast<int>(V[s]);
+    }
+  }
+  int keep[kMaxProposals];
+  int nk = 0;
+  for (int t = 0; t < nprim; ++t)
+    if (props[prim[t]].div < p.max_divergence) keep[nk++] = prim[t];
+  group_rows[gidx] = static_cast<uint32_t>(nk);
+  if (nk == 0) return;
+  const uint32_t base = atomicAdd(pool_count, static_cast<uint32_t>(nk));
+  if (base + nk > pool_cap) {
+    raise_status(st, kDevProposalOverflow, 1, static_cast<int64_t>(gidx));
+    return;
+  }
+  for (int t = 0; t < nk; ++t) {
+    const Prop& o = props[keep[t]];
+    OverlapRow r;
+    r.query = g.query;
+    r.ext_di = g.ext_di;
+    r.cur_begin = o.cb;
+    r.cur_end = o.ce;
+    r.cur_len = qi.len;
+    r.ext_begin = o.eb;
+    r.ext_end = o.ee;
+    r.ext_len = g.ext_len;
+    r.score = o.score;
+    r.chain_len = o.clen;
+    r.div = o.div;
+    r.group = gidx;
+    r.rank = static_cast<uint32_t>(t);
+    pool[base + t] = r;
+  }
+}
+
+__global__ void query_group_off_kernel(const GroupInfo* __restrict__ groups, uint64_t ngroups,
+                                       uint32_t nq, uint64_t* __restrict__ qg) {
+  const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q > nq) return;
+  uint64_t lo = 0, hi = ngroups;
+  while (lo < hi) {
+    const uint64_t mid = (lo + hi) >> 1;
+    if (groups[mid].query < q)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  qg[q] = lo;
+}
+
+__global__ void rows_limit_kernel(const uint32_t* __restrict__ group_rows,
+                                  const uint64_t* __restrict__ q_group_off, uint32_t nq,
+                                  int32_t max_overlaps, uint32_t* __restrict__ kept) {
+  const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq) return;
+  uint64_t detected = 0;
+  for (uint64_t g = q_group_off[q]; g < q_group_off[q + 1]; ++g) {
+    if (max_overlaps > 0 && detected >= static_cast<uint64_t>(max_overlaps)) {
+      kept[g] = 0;
+      continue;
+    }
+    kept[g] = group_rows[g];
+    detected += group_rows[g];
+  }
+}
+
+__global__ void rows_scatter_kernel(const OverlapRow* __restrict__ pool, uint32_t npool,
+                                    const uint32_t* __restrict__ kept,
+                                    const uint64_t* __restrict__ kept_off,
+                                    OverlapRow* __restrict__ rows) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npool) return;
+  const OverlapRow r = pool[i];
+  if (r.rank < kept[r.group]) rows[kept_off[r.group] + r.rank] = r;
+}
+
+}  // namespace
+
+cudaError_t groups_mark(const uint64_t* keys, const uint64_t* q_off, uint32_t nq, uint64_t nhits,
+                        uint32_t* flags, cudaStream_t s) {
+  if (nhits == 0) return cudaSuccess;
+  mark_ext_changes<<<grid(nhits, 256), 256, 0, s>>>(keys, nhits, flags);
+  mark_query_starts<<<grid(nq, 256), 256, 0, s>>>(q_off, nq, flags);
+  return cudaGetLastError();
+}
+
+cudaError_t groups_build(const uint64_t* keys, const uint32_t* flags, const uint64_t* gid,
+                         const uint64_t* q_off, uint32_t nq, uint64_t nhits, uint64_t ngroups,
+                         GroupInfo* groups, cudaStream_t s) {
+  if (nhits == 0) return cudaSuccess;
+  (void)ngroups;
+  build_groups<<<grid(nhits, 256), 256, 0, s>>>(keys, flags, gid, q_off, nq, nhits, groups);
+  return cudaGetLastError();
+}
+
+cudaError_t groups_prefilter_n(const uint64_t* keys, const uint32_t* vals, GroupInfo* groups,
+                               uint64_t ngroups, uint64_t nhits, const QueryInfo* qinfo,
+                               const int32_t* slot_len, const ChainParams& p,
+                               uint32_t* ext_list, uint32_t* dp_list, uint32_t* counts,
+                               cudaStream_t s) {
+  cudaMemsetAsync(counts, 0, 2 * sizeof(uint32_t), s);
+  if (ngroups == 0) return cudaGetLastError();
+  prefilter_kernel<<<grid(ngroups * 32, 256), 256, 0, s>>>(keys, vals, groups, ngroups, nhits,
+                                                           qinfo, slot_len, p, ext_list, dp_list,
+                                                           counts);
+  return cudaGetLastError();
+}
+
+cudaError_t groups_prepare_ext_sort(uint64_t* keys, uint32_t* vals, const GroupInfo* groups,
+                                    const uint32_t* ext_list, const uint32_t* counts,
+                                    uint64_t* seg_begin, uint64_t* seg_end, cudaStream_t s) {
+  prepare_ext_sort_kernel<<<2048, 256, 0, s>>>(keys, vals, groups, ext_list, counts, seg_begin,
+                                               seg_end);
+  return cudaGetLastError();
+}
+
+cudaError_t groups_split(const uint64_t* keys, const uint32_t* vals, const GroupInfo* groups,
+                         const uint32_t* dp_list, const uint32_t* counts, int32_t* cur,
+                         int32_t* ext, cudaStream_t s) {
+  split_kernel<<<2048, 256, 0, s>>>(keys, vals, groups, dp_list, counts, cur, ext);
+  return cudaGetLastError();
+}
+
+cudaError_t chain_dp(const int32_t* cur, const int32_t* ext, int32_t* score, int32_t* bt,
+                     const GroupInfo* groups, const uint32_t* dp_list, const uint32_t* counts,
+                     const ChainParams& p, int num_sms, cudaStream_t s) {
+  dp_kernel<<<num_sms * 8, kDpWarps * 32, 0, s>>>(cur, ext, score, bt, groups, dp_list, counts, p);
+  return cudaGetLastError();
+}
+
+cudaError_t chain_prepare_order(const int32_t* score, uint64_t* keys, uint32_t* vals,
+                                const GroupInfo* groups, const uint32_t* dp_list,
+                                const uint32_t* counts, uint64_t* seg_begin, uint64_t* seg_end,
+                                cudaStream_t s) {
+  prepare_order_kernel<<<2048, 256, 0, s>>>(score, keys, vals, groups, dp_list, counts, seg_begin,
+                                            seg_end);
+  return cudaGetLastError();
+}
+
+cudaError_t chain_backtrack(const int32_t* cur, const int32_t* ext, const int32_t* score,
+                            int32_t* bt, const uint32_t* order, const GroupInfo* groups,
+                            const uint32_t* dp_list, const uint32_t* counts,
+                            const QueryInfo* qinfo, const uint64_t* f_off, const int32_t* fpos,
+                            const int64_t* slot_signed, const LogfTable& logt,
+                            const ChainParams& p, OverlapRow* pool, uint64_t pool_cap,
+                            uint32_t* pool_count, uint32_t* group_rows, DeviceStatus* st,
+                            uint32_t max_groups, cudaStream_t s) {
+  if (max_groups == 0) return cudaSuccess;
+  backtrack_kernel<<<grid(max_groups, 128), 128, 0, s>>>(cur, ext, score, bt, order, groups,
+                                                         dp_list, counts, qinfo, f_off, fpos,
+                                                         slot_signed, logt, p, pool, pool_cap,
+                                                         pool_count, group_rows, st);
+  return cudaGetLastError();
+}
+
+cudaError_t query_group_offsets(const GroupInfo* groups, uint64_t ngroups, uint32_t nq,
+                                uint64_t* q_group_off, cudaStream_t s) {
+  query_group_off_kernel<<<grid(nq + 1, 256), 256, 0, s>>>(groups, ngroups, nq, q_group_off);
+  return cudaGetLastError();
+}
+
+cudaError_t rows_limit(const uint32_t* group_rows, const uint64_t* q_group_off, uint32_t nq,
+                       int32_t max_overlaps, uint32_t* kept_rows, cudaStream_t s) {
+  if (nq == 0) return cudaSuccess;
+  rows_limit_kernel<<<grid(nq, 128), 128, 0, s>>>(group_rows, q_group_off, nq, max_overlaps,
+                                                  kept_rows);
+  return cudaGetLastError();
+}
+
+cudaError_t rows_scatter(const OverlapRow* pool, uint32_t npool, const uint32_t* kept_rows,
+                         const uint64_t* kept_off, OverlapRow* rows, cudaStream_t s) {
+  if (npool == 0) return cudaSuccess;
+  rows_scatter_kernel<<<grid(npool, 256), 256, 0, s>>>(pool, npool, kept_rows, kept_off, rows);
+  return cudaGetLastError();
+}
+
+}  // namespace cuflye

@@ -1,0 +1,187 @@
+// hits.cu — candidate hit generation (the candidate loop of getSeqOverlaps).
+//
+// Per query window, in the order of
+// patches/flye/2.9.6/0002-cuflye-candidate-backend-seam.patch:55-89:
+//   repetitive k-mer  -> the window position becomes a filtered position;
+//   absent k-mer      -> nothing;
+//   otherwise every bucket entry, flipped to the other strand when the query
+//   k-mer is not in standard form, except the exact self hit.
+// hits_count() probes the table once per window and records the bucket and
+// the number of hits; an exclusive scan turns counts into offsets, and
+// hits_emit() writes each window's hits at its offset, so the output is in
+// Flye's generation order (window order, then bucket order) with no atomics.
+#include <cstdint>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace cuflye {
+namespace {
+
+constexpr uint8_t kFlagRev = 1;
+constexpr uint8_t kFlagFiltered = 2;
+constexpr uint8_t kFlagTrivial = 4;
+
+__device__ __forceinline__ uint32_t query_of(const uint64_t* __restrict__ win_off, uint32_t nq,
+                                             uint64_t w) {
+  uint32_t lo = 0, hi = nq - 1;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi + 1) >> 1;
+    if (__ldg(win_off + mid) <= w)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+struct WindowKmer {
+  uint64_t x;    // forward k-mer (Kmer::numRepr)
+  uint64_t key;  // standard form
+  bool rev;      // x is not in standard form
+};
+
+__device__ __forceinline__ WindowKmer window_kmer(const QueryBatch& q, uint32_t qi, uint64_t p,
+                                                  int k) {
+  WindowKmer w;
+  w.x = kmer_at(q.words, q.base_off[qi] + p, k);
+  const uint64_t rc = revcomp(w.x, k);
+  w.rev = rc < w.x;
+  w.key = w.rev ? rc : w.x;
+  return w;
+}
+
+__global__ void count_kernel(DeviceIndex idx, QueryBatch q, uint32_t* __restrict__ cnt,
+                             uint32_t* __restrict__ filt, uint64_t* __restrict__ wmeta,
+                             uint8_t* __restrict__ wflags) {
+  const uint64_t w = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (w >= q.nwin) return;
+  const uint32_t qi = query_of(q.win_off, q.nq, w);
+  const uint64_t p = w - q.win_off[qi];
+  const WindowKmer km = window_kmer(q, qi, p, idx.k);
+  bool found;
+  const uint64_t meta = table_probe(idx.table, idx.mask, km.key, &found);
+  uint32_t c = 0;
+  uint8_t fl = km.rev ? kFlagRev : 0;
+  if (found && (meta & kRepetitiveBit)) {
+    fl |= kFlagFiltered;
+  } else if (found) {
+    c = static_cast<uint32_t>((meta >> 40) & ((1ULL << kCountBits) - 1));
+    const int32_t qdi = q.qdi[qi];
+    if (c > 0 && qdi >= 0) {
+      // Is the query's own window among the bucket entries?  Stored form of
+      // the self hit: (qdi, p), or flipped when the lookup flips.
+      uint64_t want;
+      if (idx.transform && km.rev) {
+        const uint32_t sid = static_cast<uint32_t>(qdi) ^ 1u;
+        const int32_t slen = idx.slot_len[sid >> 1];
+        const int64_t sp = static_cast<int64_t>(slen) - static_cast<int64_t>(p) - idx.k;
+        want = sp >= 0 ? ((static_cast<uint64_t>(sid) << 32) | static_cast<uint32_t>(sp)) : ~0ULL;
+      } else {
+        want = (static_cast<uint64_t>(qdi) << 32) | static_cast<uint32_t>(p);
+      }
+      const uint64_t off = meta & kOffsetMask;
+      uint32_t self_hits = 0;
+      if (idx.transform) {
+        // built buckets are sorted by (stored id, stored position), entries unique
+        uint32_t lo = 0, hi = c;
+        while (lo < hi) {
+          const uint32_t mid = (lo + hi) >> 1;
+          if (__ldg(idx.pos + off + mid) < want)
+            lo = mid + 1;
+          else
+            hi = mid;
+        }
+        self_hits = (lo < c && __ldg(idx.pos + off + lo) == want) ? 1u : 0u;
+      } else {
+        // explicit entries keep input order and may repeat
+        for (uint32_t e = 0; e < c; ++e) self_hits += __ldg(idx.pos + off + e) == want;
+      }
+      if (self_hits) {
+        c -= self_hits;
+        fl |= kFlagTrivial;
+      }
+    }
+  }
+  cnt[w] = c;
+  filt[w] = (fl & kFlagFiltered) ? 1u : 0u;
+  wmeta[w] = meta;
+  wflags[w] = fl;
+}
+
+__global__ void emit_kernel(DeviceIndex idx, QueryBatch q, const uint64_t* __restrict__ hit_off,
+                            const uint64_t* __restrict__ filt_off,
+                            const uint64_t* __restrict__ wmeta,
+                            const uint8_t* __restrict__ wflags, uint64_t* __restrict__ keys,
+                            uint32_t* __restrict__ vals, uint64_t* __restrict__ kmers,
+                            int32_t* __restrict__ fpos) {
+  const uint64_t w = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (w >= q.nwin) return;
+  const uint8_t fl = wflags[w];
+  const uint32_t qi = query_of(q.win_off, q.nq, w);
+  const uint64_t p = w - q.win_off[qi];
+  if (fl & kFlagFiltered) {
+    fpos[filt_off[w]] = static_cast<int32_t>(p);
+    return;
+  }
+  uint64_t o = hit_off[w];
+  const uint64_t end = hit_off[w + 1];
+  if (o == end) return;
+  const uint64_t meta = wmeta[w];
+  const uint64_t off = meta & kOffsetMask;
+  const uint32_t c = static_cast<uint32_t>((meta >> 40) & ((1ULL << kCountBits) - 1));
+  const bool flip = idx.transform && (fl & kFlagRev);
+  const int32_t qdi = q.qdi[qi];
+  uint64_t x = 0;
+  if (kmers) x = kmer_at(q.words, q.base_off[qi] + p, idx.k);
+  for (uint32_t e = 0; e < c; ++e) {
+    const uint64_t sv = __ldg(idx.pos + off + e);
+    uint32_t id = static_cast<uint32_t>(sv >> 32);
+    int32_t pos = static_cast<int32_t>(sv & 0xffffffffu);
+    if (flip) {
+      pos = idx.slot_len[id >> 1] - pos - idx.k;
+      id ^= 1u;
+    }
+    if (static_cast<int32_t>(id) == qdi && pos == static_cast<int32_t>(p)) continue;
+    keys[o] = (static_cast<uint64_t>(id) << 32) | static_cast<uint32_t>(p);
+    vals[o] = static_cast<uint32_t>(pos);
+    if (kmers) kmers[o] = x;
+    ++o;
+  }
+}
+
+__global__ void gather_kernel(const uint64_t* __restrict__ win_off,
+                              const uint64_t* __restrict__ wl_off, uint32_t nq,
+                              uint64_t* __restrict__ q_off) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > nq) return;
+  q_off[i] = wl_off[win_off[i]];
+}
+
+}  // namespace
+
+cudaError_t hits_count(const DeviceIndex& idx, const QueryBatch& q, uint32_t* cnt,
+                       uint32_t* filt, uint64_t* wmeta, uint8_t* wflags, cudaStream_t s) {
+  if (q.nwin == 0) return cudaSuccess;
+  count_kernel<<<static_cast<unsigned>((q.nwin + 255) / 256), 256, 0, s>>>(idx, q, cnt, filt,
+                                                                          wmeta, wflags);
+  return cudaGetLastError();
+}
+
+cudaError_t hits_emit(const DeviceIndex& idx, const QueryBatch& q, const uint64_t* hit_off,
+                      const uint64_t* filt_off, const uint64_t* wmeta, const uint8_t* wflags,
+                      uint64_t* keys, uint32_t* vals, uint64_t* kmers, int32_t* fpos,
+                      cudaStream_t s) {
+  if (q.nwin == 0) return cudaSuccess;
+  emit_kernel<<<static_cast<unsigned>((q.nwin + 255) / 256), 256, 0, s>>>(
+      idx, q, hit_off, filt_off, wmeta, wflags, keys, vals, kmers, fpos);
+  return cudaGetLastError();
+}
+
+cudaError_t gather_query_offsets(const uint64_t* win_off, const uint64_t* wl_off, uint32_t nq,
+                                 uint64_t* q_off, cudaStream_t s) {
+  gather_kernel<<<(nq + 1 + 255) / 256, 256, 0, s>>>(win_off, wl_off, nq, q_off);
+  return cudaGetLastError();
+}
+
+}  // namespace cuflye

@@ -1,0 +1,175 @@
+// kernels.h — host-side launchers of the device stages (one stream each).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace cuflye {
+
+// ---------------------------------------------------------------- scan
+// Exclusive prefix sums (out may alias in).  temp needs scan_temp_words(n) words.
+size_t scan_temp_words(uint64_t n);
+cudaError_t exclusive_scan_u32_to_u64(const uint32_t* in, uint64_t* out, uint64_t n,
+                                      uint64_t* temp, cudaStream_t s);
+cudaError_t exclusive_scan_u64(const uint64_t* in, uint64_t* out, uint64_t n, uint64_t* temp,
+                               cudaStream_t s);
+
+// ---------------------------------------------------------------- sort
+size_t segsort_smem_bytes();
+// lists: 3 * nseg words; counts: 3 words.  l/r scratch: one word per element.
+// nseg_dev (optional) holds the live segment count on the device (<= nseg).
+cudaError_t segmented_std_sort(uint64_t* keys, uint32_t* vals, uint32_t* lscratch,
+                               uint32_t* rscratch, const uint64_t* begin, const uint64_t* end,
+                               uint32_t nseg, const uint32_t* nseg_dev, uint32_t* lists,
+                               uint32_t* counts, int num_sms, cudaStream_t stream);
+size_t radix_hist_words(uint64_t n);
+cudaError_t radix_sort_pairs(uint64_t* keys, uint64_t* vals, uint64_t* keys_alt,
+                             uint64_t* vals_alt, uint64_t n, const int* digits, int ndigits,
+                             uint32_t* hist, int* result_in_alt, cudaStream_t stream);
+
+// ---------------------------------------------------------------- sequences
+// ASCII bases -> MSB-first 2-bit words (32 bases per word, one padding word).
+cudaError_t pack_bases(const uint8_t* ascii, uint64_t nbases, uint64_t* words, cudaStream_t s);
+
+// ---------------------------------------------------------------- index
+struct DeviceIndex {
+  int k = 0;
+  bool transform = true;
+  TableEntry* table = nullptr;
+  uint64_t mask = 0;
+  uint64_t* pos = nullptr;       // (dense id << 32) | stored position, bucket order
+  uint64_t npos = 0;
+  int32_t* slot_len = nullptr;   // target length per dense slot
+  uint32_t nslots = 0;
+  uint64_t nkeys = 0, nrep = 0;
+};
+
+// Window enumeration over packed targets: keys = standard forms, vals =
+// (stored dense id << 32) | stored position.
+cudaError_t index_enumerate(const uint64_t* words, const uint64_t* base_off,
+                            const uint64_t* win_off, const int32_t* slot_len, uint32_t nslots,
+                            uint64_t nwin, int k, uint64_t* keys, uint64_t* vals,
+                            cudaStream_t s);
+// Run detection over sorted keys: flags[i] = key starts a run.
+cudaError_t index_mark_runs(const uint64_t* keys, uint64_t n, uint32_t* flags, cudaStream_t s);
+// Given run ids (exclusive scan of flags), write run starts (nruns + 1 entries).
+cudaError_t index_run_starts(const uint32_t* flags, const uint64_t* run_id, uint64_t n,
+                             uint64_t nruns, uint64_t* run_start, cudaStream_t s);
+// Per run: kept count (solid ? freq : 0) and class (0 none, 1 solid, 2 repetitive).
+cudaError_t index_classify_runs(const uint64_t* run_start, uint64_t nruns, uint32_t min_freq,
+                                uint32_t max_freq, uint32_t* kept, uint8_t* cls,
+                                cudaStream_t s);
+cudaError_t index_copy_positions(const uint64_t* vals, const uint64_t* run_id,
+                                 const uint64_t* run_start, const uint8_t* cls,
+                                 const uint64_t* kept_off, uint64_t n, uint64_t* pos,
+                                 cudaStream_t s);
+cudaError_t index_insert(const uint64_t* keys, const uint64_t* run_start, const uint8_t* cls,
+                         const uint64_t* kept_off, uint64_t nruns, TableEntry* table,
+                         uint64_t mask, DeviceStatus* st, cudaStream_t s);
+cudaError_t index_insert_repetitive(const uint64_t* rep_keys, uint64_t n, TableEntry* table,
+                                    uint64_t mask, DeviceStatus* st, cudaStream_t s);
+
+// ---------------------------------------------------------------- hits
+struct QueryBatch {
+  const uint64_t* words = nullptr;    // packed bases
+  const uint64_t* base_off = nullptr; // nq + 1
+  const uint64_t* win_off = nullptr;  // nq + 1
+  const int32_t* qdi = nullptr;       // dense internal id of the query in the index, or -1
+  uint32_t nq = 0;
+  uint64_t nwin = 0;
+};
+
+cudaError_t hits_count(const DeviceIndex& idx, const QueryBatch& q, uint32_t* cnt,
+                       uint32_t* filt, uint64_t* wmeta, uint8_t* wflags, cudaStream_t s);
+// keys[j] = (ext dense id << 32) | cur pos, vals[j] = ext pos, kmers (optional).
+cudaError_t hits_emit(const DeviceIndex& idx, const QueryBatch& q, const uint64_t* hit_off,
+                      const uint64_t* filt_off, const uint64_t* wmeta, const uint8_t* wflags,
+                      uint64_t* keys, uint32_t* vals, uint64_t* kmers, int32_t* fpos,
+                      cudaStream_t s);
+// Gather per-query segment bounds from window-level offsets.
+cudaError_t gather_query_offsets(const uint64_t* win_off, const uint64_t* wl_off, uint32_t nq,
+                                 uint64_t* q_off, cudaStream_t s);
+
+// ---------------------------------------------------------------- chaining
+struct ChainParams {
+  int32_t k, min_overlap, max_jump, max_gap, gap_jump_threshold, max_overhang;
+  int32_t check_overhang, force_local, only_max_ext, max_overlaps;
+  float large_gap_penalty, small_gap_penalty, min_kmer_survival_rate, max_divergence,
+      sample_rate;
+};
+
+struct GroupInfo {
+  uint64_t start;
+  uint32_t n;
+  uint32_t query;  // batch-local query index
+  uint32_t ext_di;
+  int32_t ext_len;
+  int32_t survive;
+  int32_t ext_sorted;
+};
+
+// Device-side overlap row before the final ABI conversion.
+struct OverlapRow {
+  uint32_t query;
+  uint32_t ext_di;
+  int32_t cur_begin, cur_end, cur_len;
+  int32_t ext_begin, ext_end, ext_len;
+  int32_t score;
+  int32_t chain_len;
+  float div;
+  uint32_t group;
+  uint32_t rank;
+};
+
+struct QueryInfo {
+  int64_t signed_id;
+  int32_t len;
+  int32_t pad;
+};
+
+cudaError_t groups_mark(const uint64_t* keys, const uint64_t* q_off, uint32_t nq, uint64_t nhits,
+                        uint32_t* flags, cudaStream_t s);
+cudaError_t groups_build(const uint64_t* keys, const uint32_t* flags, const uint64_t* gid,
+                         const uint64_t* q_off, uint32_t nq, uint64_t nhits, uint64_t ngroups,
+                         GroupInfo* groups, cudaStream_t s);
+cudaError_t groups_prefilter_n(const uint64_t* keys, const uint32_t* vals, GroupInfo* groups,
+                               uint64_t ngroups, uint64_t nhits, const QueryInfo* qinfo,
+                               const int32_t* slot_len, const ChainParams& p,
+                               uint32_t* ext_list, uint32_t* dp_list, uint32_t* counts,
+                               cudaStream_t s);
+// Rewrite ext-sorted groups as (key = ext, val = cur) for their re-sort.
+cudaError_t groups_prepare_ext_sort(uint64_t* keys, uint32_t* vals, const GroupInfo* groups,
+                                    const uint32_t* ext_list, const uint32_t* counts,
+                                    uint64_t* seg_begin, uint64_t* seg_end, cudaStream_t s);
+// Split (key, val) into CUR / EXT arrays for the DP.
+cudaError_t groups_split(const uint64_t* keys, const uint32_t* vals, const GroupInfo* groups,
+                         const uint32_t* dp_list, const uint32_t* counts, int32_t* cur,
+                         int32_t* ext, cudaStream_t s);
+cudaError_t chain_dp(const int32_t* cur, const int32_t* ext, int32_t* score, int32_t* bt,
+                     const GroupInfo* groups, const uint32_t* dp_list, const uint32_t* counts,
+                     const ChainParams& p, int num_sms, cudaStream_t s);
+// Score-order sort inputs: key = INT32_MAX - score, val = local index.
+cudaError_t chain_prepare_order(const int32_t* score, uint64_t* keys, uint32_t* vals,
+                                const GroupInfo* groups, const uint32_t* dp_list,
+                                const uint32_t* counts, uint64_t* seg_begin, uint64_t* seg_end,
+                                cudaStream_t s);
+cudaError_t chain_backtrack(const int32_t* cur, const int32_t* ext, const int32_t* score,
+                            int32_t* bt, const uint32_t* order, const GroupInfo* groups,
+                            const uint32_t* dp_list, const uint32_t* counts,
+                            const QueryInfo* qinfo, const uint64_t* f_off, const int32_t* fpos,
+                            const int64_t* slot_signed, const LogfTable& logt,
+                            const ChainParams& p, OverlapRow* pool, uint64_t pool_cap,
+                            uint32_t* pool_count, uint32_t* group_rows, DeviceStatus* st,
+                            uint32_t max_groups, cudaStream_t s);
+// max_overlaps cutoff and group-order compaction of the pooled rows.
+cudaError_t rows_limit(const uint32_t* group_rows, const uint64_t* q_group_off, uint32_t nq,
+                       int32_t max_overlaps, uint32_t* kept_rows, cudaStream_t s);
+cudaError_t rows_scatter(const OverlapRow* pool, uint32_t npool, const uint32_t* kept_rows,
+                         const uint64_t* kept_off, OverlapRow* rows, cudaStream_t s);
+cudaError_t query_group_offsets(const GroupInfo* groups, uint64_t ngroups, uint32_t nq,
+                                uint64_t* q_group_off, cudaStream_t s);
+
+}  // namespace cuflye

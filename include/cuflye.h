@@ -1,0 +1,244 @@
+/*
+ * cuflye.h — C ABI of the GB300 overlap hot-path library (libcuflye_gb300.so).
+ *
+ * Plain pointers and sizes only.  Every entry point returns a cuflye_status;
+ * on failure cuflye_last_error(ctx) holds a one-line message.  No call falls
+ * back to a CPU path: an unsupported case fails with CUFLYE_ERR_UNSUPPORTED,
+ * as the reference's CUDA stub does
+ * (patches/flye/2.9.6/0003-cuflye-cuda-backend-stub.patch:37-46).
+ *
+ * Sequences are passed the way Flye's FastaRecord carries them: a signed id
+ * (FastaRecord::Id::signedId(), +n forward / -n reverse complement) and ASCII
+ * bases (A/C/G/T, any case; any other byte encodes as A, as
+ * cuda/cuflye_cuda_read_window_smoke.cu:172-193 does).  Batches are
+ * concatenated bases plus n+1 offsets.
+ *
+ * Output buffers are caller-owned host memory with a capacity.  When a
+ * capacity is too small the call returns CUFLYE_ERR_CAPACITY and writes the
+ * required counts; repeat the call with larger buffers.  Device memory is
+ * owned by the context and is reused across calls (arena).
+ *
+ * Threading: a context serialises its own calls with an internal mutex.  Use
+ * one context per host thread for concurrency; contexts may share a device.
+ */
+#ifndef CUFLYE_H
+#define CUFLYE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum cuflye_status {
+  CUFLYE_OK = 0,
+  CUFLYE_ERR_INVALID = 1,     /* bad argument or malformed input            */
+  CUFLYE_ERR_UNSUPPORTED = 2, /* shape this backend does not handle: fail fast */
+  CUFLYE_ERR_BUDGET = 3,      /* device memory budget exceeded (never truncates) */
+  CUFLYE_ERR_CUDA = 4,        /* CUDA runtime error                          */
+  CUFLYE_ERR_CAPACITY = 5,    /* caller buffer too small; counts written     */
+  CUFLYE_ERR_TIMEOUT = 6,     /* a bounded device wait expired               */
+  CUFLYE_ERR_NO_INDEX = 7     /* call needs an index; none built             */
+} cuflye_status;
+
+typedef struct cuflye_ctx cuflye_ctx;
+
+/* --------------------------------------------------------------------------
+ * Backend seam.  Replaces candidateBackend() / cudaEnvOrDefault() in
+ * patches/flye/2.9.6/0002-cuflye-candidate-backend-seam.patch:29-43 and
+ * patches/flye/2.9.6/0003-cuflye-cuda-backend-stub.patch:37-46.
+ * Returns 0 for "cpu" (unset, empty or "cpu"), 1 for "cuda"; any other value
+ * of CUFLYE_CANDIDATE_BACKEND returns -1 and writes
+ * "Unsupported CUFLYE_CANDIDATE_BACKEND: <value>" into msg.
+ * ------------------------------------------------------------------------ */
+int cuflye_candidate_backend(char* msg, size_t msg_cap);
+
+/* Opens a context on `device` with a device-memory budget in bytes
+ * (0 = unbounded).  Replaces the CUFLYE_CUDA_DEVICE /
+ * CUFLYE_CUDA_MEMORY_BUDGET_BYTES handling of
+ * patches/flye/2.9.6/0003-cuflye-cuda-backend-stub.patch:37-44. */
+cuflye_status cuflye_open(int device, uint64_t memory_budget_bytes, cuflye_ctx** out);
+
+/* Same, reading CUFLYE_CUDA_DEVICE (default "0") and
+ * CUFLYE_CUDA_MEMORY_BUDGET_BYTES (default "unbounded") from the
+ * environment. */
+cuflye_status cuflye_open_from_env(cuflye_ctx** out);
+
+void cuflye_close(cuflye_ctx* ctx);
+const char* cuflye_last_error(const cuflye_ctx* ctx);
+
+/* Device memory the context holds now and at its peak, in bytes. */
+cuflye_status cuflye_memory_stats(const cuflye_ctx* ctx, uint64_t* in_use, uint64_t* peak);
+
+/* --------------------------------------------------------------------------
+ * Index (Flye VertexIndex equivalent, device resident).
+ * Builds an open-addressing table of standard-form k-mers over the forward
+ * strands of `n` target sequences (signed ids must be > 0 and distinct).
+ * freq(key) counts windows over all targets; keys with freq > max_freq are
+ * repetitive (query windows hitting them become filtered positions), keys
+ * with min_freq <= freq <= max_freq are solid and keep their positions.
+ * Serves isRepetitive / kmerFreq / iterKmerPos as called in
+ * patches/flye/2.9.6/0002-cuflye-candidate-backend-seam.patch:55-80.
+ * k in [1, 31].  Replaces any previous index in the context.
+ * ------------------------------------------------------------------------ */
+cuflye_status cuflye_index_build(cuflye_ctx* ctx, int k, size_t n, const int64_t* target_ids,
+                                 const int64_t* offsets, const char* bases, uint32_t min_freq,
+                                 uint32_t max_freq);
+
+/* Index from explicit, already strand-resolved entries (the flattened
+ * index.tsv of cuda/cuflye_cuda_read_window_smoke.cu and
+ * docs/abi/cuda-real-data-pack-dump-v0.md): entry i lists target signed id
+ * target_ids[i] at positions[i] under standard-form key keys[i]; buckets keep
+ * input order and lookups apply no strand transform.  rep_keys are the
+ * repetitive standard-form keys. */
+cuflye_status cuflye_index_from_entries(cuflye_ctx* ctx, int k, size_t n,
+                                        const int64_t* target_ids, const int64_t* positions,
+                                        const uint64_t* keys, size_t n_rep,
+                                        const uint64_t* rep_keys);
+
+/* Counts of the built index: distinct keys, stored positions, repetitive keys. */
+cuflye_status cuflye_index_stats(const cuflye_ctx* ctx, uint64_t* keys, uint64_t* positions,
+                                 uint64_t* repetitive);
+
+/* --------------------------------------------------------------------------
+ * Candidate records (candidate-record-v1, docs/abi/candidate-record-v1.md:31-51).
+ * Replaces collectCandidateMatchesCpu
+ * (patches/flye/2.9.6/0002-cuflye-candidate-backend-seam.patch:53-95) and the
+ * callee signature of patches/flye/2.9.6/0005-cuflye-real-data-pack-dump.patch:246-250:
+ * per query, the records are in Flye's generation order (window order, then
+ * bucket order); `filtered` receives the repetitive window positions
+ * (curFilteredPos).
+ * ------------------------------------------------------------------------ */
+typedef struct cuflye_candidate {
+  int64_t query_id;
+  int64_t target_id; /* signed; strand '+' iff > 0 */
+  uint64_t kmer;     /* forward query k-mer, Kmer::numRepr() */
+  int32_t query_pos;
+  int32_t target_pos;
+} cuflye_candidate;
+
+typedef struct cuflye_filtered_pos {
+  int64_t query_id;
+  int32_t pos;
+  int32_t reserved;
+} cuflye_filtered_pos;
+
+cuflye_status cuflye_candidates(cuflye_ctx* ctx, size_t n, const int64_t* query_ids,
+                                const int64_t* offsets, const char* bases,
+                                cuflye_candidate* out, size_t out_cap, size_t* n_out,
+                                cuflye_filtered_pos* filtered, size_t filtered_cap,
+                                size_t* n_filtered);
+
+/* --------------------------------------------------------------------------
+ * Overlaps (overlap-range-v1, docs/abi/overlap-range-v1.md:21-41).
+ * Replaces OverlapDetector::getSeqOverlaps after candidate collection:
+ * Flye's KmerMatch sort, group prefilter, ext re-sort, chaining DP,
+ * score-ordered backtrack, overlapTest, k-mer divergence, primary selection
+ * and max_overlaps (tools/replay_overlap_chains.py:196-422).  Rows come per
+ * query in Flye's emission order.
+ * ------------------------------------------------------------------------ */
+typedef struct cuflye_overlap_params {
+  int32_t kmer_size;          /* must equal the index k                      */
+  int32_t min_overlap;
+  int32_t max_jump;
+  int32_t max_gap;            /* max_jump_gap                                */
+  int32_t gap_jump_threshold;
+  int32_t max_overhang;
+  int32_t check_overhang;
+  int32_t force_local;
+  int32_t only_max_ext;
+  int32_t max_overlaps;       /* 0 = unlimited                               */
+  float large_gap_penalty;
+  float small_gap_penalty;
+  float min_kmer_survival_rate;
+  float max_divergence;
+  float sample_rate;
+} cuflye_overlap_params;
+
+typedef struct cuflye_overlap_range {
+  int64_t cur_id;
+  int64_t ext_id;
+  int32_t cur_begin, cur_end, cur_len;
+  int32_t ext_begin, ext_end, ext_len;
+  int32_t score;
+  float seq_divergence;
+} cuflye_overlap_range;
+
+cuflye_status cuflye_overlaps(cuflye_ctx* ctx, size_t n, const int64_t* query_ids,
+                              const int64_t* offsets, const char* bases,
+                              const cuflye_overlap_params* params, cuflye_overlap_range* out,
+                              size_t out_cap, size_t* n_out);
+
+/* Batch sizing: queries per device pass (0 = as many as the budget allows).
+ * 1 gives the plain one-read-per-launch path. */
+cuflye_status cuflye_set_batch_queries(cuflye_ctx* ctx, size_t queries_per_pass);
+
+/* --------------------------------------------------------------------------
+ * Read-to-graph chains (read-alignment-v1, docs/abi/read-alignment-v1.md:25-48).
+ * Replaces the per-read body of ReadAligner::alignReads
+ * (patches/flye/2.9.6/0039-cuflye-read-to-graph-input-boundary-oracle.patch:226-251,
+ * patches/flye/2.9.6/0026-cuflye-read-alignment-replay-fixture-dump.patch:215-235):
+ * quickSeqOverlaps against the edge index, the LONG_EDGE/BIG_ALN input
+ * filter, the curBegin sort, chainReadAlignments, the chain divergence
+ * filter, then good chains followed by their complements.  The index must be
+ * built from the edge sequences (ids = edge-sequence ids).  Edge e (> 0) owns
+ * edge sequence seq_ids[e] and runs left[e] -> right[e]; its complement -e
+ * runs right^1 -> left^1.
+ * ------------------------------------------------------------------------ */
+typedef struct cuflye_r2g_params {
+  int32_t max_jump;
+  int32_t max_read_overlap;
+  int32_t min_overlap;
+  int32_t max_separation;
+  int32_t long_edge;
+  int32_t big_aln;
+  float max_chain_divergence; /* read_align_ovlp_divergence */
+} cuflye_r2g_params;
+
+typedef struct cuflye_read_alignment {
+  int64_t chain_id;
+  int64_t segment_id;
+  int64_t read_id;
+  int64_t edge_id;
+  int64_t edge_seq_id;
+  int32_t read_begin, read_end, read_len;
+  int32_t edge_begin, edge_end, edge_len;
+  int32_t score;
+  float seq_divergence;
+} cuflye_read_alignment;
+
+cuflye_status cuflye_graph_set(cuflye_ctx* ctx, size_t n_edges, const int64_t* edge_ids,
+                               const int64_t* seq_ids, const int32_t* left,
+                               const int32_t* right);
+
+cuflye_status cuflye_read_to_graph(cuflye_ctx* ctx, size_t n, const int64_t* read_ids,
+                                   const int64_t* offsets, const char* bases,
+                                   const cuflye_overlap_params* params,
+                                   const cuflye_r2g_params* r2g, cuflye_read_alignment* out,
+                                   size_t out_cap, size_t* n_out);
+
+/* --------------------------------------------------------------------------
+ * The device sort every Flye sort point above runs on: sorts each segment
+ * [seg_offsets[s], seg_offsets[s+1]) of (key, value) pairs in place, leaving
+ * equal keys in exactly the order libstdc++'s std::sort(first, last,
+ * [](a, b) { return a.key < b.key; }) leaves them (introsort; see
+ * tools/replay_read_to_graph_source_pack.py:95-181 for the reference's
+ * restatement of that order).  Host arrays in, host arrays out.
+ * ------------------------------------------------------------------------ */
+cuflye_status cuflye_std_sort_segments(cuflye_ctx* ctx, uint64_t* keys, uint32_t* values,
+                                       const uint64_t* seg_offsets, size_t n_segments);
+
+/* --------------------------------------------------------------------------
+ * Timing of the last call's device work (CUDA events on the context's
+ * stream), in milliseconds, by stage: 0 hits, 1 match sort, 2 chaining,
+ * 3 output, 4 read-to-graph chains.  Bytes are the stage's algorithmic bytes.
+ * ------------------------------------------------------------------------ */
+cuflye_status cuflye_last_timing(const cuflye_ctx* ctx, double* stage_ms, uint64_t* stage_bytes,
+                                 size_t n_stages);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CUFLYE_H */

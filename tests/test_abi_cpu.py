@@ -1,0 +1,99 @@
+"""CPU: the C-ABI library builds, loads and exports every symbol that
+include/cuflye.h declares; the backend seam parses its environment like the
+reference; host-side record formatting follows the ABI text rules.  No call
+here touches a GPU."""
+
+import os
+import re
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import REPO
+
+
+def declared_symbols():
+    text = (REPO / "include" / "cuflye.h").read_text()
+    return sorted(set(re.findall(r"\b(cuflye_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    out = subprocess.run(["nm", "-D", "--defined-only", str(built_lib)], capture_output=True,
+                         text=True, check=True).stdout
+    exported = set(re.findall(r" T (cuflye_[a-z_0-9]+)$", out, re.M))
+    missing = [s for s in declared_symbols() if s not in exported]
+    assert not missing, missing
+    import ctypes
+    lib = ctypes.CDLL(str(built_lib))
+    for s in declared_symbols():
+        assert hasattr(lib, s)
+
+
+def _backend_in_subprocess(value):
+    env = dict(os.environ)
+    if value is None:
+        env.pop("CUFLYE_CANDIDATE_BACKEND", None)
+    else:
+        env["CUFLYE_CANDIDATE_BACKEND"] = value
+    code = ("import sys; sys.path.insert(0, %r)\n"
+            "from cuflye_gb300 import backend\n"
+            "try:\n print('OK', backend.candidate_backend())\n"
+            "except RuntimeError as e:\n print('ERR', e)\n") % str(REPO)
+    return subprocess.run([sys.executable, "-c", code], env=env, capture_output=True,
+                          text=True, check=True).stdout.strip()
+
+
+@pytest.mark.parametrize("value,expect", [(None, "OK cpu"), ("", "OK cpu"), ("cpu", "OK cpu"),
+                                          ("cuda", "OK cuda"),
+                                          ("opencl", "ERR Unsupported CUFLYE_CANDIDATE_BACKEND: opencl")])
+def test_backend_selection_matches_reference_seam(built_lib, value, expect):
+    """patches/flye/2.9.6/0002-cuflye-candidate-backend-seam.patch:29-43."""
+    assert _backend_in_subprocess(value) == expect
+
+
+def test_record_layouts_match_header():
+    from cuflye_gb300 import abi
+    assert abi.CANDIDATE_DTYPE.itemsize == 32
+    assert abi.OVERLAP_DTYPE.itemsize == 48
+    assert abi.READ_ALIGNMENT_DTYPE.itemsize == 72
+
+
+def test_float_text_follows_setprecision9():
+    """C++ setprecision(9) of a float: 0.01f prints 0.00999999978
+    (the reference's own TSV, tests/fixtures/read-alignment-replay-fixture-v0)."""
+    from cuflye_gb300.abi import format_float
+    assert format_float(0.01) == "0.00999999978"
+    assert format_float(0.0) == "0"
+    assert format_float(0.02) == "0.0199999996"
+
+
+def test_canonical_sha_is_order_free():
+    from cuflye_gb300.abi import canonical_sha256
+    a = ["1\t2\t3\n", "-1\t5\t6\n", "1\t10\t3\n"]
+    assert canonical_sha256(a) == canonical_sha256(list(reversed(a)))
+
+
+def test_logf_table_matches_c_library(built_lib, oracle_mod):
+    """The exception table makes logf_wide + table == this machine's logf on a
+    sample of floats in [1, 2^24) (the device applies the same table)."""
+    import struct
+    from pathlib import Path
+    tbl = Path(built_lib).parent / "logf_exceptions.bin"
+    data = tbl.read_bytes()
+    n = struct.unpack("<I", data[:4])[0]
+    pairs = np.frombuffer(data[4:], dtype=np.uint32).reshape(n, 2)
+    assert np.all(np.diff(pairs[:, 0].astype(np.int64)) > 0)
+    rng = np.random.default_rng(0)
+    xs = pairs[rng.integers(0, n, size=200), 0].view(np.float32)
+    for x, y in zip(xs, pairs[np.searchsorted(pairs[:, 0], xs.view(np.uint32)), 1].view(np.float32)):
+        assert oracle_mod.logf(float(x)) == float(y)
+
+
+def test_synthetic_generator_is_seeded():
+    from cuflye_gb300 import synth
+    a = synth.small_overlap_case(3, 20_000, 3.0, 3_000)
+    b = synth.small_overlap_case(3, 20_000, 3.0, 3_000)
+    assert np.array_equal(a.reads.bases, b.reads.bases)
+    assert np.array_equal(a.reads.offsets, b.reads.offsets)
