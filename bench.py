@@ -1,0 +1,356 @@
+#!/usr/bin/env python3
+"""Benchmark of the overlap hot path: overlapped read-bases/sec on one GB300.
+
+Workload (per GPU): a seeded 5 Mb genome carrying 30 copies of a 5 kb repeat
+at 1 % divergence and 2 % (AT)n tracts of 200-2,000 bp; HiFi-like reads at
+40x, lognormal(15 kb, 3 kb), 0.2 % substitution+indel error; k = 17; solid
+k-mers seen >= 2 times, repetitive above 5 x coverage.  Synthetic data: no
+dataset exists here, so the generator reproduces the named shapes.
+
+A step is one pass of the overlap stage (candidate hits -> Flye's KmerMatch
+sort -> chaining DP -> backtrack -> overlap rows) over every read of the
+workload against the device-resident index, batched: all reads in one pass.
+
+* ``value``: read bases per second on the device with the reads already in
+  HBM (CUDA events on the library's stream, stages 0-4);
+* ``e2e``: the same metric through the public C ABI with host buffers
+  (pinned), the host->device copy of the reads and the device->host copy of
+  the rows inside the timed region;
+* ``plain``: the one-read-per-launch path on a sample of reads, with per-read
+  p50/p99 latency;
+* ``roofline``: the dominant stage's algorithmic bytes / its event time
+  against the measured HBM copy bandwidth;
+* ``cpu_baseline``: the CPU oracle (a restatement of the reference's CPU
+  path) on the host's cores over a bounded sample of the same reads.
+
+``--impl reference`` times that CPU implementation alone, on the same
+workload, metric and unit.  Under torchrun every rank runs its own replica
+(weak scaling: the index is replicated and reads are independent queries);
+``value`` sums all ranks' bases over the slowest rank's time.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO))
+
+METRIC = "overlapped read-bases/sec on 1 GB300 (batched vs plain); p50/p99 query latency"
+UNIT = "read-bases/s"
+WORKLOAD = ("5 Mb genome, 30 x 5 kb repeat (1% div) + 2% (AT)n; HiFi 40x lognormal(15 kb, 3 kb), "
+            "0.2% error; k=17; batched: all reads in one pass")
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=world)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def reduce_max(world, x: float) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def reduce_sum(world, x: float) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def measured_peaks() -> dict:
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        return json.loads(p.read_text())
+    return {}
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (clocks, throttle reasons)."""
+
+    def __init__(self, index: int, path: Path):
+        self.path = path
+        self.proc = None
+        try:
+            self.fh = open(path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={index}", "--query-gpu=clocks.sm,clocks.max.sm,power.draw,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait(timeout=10)
+        self.fh.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def make_workload(args):
+    from cuflye_gb300 import synth
+    return synth.batched_repeats(seed=args.seed, genome_len=args.genome_len,
+                                 coverage=args.coverage)
+
+
+def oracle_baseline(wl, sample_queries: int, repeats: int = 1) -> tuple[dict, list[float]]:
+    """CPU oracle over the first `sample_queries` reads on all host cores."""
+    from oracle import oracle as O
+    O.build()
+    reads = wl.reads
+    b = O.SeqBatch(reads.ids, reads.offsets, reads.bases.tobytes())
+    t0 = time.time()
+    idx = O.Index.build(wl.k, b, wl.min_freq, wl.max_freq)
+    build_s = time.time() - t0
+    sub = reads.subset(np.arange(min(sample_queries, reads.n)))
+    qb = O.SeqBatch(sub.ids, sub.offsets, sub.bases.tobytes())
+    params = O.default_params(**wl.params)
+    threads = os.cpu_count() or 1
+    times = []
+    for _ in range(repeats):
+        t = time.perf_counter()
+        O.overlaps(idx, qb, params, threads=threads)
+        times.append(time.perf_counter() - t)
+    info = {"cores": threads, "sample_queries": int(sub.n), "sample_bases": int(sub.total_bases),
+            "index_build_s": round(build_s, 2)}
+    return info, times
+
+
+def run_reference(args, world, rank) -> None:
+    if rank != 0:
+        return
+    wl = make_workload(args)
+    info, times = oracle_baseline(wl, args.reference_sample, repeats=args.warmup + args.steps)
+    timed = times[args.warmup:]
+    v = info["sample_bases"] * len(timed) / sum(timed)
+    sample = (f"first {info['sample_queries']} reads ({info['sample_bases']} bases) of the "
+              f"workload against the full index, {info['cores']} threads")
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000 * sum(timed) / len(timed), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "reads": wl.reads.n,
+                       "read_bases": wl.reads.total_bases, "sample": sample},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": info["cores"], "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+_PINNED = []  # keeps the pinned host allocations alive for the whole run
+
+
+def pinned_like(a: np.ndarray) -> np.ndarray:
+    """A copy of `a` in page-locked host memory (torch's pinned allocator)."""
+    import torch
+    t = torch.empty(max(a.nbytes, 1), dtype=torch.uint8).pin_memory()
+    _PINNED.append(t)
+    v = t.numpy()[: a.nbytes].view(a.dtype).reshape(a.shape)
+    v[...] = a
+    return v
+
+
+def run_ours(args, world, rank, local) -> None:
+    from cuflye_gb300 import abi
+    from cuflye_gb300.backend import CudaBackend, OverlapParams, Sequences, load_library
+    import ctypes
+
+    wl = make_workload(args)
+    reads = wl.reads
+    params = OverlapParams.make(**wl.params)
+    gpu = CudaBackend(device=local, memory_budget_bytes=0)
+    t0 = time.perf_counter()
+    stats = gpu.build_index(reads, wl.k, wl.min_freq, wl.max_freq)
+    index_s = time.perf_counter() - t0
+    # pinned host inputs / outputs for the end-to-end leg
+    seqs = Sequences(pinned_like(np.ascontiguousarray(reads.ids, dtype=np.int64)),
+                     pinned_like(np.ascontiguousarray(reads.offsets, dtype=np.int64)),
+                     pinned_like(np.ascontiguousarray(reads.bases, dtype=np.uint8)))
+    out = pinned_like(np.zeros(max(1024, 64 * reads.n), dtype=abi.OVERLAP_DTYPE))
+    L = load_library()
+    launches = ctypes.c_uint64()
+    for _ in range(args.warmup):
+        rows = gpu.overlaps(seqs, params, out=out)
+    barrier(world)
+    L.cuflye_kernel_launches(ctypes.byref(launches))
+    l0 = launches.value
+    sampler = ClockSampler(local, REPO / "gpurun_out" / f"clocks_rank{rank}.csv") \
+        if (REPO / "gpurun_out").exists() else ClockSampler(local, Path("/tmp/cuflye_clocks.csv"))
+    dev_ms, wall_s, stage_tot, bytes_tot = [], [], np.zeros(7), np.zeros(7)
+    nrows = 0
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        rows = gpu.overlaps(seqs, params, out=out)
+        wall_s.append(time.perf_counter() - t)
+        ms, by = gpu.last_timing()
+        ms = np.array(ms)
+        stage_tot += ms
+        bytes_tot += np.array(by, dtype=np.float64)
+        dev_ms.append(float(ms[:5].sum()))
+        nrows = len(rows)
+    clocks = sampler.stop()
+    L.cuflye_kernel_launches(ctypes.byref(launches))
+    launches_step = (launches.value - l0) / args.steps
+    barrier(world)
+    bases = float(reads.total_bases)
+    dev_total = reduce_max(world, sum(dev_ms) / 1000.0)
+    wall_total = reduce_max(world, sum(wall_s))
+    all_bases = reduce_sum(world, bases * args.steps)
+    value = all_bases / dev_total
+    e2e = all_bases / wall_total
+    # dominant stage roofline (stages 0-4 carry algorithmic bytes)
+    names = ["hit generation", "KmerMatch sort", "group prefilter + ext re-sort",
+             "chaining DP", "score sort + backtrack + rows"]
+    dom = int(np.argmax(stage_tot[:5]))
+    peaks = measured_peaks()
+    peak = peaks.get("hbm_gbs")
+    achieved = bytes_tot[dom] / (stage_tot[dom] / 1000.0) / 1e9
+    traffic = None
+    tfile = REPO / "profiles" / "ncu_traffic.json"
+    if tfile.exists():
+        tj = json.loads(tfile.read_text())
+        per = tj.get("stages", {}).get(names[dom])
+        if per and per.get("dram_bytes_per_hit"):
+            traffic = per["dram_bytes_per_hit"] * (bytes_tot[dom] / args.steps) / max(
+                1.0, per.get("alg_bytes_per_hit", 1.0))
+    # plain path: one read per launch, sample
+    plain = None
+    lat = []
+    if rank == 0 and args.plain_sample > 0:
+        sub = reads.subset(np.arange(min(args.plain_sample, reads.n)))
+        gpu.set_batch_queries(1)
+        one = [Sequences(np.array([sub.ids[i]], dtype=np.int64),
+                         np.array([0, sub.offsets[i + 1] - sub.offsets[i]], dtype=np.int64),
+                         np.ascontiguousarray(sub.bases[sub.offsets[i]:sub.offsets[i + 1]]))
+               for i in range(sub.n)]
+        gpu.overlaps(one[0], params)
+        t = time.perf_counter()
+        for s in one:
+            t1 = time.perf_counter()
+            gpu.overlaps(s, params)
+            lat.append(time.perf_counter() - t1)
+        plain_s = time.perf_counter() - t
+        gpu.set_batch_queries(0)
+        plain = {"value": sub.total_bases / plain_s, "unit": UNIT,
+                 "sample": f"first {sub.n} reads, one read per call and per launch sequence",
+                 "batched_over_plain": (bases / (sum(wall_s) / len(wall_s))) /
+                                       (sub.total_bases / plain_s)}
+    cpu = None
+    if rank == 0 and world == 1 and args.cpu_sample > 0:
+        info, times = oracle_baseline(wl, args.cpu_sample)
+        cpu = {"value": info["sample_bases"] / times[0], "unit": UNIT, "cores": info["cores"],
+               "kind": "port",
+               "sample": f"first {info['sample_queries']} reads ({info['sample_bases']} bases) "
+                         f"against the full index, CPU oracle on {info['cores']} threads"}
+    if rank != 0:
+        return
+    mean_ms = 1000.0 * dev_total / args.steps
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": mean_ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "reads": reads.n, "read_bases": int(bases),
+                   "index_positions": stats["positions"], "index_keys": stats["keys"],
+                   "index_build_s": round(index_s, 3), "rows_per_step": nrows,
+                   "l2": "inputs larger than L2 (about 12 B x 7e9 hits per step, index 1.5 GB)"},
+        "e2e": {"value": e2e, "unit": UNIT,
+                "h2d_bytes_per_step": int(seqs.bases.nbytes + seqs.offsets.nbytes +
+                                          seqs.ids.nbytes),
+                "d2h_bytes_per_step": int(nrows * abi.OVERLAP_DTYPE.itemsize)},
+        "gpu_launches": int(round(launches_step * args.steps)),
+        "stages_ms_per_step": {n: round(float(stage_tot[i]) / args.steps, 3)
+                               for i, n in enumerate(names + ["output + D2H", "H2D"])},
+        "roofline": {"bound": "hbm", "stage": names[dom], "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": (achieved / peak) if peak else None,
+                     "traffic": traffic, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"
+                     if peak else "missing"},
+        "clocks": clocks,
+    }
+    if plain:
+        line["plain"] = plain
+        lat_ms = sorted(1000 * x for x in lat)
+        line["latency_ms"] = {"p50": lat_ms[len(lat_ms) // 2],
+                              "p99": lat_ms[min(len(lat_ms) - 1, int(0.99 * len(lat_ms)))],
+                              "mode": "plain path, one read per call through the C ABI"}
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+    gpu.close()
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--genome-len", type=int, default=5_000_000)
+    ap.add_argument("--coverage", type=float, default=40.0)
+    ap.add_argument("--plain-sample", type=int, default=200)
+    ap.add_argument("--cpu-sample", type=int, default=384)
+    ap.add_argument("--reference-sample", type=int, default=256)
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())

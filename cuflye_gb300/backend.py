@@ -279,11 +279,16 @@ class CudaBackend:
             return out[:n.value].copy(), fout[:nf.value].copy()
 
     # -- OverlapDetector::getSeqOverlaps
-    def overlaps(self, queries, params: OverlapParams, capacity: int | None = None) -> np.ndarray:
+    def overlaps(self, queries, params: OverlapParams, capacity: int | None = None,
+                 out: np.ndarray | None = None) -> np.ndarray:
+        """Rows of every query; ``out`` may supply a (pinned) output buffer."""
         q = Sequences.of(queries)
         cap = capacity if capacity is not None else max(1024, 64 * q.n)
+        if out is not None:
+            cap = len(out)
         while True:
-            out = np.empty(cap, dtype=abi.OVERLAP_DTYPE)
+            if out is None or len(out) < cap:
+                out = np.empty(cap, dtype=abi.OVERLAP_DTYPE)
             n = ctypes.c_size_t()
             st = self._L.cuflye_overlaps(self._h, q.n, _ptr(q.ids, _i64p), _ptr(q.offsets, _i64p),
                                          q.bases.ctypes.data_as(ctypes.c_char_p),
@@ -293,7 +298,7 @@ class CudaBackend:
                 cap = n.value
                 continue
             self._check(st)
-            return out[:n.value].copy()
+            return out[:n.value]
 
     # -- ReadAligner::alignReads per-read body
     def set_graph(self, edge_ids, seq_ids, left, right) -> None:

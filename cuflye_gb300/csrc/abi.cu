@@ -87,6 +87,7 @@ inline unsigned grid(uint64_t n, int b) { return static_cast<unsigned>((n + b - 
 cudaError_t rows_to_abi(const OverlapRow* rows, uint64_t n, const QueryInfo* qinfo,
                         const int64_t* slot_signed, cuflye_overlap_range* out, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
+  count_launch();
   rows_abi_kernel<<<grid(n, 256), 256, 0, s>>>(rows, n, qinfo, slot_signed, out);
   return cudaGetLastError();
 }
@@ -95,6 +96,7 @@ cudaError_t hits_to_abi(const uint64_t* keys, const uint32_t* vals, const uint64
                         uint64_t n, const uint64_t* q_off, uint32_t nq, const QueryInfo* qinfo,
                         const int64_t* slot_signed, cuflye_candidate* out, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
+  count_launch();
   hits_abi_kernel<<<grid(n, 256), 256, 0, s>>>(keys, vals, kmers, n, q_off, nq, qinfo,
                                                slot_signed, out);
   return cudaGetLastError();
@@ -103,6 +105,7 @@ cudaError_t hits_to_abi(const uint64_t* keys, const uint32_t* vals, const uint64
 cudaError_t filtered_to_abi(const int32_t* fpos, uint64_t n, const uint64_t* f_off, uint32_t nq,
                             const QueryInfo* qinfo, cuflye_filtered_pos* out, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
+  count_launch();
   filtered_abi_kernel<<<grid(n, 256), 256, 0, s>>>(fpos, n, f_off, nq, qinfo, out);
   return cudaGetLastError();
 }

@@ -75,11 +75,13 @@ struct cuflye_ctx {
   size_t queries_per_pass = 0;
   // timing
   cudaEvent_t ev[8]{};
-  double stage_ms[5]{};
-  uint64_t stage_bytes[5]{};
+  double stage_ms[7]{};
+  uint64_t stage_bytes[7]{};
 };
 
 namespace {
+
+constexpr int kStages = 7;
 
 template <typename T>
 T* buf(cuflye_ctx* c, const std::string& name, uint64_t count) {
@@ -438,9 +440,23 @@ struct PassState {
   QueryInfo* qinfo = nullptr;
 };
 
-// Upload one pass of queries and produce its hits in generation order.
-// Returns false (and leaves nothing allocated beyond the arena) when the
-// pass's hits would not fit the memory budget and the pass can be split.
+// Buffers sized by the hit count of a pass (reused by the next pass).
+const char* const kPerHitBuffers[] = {"h_keys", "h_vals", "h_kmers", "s_l", "s_r", "g_flags",
+                                      "g_id", "c_cur", "c_ext", "c_score", "c_bt", "a_cand"};
+
+// The memory budget, or the device's memory less a 4 GiB margin when unbounded.
+uint64_t effective_budget(cuflye_ctx* c) {
+  if (c->budget) return c->budget;
+  size_t free_b = 0, total_b = 0;
+  CUFLYE_CHECK(cudaMemGetInfo(&free_b, &total_b));
+  const uint64_t cap = static_cast<uint64_t>(free_b) + c->in_use;
+  const uint64_t margin = 4ull << 30;
+  return cap > margin ? cap - margin : cap / 2;
+}
+
+// Upload a run of queries starting at q0 and produce the hits of the longest
+// prefix of them that fits in device memory (ps.nq queries), in Flye's
+// generation order.
 bool run_hits(cuflye_ctx* c, const Queries& Q, size_t q0, size_t q1, bool want_kmers,
               uint64_t bytes_per_hit, PassState& ps) {
   const int k = c->idx.k;
@@ -473,7 +489,6 @@ bool run_hits(cuflye_ctx* c, const Queries& Q, size_t q0, size_t q1, bool want_k
     CUFLYE_CHECK(cudaMemcpyAsync(d_ascii, Q.bases + Q.offsets[q0], nbases, cudaMemcpyHostToDevice,
                                  st));
   uint64_t* words = buf<uint64_t>(c, "q_words", (nbases + 31) / 32 + 2);
-  CUFLYE_CHECK(pack_bases(d_ascii, nbases, words, st));
   uint64_t* d_base = buf<uint64_t>(c, "q_base", nq + 1);
   uint64_t* d_win = buf<uint64_t>(c, "q_win", nq + 1);
   int32_t* d_qdi = buf<int32_t>(c, "q_qdi", nq);
@@ -483,6 +498,9 @@ bool run_hits(cuflye_ctx* c, const Queries& Q, size_t q0, size_t q1, bool want_k
   CUFLYE_CHECK(cudaMemcpyAsync(d_qdi, qdi.data(), nq * 4ull, cudaMemcpyHostToDevice, st));
   CUFLYE_CHECK(cudaMemcpyAsync(ps.qinfo, qinfo.data(), nq * sizeof(QueryInfo),
                                cudaMemcpyHostToDevice, st));
+  // inputs are on the device from here on
+  CUFLYE_CHECK(cudaEventRecord(c->ev[5], st));
+  CUFLYE_CHECK(pack_bases(d_ascii, nbases, words, st));
   QueryBatch qb;
   qb.words = words;
   qb.base_off = d_base;
@@ -499,14 +517,43 @@ bool run_hits(cuflye_ctx* c, const Queries& Q, size_t q0, size_t q1, bool want_k
   uint64_t* filt_off = buf<uint64_t>(c, "w_filtoff", nwin + 1);
   ps.nhits = scan_u32(c, cnt, hit_off, nwin, "w_scan");
   ps.nfilt = scan_u32(c, filt, filt_off, nwin, "w_scan");
-  if (c->budget) {
-    const uint64_t need = ps.nhits * bytes_per_hit;
-    if (c->in_use + need > c->budget && nq > 1) return false;
-  }
   ps.q_off = buf<uint64_t>(c, "q_hitoff", nq + 1);
   ps.f_off = buf<uint64_t>(c, "q_filtoff", nq + 1);
   CUFLYE_CHECK(gather_query_offsets(d_win, hit_off, nq, ps.q_off, st));
   CUFLYE_CHECK(gather_query_offsets(d_win, filt_off, nq, ps.f_off, st));
+  // Keep the longest prefix of queries whose hits fit the memory left; the
+  // per-hit buffers of an earlier pass are reused, so they count as free.
+  const uint64_t limit = effective_budget(c);
+  uint64_t reusable = 0;
+  for (const char* nm : kPerHitBuffers) {
+    auto it = c->bufs.find(nm);
+    if (it != c->bufs.end()) reusable += it->second.cap;
+  }
+  const uint64_t used = c->in_use - reusable;
+  const uint64_t avail = limit > used ? limit - used : 0;
+  if (ps.nhits * bytes_per_hit > avail) {
+    std::vector<uint64_t> qoff(nq + 1);
+    CUFLYE_CHECK(cudaMemcpyAsync(qoff.data(), ps.q_off, (nq + 1) * 8ull, cudaMemcpyDeviceToHost,
+                                 st));
+    sync(c);
+    uint32_t m = 0;
+    while (m < nq && qoff[m + 1] * bytes_per_hit <= avail) ++m;
+    if (m == 0)
+      throw Error(CUFLYE_ERR_BUDGET,
+                  "device memory budget exceeded: query " + std::to_string(Q.ids[q0]) + " has " +
+                      std::to_string(qoff[1]) + " hits needing " +
+                      std::to_string(qoff[1] * bytes_per_hit) + " bytes; " +
+                      std::to_string(avail) + " available");
+    ps.nq = m;
+    ps.nhits = qoff[m];
+    ps.nwin = win_off[m];
+    qb.nq = m;
+    qb.nwin = win_off[m];
+    uint64_t fo = 0;
+    CUFLYE_CHECK(cudaMemcpyAsync(&fo, ps.f_off + m, 8, cudaMemcpyDeviceToHost, st));
+    sync(c);
+    ps.nfilt = fo;
+  }
   ps.keys = buf<uint64_t>(c, "h_keys", ps.nhits);
   ps.vals = buf<uint32_t>(c, "h_vals", ps.nhits);
   ps.kmers = want_kmers ? buf<uint64_t>(c, "h_kmers", ps.nhits) : nullptr;
@@ -581,7 +628,9 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
   // 4. DP
   int32_t* score = buf<int32_t>(c, "c_score", H);
   int32_t* bt = buf<int32_t>(c, "c_bt", H);
+  CUFLYE_CHECK(cudaEventRecord(c->ev[6], st));
   CUFLYE_CHECK(chain_dp(cur, ext, score, bt, groups, dp_list, gcounts, cp, c->num_sms, st));
+  CUFLYE_CHECK(cudaEventRecord(c->ev[7], st));
   // 5. score order (libstdc++ order of indices by score descending)
   CUFLYE_CHECK(chain_prepare_order(score, ps.keys, ps.vals, groups, dp_list, gcounts, sb, se, st));
   CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, sb, se, G32, gcounts + 1, glists,
@@ -625,19 +674,24 @@ float elapsed(cudaEvent_t a, cudaEvent_t b) {
 }
 
 void reset_timing(cuflye_ctx* c) {
-  for (int i = 0; i < 5; ++i) {
+  for (int i = 0; i < kStages; ++i) {
     c->stage_ms[i] = 0;
     c->stage_bytes[i] = 0;
   }
 }
 
+// Stages (see cuflye_last_timing): 0 hits, 1 match sort, 2 groups, 3 DP,
+// 4 backtrack + rows, 5 output + D2H, 6 H2D.
 void accumulate_timing(cuflye_ctx* c, bool chained) {
   sync(c);
-  c->stage_ms[0] += elapsed(c->ev[0], c->ev[1]);
+  c->stage_ms[6] += elapsed(c->ev[0], c->ev[5]);
+  c->stage_ms[0] += elapsed(c->ev[5], c->ev[1]);
   if (chained) {
     c->stage_ms[1] += elapsed(c->ev[1], c->ev[2]);
-    c->stage_ms[2] += elapsed(c->ev[2], c->ev[3]);
-    c->stage_ms[3] += elapsed(c->ev[3], c->ev[4]);
+    c->stage_ms[2] += elapsed(c->ev[2], c->ev[6]);
+    c->stage_ms[3] += elapsed(c->ev[6], c->ev[7]);
+    c->stage_ms[4] += elapsed(c->ev[7], c->ev[3]);
+    c->stage_ms[5] += elapsed(c->ev[3], c->ev[4]);
   }
 }
 
@@ -656,17 +710,15 @@ void for_each_pass(cuflye_ctx* c, const Queries& Q, bool kmers, uint64_t bytes_p
     size_t q1 = std::min(Q.n, q0 + step);
     PassState ps;
     CUFLYE_CHECK(cudaEventRecord(c->ev[0], c->stream));
-    if (!run_hits(c, Q, q0, q1, kmers, bytes_per_hit, ps)) {
-      step = std::max<size_t>((q1 - q0) / 2, 1);
-      continue;
-    }
+    run_hits(c, Q, q0, q1, kmers, bytes_per_hit, ps);
+    q1 = q0 + ps.nq;
     CUFLYE_CHECK(cudaEventRecord(c->ev[1], c->stream));
     body(q0, q1, ps);
     q0 = q1;
   }
 }
 
-constexpr uint64_t kChainBytesPerHit = 8 + 4 + 4 + 4 + 4 + 4 + 4 + 4 + 8;
+constexpr uint64_t kChainBytesPerHit = 8 + 4 + 4 + 4 + 4 + 8 + 4 + 4 + 4 + 4;
 
 void require_index(cuflye_ctx* c) {
   if (!c->has_index) throw Error(CUFLYE_ERR_NO_INDEX, "no k-mer index: call cuflye_index_build");
@@ -879,10 +931,11 @@ cuflye_status cuflye_overlaps(cuflye_ctx* c, size_t n, const int64_t* ids, const
   Queries Q{n, ids, offsets, bases};
   size_t total = 0;
   bool overflow = false;
-  uint64_t hits_total = 0, windows_total = 0;
-  for_each_pass(c, Q, false, kChainBytesPerHit, [&](size_t, size_t, PassState& ps) {
+  uint64_t hits_total = 0, windows_total = 0, bases_total = 0;
+  for_each_pass(c, Q, false, kChainBytesPerHit, [&](size_t q0, size_t q1, PassState& ps) {
     hits_total += ps.nhits;
     windows_total += ps.nwin;
+    bases_total += static_cast<uint64_t>(offsets[q1] - offsets[q0]);
     const uint64_t R = run_chain(c, ps, cp);
     if (!overflow && total + R <= out_cap) {
       cuflye_overlap_range* d_out = buf<cuflye_overlap_range>(c, "a_ovl", R);
@@ -898,9 +951,15 @@ cuflye_status cuflye_overlaps(cuflye_ctx* c, size_t n, const int64_t* ids, const
     total += R;
     accumulate_timing(c, true);
   });
-  c->stage_bytes[0] = windows_total * 32 + hits_total * 12;
+  // algorithmic bytes per stage: packed bases + one 32-byte sector per window
+  // probe + bucket entries read (8 B) + hit records written (12 B); a read and a
+  // write of every 12-byte record per sort; the DP reads (cur, ext) and writes
+  // (score, backtrack)
+  c->stage_bytes[0] = bases_total / 4 + windows_total * 32 + hits_total * 20;
   c->stage_bytes[1] = hits_total * 24;
-  c->stage_bytes[2] = hits_total * 36;
+  c->stage_bytes[2] = hits_total * 20;
+  c->stage_bytes[3] = hits_total * 16;
+  c->stage_bytes[4] = hits_total * 28;
   if (n_out) *n_out = total;
   if (overflow)
     throw Error(CUFLYE_ERR_CAPACITY,
@@ -1091,10 +1150,16 @@ cuflye_status cuflye_std_sort_segments(cuflye_ctx* c, uint64_t* keys, uint32_t* 
 cuflye_status cuflye_last_timing(const cuflye_ctx* c, double* stage_ms, uint64_t* stage_bytes,
                                  size_t n_stages) {
   if (!c) return CUFLYE_ERR_INVALID;
-  for (size_t i = 0; i < n_stages && i < 5; ++i) {
+  for (size_t i = 0; i < n_stages && i < static_cast<size_t>(kStages); ++i) {
     if (stage_ms) stage_ms[i] = c->stage_ms[i];
     if (stage_bytes) stage_bytes[i] = c->stage_bytes[i];
   }
+  return CUFLYE_OK;
+}
+
+cuflye_status cuflye_kernel_launches(uint64_t* total) {
+  if (!total) return CUFLYE_ERR_INVALID;
+  *total = launches_total();
   return CUFLYE_OK;
 }
 

@@ -554,7 +554,9 @@ __global__ void rows_scatter_kernel(const OverlapRow* __restrict__ pool, uint32_
 cudaError_t groups_mark(const uint64_t* keys, const uint64_t* q_off, uint32_t nq, uint64_t nhits,
                         uint32_t* flags, cudaStream_t s) {
   if (nhits == 0) return cudaSuccess;
+  count_launch();
   mark_ext_changes<<<grid(nhits, 256), 256, 0, s>>>(keys, nhits, flags);
+  count_launch();
   mark_query_starts<<<grid(nq, 256), 256, 0, s>>>(q_off, nq, flags);
   return cudaGetLastError();
 }
@@ -564,6 +566,7 @@ cudaError_t groups_build(const uint64_t* keys, const uint32_t* flags, const uint
                          GroupInfo* groups, cudaStream_t s) {
   if (nhits == 0) return cudaSuccess;
   (void)ngroups;
+  count_launch();
   build_groups<<<grid(nhits, 256), 256, 0, s>>>(keys, flags, gid, q_off, nq, nhits, groups);
   return cudaGetLastError();
 }
@@ -575,6 +578,7 @@ cudaError_t groups_prefilter_n(const uint64_t* keys, const uint32_t* vals, Group
                                cudaStream_t s) {
   cudaMemsetAsync(counts, 0, 2 * sizeof(uint32_t), s);
   if (ngroups == 0) return cudaGetLastError();
+  count_launch();
   prefilter_kernel<<<grid(ngroups * 32, 256), 256, 0, s>>>(keys, vals, groups, ngroups, nhits,
                                                            qinfo, slot_len, p, ext_list, dp_list,
                                                            counts);
@@ -584,6 +588,7 @@ cudaError_t groups_prefilter_n(const uint64_t* keys, const uint32_t* vals, Group
 cudaError_t groups_prepare_ext_sort(uint64_t* keys, uint32_t* vals, const GroupInfo* groups,
                                     const uint32_t* ext_list, const uint32_t* counts,
                                     uint64_t* seg_begin, uint64_t* seg_end, cudaStream_t s) {
+  count_launch();
   prepare_ext_sort_kernel<<<2048, 256, 0, s>>>(keys, vals, groups, ext_list, counts, seg_begin,
                                                seg_end);
   return cudaGetLastError();
@@ -592,6 +597,7 @@ cudaError_t groups_prepare_ext_sort(uint64_t* keys, uint32_t* vals, const GroupI
 cudaError_t groups_split(const uint64_t* keys, const uint32_t* vals, const GroupInfo* groups,
                          const uint32_t* dp_list, const uint32_t* counts, int32_t* cur,
                          int32_t* ext, cudaStream_t s) {
+  count_launch();
   split_kernel<<<2048, 256, 0, s>>>(keys, vals, groups, dp_list, counts, cur, ext);
   return cudaGetLastError();
 }
@@ -599,6 +605,7 @@ cudaError_t groups_split(const uint64_t* keys, const uint32_t* vals, const Group
 cudaError_t chain_dp(const int32_t* cur, const int32_t* ext, int32_t* score, int32_t* bt,
                      const GroupInfo* groups, const uint32_t* dp_list, const uint32_t* counts,
                      const ChainParams& p, int num_sms, cudaStream_t s) {
+  count_launch();
   dp_kernel<<<num_sms * 8, kDpWarps * 32, 0, s>>>(cur, ext, score, bt, groups, dp_list, counts, p);
   return cudaGetLastError();
 }
@@ -607,6 +614,7 @@ cudaError_t chain_prepare_order(const int32_t* score, uint64_t* keys, uint32_t* 
                                 const GroupInfo* groups, const uint32_t* dp_list,
                                 const uint32_t* counts, uint64_t* seg_begin, uint64_t* seg_end,
                                 cudaStream_t s) {
+  count_launch();
   prepare_order_kernel<<<2048, 256, 0, s>>>(score, keys, vals, groups, dp_list, counts, seg_begin,
                                             seg_end);
   return cudaGetLastError();
@@ -621,6 +629,7 @@ cudaError_t chain_backtrack(const int32_t* cur, const int32_t* ext, const int32_
                             uint32_t* pool_count, uint32_t* group_rows, DeviceStatus* st,
                             uint32_t max_groups, cudaStream_t s) {
   if (max_groups == 0) return cudaSuccess;
+  count_launch();
   backtrack_kernel<<<grid(max_groups, 128), 128, 0, s>>>(cur, ext, score, bt, order, groups,
                                                          dp_list, counts, qinfo, f_off, fpos,
                                                          slot_signed, logt, p, pool, pool_cap,
@@ -630,6 +639,7 @@ cudaError_t chain_backtrack(const int32_t* cur, const int32_t* ext, const int32_
 
 cudaError_t query_group_offsets(const GroupInfo* groups, uint64_t ngroups, uint32_t nq,
                                 uint64_t* q_group_off, cudaStream_t s) {
+  count_launch();
   query_group_off_kernel<<<grid(nq + 1, 256), 256, 0, s>>>(groups, ngroups, nq, q_group_off);
   return cudaGetLastError();
 }
@@ -637,6 +647,7 @@ cudaError_t query_group_offsets(const GroupInfo* groups, uint64_t ngroups, uint3
 cudaError_t rows_limit(const uint32_t* group_rows, const uint64_t* q_group_off, uint32_t nq,
                        int32_t max_overlaps, uint32_t* kept_rows, cudaStream_t s) {
   if (nq == 0) return cudaSuccess;
+  count_launch();
   rows_limit_kernel<<<grid(nq, 128), 128, 0, s>>>(group_rows, q_group_off, nq, max_overlaps,
                                                   kept_rows);
   return cudaGetLastError();
@@ -645,6 +656,7 @@ cudaError_t rows_limit(const uint32_t* group_rows, const uint64_t* q_group_off, 
 cudaError_t rows_scatter(const OverlapRow* pool, uint32_t npool, const uint32_t* kept_rows,
                          const uint64_t* kept_off, OverlapRow* rows, cudaStream_t s) {
   if (npool == 0) return cudaSuccess;
+  count_launch();
   rows_scatter_kernel<<<grid(npool, 256), 256, 0, s>>>(pool, npool, kept_rows, kept_off, rows);
   return cudaGetLastError();
 }

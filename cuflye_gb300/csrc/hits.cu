@@ -163,6 +163,7 @@ __global__ void gather_kernel(const uint64_t* __restrict__ win_off,
 cudaError_t hits_count(const DeviceIndex& idx, const QueryBatch& q, uint32_t* cnt,
                        uint32_t* filt, uint64_t* wmeta, uint8_t* wflags, cudaStream_t s) {
   if (q.nwin == 0) return cudaSuccess;
+  count_launch();
   count_kernel<<<static_cast<unsigned>((q.nwin + 255) / 256), 256, 0, s>>>(idx, q, cnt, filt,
                                                                           wmeta, wflags);
   return cudaGetLastError();
@@ -173,6 +174,7 @@ cudaError_t hits_emit(const DeviceIndex& idx, const QueryBatch& q, const uint64_
                       uint64_t* keys, uint32_t* vals, uint64_t* kmers, int32_t* fpos,
                       cudaStream_t s) {
   if (q.nwin == 0) return cudaSuccess;
+  count_launch();
   emit_kernel<<<static_cast<unsigned>((q.nwin + 255) / 256), 256, 0, s>>>(
       idx, q, hit_off, filt_off, wmeta, wflags, keys, vals, kmers, fpos);
   return cudaGetLastError();
@@ -180,6 +182,7 @@ cudaError_t hits_emit(const DeviceIndex& idx, const QueryBatch& q, const uint64_
 
 cudaError_t gather_query_offsets(const uint64_t* win_off, const uint64_t* wl_off, uint32_t nq,
                                  uint64_t* q_off, cudaStream_t s) {
+  count_launch();
   gather_kernel<<<(nq + 1 + 255) / 256, 256, 0, s>>>(win_off, wl_off, nq, q_off);
   return cudaGetLastError();
 }

@@ -162,6 +162,7 @@ cudaError_t index_enumerate(const uint64_t* words, const uint64_t* base_off,
                             uint64_t nwin, int k, uint64_t* keys, uint64_t* vals,
                             cudaStream_t s) {
   if (nwin == 0) return cudaSuccess;
+  count_launch();
   enumerate_kernel<<<grid(nwin, 256), 256, 0, s>>>(words, base_off, win_off, slot_len, nslots,
                                                    nwin, k, keys, vals);
   return cudaGetLastError();
@@ -169,12 +170,14 @@ cudaError_t index_enumerate(const uint64_t* words, const uint64_t* base_off,
 
 cudaError_t index_mark_runs(const uint64_t* keys, uint64_t n, uint32_t* flags, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
+  count_launch();
   mark_runs_kernel<<<grid(n, 256), 256, 0, s>>>(keys, n, flags);
   return cudaGetLastError();
 }
 
 cudaError_t index_run_starts(const uint32_t* flags, const uint64_t* run_id, uint64_t n,
                              uint64_t nruns, uint64_t* run_start, cudaStream_t s) {
+  count_launch();
   run_starts_kernel<<<grid(n > 0 ? n : 1, 256), 256, 0, s>>>(flags, run_id, n, nruns,
                                                              run_start);
   return cudaGetLastError();
@@ -184,6 +187,7 @@ cudaError_t index_classify_runs(const uint64_t* run_start, uint64_t nruns, uint3
                                 uint32_t max_freq, uint32_t* kept, uint8_t* cls,
                                 cudaStream_t s) {
   if (nruns == 0) return cudaSuccess;
+  count_launch();
   classify_runs_kernel<<<grid(nruns, 256), 256, 0, s>>>(run_start, nruns, min_freq, max_freq,
                                                         kept, cls);
   return cudaGetLastError();
@@ -194,6 +198,7 @@ cudaError_t index_copy_positions(const uint64_t* vals, const uint64_t* run_id,
                                  const uint64_t* kept_off, uint64_t n, uint64_t* pos,
                                  cudaStream_t s) {
   if (n == 0) return cudaSuccess;
+  count_launch();
   copy_positions_kernel<<<grid(n, 256), 256, 0, s>>>(vals, run_id, run_start, cls, kept_off, n,
                                                      pos);
   return cudaGetLastError();
@@ -203,6 +208,7 @@ cudaError_t index_insert(const uint64_t* keys, const uint64_t* run_start, const 
                          const uint64_t* kept_off, uint64_t nruns, TableEntry* table,
                          uint64_t mask, DeviceStatus* st, cudaStream_t s) {
   if (nruns == 0) return cudaSuccess;
+  count_launch();
   insert_kernel<<<grid(nruns, 256), 256, 0, s>>>(keys, run_start, cls, kept_off, nruns, table,
                                                  mask, st);
   return cudaGetLastError();
@@ -211,6 +217,7 @@ cudaError_t index_insert(const uint64_t* keys, const uint64_t* run_start, const 
 cudaError_t index_insert_repetitive(const uint64_t* rep_keys, uint64_t n, TableEntry* table,
                                     uint64_t mask, DeviceStatus* st, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
+  count_launch();
   insert_rep_kernel<<<grid(n, 256), 256, 0, s>>>(rep_keys, n, table, mask, st);
   return cudaGetLastError();
 }

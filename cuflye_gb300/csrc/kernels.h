@@ -9,6 +9,10 @@
 
 namespace cuflye {
 
+// Every kernel launch of the library is counted (cuflye_kernel_launches).
+void count_launch();
+unsigned long long launches_total();
+
 // ---------------------------------------------------------------- scan
 // Exclusive prefix sums (out may alias in).  temp needs scan_temp_words(n) words.
 size_t scan_temp_words(uint64_t n);

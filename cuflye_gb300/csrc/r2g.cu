@@ -300,6 +300,7 @@ __global__ void emit_kernel(const OverlapRow* __restrict__ a, const uint64_t* __
 cudaError_t r2g_filter(const OverlapRow* rows, uint64_t n, const R2GParams& rp, uint32_t* keep,
                        cudaStream_t s) {
   if (n == 0) return cudaSuccess;
+  count_launch();
   filter_kernel<<<grid(n, 256), 256, 0, s>>>(rows, n, rp, keep);
   return cudaGetLastError();
 }
@@ -307,6 +308,7 @@ cudaError_t r2g_filter(const OverlapRow* rows, uint64_t n, const R2GParams& rp, 
 cudaError_t r2g_compact(const OverlapRow* rows, uint64_t n, const uint32_t* keep,
                         const uint64_t* pos, OverlapRow* out, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
+  count_launch();
   compact_kernel<<<grid(n, 256), 256, 0, s>>>(rows, n, keep, pos, out);
   return cudaGetLastError();
 }
@@ -314,6 +316,7 @@ cudaError_t r2g_compact(const OverlapRow* rows, uint64_t n, const uint32_t* keep
 cudaError_t r2g_sort_keys(const OverlapRow* a, const uint64_t* a_off, uint32_t nq,
                           uint64_t* keys, uint32_t* vals, cudaStream_t s) {
   if (nq == 0) return cudaSuccess;
+  count_launch();
   sort_keys_kernel<<<nq, 128, 0, s>>>(a, a_off, nq, keys, vals);
   return cudaGetLastError();
 }
@@ -321,6 +324,7 @@ cudaError_t r2g_sort_keys(const OverlapRow* a, const uint64_t* a_off, uint32_t n
 cudaError_t r2g_permute(const OverlapRow* a, const uint64_t* a_off, uint32_t nq,
                         const uint32_t* vals, OverlapRow* out, cudaStream_t s) {
   if (nq == 0) return cudaSuccess;
+  count_launch();
   permute_kernel<<<nq, 128, 0, s>>>(a, a_off, nq, vals, out);
   return cudaGetLastError();
 }
@@ -332,6 +336,7 @@ cudaError_t r2g_chain(const OverlapRow* a, const uint64_t* a_off, uint32_t nq,
                       int32_t* frozen, int32_t* good, uint32_t* n_good, uint32_t* n_rows,
                       cudaStream_t s) {
   if (nq == 0) return cudaSuccess;
+  count_launch();
   chain_kernel<<<grid(nq, 64), 64, 0, s>>>(a, a_off, nq, g, rp, static_cast<ChainRec*>(recs),
                                            active, frozen, good, n_good, n_rows);
   return cudaGetLastError();
@@ -342,6 +347,7 @@ cudaError_t r2g_emit(const OverlapRow* a, const uint64_t* a_off, uint32_t nq, co
                      const uint32_t* n_good, const uint64_t* chain_off, const uint64_t* row_off,
                      int32_t* tmp, cuflye_read_alignment* out, cudaStream_t s) {
   if (nq == 0) return cudaSuccess;
+  count_launch();
   emit_kernel<<<grid(nq, 64), 64, 0, s>>>(a, a_off, nq, g, qinfo,
                                           static_cast<const ChainRec*>(recs), good, n_good,
                                           chain_off, row_off, tmp, out);

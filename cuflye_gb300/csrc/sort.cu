@@ -485,10 +485,14 @@ cudaError_t segmented_std_sort(uint64_t* keys, uint32_t* vals, uint32_t* lscratc
   uint32_t* tiny = lists;
   uint32_t* mid = lists + nseg;
   uint32_t* big = lists + 2 * static_cast<size_t>(nseg);
+  count_launch();
   classify_segments<<<(nseg + 255) / 256, 256, 0, stream>>>(begin, end, nseg, nseg_dev, tiny,
                                                             mid, big, counts);
+  count_launch();
   sort_tiny<<<num_sms * 4, 128, 0, stream>>>(keys, vals, begin, end, tiny, counts);
+  count_launch();
   sort_mid<<<num_sms, kBlock, sizeof(SortSmem), stream>>>(keys, vals, begin, end, mid, counts);
+  count_launch();
   sort_big<<<num_sms, kBlock, sizeof(SortSmem), stream>>>(keys, vals, lscratch, rscratch, begin,
                                                           end, big, counts);
   return cudaGetLastError();
@@ -501,8 +505,11 @@ cudaError_t radix_sort_pairs(uint64_t* keys, uint64_t* vals, uint64_t* keys_alt,
   uint64_t *ki = keys, *vi = vals, *ko = keys_alt, *vo = vals_alt;
   for (int p = 0; p < ndigits; ++p) {
     const int d = digits[p];
+    count_launch();
     radix_histogram<<<ntiles, kRadixBlock, 0, stream>>>(ki, vi, n, d, hist, ntiles);
+    count_launch();
     radix_scan<<<1, 1024, 0, stream>>>(hist, 256u * ntiles);
+    count_launch();
     radix_scatter<<<ntiles, kRadixBlock, 0, stream>>>(ki, vi, ko, vo, n, d, hist, ntiles);
     uint64_t* t = ki;
     ki = ko;

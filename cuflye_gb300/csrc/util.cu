@@ -1,10 +1,16 @@
 // util.cu — exclusive prefix sums and 2-bit packing.
+#include <atomic>
 #include <cstdint>
 
 #include "common.cuh"
 #include "kernels.h"
 
 namespace cuflye {
+
+static std::atomic<unsigned long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+unsigned long long launches_total() { return g_launches.load(std::memory_order_relaxed); }
+
 namespace {
 
 constexpr int kScanBlock = 256;
@@ -146,8 +152,11 @@ static cudaError_t run_scan(const In* in, uint64_t* out, uint64_t n, uint64_t* t
     return cudaGetLastError();
   }
   const uint64_t ntiles = (n + kScanTile - 1) / kScanTile;
+  count_launch();
   scan_tile_sums<In><<<static_cast<unsigned>(ntiles), kScanBlock, 0, s>>>(in, n, temp);
+  count_launch();
   scan_sums<<<1, 1024, 0, s>>>(temp, ntiles);
+  count_launch();
   scan_downsweep<In><<<static_cast<unsigned>(ntiles), kScanBlock, 0, s>>>(in, out, n, temp);
   return cudaGetLastError();
 }
@@ -164,6 +173,7 @@ cudaError_t exclusive_scan_u64(const uint64_t* in, uint64_t* out, uint64_t n, ui
 
 cudaError_t pack_bases(const uint8_t* ascii, uint64_t nbases, uint64_t* words, cudaStream_t s) {
   const uint64_t nwords = (nbases + 31) / 32 + 1;
+  count_launch();
   pack_kernel<<<static_cast<unsigned>((nwords + 255) / 256), 256, 0, s>>>(ascii, nbases, words,
                                                                          nwords);
   return cudaGetLastError();

@@ -231,11 +231,17 @@ cuflye_status cuflye_std_sort_segments(cuflye_ctx* ctx, uint64_t* keys, uint32_t
 
 /* --------------------------------------------------------------------------
  * Timing of the last call's device work (CUDA events on the context's
- * stream), in milliseconds, by stage: 0 hits, 1 match sort, 2 chaining,
- * 3 output, 4 read-to-graph chains.  Bytes are the stage's algorithmic bytes.
+ * stream), in milliseconds, by stage: 0 hit generation, 1 KmerMatch sort,
+ * 2 group prefilter + ext re-sort, 3 chaining DP, 4 score sort + backtrack +
+ * row compaction, 5 output conversion + device-to-host copy, 6 host-to-device
+ * copy of the queries.  Stages 0-4 run on inputs already in device memory.
+ * stage_bytes gives the algorithmic bytes of stages 0-4 (overlaps only).
  * ------------------------------------------------------------------------ */
 cuflye_status cuflye_last_timing(const cuflye_ctx* ctx, double* stage_ms, uint64_t* stage_bytes,
                                  size_t n_stages);
+
+/* Kernel launches issued by the library in this process so far. */
+cuflye_status cuflye_kernel_launches(uint64_t* total);
 
 #ifdef __cplusplus
 }

@@ -159,7 +159,6 @@ Index* buildIndex(int k, int n, const int64_t* ids, const int64_t* offs,
     uint32_t id;
     int32_t pos;
   };
-  std::vector<Entry> entries;
   Index* idx = new Index();
   idx->k = k;
   idx->transform = true;
@@ -168,21 +167,68 @@ Index* buildIndex(int k, int n, const int64_t* ids, const int64_t* offs,
     int64_t len = offs[t + 1] - offs[t];
     idx->seqLen[fid] = static_cast<int32_t>(len);
     idx->seqLen[fid ^ 1u] = static_cast<int32_t>(len);
-    const char* s = bases + offs[t];
-    for (int64_t p = 0; p + k <= len; ++p) {
-      uint64_t x = encodeKmer(s + p, k);
-      uint64_t rc = revComp(x, k);
-      if (rc < x)
-        entries.push_back({rc, fid ^ 1u, static_cast<int32_t>(len - p - k)});
-      else
-        entries.push_back({x, fid, static_cast<int32_t>(p)});
+  }
+  // Entries are unique, so (key, id, pos) is a total order and any correct
+  // sort gives the same index: enumerate per thread, bucket by the key's top
+  // bits, sort the buckets in parallel, concatenate in bucket order.
+  unsigned nt = std::thread::hardware_concurrency();
+  if (nt == 0) nt = 1;
+  if (nt > 64) nt = 64;
+  const int topBits = 2 * k >= 10 ? 10 : 2 * k;
+  const size_t nb = size_t(1) << topBits;
+  auto bucketOf = [&](uint64_t key) { return static_cast<size_t>(key >> (2 * k - topBits)); };
+  std::vector<std::vector<Entry>> local(nt);
+  {
+    std::vector<std::thread> pool;
+    for (unsigned w = 0; w < nt; ++w)
+      pool.emplace_back([&, w]() {
+        for (int t = static_cast<int>(w); t < n; t += static_cast<int>(nt)) {
+          uint32_t fid = internalId(ids[t]);
+          int64_t len = offs[t + 1] - offs[t];
+          const char* s = bases + offs[t];
+          for (int64_t p = 0; p + k <= len; ++p) {
+            uint64_t x = encodeKmer(s + p, k);
+            uint64_t rc = revComp(x, k);
+            if (rc < x)
+              local[w].push_back({rc, fid ^ 1u, static_cast<int32_t>(len - p - k)});
+            else
+              local[w].push_back({x, fid, static_cast<int32_t>(p)});
+          }
+        }
+      });
+    for (auto& th : pool) th.join();
+  }
+  std::vector<size_t> bstart(nb + 1, 0);
+  for (auto& v : local)
+    for (const Entry& e : v) ++bstart[bucketOf(e.key) + 1];
+  for (size_t b = 0; b < nb; ++b) bstart[b + 1] += bstart[b];
+  std::vector<Entry> entries(bstart[nb]);
+  {
+    std::vector<size_t> fill(bstart.begin(), bstart.end() - 1);
+    for (auto& v : local) {
+      for (const Entry& e : v) entries[fill[bucketOf(e.key)]++] = e;
+      std::vector<Entry>().swap(v);
     }
   }
-  std::sort(entries.begin(), entries.end(), [](const Entry& a, const Entry& b) {
-    if (a.key != b.key) return a.key < b.key;
-    if (a.id != b.id) return a.id < b.id;
-    return a.pos < b.pos;
-  });
+  {
+    std::atomic<size_t> next(0);
+    std::vector<std::thread> pool;
+    for (unsigned w = 0; w < nt; ++w)
+      pool.emplace_back([&]() {
+        for (;;) {
+          size_t b = next.fetch_add(1);
+          if (b >= nb) break;
+          std::sort(entries.begin() + bstart[b], entries.begin() + bstart[b + 1],
+                    [](const Entry& a, const Entry& c) {
+                      if (a.key != c.key) return a.key < c.key;
+                      if (a.id != c.id) return a.id < c.id;
+                      return a.pos < c.pos;
+                    });
+        }
+      });
+    for (auto& th : pool) th.join();
+  }
+  idx->table.reserve(bstart[nb] / 4 + 16);
   size_t i = 0;
   while (i < entries.size()) {
     size_t j = i;
@@ -673,7 +719,10 @@ static void overlapsRange(const Index* idx, int q0, int q1, const int64_t* qids,
     int64_t len = qoffs[q + 1] - qoffs[q];
     collectCandidates(*idx, qids[q], qbases + qoffs[q], len, m, f);
     sortMatches(m);
-    chainSorted(m, qids[q], static_cast<int32_t>(len), idx->seqLen, f, *p, *out);
+    // detectedOverlaps is per getSeqOverlaps call, so max_overlaps counts per query
+    std::vector<Overlap> detected;
+    chainSorted(m, qids[q], static_cast<int32_t>(len), idx->seqLen, f, *p, detected);
+    out->insert(out->end(), detected.begin(), detected.end());
   }
 }
 
