@@ -216,7 +216,7 @@ def run_ours(args, world, rank, local) -> None:
     seqs = Sequences(pinned_like(np.ascontiguousarray(reads.ids, dtype=np.int64)),
                      pinned_like(np.ascontiguousarray(reads.offsets, dtype=np.int64)),
                      pinned_like(np.ascontiguousarray(reads.bases, dtype=np.uint8)))
-    out = pinned_like(np.zeros(max(1024, 64 * reads.n), dtype=abi.OVERLAP_DTYPE))
+    out = pinned_like(np.zeros(max(1024, 256 * reads.n), dtype=abi.OVERLAP_DTYPE))
     L = load_library()
     launches = ctypes.c_uint64()
     for _ in range(args.warmup):

@@ -129,6 +129,8 @@ def load_library(path: Path | None = None) -> ctypes.CDLL:
                                        _vp, ctypes.c_size_t, _szp]
     L.cuflye_std_sort_segments.restype = S
     L.cuflye_std_sort_segments.argtypes = [_vp, _u64p, _u32p, _u64p, ctypes.c_size_t]
+    L.cuflye_kernel_launches.restype = S
+    L.cuflye_kernel_launches.argtypes = [_u64p]
     L.cuflye_last_timing.restype = S
     L.cuflye_last_timing.argtypes = [_vp, ctypes.POINTER(ctypes.c_double), _u64p, ctypes.c_size_t]
     _LIB = L
@@ -226,9 +228,9 @@ class CudaBackend:
         self._check(self._L.cuflye_set_batch_queries(self._h, int(n)))
 
     def last_timing(self) -> tuple[list[float], list[int]]:
-        ms = (ctypes.c_double * 5)()
-        by = (ctypes.c_uint64 * 5)()
-        self._check(self._L.cuflye_last_timing(self._h, ms, by, 5))
+        ms = (ctypes.c_double * 7)()
+        by = (ctypes.c_uint64 * 7)()
+        self._check(self._L.cuflye_last_timing(self._h, ms, by, 7))
         return list(ms), list(by)
 
     # -- index

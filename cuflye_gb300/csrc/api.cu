@@ -591,7 +591,7 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
   const uint32_t nq = ps.nq;
   uint32_t* lscr = buf<uint32_t>(c, "s_l", H + 1);
   uint32_t* rscr = buf<uint32_t>(c, "s_r", H + 1);
-  uint32_t* lists = buf<uint32_t>(c, "s_lists", 3ull * std::max<uint64_t>(nq, 1));
+  uint32_t* lists = buf<uint32_t>(c, "s_lists", 4ull * std::max<uint64_t>(nq, 1));
   uint32_t* scounts = buf<uint32_t>(c, "s_counts", 4);
   // 1. KmerMatch sort per query: (ext id, cur pos) with libstdc++ order
   uint64_t* qb = buf<uint64_t>(c, "s_qb", nq + 1);
@@ -616,7 +616,7 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
                                   ext_list, dp_list, gcounts, st));
   uint64_t* sb = buf<uint64_t>(c, "g_sb", G);
   uint64_t* se = buf<uint64_t>(c, "g_se", G);
-  uint32_t* glists = buf<uint32_t>(c, "g_lists", 3 * std::max<uint64_t>(G, 1));
+  uint32_t* glists = buf<uint32_t>(c, "g_lists", 4 * std::max<uint64_t>(G, 1));
   const uint32_t G32 = static_cast<uint32_t>(G);
   // 3. ext-sorted groups: re-sort by ext pos
   CUFLYE_CHECK(groups_prepare_ext_sort(ps.keys, ps.vals, groups, ext_list, gcounts, sb, se, st));
@@ -1059,7 +1059,7 @@ cuflye_status cuflye_read_to_graph(cuflye_ctx* c, size_t n, const int64_t* ids,
     CUFLYE_CHECK(r2g_sort_keys(aln, d_aoff, nq, skeys, svals, st));
     uint32_t* sl = buf<uint32_t>(c, "r_sl", A + 1);
     uint32_t* sr = buf<uint32_t>(c, "r_sr", A + 1);
-    uint32_t* slists = buf<uint32_t>(c, "r_slists", 3ull * nq);
+    uint32_t* slists = buf<uint32_t>(c, "r_slists", 4ull * nq);
     uint32_t* scounts = buf<uint32_t>(c, "r_scounts", 4);
     CUFLYE_CHECK(segmented_std_sort(skeys, svals, sl, sr, d_aoff, d_aoff + 1, nq, nullptr, slists,
                                     scounts, c->num_sms, st));
@@ -1131,7 +1131,7 @@ cuflye_status cuflye_std_sort_segments(cuflye_ctx* c, uint64_t* keys, uint32_t* 
   uint32_t* dl = buf<uint32_t>(c, "t_l", m + 1);
   uint32_t* dr = buf<uint32_t>(c, "t_r", m + 1);
   uint64_t* off = buf<uint64_t>(c, "t_off", n_segments + 1);
-  uint32_t* lists = buf<uint32_t>(c, "t_lists", 3 * n_segments);
+  uint32_t* lists = buf<uint32_t>(c, "t_lists", 4 * n_segments);
   uint32_t* counts = buf<uint32_t>(c, "t_counts", 4);
   std::vector<uint64_t> rel(n_segments + 1);
   for (size_t s = 0; s <= n_segments; ++s) rel[s] = seg_offsets[s] - base;

@@ -23,7 +23,7 @@ cudaError_t exclusive_scan_u64(const uint64_t* in, uint64_t* out, uint64_t n, ui
 
 // ---------------------------------------------------------------- sort
 size_t segsort_smem_bytes();
-// lists: 3 * nseg words; counts: 3 words.  l/r scratch: one word per element.
+// lists: 4 * nseg words; counts: 4 words.  l/r scratch: one word per element.
 // nseg_dev (optional) holds the live segment count on the device (<= nseg).
 cudaError_t segmented_std_sort(uint64_t* keys, uint32_t* vals, uint32_t* lscratch,
                                uint32_t* rscratch, const uint64_t* begin, const uint64_t* end,

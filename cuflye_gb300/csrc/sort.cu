@@ -1,20 +1,20 @@
-// sort.cu — segmented libstdc++-order sort and stable LSD radix sort.
+// sort.cu — segmented sort of (u64 key, u32 value) pairs in libstdc++ std::sort
+// order (see introsort.cuh for why and for the parallel partition).
 //
-// segmented_std_sort(): every segment [begin[s], end[s]) of (key, value)
-// pairs is put in exactly the order libstdc++'s std::sort with `key < key`
-// gives (introsort.cuh explains the parallel formulation).  Segments are
-// classified by size:
-//   * <= kSerialMax elements: one thread runs the serial algorithm;
-//   * <= kSmemCap: one CTA loads the segment into shared memory, partitions
-//     block-wide while tasks are large and finishes small tasks per thread;
-//   * larger: one CTA partitions in global memory (prefix counts tiled over
-//     the task) until tasks fit in shared memory.
-//
-// radix_sort_pairs(): stable least-significant-digit radix sort of
-// (u64 key, u64 value) on a digit range, 8 bits per pass; used to build the
-// k-mer index with entries in (key, stored id, stored position) order.
+// Segments are classified by size and sorted by four kernels:
+//   * <= kTiny elements:      one thread runs the serial algorithm;
+//   * <= kWarpSeg elements:   one warp, segment staged in its own shared-memory
+//                             slice, partitions by warp ballots, leaves per lane;
+//   * <= kCap elements:       one CTA, segment in shared memory; block-wide
+//                             partitions while tasks exceed kWarpMax, then all
+//                             16 warps partition different tasks concurrently
+//                             (level by level), then one thread per leaf task;
+//   * larger:                 one CTA partitions in global memory until its
+//                             tasks fit kCap, then finishes each in shared memory.
+// Every partition is a single pass: L stoppers get ranks from the left, R
+// stoppers left ranks too (the k-th R stopper from the right is the
+// (TR - k)-th from the left), so a partition reads its keys once.
 #include <cstdint>
-#include <cstdio>
 
 #include "common.cuh"
 #include "introsort.cuh"
@@ -24,30 +24,75 @@ namespace cuflye {
 namespace {
 
 constexpr int kBlock = 512;
-constexpr uint32_t kSmemCap = 8192;
-constexpr uint32_t kSerialMax = 128;
-constexpr int kMaxTasks = 96;
-constexpr int kMaxSerial = 256;
+constexpr int kWarps = kBlock / 32;
+constexpr uint32_t kCap = 8192;       // CTA shared-memory segment capacity
+constexpr uint32_t kWarpMax = 2048;   // tasks up to this size go to single warps
+constexpr uint32_t kSerial = 32;      // tasks up to this size go to single threads
+constexpr uint32_t kTiny = 64;        // segments up to this size: thread kernel
+constexpr uint32_t kWarpSeg = 2048;   // segments up to this size: warp kernel
+constexpr int kWarpSegWarps = 6;      // warps per CTA in the warp kernel
+constexpr int kMaxWarpTasks = 256;    // disjoint tasks > kSerial in kCap elements
+constexpr int kMaxSerial = 1024;
+constexpr int kSerialFlush = 512;
 
-struct SortSmem {
-  uint64_t K[kSmemCap];
-  uint32_t V[kSmemCap];
-  uint32_t L[kSmemCap + 1];
-  uint32_t R[kSmemCap + 1];
-  uint32_t tf[kMaxTasks], tl[kMaxTasks];
-  int td[kMaxTasks];
-  uint32_t sf[kMaxSerial], sl[kMaxSerial];
-  int sd[kMaxSerial];
-  uint64_t warp_sums[kBlock / 32 + 1];
-  int ntask, nserial;
+// ---------------------------------------------------------------- partitions
+
+// Warp-wide unguarded partition of [f, l) (l - f > 16).  Rank maps: the k-th L
+// stopper (k >= 1) at Lr[f + k - 1], the j-th R stopper from the left (j >= 0)
+// at Rr[f + j]; both stay inside [f, l).
+template <typename RT>
+__device__ uint32_t warp_partition(uint64_t* K, uint32_t* V, RT* Lr, RT* Rr, uint32_t f,
+                                   uint32_t l) {
+  const int lane = threadIdx.x & 31;
+  if (lane == 0) isort::median_to_first(K, V, f, f + 1, f + (l - f) / 2, l - 1);
+  __syncwarp();
+  const uint64_t p = K[f];
+  const unsigned lt = (1u << lane) - 1u;
+  uint32_t tl = 0, tr = 0;
+  for (uint32_t base = f; base < l; base += 32) {
+    const uint32_t i = base + lane;
+    const bool valid = i < l;
+    const uint64_t k = valid ? K[i] : 0;
+    const bool isL = valid && i > f && !(k < p);
+    const bool isR = valid && !(p < k);
+    const unsigned bl = __ballot_sync(0xffffffffu, isL);
+    const unsigned br = __ballot_sync(0xffffffffu, isR);
+    if (isL) Lr[f + tl + __popc(bl & lt)] = static_cast<RT>(i);
+    if (isR) Rr[f + tr + __popc(br & lt)] = static_cast<RT>(i);
+    tl += __popc(bl);
+    tr += __popc(br);
+  }
+  __syncwarp();
+  // m = largest k with l_k < r_k, l_k = Lr[f + k - 1], r_k = Rr[f + tr - k]
+  uint32_t lo = 0, hi = tl < tr ? tl : tr;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi + 1) >> 1;
+    if (static_cast<uint32_t>(Lr[f + mid - 1]) < static_cast<uint32_t>(Rr[f + tr - mid]))
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  const uint32_t m = lo;
+  uint32_t cut;
+  if (m == 0) {
+    cut = Lr[f];
+  } else {
+    cut = Rr[f + tr - m];
+    if (m + 1 <= tl && static_cast<uint32_t>(Lr[f + m]) < cut) cut = Lr[f + m];
+  }
+  __syncwarp();
+  for (uint32_t k = 1 + lane; k <= m; k += 32) isort::swap_kv(K, V, Lr[f + k - 1], Rr[f + tr - k]);
+  __syncwarp();
+  return cut;
+}
+
+struct BlockScratch {
+  uint64_t warp_sums[kWarps + 1];
   uint32_t scalar[4];
 };
 
-// Exclusive block scan of a packed pair of 32-bit counters; returns the
-// exclusive prefix and the block total (to every thread).
-__device__ __forceinline__ uint64_t block_exclusive_scan(uint64_t v, uint64_t* warp_sums,
+__device__ __forceinline__ uint64_t block_exclusive_scan(uint64_t v, BlockScratch& bs,
                                                          uint64_t* total) {
-  constexpr int kWarps = kBlock / 32;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint64_t inc = v;
 #pragma unroll
@@ -55,69 +100,36 @@ __device__ __forceinline__ uint64_t block_exclusive_scan(uint64_t v, uint64_t* w
     const uint64_t o = __shfl_up_sync(0xffffffffu, inc, d);
     if (lane >= d) inc += o;
   }
-  if (lane == 31) warp_sums[warp] = inc;
+  if (lane == 31) bs.warp_sums[warp] = inc;
   __syncthreads();
   if (warp == 0) {
-    const uint64_t w = lane < kWarps ? warp_sums[lane] : 0;
+    const uint64_t w = lane < kWarps ? bs.warp_sums[lane] : 0;
     uint64_t wi = w;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
       const uint64_t o = __shfl_up_sync(0xffffffffu, wi, d);
       if (lane >= d) wi += o;
     }
-    if (lane < kWarps) warp_sums[lane] = wi - w;
-    if (lane == kWarps - 1) warp_sums[kWarps] = wi;
+    if (lane < kWarps) bs.warp_sums[lane] = wi - w;
+    if (lane == kWarps - 1) bs.warp_sums[kWarps] = wi;
   }
   __syncthreads();
-  const uint64_t r = warp_sums[warp] + inc - v;
-  *total = warp_sums[kWarps];
+  const uint64_t r = bs.warp_sums[warp] + inc - v;
+  *total = bs.warp_sums[kWarps];
   __syncthreads();
   return r;
 }
 
-// Largest m in [0, hi] with L[m] < R[m] (L[0] = 0 < R[0] = inf by convention).
-__device__ __forceinline__ uint32_t find_swaps(const uint32_t* L, const uint32_t* R,
-                                               uint32_t hi) {
-  uint32_t lo = 0;
-  while (lo < hi) {
-    const uint32_t mid = (lo + hi + 1) >> 1;
-    if (L[mid] < R[mid])
-      lo = mid;
-    else
-      hi = mid - 1;
-  }
-  return lo;
-}
-
-// Block-wide unguarded partition of [f, l) (shared or global arrays; L and R
-// are 1-based rank -> position maps with room for l - f + 1 entries).
-__device__ uint32_t block_partition(uint64_t* K, uint32_t* V, uint32_t* L, uint32_t* R,
-                                    uint32_t f, uint32_t l, SortSmem& sm) {
+// Block-wide unguarded partition of [f, l), one pass over the keys in tiles
+// of kBlock * 16 (each thread owns 16 consecutive positions of a tile).
+template <typename RT>
+__device__ uint32_t block_partition(uint64_t* K, uint32_t* V, RT* Lr, RT* Rr, uint32_t f,
+                                    uint32_t l, BlockScratch& bs) {
   if (threadIdx.x == 0) isort::median_to_first(K, V, f, f + 1, f + (l - f) / 2, l - 1);
   __syncthreads();
   const uint64_t p = K[f];
-  const uint32_t n = l - f;
-  const uint32_t tile = kBlock * 16u;
-  // pass 1: totals
-  {
-    uint32_t cl = 0, cr = 0;
-    for (uint32_t i = f + threadIdx.x; i < l; i += kBlock) {
-      const uint64_t k = K[i];
-      cl += (i > f) && !(k < p);
-      cr += !(p < k);
-    }
-    uint64_t tot;
-    block_exclusive_scan((static_cast<uint64_t>(cl) << 32) | cr, sm.warp_sums, &tot);
-    if (threadIdx.x == 0) {
-      sm.scalar[0] = static_cast<uint32_t>(tot >> 32);
-      sm.scalar[1] = static_cast<uint32_t>(tot & 0xffffffffu);
-    }
-    __syncthreads();
-  }
-  const uint32_t TL = sm.scalar[0], TR = sm.scalar[1];
-  // pass 2: ranks, tile by tile, each thread owning 16 consecutive items
-  uint64_t carry = 0;
-  for (uint32_t t0 = f; t0 < l; t0 += tile) {
+  uint64_t carry = 0;  // (L count << 32) | R count before the tile
+  for (uint32_t t0 = f; t0 < l; t0 += kBlock * 16u) {
     const uint32_t a = t0 + threadIdx.x * 16u;
     uint32_t cl = 0, cr = 0;
     for (uint32_t i = a; i < a + 16u && i < l; ++i) {
@@ -126,108 +138,156 @@ __device__ uint32_t block_partition(uint64_t* K, uint32_t* V, uint32_t* L, uint3
       cr += !(p < k);
     }
     uint64_t tile_tot;
-    const uint64_t ex = block_exclusive_scan((static_cast<uint64_t>(cl) << 32) | cr,
-                                             sm.warp_sums, &tile_tot);
-    if (threadIdx.x == 0) {
-      sm.scalar[2] = static_cast<uint32_t>(tile_tot >> 32);
-      sm.scalar[3] = static_cast<uint32_t>(tile_tot & 0xffffffffu);
-    }
-    uint32_t rl = static_cast<uint32_t>((carry + ex) >> 32);
-    uint32_t rr = static_cast<uint32_t>((carry + ex) & 0xffffffffu);
+    const uint64_t ex = carry + block_exclusive_scan((static_cast<uint64_t>(cl) << 32) | cr, bs,
+                                                     &tile_tot);
+    uint32_t rl = static_cast<uint32_t>(ex >> 32);
+    uint32_t rr = static_cast<uint32_t>(ex & 0xffffffffu);
     for (uint32_t i = a; i < a + 16u && i < l; ++i) {
       const uint64_t k = K[i];
-      if ((i > f) && !(k < p)) L[++rl] = i;
-      if (!(p < k)) {
-        R[TR - rr] = i;
-        ++rr;
-      }
+      if ((i > f) && !(k < p)) Lr[f + rl++] = static_cast<RT>(i);
+      if (!(p < k)) Rr[f + rr++] = static_cast<RT>(i);
     }
-    __syncthreads();
-    carry += (static_cast<uint64_t>(sm.scalar[2]) << 32) | sm.scalar[3];
-    __syncthreads();
+    carry += tile_tot;
   }
+  __syncthreads();
+  const uint32_t tl = static_cast<uint32_t>(carry >> 32);
+  const uint32_t tr = static_cast<uint32_t>(carry & 0xffffffffu);
   if (threadIdx.x == 0) {
-    const uint32_t hi = TL < TR ? TL : TR;
-    const uint32_t m = find_swaps(L, R, hi);
+    uint32_t lo = 0, hi = tl < tr ? tl : tr;
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi + 1) >> 1;
+      if (static_cast<uint32_t>(Lr[f + mid - 1]) < static_cast<uint32_t>(Rr[f + tr - mid]))
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    const uint32_t m = lo;
     uint32_t cut;
     if (m == 0) {
-      cut = L[1];
+      cut = Lr[f];
     } else {
-      cut = R[m];
-      if (m + 1 <= TL && L[m + 1] < cut) cut = L[m + 1];
+      cut = Rr[f + tr - m];
+      if (m + 1 <= tl && static_cast<uint32_t>(Lr[f + m]) < cut) cut = Lr[f + m];
     }
-    sm.scalar[0] = m;
-    sm.scalar[1] = cut;
+    bs.scalar[0] = m;
+    bs.scalar[1] = cut;
   }
   __syncthreads();
-  const uint32_t m = sm.scalar[0], cut = sm.scalar[1];
-  for (uint32_t k = 1 + threadIdx.x; k <= m; k += kBlock) isort::swap_kv(K, V, L[k], R[k]);
+  const uint32_t m = bs.scalar[0], cut = bs.scalar[1];
+  for (uint32_t k = 1 + threadIdx.x; k <= m; k += kBlock)
+    isort::swap_kv(K, V, Lr[f + k - 1], Rr[f + tr - k]);
   __syncthreads();
-  (void)n;
   return cut;
 }
 
-// Sorts [0, n) held in shared memory starting at recursion budget depth0.
-__device__ void smem_sort(SortSmem& sm, uint32_t n, int depth0) {
-  if (threadIdx.x == 0) {
-    sm.ntask = 0;
-    sm.nserial = 0;
-    sm.tf[0] = 0;
-    sm.tl[0] = n;
-    sm.td[0] = depth0;
-    sm.ntask = 1;
+// ---------------------------------------------------------------- CTA sort
+
+struct CtaSmem {
+  uint64_t K[kCap];
+  uint32_t V[kCap];
+  uint16_t Lr[kCap];
+  uint16_t Rr[kCap];
+  uint32_t bf[64], bl[64];
+  int bd[64];
+  uint32_t wf[2][kMaxWarpTasks], wl[2][kMaxWarpTasks];
+  int wd[2][kMaxWarpTasks];
+  uint32_t sf[kMaxSerial], sl[kMaxSerial];
+  int sd[kMaxSerial];
+  int nb, wn[2], ns;
+  BlockScratch bs;
+};
+
+// Routes a task to the serial list, the next warp round or the block stack.
+// Called by one thread (block phase) or one lane (warp phase); lists are
+// appended with atomics because several warps add concurrently.
+__device__ __forceinline__ void route_task(CtaSmem& sm, int next, uint32_t f, uint32_t l, int d) {
+  const uint32_t n = l - f;
+  if (n <= 1) return;
+  if (n <= kSerial || d == 0) {
+    const int s = atomicAdd(&sm.ns, 1);
+    sm.sf[s] = f;
+    sm.sl[s] = l;
+    sm.sd[s] = d;
+  } else if (n <= kWarpMax) {
+    const int s = atomicAdd(&sm.wn[next], 1);
+    sm.wf[next][s] = f;
+    sm.wl[next][s] = l;
+    sm.wd[next][s] = d;
+  } else {
+    const int s = atomicAdd(&sm.nb, 1);
+    sm.bf[s] = f;
+    sm.bl[s] = l;
+    sm.bd[s] = d;
   }
-  __syncthreads();
-  for (;;) {
-    const int nt = sm.ntask;
-    if (nt == 0) break;
-    const uint32_t f = sm.tf[nt - 1], l = sm.tl[nt - 1];
-    const int d = sm.td[nt - 1];
-    __syncthreads();
-    if (l - f <= kSerialMax || d == 0) {
-      if (threadIdx.x == 0) {
-        sm.ntask = nt - 1;
-        sm.sf[sm.nserial] = f;
-        sm.sl[sm.nserial] = l;
-        sm.sd[sm.nserial] = d;
-        ++sm.nserial;
-      }
-      __syncthreads();
-      if (sm.nserial == kMaxSerial) {
-        // the ranges are disjoint, so finishing them early changes nothing
-        for (int s = threadIdx.x; s < kMaxSerial; s += kBlock)
-          isort::serial_introsort(sm.K, sm.V, sm.sf[s], sm.sl[s], sm.sd[s]);
-        __syncthreads();
-        if (threadIdx.x == 0) sm.nserial = 0;
-        __syncthreads();
-      }
-      continue;
-    }
-    const uint32_t cut = block_partition(sm.K, sm.V, sm.L, sm.R, f, l, sm);
-    if (threadIdx.x == 0) {
-      sm.tf[nt - 1] = cut;
-      sm.tl[nt - 1] = l;
-      sm.td[nt - 1] = d - 1;
-      sm.tf[nt] = f;
-      sm.tl[nt] = cut;
-      sm.td[nt] = d - 1;
-      sm.ntask = nt + 1;
-    }
-    __syncthreads();
-  }
-  for (int s = threadIdx.x; s < sm.nserial; s += kBlock)
+}
+
+__device__ __forceinline__ void flush_serial(CtaSmem& sm) {
+  for (int s = threadIdx.x; s < sm.ns; s += kBlock)
     isort::serial_introsort(sm.K, sm.V, sm.sf[s], sm.sl[s], sm.sd[s]);
+  __syncthreads();
+  if (threadIdx.x == 0) sm.ns = 0;
   __syncthreads();
 }
 
-__device__ void load_sort_store(uint64_t* K, uint32_t* V, uint64_t begin, uint32_t n, int depth,
-                                SortSmem& sm) {
+// Sorts sm.K/sm.V[0, n) from recursion budget depth0.
+__device__ void cta_sort(CtaSmem& sm, uint32_t n, int depth0) {
+  if (threadIdx.x == 0) {
+    sm.nb = 0;
+    sm.wn[0] = 0;
+    sm.wn[1] = 0;
+    sm.ns = 0;
+    route_task(sm, 0, 0, n, depth0);
+  }
+  __syncthreads();
+  // block phase: tasks larger than kWarpMax, one at a time
+  for (;;) {
+    const int nb = sm.nb;
+    if (nb == 0) break;
+    const uint32_t f = sm.bf[nb - 1], l = sm.bl[nb - 1];
+    const int d = sm.bd[nb - 1];
+    __syncthreads();
+    if (threadIdx.x == 0) sm.nb = nb - 1;
+    const uint32_t cut = block_partition<uint16_t>(sm.K, sm.V, sm.Lr, sm.Rr, f, l, sm.bs);
+    if (threadIdx.x == 0) {
+      route_task(sm, 0, f, cut, d - 1);
+      route_task(sm, 0, cut, l, d - 1);
+    }
+    __syncthreads();
+    if (sm.ns > kSerialFlush) flush_serial(sm);
+  }
+  // warp phase: level by level, every warp takes different tasks
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int cur = 0;
+  for (;;) {
+    const int cnt = sm.wn[cur];
+    if (cnt == 0) break;
+    if (threadIdx.x == 0) sm.wn[cur ^ 1] = 0;
+    __syncthreads();
+    for (int t = warp; t < cnt; t += kWarps) {
+      const uint32_t f = sm.wf[cur][t], l = sm.wl[cur][t];
+      const int d = sm.wd[cur][t];
+      const uint32_t cut = warp_partition<uint16_t>(sm.K, sm.V, sm.Lr, sm.Rr, f, l);
+      if (lane == 0) {
+        route_task(sm, cur ^ 1, f, cut, d - 1);
+        route_task(sm, cur ^ 1, cut, l, d - 1);
+      }
+      __syncwarp();
+    }
+    __syncthreads();
+    if (sm.ns > kSerialFlush) flush_serial(sm);
+    cur ^= 1;
+  }
+  flush_serial(sm);
+}
+
+__device__ void cta_load_sort_store(uint64_t* K, uint32_t* V, uint64_t begin, uint32_t n,
+                                    int depth, CtaSmem& sm) {
   for (uint32_t i = threadIdx.x; i < n; i += kBlock) {
     sm.K[i] = K[begin + i];
     sm.V[i] = V[begin + i];
   }
   __syncthreads();
-  smem_sort(sm, n, depth);
+  cta_sort(sm, n, depth);
   for (uint32_t i = threadIdx.x; i < n; i += kBlock) {
     K[begin + i] = sm.K[i];
     V[begin + i] = sm.V[i];
@@ -235,21 +295,26 @@ __device__ void load_sort_store(uint64_t* K, uint32_t* V, uint64_t begin, uint32
   __syncthreads();
 }
 
+// ---------------------------------------------------------------- kernels
+
 __global__ void classify_segments(const uint64_t* __restrict__ begin,
                                   const uint64_t* __restrict__ end, uint32_t nseg,
-                                  const uint32_t* __restrict__ nseg_dev, uint32_t* tiny,
-                                  uint32_t* mid, uint32_t* big, uint32_t* counts) {
+                                  const uint32_t* __restrict__ nseg_dev, uint32_t* lists,
+                                  uint32_t* counts) {
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nseg || (nseg_dev && s >= *nseg_dev)) return;
   const uint64_t n = end[s] - begin[s];
   if (n <= 1) return;
-  if (n <= kSerialMax) {
-    tiny[atomicAdd(&counts[0], 1u)] = s;
-  } else if (n <= kSmemCap) {
-    mid[atomicAdd(&counts[1], 1u)] = s;
-  } else {
-    big[atomicAdd(&counts[2], 1u)] = s;
-  }
+  int c;
+  if (n <= kTiny)
+    c = 0;
+  else if (n <= kWarpSeg)
+    c = 1;
+  else if (n <= kCap)
+    c = 2;
+  else
+    c = 3;
+  lists[static_cast<size_t>(c) * nseg + atomicAdd(&counts[c], 1u)] = s;
 }
 
 __global__ void sort_tiny(uint64_t* K, uint32_t* V, const uint64_t* __restrict__ begin,
@@ -265,19 +330,101 @@ __global__ void sort_tiny(uint64_t* K, uint32_t* V, const uint64_t* __restrict__
   }
 }
 
-__global__ void __launch_bounds__(kBlock) sort_mid(uint64_t* K, uint32_t* V,
+struct WarpSlice {
+  uint64_t K[kWarpSeg];
+  uint32_t V[kWarpSeg];
+  uint16_t Lr[kWarpSeg];
+  uint16_t Rr[kWarpSeg];
+  uint32_t sf[64], sl[64];
+  int sd[64];
+};
+
+// One warp per segment of (kTiny, kWarpSeg] elements.
+__global__ void __launch_bounds__(kWarpSegWarps * 32) sort_warp(
+    uint64_t* K, uint32_t* V, const uint64_t* __restrict__ begin,
+    const uint64_t* __restrict__ end, const uint32_t* __restrict__ list,
+    const uint32_t* __restrict__ counts) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  WarpSlice& ws = reinterpret_cast<WarpSlice*>(smem_raw)[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  const uint32_t cnt = counts[1];
+  const uint32_t nwarps = gridDim.x * kWarpSegWarps;
+  for (uint32_t li = blockIdx.x * kWarpSegWarps + (threadIdx.x >> 5); li < cnt; li += nwarps) {
+    const uint32_t s = list[li];
+    const uint64_t b = begin[s];
+    const uint32_t n = static_cast<uint32_t>(end[s] - b);
+    for (uint32_t i = lane; i < n; i += 32) {
+      ws.K[i] = K[b + i];
+      ws.V[i] = V[b + i];
+    }
+    __syncwarp();
+    // task stack (identical in every lane) and a per-warp leaf list
+    uint32_t tf[40], tl[40];
+    int td[40];
+    int top = 0, ns = 0;
+    tf[0] = 0;
+    tl[0] = n;
+    td[0] = isort::depth_limit(n);
+    top = 1;
+    while (top > 0) {
+      --top;
+      const uint32_t f = tf[top], l = tl[top];
+      const int d = td[top];
+      if (l - f <= kSerial || d == 0) {
+        if (lane == 0) {
+          ws.sf[ns] = f;
+          ws.sl[ns] = l;
+          ws.sd[ns] = d;
+        }
+        ++ns;
+        if (ns == 64) {
+          __syncwarp();
+          for (int t = lane; t < ns; t += 32)
+            isort::serial_introsort(ws.K, ws.V, ws.sf[t], ws.sl[t], ws.sd[t]);
+          __syncwarp();
+          ns = 0;
+        }
+        continue;
+      }
+      const uint32_t cut = warp_partition<uint16_t>(ws.K, ws.V, ws.Lr, ws.Rr, f, l);
+      if (cut - f > 1) {
+        tf[top] = f;
+        tl[top] = cut;
+        td[top] = d - 1;
+        ++top;
+      }
+      if (l - cut > 1) {
+        tf[top] = cut;
+        tl[top] = l;
+        td[top] = d - 1;
+        ++top;
+      }
+    }
+    __syncwarp();
+    for (int t = lane; t < ns; t += 32)
+      isort::serial_introsort(ws.K, ws.V, ws.sf[t], ws.sl[t], ws.sd[t]);
+    __syncwarp();
+    for (uint32_t i = lane; i < n; i += 32) {
+      K[b + i] = ws.K[i];
+      V[b + i] = ws.V[i];
+    }
+    __syncwarp();
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) sort_cta(uint64_t* K, uint32_t* V,
                                                    const uint64_t* __restrict__ begin,
                                                    const uint64_t* __restrict__ end,
                                                    const uint32_t* __restrict__ list,
                                                    const uint32_t* __restrict__ counts) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  SortSmem& sm = *reinterpret_cast<SortSmem*>(smem_raw);
-  const uint32_t cnt = counts[1];
+  CtaSmem& sm = *reinterpret_cast<CtaSmem*>(smem_raw);
+  const uint32_t cnt = counts[2];
   for (uint32_t i = blockIdx.x; i < cnt; i += gridDim.x) {
     const uint32_t s = list[i];
     const uint64_t b = begin[s];
     const uint32_t n = static_cast<uint32_t>(end[s] - b);
-    load_sort_store(K, V, b, n, isort::depth_limit(n), sm);
+    cta_load_sort_store(K, V, b, n, isort::depth_limit(n), sm);
   }
 }
 
@@ -288,19 +435,18 @@ __global__ void __launch_bounds__(kBlock) sort_big(uint64_t* K, uint32_t* V, uin
                                                    const uint32_t* __restrict__ list,
                                                    const uint32_t* __restrict__ counts) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  SortSmem& sm = *reinterpret_cast<SortSmem*>(smem_raw);
-  __shared__ uint32_t gf[kMaxTasks], gl[kMaxTasks];
-  __shared__ int gd[kMaxTasks];
+  CtaSmem& sm = *reinterpret_cast<CtaSmem*>(smem_raw);
+  __shared__ uint32_t gf[96], gl[96];
+  __shared__ int gd[96];
   __shared__ int gn;
-  const uint32_t cnt = counts[2];
+  const uint32_t cnt = counts[3];
   for (uint32_t i = blockIdx.x; i < cnt; i += gridDim.x) {
     const uint32_t s = list[i];
     const uint64_t b = begin[s];
     const uint32_t n = static_cast<uint32_t>(end[s] - b);
     uint64_t* Ks = K + b;
     uint32_t* Vs = V + b;
-    // rank maps share the segment's index range in the scratch arrays
-    uint32_t* Ls = Lg + b;
+    uint32_t* Ls = Lg + b;  // rank maps share the segment's index range
     uint32_t* Rs = Rg + b;
     if (threadIdx.x == 0) {
       gf[0] = 0;
@@ -315,10 +461,10 @@ __global__ void __launch_bounds__(kBlock) sort_big(uint64_t* K, uint32_t* V, uin
       const uint32_t f = gf[nt - 1], l = gl[nt - 1];
       const int d = gd[nt - 1];
       __syncthreads();
-      if (l - f <= kSmemCap) {
+      if (l - f <= kCap) {
         if (threadIdx.x == 0) gn = nt - 1;
         __syncthreads();
-        if (l - f > 1) load_sort_store(Ks, Vs, f, l - f, d, sm);
+        if (l - f > 1) cta_load_sort_store(Ks, Vs, f, l - f, d, sm);
         continue;
       }
       if (d == 0) {
@@ -329,10 +475,7 @@ __global__ void __launch_bounds__(kBlock) sort_big(uint64_t* K, uint32_t* V, uin
         __syncthreads();
         continue;
       }
-      // rank maps are indexed from the task start
-      // rank k of this task lives at index f - 1 + k, inside [f, l)
-      const int64_t rb = static_cast<int64_t>(f) - 1;
-      const uint32_t cut = block_partition(Ks, Vs, Ls + rb, Rs + rb, f, l, sm);
+      const uint32_t cut = block_partition<uint32_t>(Ks, Vs, Ls, Rs, f, l, sm.bs);
       if (threadIdx.x == 0) {
         gf[nt - 1] = cut;
         gl[nt - 1] = l;
@@ -347,126 +490,9 @@ __global__ void __launch_bounds__(kBlock) sort_big(uint64_t* K, uint32_t* V, uin
   }
 }
 
-// ---------------------------------------------------------------- radix sort
-
-constexpr int kRadixBlock = 256;
-constexpr int kRadixItems = 16;  // items per thread per tile
-constexpr uint32_t kRadixTile = kRadixBlock * kRadixItems;
-
-__device__ __forceinline__ uint32_t digit_of(uint64_t key, uint64_t val, int d) {
-  // digits 0..7: value bytes (least significant first); 8..15: key bytes
-  return d < 8 ? static_cast<uint32_t>((val >> (8 * d)) & 0xffu)
-               : static_cast<uint32_t>((key >> (8 * (d - 8))) & 0xffu);
-}
-
-__global__ void radix_histogram(const uint64_t* __restrict__ keys,
-                                const uint64_t* __restrict__ vals, uint64_t n, int d,
-                                uint32_t* __restrict__ hist, uint32_t ntiles) {
-  __shared__ uint32_t h[256];
-  for (int i = threadIdx.x; i < 256; i += blockDim.x) h[i] = 0;
-  __syncthreads();
-  const uint64_t t0 = static_cast<uint64_t>(blockIdx.x) * kRadixTile;
-  for (uint32_t j = threadIdx.x; j < kRadixTile; j += blockDim.x) {
-    const uint64_t i = t0 + j;
-    if (i < n) atomicAdd(&h[digit_of(keys[i], vals[i], d)], 1u);
-  }
-  __syncthreads();
-  for (int b = threadIdx.x; b < 256; b += blockDim.x) hist[b * ntiles + blockIdx.x] = h[b];
-}
-
-// Exclusive scan over the digit-major histogram (256 * ntiles counters) by
-// one block; counts fit 32 bits because a pass covers < 2^32 elements.
-__global__ void radix_scan(uint32_t* hist, uint32_t total) {
-  __shared__ uint32_t carry;
-  if (threadIdx.x == 0) carry = 0;
-  __syncthreads();
-  for (uint32_t base = 0; base < total; base += blockDim.x) {
-    const uint32_t i = base + threadIdx.x;
-    const uint32_t v = i < total ? hist[i] : 0;
-    uint32_t inc = v;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int dd = 1; dd < 32; dd <<= 1) {
-      const uint32_t o = __shfl_up_sync(0xffffffffu, inc, dd);
-      if (lane >= dd) inc += o;
-    }
-    __shared__ uint32_t ws[32];
-    if (lane == 31) ws[warp] = inc;
-    __syncthreads();
-    if (warp == 0) {
-      const uint32_t nw = blockDim.x / 32;
-      uint32_t w = lane < static_cast<int>(nw) ? ws[lane] : 0;
-      uint32_t wi = w;
-      for (int dd = 1; dd < 32; dd <<= 1) {
-        const uint32_t o = __shfl_up_sync(0xffffffffu, wi, dd);
-        if (lane >= dd) wi += o;
-      }
-      if (lane < static_cast<int>(nw)) ws[lane] = wi - w;
-    }
-    __syncthreads();
-    const uint32_t ex = carry + ws[warp] + inc - v;
-    if (i < total) hist[i] = ex;
-    __syncthreads();
-    if (threadIdx.x == blockDim.x - 1) carry = ex + v;
-    __syncthreads();
-  }
-}
-
-// Stable scatter: within a tile, elements keep their order per digit.  Each
-// warp ranks its 32-element chunks with match_any, chunks are visited in
-// order, and per-digit running offsets live in shared memory.
-__global__ void radix_scatter(const uint64_t* __restrict__ keys_in,
-                              const uint64_t* __restrict__ vals_in, uint64_t* __restrict__ keys_out,
-                              uint64_t* __restrict__ vals_out, uint64_t n, int d,
-                              const uint32_t* __restrict__ hist, uint32_t ntiles) {
-  __shared__ uint32_t base[256];
-  __shared__ uint32_t wcount[kRadixBlock / 32][256];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  constexpr int nwarps = kRadixBlock / 32;
-  for (int b = threadIdx.x; b < 256; b += blockDim.x) base[b] = hist[b * ntiles + blockIdx.x];
-  const uint64_t t0 = static_cast<uint64_t>(blockIdx.x) * kRadixTile;
-  // The tile is processed in rounds of nwarps*32 consecutive elements;
-  // within a round warp w owns elements [w*32, w*32+32).
-  for (uint32_t r0 = 0; r0 < kRadixTile; r0 += nwarps * 32) {
-    for (int b = threadIdx.x; b < 256 * nwarps; b += blockDim.x)
-      wcount[b / 256][b % 256] = 0;
-    __syncthreads();
-    const uint64_t i = t0 + r0 + warp * 32 + lane;
-    const bool valid = i < n;
-    uint64_t k = 0, v = 0;
-    uint32_t dig = 0xffffffffu;
-    if (valid) {
-      k = keys_in[i];
-      v = vals_in[i];
-      dig = digit_of(k, v, d);
-    }
-    const uint32_t peers = __match_any_sync(0xffffffffu, dig);
-    const uint32_t rank_in_warp = __popc(peers & ((1u << lane) - 1u));
-    const int leader = __ffs(peers) - 1;
-    if (valid && lane == leader) wcount[warp][dig] = __popc(peers);
-    __syncthreads();
-    // exclusive prefix over warps for this element's digit
-    uint32_t before = 0;
-    if (valid)
-      for (int w = 0; w < warp; ++w) before += wcount[w][dig];
-    if (valid) {
-      const uint32_t dst = base[dig] + before + rank_in_warp;
-      keys_out[dst] = k;
-      vals_out[dst] = v;
-    }
-    __syncthreads();
-    // advance per-digit bases by this round's totals
-    for (int b = threadIdx.x; b < 256; b += blockDim.x) {
-      uint32_t s = 0;
-      for (int w = 0; w < nwarps; ++w) s += wcount[w][b];
-      base[b] += s;
-    }
-    __syncthreads();
-  }
-}
-
 }  // namespace
 
-size_t segsort_smem_bytes() { return sizeof(SortSmem); }
+size_t segsort_smem_bytes() { return sizeof(CtaSmem); }
 
 cudaError_t segmented_std_sort(uint64_t* keys, uint32_t* vals, uint32_t* lscratch,
                                uint32_t* rscratch, const uint64_t* begin, const uint64_t* end,
@@ -474,56 +500,33 @@ cudaError_t segmented_std_sort(uint64_t* keys, uint32_t* vals, uint32_t* lscratc
                                uint32_t* counts, int num_sms, cudaStream_t stream) {
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(sort_mid, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         static_cast<int>(sizeof(SortSmem)));
+    cudaFuncSetAttribute(sort_cta, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         static_cast<int>(sizeof(CtaSmem)));
     cudaFuncSetAttribute(sort_big, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         static_cast<int>(sizeof(SortSmem)));
+                         static_cast<int>(sizeof(CtaSmem)));
+    cudaFuncSetAttribute(sort_warp, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         static_cast<int>(sizeof(WarpSlice) * kWarpSegWarps));
     attr = true;
   }
   if (nseg == 0) return cudaSuccess;
-  cudaMemsetAsync(counts, 0, 3 * sizeof(uint32_t), stream);
-  uint32_t* tiny = lists;
-  uint32_t* mid = lists + nseg;
-  uint32_t* big = lists + 2 * static_cast<size_t>(nseg);
+  cudaMemsetAsync(counts, 0, 4 * sizeof(uint32_t), stream);
   count_launch();
-  classify_segments<<<(nseg + 255) / 256, 256, 0, stream>>>(begin, end, nseg, nseg_dev, tiny,
-                                                            mid, big, counts);
+  classify_segments<<<(nseg + 255) / 256, 256, 0, stream>>>(begin, end, nseg, nseg_dev, lists,
+                                                            counts);
   count_launch();
-  sort_tiny<<<num_sms * 4, 128, 0, stream>>>(keys, vals, begin, end, tiny, counts);
+  sort_tiny<<<num_sms * 4, 128, 0, stream>>>(keys, vals, begin, end, lists, counts);
   count_launch();
-  sort_mid<<<num_sms, kBlock, sizeof(SortSmem), stream>>>(keys, vals, begin, end, mid, counts);
+  sort_warp<<<num_sms, kWarpSegWarps * 32, sizeof(WarpSlice) * kWarpSegWarps, stream>>>(
+      keys, vals, begin, end, lists + nseg, counts);
   count_launch();
-  sort_big<<<num_sms, kBlock, sizeof(SortSmem), stream>>>(keys, vals, lscratch, rscratch, begin,
-                                                          end, big, counts);
+  sort_cta<<<num_sms, kBlock, sizeof(CtaSmem), stream>>>(keys, vals, begin, end,
+                                                         lists + 2 * static_cast<size_t>(nseg),
+                                                         counts);
+  count_launch();
+  sort_big<<<num_sms, kBlock, sizeof(CtaSmem), stream>>>(keys, vals, lscratch, rscratch, begin,
+                                                         end, lists + 3 * static_cast<size_t>(nseg),
+                                                         counts);
   return cudaGetLastError();
-}
-
-cudaError_t radix_sort_pairs(uint64_t* keys, uint64_t* vals, uint64_t* keys_alt,
-                             uint64_t* vals_alt, uint64_t n, const int* digits, int ndigits,
-                             uint32_t* hist, int* result_in_alt, cudaStream_t stream) {
-  const uint32_t ntiles = static_cast<uint32_t>((n + kRadixTile - 1) / kRadixTile);
-  uint64_t *ki = keys, *vi = vals, *ko = keys_alt, *vo = vals_alt;
-  for (int p = 0; p < ndigits; ++p) {
-    const int d = digits[p];
-    count_launch();
-    radix_histogram<<<ntiles, kRadixBlock, 0, stream>>>(ki, vi, n, d, hist, ntiles);
-    count_launch();
-    radix_scan<<<1, 1024, 0, stream>>>(hist, 256u * ntiles);
-    count_launch();
-    radix_scatter<<<ntiles, kRadixBlock, 0, stream>>>(ki, vi, ko, vo, n, d, hist, ntiles);
-    uint64_t* t = ki;
-    ki = ko;
-    ko = t;
-    t = vi;
-    vi = vo;
-    vo = t;
-  }
-  *result_in_alt = (ki == keys_alt);
-  return cudaGetLastError();
-}
-
-size_t radix_hist_words(uint64_t n) {
-  return 256 * ((n + kRadixTile - 1) / kRadixTile);
 }
 
 }  // namespace cuflye
