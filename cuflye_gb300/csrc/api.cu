@@ -450,7 +450,7 @@ uint64_t effective_budget(cuflye_ctx* c) {
   size_t free_b = 0, total_b = 0;
   CUFLYE_CHECK(cudaMemGetInfo(&free_b, &total_b));
   const uint64_t cap = static_cast<uint64_t>(free_b) + c->in_use;
-  const uint64_t margin = 4ull << 30;
+  const uint64_t margin = 8ull << 30;
   return cap > margin ? cap - margin : cap / 2;
 }
 
@@ -583,6 +583,13 @@ ChainParams to_chain_params(const cuflye_overlap_params* p) {
   return cp;
 }
 
+// Task-list buffers for the segmented sort, named by `prefix`.
+SortTasks sort_tasks(cuflye_ctx* c, const std::string& prefix, uint64_t nelems, uint32_t nseg) {
+  const uint64_t w = segsort_task_words(nelems, nseg);
+  return SortTasks{buf<uint64_t>(c, prefix + "_tf", w), buf<uint32_t>(c, prefix + "_tn", w),
+                   buf<int>(c, prefix + "_td", w)};
+}
+
 // Sort + chaining of the pass's hits; returns the number of overlap rows left
 // on the device in "o_rows" (OverlapRow, query order, Flye emission order).
 uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
@@ -592,13 +599,13 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
   uint32_t* lscr = buf<uint32_t>(c, "s_l", H + 1);
   uint32_t* rscr = buf<uint32_t>(c, "s_r", H + 1);
   uint32_t* lists = buf<uint32_t>(c, "s_lists", 4ull * std::max<uint64_t>(nq, 1));
-  uint32_t* scounts = buf<uint32_t>(c, "s_counts", 4);
+  uint32_t* scounts = buf<uint32_t>(c, "s_counts", 8);
   // 1. KmerMatch sort per query: (ext id, cur pos) with libstdc++ order
   uint64_t* qb = buf<uint64_t>(c, "s_qb", nq + 1);
   CUFLYE_CHECK(cudaMemcpyAsync(qb, ps.q_off, (nq + 1) * 8ull, cudaMemcpyDeviceToDevice, st));
   CUFLYE_CHECK(cudaEventRecord(c->ev[1], st));
   CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, qb, qb + 1, nq, nullptr, lists,
-                                  scounts, c->num_sms, st));
+                                  scounts, c->num_sms, st, sort_tasks(c, "s", H, nq)));
   CUFLYE_CHECK(cudaEventRecord(c->ev[2], st));
   // 2. groups
   uint32_t* gflags = buf<uint32_t>(c, "g_flags", H);
@@ -621,7 +628,7 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
   // 3. ext-sorted groups: re-sort by ext pos
   CUFLYE_CHECK(groups_prepare_ext_sort(ps.keys, ps.vals, groups, ext_list, gcounts, sb, se, st));
   CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, sb, se, G32, gcounts + 0, glists,
-                                  scounts, c->num_sms, st));
+                                  scounts, c->num_sms, st, sort_tasks(c, "s", H, G32)));
   int32_t* cur = buf<int32_t>(c, "c_cur", H);
   int32_t* ext = buf<int32_t>(c, "c_ext", H);
   CUFLYE_CHECK(groups_split(ps.keys, ps.vals, groups, dp_list, gcounts, cur, ext, st));
@@ -634,9 +641,11 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
   // 5. score order (libstdc++ order of indices by score descending)
   CUFLYE_CHECK(chain_prepare_order(score, ps.keys, ps.vals, groups, dp_list, gcounts, sb, se, st));
   CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, sb, se, G32, gcounts + 1, glists,
-                                  scounts, c->num_sms, st));
-  // 6. backtrack, proposals, primary selection
-  const uint64_t pool_cap = 8 * G + 1024;
+                                  scounts, c->num_sms, st, sort_tasks(c, "s", H, G32)));
+  // 6. backtrack, proposals, primary selection; the row pool is sized by the
+  // groups that survived the prefilter
+  const uint32_t survivors = read_scalar(c, gcounts + 1);
+  const uint64_t pool_cap = 8ull * survivors + 1024;
   OverlapRow* pool = buf<OverlapRow>(c, "o_pool", pool_cap);
   uint32_t* pool_count = buf<uint32_t>(c, "o_poolcount", 1);
   uint32_t* group_rows = buf<uint32_t>(c, "o_grows", G);
@@ -718,7 +727,10 @@ void for_each_pass(cuflye_ctx* c, const Queries& Q, bool kmers, uint64_t bytes_p
   }
 }
 
-constexpr uint64_t kChainBytesPerHit = 8 + 4 + 4 + 4 + 4 + 8 + 4 + 4 + 4 + 4;
+// Device bytes per hit of one pass: keys, values, the two rank maps, group
+// flags and ids, cur / ext / score / backtrack, plus about 2 bytes for the
+// per-group tables and the sort's task list.
+constexpr uint64_t kChainBytesPerHit = 8 + 4 + 4 + 4 + 4 + 8 + 4 + 4 + 4 + 4 + 2;
 
 void require_index(cuflye_ctx* c) {
   if (!c->has_index) throw Error(CUFLYE_ERR_NO_INDEX, "no k-mer index: call cuflye_index_build");
@@ -1060,9 +1072,9 @@ cuflye_status cuflye_read_to_graph(cuflye_ctx* c, size_t n, const int64_t* ids,
     uint32_t* sl = buf<uint32_t>(c, "r_sl", A + 1);
     uint32_t* sr = buf<uint32_t>(c, "r_sr", A + 1);
     uint32_t* slists = buf<uint32_t>(c, "r_slists", 4ull * nq);
-    uint32_t* scounts = buf<uint32_t>(c, "r_scounts", 4);
+    uint32_t* scounts = buf<uint32_t>(c, "r_scounts", 8);
     CUFLYE_CHECK(segmented_std_sort(skeys, svals, sl, sr, d_aoff, d_aoff + 1, nq, nullptr, slists,
-                                    scounts, c->num_sms, st));
+                                    scounts, c->num_sms, st, sort_tasks(c, "r", A, nq)));
     OverlapRow* sorted = buf<OverlapRow>(c, "r_sorted", A);
     CUFLYE_CHECK(r2g_permute(aln, d_aoff, nq, svals, sorted, st));
     void* recs = buf<uint8_t>(c, "r_recs", A * r2g_rec_bytes());
@@ -1132,7 +1144,7 @@ cuflye_status cuflye_std_sort_segments(cuflye_ctx* c, uint64_t* keys, uint32_t* 
   uint32_t* dr = buf<uint32_t>(c, "t_r", m + 1);
   uint64_t* off = buf<uint64_t>(c, "t_off", n_segments + 1);
   uint32_t* lists = buf<uint32_t>(c, "t_lists", 4 * n_segments);
-  uint32_t* counts = buf<uint32_t>(c, "t_counts", 4);
+  uint32_t* counts = buf<uint32_t>(c, "t_counts", 8);
   std::vector<uint64_t> rel(n_segments + 1);
   for (size_t s = 0; s <= n_segments; ++s) rel[s] = seg_offsets[s] - base;
   CUFLYE_CHECK(cudaMemcpyAsync(dk, keys + base, m * 8, cudaMemcpyHostToDevice, st));
@@ -1140,7 +1152,8 @@ cuflye_status cuflye_std_sort_segments(cuflye_ctx* c, uint64_t* keys, uint32_t* 
   CUFLYE_CHECK(cudaMemcpyAsync(off, rel.data(), rel.size() * 8, cudaMemcpyHostToDevice, st));
   CUFLYE_CHECK(segmented_std_sort(dk, dv, dl, dr, off, off + 1,
                                   static_cast<uint32_t>(n_segments), nullptr, lists, counts,
-                                  c->num_sms, st));
+                                  c->num_sms, st,
+                                  sort_tasks(c, "t", m, static_cast<uint32_t>(n_segments))));
   CUFLYE_CHECK(cudaMemcpyAsync(keys + base, dk, m * 8, cudaMemcpyDeviceToHost, st));
   CUFLYE_CHECK(cudaMemcpyAsync(values + base, dv, m * 4, cudaMemcpyDeviceToHost, st));
   sync(c);

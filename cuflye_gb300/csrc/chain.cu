@@ -391,21 +391,30 @@ __device__ __forceinline__ uint32_t lower_bound_i32(const int32_t* a, uint32_t n
   return lo;
 }
 
-__global__ void backtrack_kernel(const int32_t* __restrict__ cur, const int32_t* __restrict__ ext,
-                                 const int32_t* __restrict__ score, int32_t* __restrict__ bt,
-                                 const uint32_t* __restrict__ order,
-                                 const GroupInfo* __restrict__ groups,
-                                 const uint32_t* __restrict__ dp_list,
-                                 const uint32_t* __restrict__ counts,
-                                 const QueryInfo* __restrict__ qinfo,
-                                 const uint64_t* __restrict__ f_off,
-                                 const int32_t* __restrict__ fpos,
-                                 const int64_t* __restrict__ slot_signed, LogfTable logt,
-                                 ChainParams p, OverlapRow* __restrict__ pool, uint64_t pool_cap,
-                                 uint32_t* __restrict__ pool_count,
-                                 uint32_t* __restrict__ group_rows, DeviceStatus* st) {
-  const uint32_t li = blockIdx.x * blockDim.x + threadIdx.x;
-  if (li >= counts[1]) return;
+// One warp per group.  The group's backtrack array is staged in shared memory
+// as 16-bit indices (0xFFFF = -1) when it fits kBtCap; the warp tests 32
+// score-ordered chain starts per step with a ballot, and lane 0 walks each
+// live chain (Flye's serial order) and builds its proposal.  After a walk the
+// remaining starts of the step are tested again, since the walk may have
+// consumed them.
+constexpr uint32_t kBtCap = 16384;
+constexpr int kBtWarps = 6;
+
+__global__ void __launch_bounds__(kBtWarps * 32) backtrack_kernel(
+    const int32_t* __restrict__ cur, const int32_t* __restrict__ ext,
+    const int32_t* __restrict__ score, int32_t* bt, const uint32_t* __restrict__ order,
+    const GroupInfo* __restrict__ groups, const uint32_t* __restrict__ dp_list,
+    const uint32_t* __restrict__ counts, const QueryInfo* __restrict__ qinfo,
+    const uint64_t* __restrict__ f_off, const int32_t* __restrict__ fpos,
+    const int64_t* __restrict__ slot_signed, LogfTable logt, ChainParams p,
+    OverlapRow* __restrict__ pool, uint64_t pool_cap, uint32_t* __restrict__ pool_count,
+    uint32_t* __restrict__ group_rows, DeviceStatus* st) {
+  extern __shared__ uint16_t bt_stage[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  uint16_t* bts = bt_stage + static_cast<size_t>(wib) * kBtCap;
+  const uint32_t cnt = counts[1];
+  const uint32_t nwarps = gridDim.x * kBtWarps;
+  for (uint32_t li = blockIdx.x * kBtWarps + wib; li < cnt; li += nwarps) {
   const uint32_t gidx = dp_list[li];
   const GroupInfo g = groups[gidx];
   const uint64_t b = g.start;
@@ -415,42 +424,86 @@ __global__ void backtrack_kernel(const int32_t* __restrict__ cur, const int32_t*
                                              : slot_signed[g.ext_di >> 1];
   const int32_t* fq = fpos + f_off[g.query];
   const uint32_t nf = static_cast<uint32_t>(f_off[g.query + 1] - f_off[g.query]);
+  const bool staged = g.n <= kBtCap;
+  if (staged) {
+    for (uint32_t j = lane; j < g.n; j += 32) {
+      const int32_t v = bt[b + j];
+      bts[j] = v < 0 ? 0xFFFFu : static_cast<uint16_t>(v);
+    }
+  }
+  __syncwarp();
   Prop props[kMaxProposals];
   int np = 0;
-  for (uint32_t oi = 0; oi < g.n; ++oi) {
-    const uint32_t start = order[b + oi];
-    if (bt[b + start] == -1) continue;
-    int32_t pos = static_cast<int32_t>(start), first = 0, clen = 0;
-    while (pos != -1) {
-      first = pos;
-      ++clen;
-      const int32_t nx = bt[b + pos];
-      bt[b + pos] = -1;
-      pos = nx;
+  bool overflow = false;
+  for (uint32_t o0 = 0; o0 < g.n; o0 += 32) {
+    const uint32_t oi = o0 + lane;
+    const bool valid = oi < g.n;
+    const uint32_t start = valid ? order[b + oi] : 0;
+    unsigned mask = __ballot_sync(0xffffffffu, valid && (staged ? bts[start] != 0xFFFFu
+                                                                 : bt[b + start] != -1));
+    while (mask) {
+      const int j = __ffs(mask) - 1;
+      const uint32_t s0 = __shfl_sync(0xffffffffu, start, j);
+      if (lane == 0 && !overflow) {
+        int32_t pos = static_cast<int32_t>(s0), first = 0, clen = 0;
+        if (staged) {
+          while (pos != -1) {
+            first = pos;
+            ++clen;
+            const uint16_t nx = bts[pos];
+            bts[pos] = 0xFFFFu;
+            pos = nx == 0xFFFFu ? -1 : static_cast<int32_t>(nx);
+          }
+        } else {
+          while (pos != -1) {
+            first = pos;
+            ++clen;
+            const int32_t nx = bt[b + pos];
+            bt[b + pos] = -1;
+            pos = nx;
+          }
+        }
+        Prop o;
+        o.cb = cur[b + first];
+        o.ce = cur[b + s0] + k - 1;
+        o.eb = ext[b + first];
+        o.ee = ext[b + s0] + k - 1;
+        o.score = score[b + s0] - score[b + first] + k - 1;
+        o.clen = clen;
+        bool keep = overlap_test(o, qi.signed_id, ext_signed, qi.len, g.ext_len, p);
+        if (keep) {
+          const uint32_t lo = lower_bound_i32(fq, nf, o.cb);
+          const uint32_t hi = lower_bound_i32(fq, nf, o.ce + 1);
+          const int32_t norm = max(o.ce - o.cb, o.ee - o.eb) - static_cast<int32_t>(hi - lo);
+          keep = norm > 0;
+          if (keep) {
+            float rate =
+                fdiv(fmul(static_cast<float>(clen), p.sample_rate), static_cast<float>(norm));
+            rate = rate < 1.0f ? rate : 1.0f;
+            const float x = fdiv(1.0f, rate);
+            if (!(x < 16777216.0f)) raise_status(st, kDevLogDomain, 0, static_cast<int64_t>(gidx));
+            o.div = fdiv(flye_logf(x, logt), static_cast<float>(k));
+          }
+        }
+        if (keep) {
+          if (np == kMaxProposals) {
+            raise_status(st, kDevProposalOverflow, 0, static_cast<int64_t>(gidx));
+            overflow = true;
+          } else {
+            props[np++] = o;
+          }
+        }
+      }
+      __syncwarp();
+      mask = __ballot_sync(0xffffffffu, valid && lane > j &&
+                                            (staged ? bts[start] != 0xFFFFu : bt[b + start] != -1));
     }
-    Prop o;
-    o.cb = cur[b + first];
-    o.ce = cur[b + start] + k - 1;
-    o.eb = ext[b + first];
-    o.ee = ext[b + start] + k - 1;
-    o.score = score[b + start] - score[b + first] + k - 1;
-    o.clen = clen;
-    if (!overlap_test(o, qi.signed_id, ext_signed, qi.len, g.ext_len, p)) continue;
-    const uint32_t lo = lower_bound_i32(fq, nf, o.cb);
-    const uint32_t hi = lower_bound_i32(fq, nf, o.ce + 1);
-    const int32_t norm = max(o.ce - o.cb, o.ee - o.eb) - static_cast<int32_t>(hi - lo);
-    if (norm <= 0) continue;
-    float rate = fdiv(fmul(static_cast<float>(clen), p.sample_rate), static_cast<float>(norm));
-    rate = rate < 1.0f ? rate : 1.0f;
-    const float x = fdiv(1.0f, rate);
-    if (!(x < 16777216.0f)) raise_status(st, kDevLogDomain, 0, static_cast<int64_t>(gidx));
-    o.div = fdiv(flye_logf(x, logt), static_cast<float>(k));
-    if (np == kMaxProposals) {
-      raise_status(st, kDevProposalOverflow, 0, static_cast<int64_t>(gidx));
-      group_rows[gidx] = 0;
-      return;
-    }
-    props[np++] = o;
+  }
+  __syncwarp();
+  if (lane != 0) continue;
+  if (overflow) {
+    group_rows[gidx] = 0;
+    continue;
   }
   // proposals by score descending, libstdc++ order
   uint64_t K[kMaxProposals];
@@ -482,11 +535,11 @@ __global__ void backtrack_kernel(const int32_t* __restrict__ cur, const int32_t*
   for (int t = 0; t < nprim; ++t)
     if (props[prim[t]].div < p.max_divergence) keep[nk++] = prim[t];
   group_rows[gidx] = static_cast<uint32_t>(nk);
-  if (nk == 0) return;
+  if (nk == 0) continue;
   const uint32_t base = atomicAdd(pool_count, static_cast<uint32_t>(nk));
   if (base + nk > pool_cap) {
     raise_status(st, kDevProposalOverflow, 1, static_cast<int64_t>(gidx));
-    return;
+    continue;
   }
   for (int t = 0; t < nk; ++t) {
     const Prop& o = props[keep[t]];
@@ -505,6 +558,7 @@ __global__ void backtrack_kernel(const int32_t* __restrict__ cur, const int32_t*
     r.group = gidx;
     r.rank = static_cast<uint32_t>(t);
     pool[base + t] = r;
+  }
   }
 }
 
@@ -629,11 +683,20 @@ cudaError_t chain_backtrack(const int32_t* cur, const int32_t* ext, const int32_
                             uint32_t* pool_count, uint32_t* group_rows, DeviceStatus* st,
                             uint32_t max_groups, cudaStream_t s) {
   if (max_groups == 0) return cudaSuccess;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(backtrack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         static_cast<int>(kBtCap * sizeof(uint16_t) * kBtWarps));
+    attr = true;
+  }
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (sms <= 0) sms = 1;
   count_launch();
-  backtrack_kernel<<<grid(max_groups, 128), 128, 0, s>>>(cur, ext, score, bt, order, groups,
-                                                         dp_list, counts, qinfo, f_off, fpos,
-                                                         slot_signed, logt, p, pool, pool_cap,
-                                                         pool_count, group_rows, st);
+  backtrack_kernel<<<sms, kBtWarps * 32, kBtCap * sizeof(uint16_t) * kBtWarps, s>>>(
+      cur, ext, score, bt, order, groups, dp_list, counts, qinfo, f_off, fpos, slot_signed, logt,
+      p, pool, pool_cap, pool_count, group_rows, st);
   return cudaGetLastError();
 }
 

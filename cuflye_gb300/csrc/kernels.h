@@ -23,12 +23,21 @@ cudaError_t exclusive_scan_u64(const uint64_t* in, uint64_t* out, uint64_t n, ui
 
 // ---------------------------------------------------------------- sort
 size_t segsort_smem_bytes();
-// lists: 4 * nseg words; counts: 4 words.  l/r scratch: one word per element.
+// Task list handed from the global phase of large segments to the
+// shared-memory phase: segsort_task_words(n, nseg) entries each.
+struct SortTasks {
+  uint64_t* f;
+  uint32_t* n;
+  int* d;
+};
+size_t segsort_task_words(uint64_t nelems, uint32_t nseg);
+// lists: 4 * nseg words; counts: 5 words.  l/r scratch: one word per element.
 // nseg_dev (optional) holds the live segment count on the device (<= nseg).
 cudaError_t segmented_std_sort(uint64_t* keys, uint32_t* vals, uint32_t* lscratch,
                                uint32_t* rscratch, const uint64_t* begin, const uint64_t* end,
                                uint32_t nseg, const uint32_t* nseg_dev, uint32_t* lists,
-                               uint32_t* counts, int num_sms, cudaStream_t stream);
+                               uint32_t* counts, int num_sms, cudaStream_t stream,
+                               SortTasks tasks);
 size_t radix_hist_words(uint64_t n);
 cudaError_t radix_sort_pairs(uint64_t* keys, uint64_t* vals, uint64_t* keys_alt,
                              uint64_t* vals_alt, uint64_t n, const int* digits, int ndigits,

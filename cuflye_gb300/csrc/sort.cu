@@ -428,17 +428,151 @@ __global__ void __launch_bounds__(kBlock) sort_cta(uint64_t* K, uint32_t* V,
   }
 }
 
-__global__ void __launch_bounds__(kBlock) sort_big(uint64_t* K, uint32_t* V, uint32_t* Lg,
-                                                   uint32_t* Rg,
-                                                   const uint64_t* __restrict__ begin,
-                                                   const uint64_t* __restrict__ end,
-                                                   const uint32_t* __restrict__ list,
-                                                   const uint32_t* __restrict__ counts) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  CtaSmem& sm = *reinterpret_cast<CtaSmem*>(smem_raw);
-  __shared__ uint32_t gf[96], gl[96];
-  __shared__ int gd[96];
-  __shared__ int gn;
+// ---------------------------------------------------------------- large segments
+//
+// Global phase: one CTA of kBigBlock threads per segment partitions in global
+// memory until every task fits kCap, and appends the final tasks to a list
+// that sort_tasks finishes in shared memory.  A tile holds kRounds rounds of
+// kBigBlock consecutive positions; in round r thread t owns position
+// r * kBigBlock + t, so loads are coalesced and independent, and the
+// (round, warp, lane) order equals position order, which gives the ranks.
+
+constexpr int kBigBlock = 256;
+constexpr int kBigWarps = kBigBlock / 32;
+constexpr int kRounds = 16;
+constexpr uint32_t kBigTile = kBigBlock * kRounds;
+
+struct BigSmem {
+  uint32_t cl[kRounds * kBigWarps], cr[kRounds * kBigWarps];  // counts, then offsets
+  uint32_t tot[2];
+  uint32_t scalar[2];
+  uint32_t gf[96], gl[96];
+  int gd[96];
+  int gn;
+};
+
+// Exclusive scan of sm.cl / sm.cr (kRounds * kBigWarps = 128 entries each) by
+// the first four warps; totals to sm.tot.
+__device__ __forceinline__ void scan_round_counts(BigSmem& sm) {
+  static_assert(kRounds * kBigWarps == 128, "scan below covers 128 entries");
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  __shared__ uint32_t wsum[2][4];
+  uint32_t vl = 0, vr = 0, il = 0, ir = 0;
+  if (t < 128) {
+    vl = sm.cl[t];
+    vr = sm.cr[t];
+    il = vl;
+    ir = vr;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t a = __shfl_up_sync(0xffffffffu, il, d);
+      const uint32_t b = __shfl_up_sync(0xffffffffu, ir, d);
+      if (lane >= d) {
+        il += a;
+        ir += b;
+      }
+    }
+    if (lane == 31) {
+      wsum[0][warp] = il;
+      wsum[1][warp] = ir;
+    }
+  }
+  __syncthreads();
+  if (t < 128) {
+    uint32_t bl = 0, br = 0;
+    for (int w = 0; w < warp; ++w) {
+      bl += wsum[0][w];
+      br += wsum[1][w];
+    }
+    sm.cl[t] = bl + il - vl;
+    sm.cr[t] = br + ir - vr;
+    if (t == 127) {
+      sm.tot[0] = bl + il;
+      sm.tot[1] = br + ir;
+    }
+  }
+  __syncthreads();
+}
+
+__device__ uint32_t big_partition_task(uint64_t* K, uint32_t* V, uint32_t* Lr, uint32_t* Rr,
+                                       uint32_t f, uint32_t l, BigSmem& sm) {
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  if (t == 0) isort::median_to_first(K, V, f, f + 1, f + (l - f) / 2, l - 1);
+  __syncthreads();
+  const uint64_t p = K[f];
+  uint32_t carry_l = 0, carry_r = 0;
+  for (uint32_t t0 = f; t0 < l; t0 += kBigTile) {
+    uint64_t k[kRounds];
+#pragma unroll
+    for (int r = 0; r < kRounds; ++r) {
+      const uint32_t i = t0 + r * kBigBlock + t;
+      k[r] = i < l ? K[i] : 0;
+    }
+    unsigned bl[kRounds], br[kRounds];
+#pragma unroll
+    for (int r = 0; r < kRounds; ++r) {
+      const uint32_t i = t0 + r * kBigBlock + t;
+      const bool valid = i < l;
+      bl[r] = __ballot_sync(0xffffffffu, valid && i > f && !(k[r] < p));
+      br[r] = __ballot_sync(0xffffffffu, valid && !(p < k[r]));
+      if (lane == 0) {
+        sm.cl[r * kBigWarps + warp] = __popc(bl[r]);
+        sm.cr[r * kBigWarps + warp] = __popc(br[r]);
+      }
+    }
+    __syncthreads();
+    scan_round_counts(sm);
+#pragma unroll
+    for (int r = 0; r < kRounds; ++r) {
+      const uint32_t i = t0 + r * kBigBlock + t;
+      if ((bl[r] >> lane) & 1u)
+        Lr[f + carry_l + sm.cl[r * kBigWarps + warp] + __popc(bl[r] & lt)] = i;
+      if ((br[r] >> lane) & 1u)
+        Rr[f + carry_r + sm.cr[r * kBigWarps + warp] + __popc(br[r] & lt)] = i;
+    }
+    carry_l += sm.tot[0];
+    carry_r += sm.tot[1];
+    __syncthreads();
+  }
+  const uint32_t tl = carry_l, tr = carry_r;
+  __syncthreads();
+  if (t == 0) {
+    uint32_t lo = 0, hi = tl < tr ? tl : tr;
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi + 1) >> 1;
+      if (Lr[f + mid - 1] < Rr[f + tr - mid])
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    const uint32_t m = lo;
+    uint32_t cut;
+    if (m == 0) {
+      cut = Lr[f];
+    } else {
+      cut = Rr[f + tr - m];
+      if (m + 1 <= tl && Lr[f + m] < cut) cut = Lr[f + m];
+    }
+    sm.scalar[0] = m;
+    sm.scalar[1] = cut;
+  }
+  __syncthreads();
+  const uint32_t m = sm.scalar[0], cut = sm.scalar[1];
+  for (uint32_t q = 1 + t; q <= m; q += kBigBlock) isort::swap_kv(K, V, Lr[f + q - 1], Rr[f + tr - q]);
+  __syncthreads();
+  return cut;
+}
+
+__global__ void __launch_bounds__(kBigBlock) sort_big(uint64_t* K, uint32_t* V, uint32_t* Lg,
+                                                      uint32_t* Rg,
+                                                      const uint64_t* __restrict__ begin,
+                                                      const uint64_t* __restrict__ end,
+                                                      const uint32_t* __restrict__ list,
+                                                      const uint32_t* __restrict__ counts,
+                                                      uint64_t* task_f, uint32_t* task_n,
+                                                      int* task_d, uint32_t* task_count) {
+  __shared__ BigSmem sm;
   const uint32_t cnt = counts[3];
   for (uint32_t i = blockIdx.x; i < cnt; i += gridDim.x) {
     const uint32_t s = list[i];
@@ -449,67 +583,94 @@ __global__ void __launch_bounds__(kBlock) sort_big(uint64_t* K, uint32_t* V, uin
     uint32_t* Ls = Lg + b;  // rank maps share the segment's index range
     uint32_t* Rs = Rg + b;
     if (threadIdx.x == 0) {
-      gf[0] = 0;
-      gl[0] = n;
-      gd[0] = isort::depth_limit(n);
-      gn = 1;
+      sm.gf[0] = 0;
+      sm.gl[0] = n;
+      sm.gd[0] = isort::depth_limit(n);
+      sm.gn = 1;
     }
     __syncthreads();
     for (;;) {
-      const int nt = gn;
+      const int nt = sm.gn;
       if (nt == 0) break;
-      const uint32_t f = gf[nt - 1], l = gl[nt - 1];
-      const int d = gd[nt - 1];
+      const uint32_t f = sm.gf[nt - 1], l = sm.gl[nt - 1];
+      const int d = sm.gd[nt - 1];
       __syncthreads();
       if (l - f <= kCap) {
-        if (threadIdx.x == 0) gn = nt - 1;
+        if (threadIdx.x == 0) {
+          sm.gn = nt - 1;
+          if (l - f > 1) {
+            const uint32_t slot = atomicAdd(task_count, 1u);
+            task_f[slot] = b + f;
+            task_n[slot] = l - f;
+            task_d[slot] = d;
+          }
+        }
         __syncthreads();
-        if (l - f > 1) cta_load_sort_store(Ks, Vs, f, l - f, d, sm);
         continue;
       }
       if (d == 0) {
         if (threadIdx.x == 0) {
           isort::heap_sort(Ks, Vs, f, l);
-          gn = nt - 1;
+          sm.gn = nt - 1;
         }
         __syncthreads();
         continue;
       }
-      const uint32_t cut = block_partition<uint32_t>(Ks, Vs, Ls, Rs, f, l, sm.bs);
+      const uint32_t cut = big_partition_task(Ks, Vs, Ls, Rs, f, l, sm);
       if (threadIdx.x == 0) {
-        gf[nt - 1] = cut;
-        gl[nt - 1] = l;
-        gd[nt - 1] = d - 1;
-        gf[nt] = f;
-        gl[nt] = cut;
-        gd[nt] = d - 1;
-        gn = nt + 1;
+        sm.gf[nt - 1] = cut;
+        sm.gl[nt - 1] = l;
+        sm.gd[nt - 1] = d - 1;
+        sm.gf[nt] = f;
+        sm.gl[nt] = cut;
+        sm.gd[nt] = d - 1;
+        sm.gn = nt + 1;
       }
       __syncthreads();
     }
   }
 }
 
+// Finishes the <= kCap tasks left by sort_big, one CTA per task.
+__global__ void __launch_bounds__(kBlock) sort_tasks(uint64_t* K, uint32_t* V,
+                                                     const uint64_t* __restrict__ task_f,
+                                                     const uint32_t* __restrict__ task_n,
+                                                     const int* __restrict__ task_d,
+                                                     const uint32_t* __restrict__ task_count) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  CtaSmem& sm = *reinterpret_cast<CtaSmem*>(smem_raw);
+  const uint32_t cnt = *task_count;
+  for (uint32_t i = blockIdx.x; i < cnt; i += gridDim.x)
+    cta_load_sort_store(K, V, task_f[i], task_n[i], task_d[i], sm);
+}
+
 }  // namespace
 
 size_t segsort_smem_bytes() { return sizeof(CtaSmem); }
 
+size_t segsort_task_words(uint64_t nelems, uint32_t nseg) {
+  // final tasks of the global phase are disjoint and come from partitions of
+  // tasks larger than kCap (at most depth_limit levels of them)
+  return nseg + 2 * (nelems / kCap + 1) * 64;
+}
+
 cudaError_t segmented_std_sort(uint64_t* keys, uint32_t* vals, uint32_t* lscratch,
                                uint32_t* rscratch, const uint64_t* begin, const uint64_t* end,
                                uint32_t nseg, const uint32_t* nseg_dev, uint32_t* lists,
-                               uint32_t* counts, int num_sms, cudaStream_t stream) {
+                               uint32_t* counts, int num_sms, cudaStream_t stream,
+                               SortTasks tasks) {
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(sort_cta, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          static_cast<int>(sizeof(CtaSmem)));
-    cudaFuncSetAttribute(sort_big, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(sort_tasks, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          static_cast<int>(sizeof(CtaSmem)));
     cudaFuncSetAttribute(sort_warp, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          static_cast<int>(sizeof(WarpSlice) * kWarpSegWarps));
     attr = true;
   }
   if (nseg == 0) return cudaSuccess;
-  cudaMemsetAsync(counts, 0, 4 * sizeof(uint32_t), stream);
+  cudaMemsetAsync(counts, 0, 5 * sizeof(uint32_t), stream);
   count_launch();
   classify_segments<<<(nseg + 255) / 256, 256, 0, stream>>>(begin, end, nseg, nseg_dev, lists,
                                                             counts);
@@ -523,9 +684,12 @@ cudaError_t segmented_std_sort(uint64_t* keys, uint32_t* vals, uint32_t* lscratc
                                                          lists + 2 * static_cast<size_t>(nseg),
                                                          counts);
   count_launch();
-  sort_big<<<num_sms, kBlock, sizeof(CtaSmem), stream>>>(keys, vals, lscratch, rscratch, begin,
-                                                         end, lists + 3 * static_cast<size_t>(nseg),
-                                                         counts);
+  sort_big<<<num_sms * 4, kBigBlock, 0, stream>>>(keys, vals, lscratch, rscratch, begin, end,
+                                                  lists + 3 * static_cast<size_t>(nseg), counts,
+                                                  tasks.f, tasks.n, tasks.d, counts + 4);
+  count_launch();
+  sort_tasks<<<num_sms, kBlock, sizeof(CtaSmem), stream>>>(keys, vals, tasks.f, tasks.n, tasks.d,
+                                                           counts + 4);
   return cudaGetLastError();
 }
 
