@@ -23,17 +23,14 @@
 namespace cuflye {
 namespace {
 
-constexpr int kBlock = 512;
+constexpr int kBlock = 256;
 constexpr int kWarps = kBlock / 32;
-constexpr uint32_t kCap = 8192;       // CTA shared-memory segment capacity
-constexpr uint32_t kWarpMax = 2048;   // tasks up to this size go to single warps
-constexpr uint32_t kSerial = 32;      // tasks up to this size go to single threads
+constexpr uint32_t kCap = 4096;       // CTA shared-memory segment capacity
+constexpr uint32_t kWarpMax = 512;    // tasks up to this size become warp subtrees
 constexpr uint32_t kTiny = 64;        // segments up to this size: thread kernel
 constexpr uint32_t kWarpSeg = 2048;   // segments up to this size: warp kernel
 constexpr int kWarpSegWarps = 6;      // warps per CTA in the warp kernel
-constexpr int kMaxWarpTasks = 256;    // disjoint tasks > kSerial in kCap elements
-constexpr int kMaxSerial = 1024;
-constexpr int kSerialFlush = 512;
+constexpr int kMaxWarpTasks = 256;    // warp subtrees per CTA task (<= 2 per partition)
 
 // ---------------------------------------------------------------- partitions
 
@@ -86,73 +83,119 @@ __device__ uint32_t warp_partition(uint64_t* K, uint32_t* V, RT* Lr, RT* Rr, uin
   return cut;
 }
 
-struct BlockScratch {
-  uint64_t warp_sums[kWarps + 1];
-  uint32_t scalar[4];
+// Block-wide unguarded partition of [f, l) by BLOCK threads, one pass over
+// the keys in tiles of kRounds rounds: in round r thread t owns position
+// t0 + r * BLOCK + t, so loads are coalesced (and bank-conflict free in
+// shared memory) and independent; (round, warp, lane) order is position
+// order, so per-(round, warp) ballot counts scanned in that order give ranks.
+constexpr int kRounds = 16;
+
+template <int BLOCK, int ROUNDS = kRounds>
+struct RoundScratch {
+  static constexpr int kW = BLOCK / 32;
+  static constexpr int kR = ROUNDS;
+  static constexpr int kN = ROUNDS * kW;
+  uint32_t cl[kN], cr[kN];  // counts, then exclusive offsets
+  uint32_t wsum[2][kN / 32];
+  uint32_t tot[2];
+  uint32_t scalar[2];
 };
 
-__device__ __forceinline__ uint64_t block_exclusive_scan(uint64_t v, BlockScratch& bs,
-                                                         uint64_t* total) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint64_t inc = v;
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    const uint64_t o = __shfl_up_sync(0xffffffffu, inc, d);
-    if (lane >= d) inc += o;
-  }
-  if (lane == 31) bs.warp_sums[warp] = inc;
-  __syncthreads();
-  if (warp == 0) {
-    const uint64_t w = lane < kWarps ? bs.warp_sums[lane] : 0;
-    uint64_t wi = w;
+template <class RS>
+__device__ __forceinline__ void round_scan(RS& rs) {
+  constexpr int kN = RS::kN;
+  static_assert(kN % 32 == 0 && kN <= RS::kW * 32, "one entry per thread");
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  uint32_t vl = 0, vr = 0, il = 0, ir = 0;
+  if (t < kN) {
+    vl = rs.cl[t];
+    vr = rs.cr[t];
+    il = vl;
+    ir = vr;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
-      const uint64_t o = __shfl_up_sync(0xffffffffu, wi, d);
-      if (lane >= d) wi += o;
+      const uint32_t a = __shfl_up_sync(0xffffffffu, il, d);
+      const uint32_t b = __shfl_up_sync(0xffffffffu, ir, d);
+      if (lane >= d) {
+        il += a;
+        ir += b;
+      }
     }
-    if (lane < kWarps) bs.warp_sums[lane] = wi - w;
-    if (lane == kWarps - 1) bs.warp_sums[kWarps] = wi;
+    if (lane == 31) {
+      rs.wsum[0][warp] = il;
+      rs.wsum[1][warp] = ir;
+    }
   }
   __syncthreads();
-  const uint64_t r = bs.warp_sums[warp] + inc - v;
-  *total = bs.warp_sums[kWarps];
+  if (t < kN) {
+    uint32_t bl = 0, br = 0;
+    for (int w = 0; w < warp; ++w) {
+      bl += rs.wsum[0][w];
+      br += rs.wsum[1][w];
+    }
+    rs.cl[t] = bl + il - vl;
+    rs.cr[t] = br + ir - vr;
+    if (t == kN - 1) {
+      rs.tot[0] = bl + il;
+      rs.tot[1] = br + ir;
+    }
+  }
   __syncthreads();
-  return r;
 }
 
-// Block-wide unguarded partition of [f, l), one pass over the keys in tiles
-// of kBlock * 16 (each thread owns 16 consecutive positions of a tile).
-template <typename RT>
-__device__ uint32_t block_partition(uint64_t* K, uint32_t* V, RT* Lr, RT* Rr, uint32_t f,
-                                    uint32_t l, BlockScratch& bs) {
-  if (threadIdx.x == 0) isort::median_to_first(K, V, f, f + 1, f + (l - f) / 2, l - 1);
+template <int BLOCK, typename RT, class RS>
+__device__ uint32_t round_partition(uint64_t* K, uint32_t* V, RT* Lr, RT* Rr, uint32_t f,
+                                    uint32_t l, RS& rs) {
+  constexpr int kW = RS::kW;
+  constexpr int kRounds = RS::kR;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  if (t == 0) isort::median_to_first(K, V, f, f + 1, f + (l - f) / 2, l - 1);
   __syncthreads();
   const uint64_t p = K[f];
-  uint64_t carry = 0;  // (L count << 32) | R count before the tile
-  for (uint32_t t0 = f; t0 < l; t0 += kBlock * 16u) {
-    const uint32_t a = t0 + threadIdx.x * 16u;
-    uint32_t cl = 0, cr = 0;
-    for (uint32_t i = a; i < a + 16u && i < l; ++i) {
-      const uint64_t k = K[i];
-      cl += (i > f) && !(k < p);
-      cr += !(p < k);
+  uint32_t carry_l = 0, carry_r = 0;
+  for (uint32_t t0 = f; t0 < l; t0 += BLOCK * kRounds) {
+    // rounds this tile actually covers (uniform across the block)
+    const uint32_t nr = (l - t0 + BLOCK - 1) / BLOCK;
+    uint64_t k[kRounds];
+#pragma unroll
+    for (int r = 0; r < kRounds; ++r) {
+      const uint32_t i = t0 + r * BLOCK + t;
+      k[r] = (static_cast<uint32_t>(r) < nr && i < l) ? K[i] : 0;
     }
-    uint64_t tile_tot;
-    const uint64_t ex = carry + block_exclusive_scan((static_cast<uint64_t>(cl) << 32) | cr, bs,
-                                                     &tile_tot);
-    uint32_t rl = static_cast<uint32_t>(ex >> 32);
-    uint32_t rr = static_cast<uint32_t>(ex & 0xffffffffu);
-    for (uint32_t i = a; i < a + 16u && i < l; ++i) {
-      const uint64_t k = K[i];
-      if ((i > f) && !(k < p)) Lr[f + rl++] = static_cast<RT>(i);
-      if (!(p < k)) Rr[f + rr++] = static_cast<RT>(i);
+    unsigned bl[kRounds], br[kRounds];
+#pragma unroll
+    for (int r = 0; r < kRounds; ++r) {
+      bl[r] = 0;
+      br[r] = 0;
+      if (static_cast<uint32_t>(r) < nr) {
+        const uint32_t i = t0 + r * BLOCK + t;
+        const bool valid = i < l;
+        bl[r] = __ballot_sync(0xffffffffu, valid && i > f && !(k[r] < p));
+        br[r] = __ballot_sync(0xffffffffu, valid && !(p < k[r]));
+      }
+      if (lane == 0) {
+        rs.cl[r * kW + warp] = __popc(bl[r]);
+        rs.cr[r * kW + warp] = __popc(br[r]);
+      }
     }
-    carry += tile_tot;
+    __syncthreads();
+    round_scan(rs);
+#pragma unroll
+    for (int r = 0; r < kRounds; ++r) {
+      if (static_cast<uint32_t>(r) >= nr) continue;
+      const uint32_t i = t0 + r * BLOCK + t;
+      if ((bl[r] >> lane) & 1u)
+        Lr[f + carry_l + rs.cl[r * kW + warp] + __popc(bl[r] & lt)] = static_cast<RT>(i);
+      if ((br[r] >> lane) & 1u)
+        Rr[f + carry_r + rs.cr[r * kW + warp] + __popc(br[r] & lt)] = static_cast<RT>(i);
+    }
+    carry_l += rs.tot[0];
+    carry_r += rs.tot[1];
+    __syncthreads();
   }
-  __syncthreads();
-  const uint32_t tl = static_cast<uint32_t>(carry >> 32);
-  const uint32_t tr = static_cast<uint32_t>(carry & 0xffffffffu);
-  if (threadIdx.x == 0) {
+  const uint32_t tl = carry_l, tr = carry_r;
+  if (t == 0) {
     uint32_t lo = 0, hi = tl < tr ? tl : tr;
     while (lo < hi) {
       const uint32_t mid = (lo + hi + 1) >> 1;
@@ -169,18 +212,111 @@ __device__ uint32_t block_partition(uint64_t* K, uint32_t* V, RT* Lr, RT* Rr, ui
       cut = Rr[f + tr - m];
       if (m + 1 <= tl && static_cast<uint32_t>(Lr[f + m]) < cut) cut = Lr[f + m];
     }
-    bs.scalar[0] = m;
-    bs.scalar[1] = cut;
+    rs.scalar[0] = m;
+    rs.scalar[1] = cut;
   }
   __syncthreads();
-  const uint32_t m = bs.scalar[0], cut = bs.scalar[1];
-  for (uint32_t k = 1 + threadIdx.x; k <= m; k += kBlock)
-    isort::swap_kv(K, V, Lr[f + k - 1], Rr[f + tr - k]);
+  const uint32_t m = rs.scalar[0], cut = rs.scalar[1];
+  for (uint32_t q = 1 + t; q <= m; q += BLOCK) isort::swap_kv(K, V, Lr[f + q - 1], Rr[f + tr - q]);
   __syncthreads();
   return cut;
 }
 
 // ---------------------------------------------------------------- CTA sort
+
+// Leaves: libstdc++ finishes every block of <= 16 elements with a stable
+// insertion sort, i.e. the stable sorted order.  Each half-warp sorts one leaf
+// in registers: element i moves to (number of smaller keys) + (number of equal
+// keys before it).  Lanes read consecutive positions, so shared-memory banks
+// do not conflict.
+constexpr uint32_t kLeafMax = isort::kLeaf;  // 16
+constexpr int kLeafBuf = 64;
+
+struct LeafBuf {
+  uint32_t f[kLeafBuf], l[kLeafBuf];
+};
+
+__device__ void flush_leaves(uint64_t* K, uint32_t* V, const LeafBuf& lb, int ns) {
+  const int lane = threadIdx.x & 31, half = lane >> 4, hl = lane & 15;
+  for (int t0 = 0; t0 < ns; t0 += 2) {
+    const int t = t0 + half;
+    const bool live = t < ns;
+    const uint32_t f = live ? lb.f[t] : 0;
+    const uint32_t n = live ? lb.l[t] - f : 0;
+    const bool valid = static_cast<uint32_t>(hl) < n;
+    const uint64_t k = valid ? K[f + hl] : 0;
+    const uint32_t v = valid ? V[f + hl] : 0;
+    uint32_t rank = 0;
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      const uint64_t kj = __shfl_sync(0xffffffffu, k, (half << 4) + j);
+      if (static_cast<uint32_t>(j) < n) rank += (kj < k) || (kj == k && j < hl);
+    }
+    __syncwarp();
+    if (valid) {
+      K[f + rank] = k;
+      V[f + rank] = v;
+    }
+    __syncwarp();
+  }
+}
+
+// A warp sorts the subtree of task [f, l) on its own: warp partitions while a
+// task exceeds 16 elements (heapsort by one lane once the recursion budget is
+// spent), leaves collected in the warp's list and finished two at a time.
+// The task stack is identical in every lane; rank maps live in the task's own
+// index range of Lr / Rr.
+__device__ void warp_subtree_sort(uint64_t* K, uint32_t* V, uint16_t* Lr, uint16_t* Rr,
+                                  uint32_t f0, uint32_t l0, int d0, LeafBuf& lb) {
+  const int lane = threadIdx.x & 31;
+  uint32_t tf[40], tl[40];
+  int td[40];
+  int top = 0, ns = 0;
+  tf[0] = f0;
+  tl[0] = l0;
+  td[0] = d0;
+  top = 1;
+  while (top > 0) {
+    --top;
+    const uint32_t f = tf[top], l = tl[top];
+    const int d = td[top];
+    if (l - f <= kLeafMax) {
+      if (l - f > 1) {
+        if (lane == 0) {
+          lb.f[ns] = f;
+          lb.l[ns] = l;
+        }
+        ++ns;
+        if (ns == kLeafBuf) {
+          __syncwarp();
+          flush_leaves(K, V, lb, ns);
+          ns = 0;
+        }
+      }
+      continue;
+    }
+    if (d == 0) {
+      if (lane == 0) isort::heap_sort(K, V, f, l);
+      __syncwarp();
+      continue;
+    }
+    const uint32_t cut = warp_partition<uint16_t>(K, V, Lr, Rr, f, l);
+    if (cut - f > 1) {
+      tf[top] = f;
+      tl[top] = cut;
+      td[top] = d - 1;
+      ++top;
+    }
+    if (l - cut > 1) {
+      tf[top] = cut;
+      tl[top] = l;
+      td[top] = d - 1;
+      ++top;
+    }
+  }
+  __syncwarp();
+  flush_leaves(K, V, lb, ns);
+}
 
 struct CtaSmem {
   uint64_t K[kCap];
@@ -189,57 +325,41 @@ struct CtaSmem {
   uint16_t Rr[kCap];
   uint32_t bf[64], bl[64];
   int bd[64];
-  uint32_t wf[2][kMaxWarpTasks], wl[2][kMaxWarpTasks];
-  int wd[2][kMaxWarpTasks];
-  uint32_t sf[kMaxSerial], sl[kMaxSerial];
-  int sd[kMaxSerial];
-  int nb, wn[2], ns;
-  BlockScratch bs;
+  uint32_t tf[kMaxWarpTasks], tl[kMaxWarpTasks];
+  int td[kMaxWarpTasks];
+  LeafBuf leaves[kWarps];
+  int nb, nt, next;
+  RoundScratch<kBlock> rs;
 };
 
-// Routes a task to the serial list, the next warp round or the block stack.
-// Called by one thread (block phase) or one lane (warp phase); lists are
-// appended with atomics because several warps add concurrently.
-__device__ __forceinline__ void route_task(CtaSmem& sm, int next, uint32_t f, uint32_t l, int d) {
+// Block phase routing: tasks above kWarpMax stay on the block stack, every
+// other task (> 1 element) becomes a warp subtree.
+__device__ __forceinline__ void route_task(CtaSmem& sm, uint32_t f, uint32_t l, int d) {
   const uint32_t n = l - f;
   if (n <= 1) return;
-  if (n <= kSerial || d == 0) {
-    const int s = atomicAdd(&sm.ns, 1);
-    sm.sf[s] = f;
-    sm.sl[s] = l;
-    sm.sd[s] = d;
-  } else if (n <= kWarpMax) {
-    const int s = atomicAdd(&sm.wn[next], 1);
-    sm.wf[next][s] = f;
-    sm.wl[next][s] = l;
-    sm.wd[next][s] = d;
+  if (n > kWarpMax && d > 0) {
+    sm.bf[sm.nb] = f;
+    sm.bl[sm.nb] = l;
+    sm.bd[sm.nb] = d;
+    ++sm.nb;
   } else {
-    const int s = atomicAdd(&sm.nb, 1);
-    sm.bf[s] = f;
-    sm.bl[s] = l;
-    sm.bd[s] = d;
+    sm.tf[sm.nt] = f;
+    sm.tl[sm.nt] = l;
+    sm.td[sm.nt] = d;
+    ++sm.nt;
   }
 }
 
-__device__ __forceinline__ void flush_serial(CtaSmem& sm) {
-  for (int s = threadIdx.x; s < sm.ns; s += kBlock)
-    isort::serial_introsort(sm.K, sm.V, sm.sf[s], sm.sl[s], sm.sd[s]);
-  __syncthreads();
-  if (threadIdx.x == 0) sm.ns = 0;
-  __syncthreads();
-}
-
-// Sorts sm.K/sm.V[0, n) from recursion budget depth0.
+// Sorts sm.K/sm.V[0, n) from recursion budget depth0: block-wide partitions
+// while tasks exceed kWarpMax, then warps take whole subtrees from the list.
 __device__ void cta_sort(CtaSmem& sm, uint32_t n, int depth0) {
   if (threadIdx.x == 0) {
     sm.nb = 0;
-    sm.wn[0] = 0;
-    sm.wn[1] = 0;
-    sm.ns = 0;
-    route_task(sm, 0, 0, n, depth0);
+    sm.nt = 0;
+    sm.next = 0;
+    route_task(sm, 0, n, depth0);
   }
   __syncthreads();
-  // block phase: tasks larger than kWarpMax, one at a time
   for (;;) {
     const int nb = sm.nb;
     if (nb == 0) break;
@@ -247,37 +367,30 @@ __device__ void cta_sort(CtaSmem& sm, uint32_t n, int depth0) {
     const int d = sm.bd[nb - 1];
     __syncthreads();
     if (threadIdx.x == 0) sm.nb = nb - 1;
-    const uint32_t cut = block_partition<uint16_t>(sm.K, sm.V, sm.Lr, sm.Rr, f, l, sm.bs);
+    const uint32_t cut = round_partition<kBlock, uint16_t>(sm.K, sm.V, sm.Lr, sm.Rr, f, l, sm.rs);
     if (threadIdx.x == 0) {
-      route_task(sm, 0, f, cut, d - 1);
-      route_task(sm, 0, cut, l, d - 1);
+      route_task(sm, f, cut, d - 1);
+      route_task(sm, cut, l, d - 1);
     }
     __syncthreads();
-    if (sm.ns > kSerialFlush) flush_serial(sm);
   }
-  // warp phase: level by level, every warp takes different tasks
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  int cur = 0;
+  const int nt = sm.nt;
   for (;;) {
-    const int cnt = sm.wn[cur];
-    if (cnt == 0) break;
-    if (threadIdx.x == 0) sm.wn[cur ^ 1] = 0;
-    __syncthreads();
-    for (int t = warp; t < cnt; t += kWarps) {
-      const uint32_t f = sm.wf[cur][t], l = sm.wl[cur][t];
-      const int d = sm.wd[cur][t];
-      const uint32_t cut = warp_partition<uint16_t>(sm.K, sm.V, sm.Lr, sm.Rr, f, l);
-      if (lane == 0) {
-        route_task(sm, cur ^ 1, f, cut, d - 1);
-        route_task(sm, cur ^ 1, cut, l, d - 1);
-      }
+    int t = 0;
+    if (lane == 0) t = atomicAdd(&sm.next, 1);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t >= nt) break;
+    const uint32_t f = sm.tf[t], l = sm.tl[t];
+    const int d = sm.td[t];
+    if (d == 0) {
+      if (lane == 0) isort::heap_sort(sm.K, sm.V, f, l);
       __syncwarp();
+    } else {
+      warp_subtree_sort(sm.K, sm.V, sm.Lr, sm.Rr, f, l, d, sm.leaves[warp]);
     }
-    __syncthreads();
-    if (sm.ns > kSerialFlush) flush_serial(sm);
-    cur ^= 1;
   }
-  flush_serial(sm);
+  __syncthreads();
 }
 
 __device__ void cta_load_sort_store(uint64_t* K, uint32_t* V, uint64_t begin, uint32_t n,
@@ -335,8 +448,7 @@ struct WarpSlice {
   uint32_t V[kWarpSeg];
   uint16_t Lr[kWarpSeg];
   uint16_t Rr[kWarpSeg];
-  uint32_t sf[64], sl[64];
-  int sd[64];
+  LeafBuf leaves;
 };
 
 // One warp per segment of (kTiny, kWarpSeg] elements.
@@ -358,52 +470,7 @@ __global__ void __launch_bounds__(kWarpSegWarps * 32) sort_warp(
       ws.V[i] = V[b + i];
     }
     __syncwarp();
-    // task stack (identical in every lane) and a per-warp leaf list
-    uint32_t tf[40], tl[40];
-    int td[40];
-    int top = 0, ns = 0;
-    tf[0] = 0;
-    tl[0] = n;
-    td[0] = isort::depth_limit(n);
-    top = 1;
-    while (top > 0) {
-      --top;
-      const uint32_t f = tf[top], l = tl[top];
-      const int d = td[top];
-      if (l - f <= kSerial || d == 0) {
-        if (lane == 0) {
-          ws.sf[ns] = f;
-          ws.sl[ns] = l;
-          ws.sd[ns] = d;
-        }
-        ++ns;
-        if (ns == 64) {
-          __syncwarp();
-          for (int t = lane; t < ns; t += 32)
-            isort::serial_introsort(ws.K, ws.V, ws.sf[t], ws.sl[t], ws.sd[t]);
-          __syncwarp();
-          ns = 0;
-        }
-        continue;
-      }
-      const uint32_t cut = warp_partition<uint16_t>(ws.K, ws.V, ws.Lr, ws.Rr, f, l);
-      if (cut - f > 1) {
-        tf[top] = f;
-        tl[top] = cut;
-        td[top] = d - 1;
-        ++top;
-      }
-      if (l - cut > 1) {
-        tf[top] = cut;
-        tl[top] = l;
-        td[top] = d - 1;
-        ++top;
-      }
-    }
-    __syncwarp();
-    for (int t = lane; t < ns; t += 32)
-      isort::serial_introsort(ws.K, ws.V, ws.sf[t], ws.sl[t], ws.sd[t]);
-    __syncwarp();
+    warp_subtree_sort(ws.K, ws.V, ws.Lr, ws.Rr, 0, n, isort::depth_limit(n), ws.leaves);
     for (uint32_t i = lane; i < n; i += 32) {
       K[b + i] = ws.K[i];
       V[b + i] = ws.V[i];
@@ -431,140 +498,19 @@ __global__ void __launch_bounds__(kBlock) sort_cta(uint64_t* K, uint32_t* V,
 // ---------------------------------------------------------------- large segments
 //
 // Global phase: one CTA of kBigBlock threads per segment partitions in global
-// memory until every task fits kCap, and appends the final tasks to a list
-// that sort_tasks finishes in shared memory.  A tile holds kRounds rounds of
-// kBigBlock consecutive positions; in round r thread t owns position
-// r * kBigBlock + t, so loads are coalesced and independent, and the
-// (round, warp, lane) order equals position order, which gives the ranks.
+// memory (round_partition) until every task fits kCap, and appends the final
+// tasks to a list that sort_tasks finishes in shared memory.
 
 constexpr int kBigBlock = 256;
-constexpr int kBigWarps = kBigBlock / 32;
-constexpr int kRounds = 16;
-constexpr uint32_t kBigTile = kBigBlock * kRounds;
 
 struct BigSmem {
-  uint32_t cl[kRounds * kBigWarps], cr[kRounds * kBigWarps];  // counts, then offsets
-  uint32_t tot[2];
-  uint32_t scalar[2];
+  RoundScratch<kBigBlock, 8> rs;
   uint32_t gf[96], gl[96];
   int gd[96];
   int gn;
 };
 
-// Exclusive scan of sm.cl / sm.cr (kRounds * kBigWarps = 128 entries each) by
-// the first four warps; totals to sm.tot.
-__device__ __forceinline__ void scan_round_counts(BigSmem& sm) {
-  static_assert(kRounds * kBigWarps == 128, "scan below covers 128 entries");
-  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  __shared__ uint32_t wsum[2][4];
-  uint32_t vl = 0, vr = 0, il = 0, ir = 0;
-  if (t < 128) {
-    vl = sm.cl[t];
-    vr = sm.cr[t];
-    il = vl;
-    ir = vr;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      const uint32_t a = __shfl_up_sync(0xffffffffu, il, d);
-      const uint32_t b = __shfl_up_sync(0xffffffffu, ir, d);
-      if (lane >= d) {
-        il += a;
-        ir += b;
-      }
-    }
-    if (lane == 31) {
-      wsum[0][warp] = il;
-      wsum[1][warp] = ir;
-    }
-  }
-  __syncthreads();
-  if (t < 128) {
-    uint32_t bl = 0, br = 0;
-    for (int w = 0; w < warp; ++w) {
-      bl += wsum[0][w];
-      br += wsum[1][w];
-    }
-    sm.cl[t] = bl + il - vl;
-    sm.cr[t] = br + ir - vr;
-    if (t == 127) {
-      sm.tot[0] = bl + il;
-      sm.tot[1] = br + ir;
-    }
-  }
-  __syncthreads();
-}
-
-__device__ uint32_t big_partition_task(uint64_t* K, uint32_t* V, uint32_t* Lr, uint32_t* Rr,
-                                       uint32_t f, uint32_t l, BigSmem& sm) {
-  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  const unsigned lt = (1u << lane) - 1u;
-  if (t == 0) isort::median_to_first(K, V, f, f + 1, f + (l - f) / 2, l - 1);
-  __syncthreads();
-  const uint64_t p = K[f];
-  uint32_t carry_l = 0, carry_r = 0;
-  for (uint32_t t0 = f; t0 < l; t0 += kBigTile) {
-    uint64_t k[kRounds];
-#pragma unroll
-    for (int r = 0; r < kRounds; ++r) {
-      const uint32_t i = t0 + r * kBigBlock + t;
-      k[r] = i < l ? K[i] : 0;
-    }
-    unsigned bl[kRounds], br[kRounds];
-#pragma unroll
-    for (int r = 0; r < kRounds; ++r) {
-      const uint32_t i = t0 + r * kBigBlock + t;
-      const bool valid = i < l;
-      bl[r] = __ballot_sync(0xffffffffu, valid && i > f && !(k[r] < p));
-      br[r] = __ballot_sync(0xffffffffu, valid && !(p < k[r]));
-      if (lane == 0) {
-        sm.cl[r * kBigWarps + warp] = __popc(bl[r]);
-        sm.cr[r * kBigWarps + warp] = __popc(br[r]);
-      }
-    }
-    __syncthreads();
-    scan_round_counts(sm);
-#pragma unroll
-    for (int r = 0; r < kRounds; ++r) {
-      const uint32_t i = t0 + r * kBigBlock + t;
-      if ((bl[r] >> lane) & 1u)
-        Lr[f + carry_l + sm.cl[r * kBigWarps + warp] + __popc(bl[r] & lt)] = i;
-      if ((br[r] >> lane) & 1u)
-        Rr[f + carry_r + sm.cr[r * kBigWarps + warp] + __popc(br[r] & lt)] = i;
-    }
-    carry_l += sm.tot[0];
-    carry_r += sm.tot[1];
-    __syncthreads();
-  }
-  const uint32_t tl = carry_l, tr = carry_r;
-  __syncthreads();
-  if (t == 0) {
-    uint32_t lo = 0, hi = tl < tr ? tl : tr;
-    while (lo < hi) {
-      const uint32_t mid = (lo + hi + 1) >> 1;
-      if (Lr[f + mid - 1] < Rr[f + tr - mid])
-        lo = mid;
-      else
-        hi = mid - 1;
-    }
-    const uint32_t m = lo;
-    uint32_t cut;
-    if (m == 0) {
-      cut = Lr[f];
-    } else {
-      cut = Rr[f + tr - m];
-      if (m + 1 <= tl && Lr[f + m] < cut) cut = Lr[f + m];
-    }
-    sm.scalar[0] = m;
-    sm.scalar[1] = cut;
-  }
-  __syncthreads();
-  const uint32_t m = sm.scalar[0], cut = sm.scalar[1];
-  for (uint32_t q = 1 + t; q <= m; q += kBigBlock) isort::swap_kv(K, V, Lr[f + q - 1], Rr[f + tr - q]);
-  __syncthreads();
-  return cut;
-}
-
-__global__ void __launch_bounds__(kBigBlock) sort_big(uint64_t* K, uint32_t* V, uint32_t* Lg,
+__global__ void __launch_bounds__(kBigBlock, 4) sort_big(uint64_t* K, uint32_t* V, uint32_t* Lg,
                                                       uint32_t* Rg,
                                                       const uint64_t* __restrict__ begin,
                                                       const uint64_t* __restrict__ end,
@@ -616,7 +562,7 @@ __global__ void __launch_bounds__(kBigBlock) sort_big(uint64_t* K, uint32_t* V, 
         __syncthreads();
         continue;
       }
-      const uint32_t cut = big_partition_task(Ks, Vs, Ls, Rs, f, l, sm);
+      const uint32_t cut = round_partition<kBigBlock, uint32_t>(Ks, Vs, Ls, Rs, f, l, sm.rs);
       if (threadIdx.x == 0) {
         sm.gf[nt - 1] = cut;
         sm.gl[nt - 1] = l;
@@ -680,7 +626,7 @@ cudaError_t segmented_std_sort(uint64_t* keys, uint32_t* vals, uint32_t* lscratc
   sort_warp<<<num_sms, kWarpSegWarps * 32, sizeof(WarpSlice) * kWarpSegWarps, stream>>>(
       keys, vals, begin, end, lists + nseg, counts);
   count_launch();
-  sort_cta<<<num_sms, kBlock, sizeof(CtaSmem), stream>>>(keys, vals, begin, end,
+  sort_cta<<<num_sms * 3, kBlock, sizeof(CtaSmem), stream>>>(keys, vals, begin, end,
                                                          lists + 2 * static_cast<size_t>(nseg),
                                                          counts);
   count_launch();
@@ -688,7 +634,7 @@ cudaError_t segmented_std_sort(uint64_t* keys, uint32_t* vals, uint32_t* lscratc
                                                   lists + 3 * static_cast<size_t>(nseg), counts,
                                                   tasks.f, tasks.n, tasks.d, counts + 4);
   count_launch();
-  sort_tasks<<<num_sms, kBlock, sizeof(CtaSmem), stream>>>(keys, vals, tasks.f, tasks.n, tasks.d,
+  sort_tasks<<<num_sms * 3, kBlock, sizeof(CtaSmem), stream>>>(keys, vals, tasks.f, tasks.n, tasks.d,
                                                            counts + 4);
   return cudaGetLastError();
 }
