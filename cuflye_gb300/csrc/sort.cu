@@ -195,29 +195,73 @@ __device__ uint32_t round_partition(uint64_t* K, uint32_t* V, RT* Lr, RT* Rr, ui
     __syncthreads();
   }
   const uint32_t tl = carry_l, tr = carry_r;
-  if (t == 0) {
+  if (warp == 0) {
+    // m = largest k in [0, min(tl, tr)] with l_k < r_k (true for k = 0 and
+    // monotone): 32-way search, each lane probing one candidate per round.
     uint32_t lo = 0, hi = tl < tr ? tl : tr;
     while (lo < hi) {
-      const uint32_t mid = (lo + hi + 1) >> 1;
-      if (static_cast<uint32_t>(Lr[f + mid - 1]) < static_cast<uint32_t>(Rr[f + tr - mid]))
-        lo = mid;
-      else
-        hi = mid - 1;
+      const uint32_t step = (hi - lo + 31) / 32;
+      const uint32_t k = lo + (lane + 1) * step;
+      bool ok = false;
+      if (k <= hi)
+        ok = static_cast<uint32_t>(Lr[f + k - 1]) < static_cast<uint32_t>(Rr[f + tr - k]);
+      const unsigned mask = __ballot_sync(0xffffffffu, ok);
+      if (mask == 0) {
+        hi = lo + step - 1;
+      } else {
+        const uint32_t j = 31u - __clz(mask);
+        const uint32_t nlo = lo + (j + 1) * step;
+        hi = (nlo + step - 1 < hi) ? nlo + step - 1 : hi;
+        lo = nlo;
+      }
     }
-    const uint32_t m = lo;
-    uint32_t cut;
-    if (m == 0) {
-      cut = Lr[f];
-    } else {
-      cut = Rr[f + tr - m];
-      if (m + 1 <= tl && static_cast<uint32_t>(Lr[f + m]) < cut) cut = Lr[f + m];
+    if (lane == 0) {
+      const uint32_t m = lo;
+      uint32_t cut;
+      if (m == 0) {
+        cut = Lr[f];
+      } else {
+        cut = Rr[f + tr - m];
+        if (m + 1 <= tl && static_cast<uint32_t>(Lr[f + m]) < cut) cut = Lr[f + m];
+      }
+      rs.scalar[0] = m;
+      rs.scalar[1] = cut;
     }
-    rs.scalar[0] = m;
-    rs.scalar[1] = cut;
   }
   __syncthreads();
   const uint32_t m = rs.scalar[0], cut = rs.scalar[1];
-  for (uint32_t q = 1 + t; q <= m; q += BLOCK) isort::swap_kv(K, V, Lr[f + q - 1], Rr[f + tr - q]);
+  // swaps, four per thread per iteration so their loads overlap
+  for (uint32_t q0 = 1 + t; q0 <= m; q0 += 4 * BLOCK) {
+    uint32_t a[4], b[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t q = q0 + u * BLOCK;
+      if (q <= m) {
+        a[u] = Lr[f + q - 1];
+        b[u] = Rr[f + tr - q];
+      }
+    }
+    uint64_t ka[4], kb[4];
+    uint32_t va[4], vb[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      if (q0 + u * BLOCK <= m) {
+        ka[u] = K[a[u]];
+        kb[u] = K[b[u]];
+        va[u] = V[a[u]];
+        vb[u] = V[b[u]];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      if (q0 + u * BLOCK <= m) {
+        K[a[u]] = kb[u];
+        K[b[u]] = ka[u];
+        V[a[u]] = vb[u];
+        V[b[u]] = va[u];
+      }
+    }
+  }
   __syncthreads();
   return cut;
 }
@@ -479,7 +523,7 @@ __global__ void __launch_bounds__(kWarpSegWarps * 32) sort_warp(
   }
 }
 
-__global__ void __launch_bounds__(kBlock) sort_cta(uint64_t* K, uint32_t* V,
+__global__ void __launch_bounds__(kBlock, 3) sort_cta(uint64_t* K, uint32_t* V,
                                                    const uint64_t* __restrict__ begin,
                                                    const uint64_t* __restrict__ end,
                                                    const uint32_t* __restrict__ list,
@@ -578,7 +622,7 @@ __global__ void __launch_bounds__(kBigBlock, 4) sort_big(uint64_t* K, uint32_t* 
 }
 
 // Finishes the <= kCap tasks left by sort_big, one CTA per task.
-__global__ void __launch_bounds__(kBlock) sort_tasks(uint64_t* K, uint32_t* V,
+__global__ void __launch_bounds__(kBlock, 3) sort_tasks(uint64_t* K, uint32_t* V,
                                                      const uint64_t* __restrict__ task_f,
                                                      const uint32_t* __restrict__ task_n,
                                                      const int* __restrict__ task_d,
