@@ -230,6 +230,33 @@ cuflye_status cuflye_std_sort_segments(cuflye_ctx* ctx, uint64_t* keys, uint32_t
                                        const uint64_t* seg_offsets, size_t n_segments);
 
 /* --------------------------------------------------------------------------
+ * Allocation-free variant of cuflye_std_sort_segments, for callers that may
+ * not allocate device memory (for example a host process whose GPU memory
+ * is entirely owned by another allocator, or a worker held to a fixed,
+ * pre-declared footprint).  No counterpart in the reference.
+ *
+ * keys / values: the caller's DEVICE arrays, sorted in place.
+ * seg_offsets:   HOST array of n_segments + 1 offsets into them, all within
+ *                [0, n_elements].
+ * stream:        a cudaStream_t (NULL = default stream); the call returns
+ *                once the work is queued.
+ * Needs no context and makes no cudaMalloc / cudaFree or other allocating
+ * call: its scratch is one fixed device array of about 13.6 MiB that every
+ * GPU loading the library holds until exit.  Limits: n_elements <=
+ * CUFLYE_NOALLOC_MAX_ELEMENTS, n_segments <= CUFLYE_NOALLOC_MAX_SEGMENTS
+ * (larger requests return CUFLYE_ERR_UNSUPPORTED without doing anything).
+ * The first call on each device looks up that array's device address (with
+ * that device current); make that first call before any stream capture.
+ * Calls share the array: calls whose work overlaps on the GPU race and must
+ * not be issued.
+ * ------------------------------------------------------------------------ */
+#define CUFLYE_NOALLOC_MAX_ELEMENTS 1048576u
+#define CUFLYE_NOALLOC_MAX_SEGMENTS 65536u
+cuflye_status cuflye_std_sort_segments_noalloc(uint64_t* keys, uint32_t* values,
+                                               const uint64_t* seg_offsets, size_t n_segments,
+                                               size_t n_elements, void* stream);
+
+/* --------------------------------------------------------------------------
  * Timing of the last call's device work (CUDA events on the context's
  * stream), in milliseconds, by stage: 0 hit generation, 1 KmerMatch sort,
  * 2 group prefilter + ext re-sort, 3 chaining DP, 4 score sort + backtrack +
