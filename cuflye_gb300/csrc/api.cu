@@ -209,7 +209,7 @@ void build_index(cuflye_ctx* c, int k, size_t n, const int64_t* ids, const int64
   if (k < 1 || k > 31) throw Error(CUFLYE_ERR_UNSUPPORTED, "k must be in [1, 31]");
   if (n == 0) throw Error(CUFLYE_ERR_INVALID, "index needs at least one target");
   if (max_freq >= (1u << kCountBits) - 1)
-    throw Error(CUFLYE_ERR_UNSUPPORTED, "max_freq must be below 2^23 - 1");
+    throw Error(CUFLYE_ERR_UNSUPPORTED, "max_freq must be below 2^22 - 1");
   std::vector<size_t> order(n);
   for (size_t i = 0; i < n; ++i) {
     if (ids[i] <= 0) throw Error(CUFLYE_ERR_INVALID, "index target ids must be > 0");
@@ -299,7 +299,8 @@ void build_index(cuflye_ctx* c, int k, size_t n, const int64_t* ids, const int64
   while (cap < 2 * nruns) cap <<= 1;
   TableEntry* table = buf<TableEntry>(c, "ix_table", cap);
   CUFLYE_CHECK(cudaMemsetAsync(table, 0xff, cap * sizeof(TableEntry), st));
-  CUFLYE_CHECK(index_insert(keys, run_start, cls, kept_off, nruns, table, cap - 1, c->status, st));
+  CUFLYE_CHECK(index_insert(keys, vals, run_start, cls, kept_off, nruns, true, table, cap - 1,
+                            c->status, st));
   check_device_status(c);
   // statistics
   std::vector<uint8_t> h_cls(nruns);
@@ -395,7 +396,8 @@ void build_index_entries(cuflye_ctx* c, int k, size_t n, const int64_t* tids, co
   while (cap < 2 * (nruns + nrep)) cap <<= 1;
   TableEntry* table = buf<TableEntry>(c, "ix_table", cap);
   CUFLYE_CHECK(cudaMemsetAsync(table, 0xff, cap * sizeof(TableEntry), st));
-  CUFLYE_CHECK(index_insert(keys, run_start, cls, kept_off, nruns, table, cap - 1, c->status, st));
+  CUFLYE_CHECK(index_insert(keys, vals, run_start, cls, kept_off, nruns, false, table, cap - 1,
+                            c->status, st));
   if (nrep) {
     uint64_t* d_rep = buf<uint64_t>(c, "ib_rep", nrep);
     CUFLYE_CHECK(cudaMemcpyAsync(d_rep, rep_h, nrep * 8, cudaMemcpyHostToDevice, st));
@@ -438,11 +440,13 @@ struct PassState {
   uint64_t* q_off = nullptr;  // nq + 1 hit offsets
   uint64_t* f_off = nullptr;  // nq + 1 filtered offsets
   QueryInfo* qinfo = nullptr;
+  uint32_t* q_tie = nullptr;  // per query: its KmerMatch keys may repeat
 };
 
 // Buffers sized by the hit count of a pass (reused by the next pass).
-const char* const kPerHitBuffers[] = {"h_keys", "h_vals", "h_kmers", "s_l", "s_r", "g_flags",
-                                      "g_id", "c_cur", "c_ext", "c_score", "c_bt", "a_cand"};
+const char* const kPerHitBuffers[] = {"h_keys",  "h_vals", "h_kmers", "s_l",     "s_r",
+                                      "g_flags", "g_id",   "c_cur",   "c_ext",   "c_score",
+                                      "c_bt",    "a_cand", "m_tiles", "m_counts"};
 
 // The memory budget, or the device's memory less a 4 GiB margin when unbounded.
 uint64_t effective_budget(cuflye_ctx* c) {
@@ -512,7 +516,9 @@ bool run_hits(cuflye_ctx* c, const Queries& Q, size_t q0, size_t q1, bool want_k
   uint32_t* filt = buf<uint32_t>(c, "w_filt", nwin);
   uint64_t* wmeta = buf<uint64_t>(c, "w_meta", nwin);
   uint8_t* wflags = buf<uint8_t>(c, "w_flags", nwin);
-  CUFLYE_CHECK(hits_count(c->idx, qb, cnt, filt, wmeta, wflags, st));
+  ps.q_tie = buf<uint32_t>(c, "q_tie", nq);
+  CUFLYE_CHECK(cudaMemsetAsync(ps.q_tie, 0, std::max<uint64_t>(nq, 1) * 4ull, st));
+  CUFLYE_CHECK(hits_count(c->idx, qb, cnt, filt, wmeta, wflags, ps.q_tie, st));
   uint64_t* hit_off = buf<uint64_t>(c, "w_hitoff", nwin + 1);
   uint64_t* filt_off = buf<uint64_t>(c, "w_filtoff", nwin + 1);
   ps.nhits = scan_u32(c, cnt, hit_off, nwin, "w_scan");
@@ -600,11 +606,29 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
   uint32_t* rscr = buf<uint32_t>(c, "s_r", H + 1);
   uint32_t* lists = buf<uint32_t>(c, "s_lists", 4ull * std::max<uint64_t>(nq, 1));
   uint32_t* scounts = buf<uint32_t>(c, "s_counts", 8);
-  // 1. KmerMatch sort per query: (ext id, cur pos) with libstdc++ order
-  uint64_t* qb = buf<uint64_t>(c, "s_qb", nq + 1);
-  CUFLYE_CHECK(cudaMemcpyAsync(qb, ps.q_off, (nq + 1) * 8ull, cudaMemcpyDeviceToDevice, st));
+  uint32_t* ecount = buf<uint32_t>(c, "s_ecount", 1);
+  // 1. KmerMatch sort per query by (ext id, cur pos) in libstdc++ order:
+  // queries whose keys are distinct by a radix sort on the ext id, the others
+  // by the emulated introsort
+  uint64_t* qb = buf<uint64_t>(c, "s_qb", nq);
+  uint64_t* qe = buf<uint64_t>(c, "s_qe", nq);
+  uint32_t* ntiles = buf<uint32_t>(c, "m_ntiles", nq);
+  uint64_t* tile_off = buf<uint64_t>(c, "m_tileoff", nq + 1);
+  uint32_t* alt_h = reinterpret_cast<uint32_t*>(buf<int32_t>(c, "c_score", H));
+  uint32_t* alt_l = reinterpret_cast<uint32_t*>(buf<int32_t>(c, "c_cur", H));
+  uint32_t* alt_v = reinterpret_cast<uint32_t*>(buf<int32_t>(c, "c_ext", H));
+  int id_bits = 0;
+  while (id_bits < 32 && ((2ull * c->idx.nslots - 1) >> id_bits) != 0) ++id_bits;
   CUFLYE_CHECK(cudaEventRecord(c->ev[1], st));
-  CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, qb, qb + 1, nq, nullptr, lists,
+  CUFLYE_CHECK(match_plan(ps.q_off, ps.q_tie, nq, ntiles, qb, qe, ecount, st));
+  const uint64_t NT = scan_u32(c, ntiles, tile_off, nq, "m_scan");
+  MatchTile* tiles = buf<MatchTile>(c, "m_tiles", NT);
+  uint32_t* mcounts = buf<uint32_t>(c, "m_counts", 256 * NT);
+  CUFLYE_CHECK(match_tiles(ps.q_off, ntiles, tile_off, nq, tiles, st));
+  CUFLYE_CHECK(match_radix(ps.keys, ps.vals, alt_h, alt_l, alt_v, tiles,
+                           static_cast<uint32_t>(NT), ps.q_off, ntiles, tile_off, nq, id_bits,
+                           mcounts, c->num_sms, st));
+  CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, qb, qe, nq, ecount, lists,
                                   scounts, c->num_sms, st, sort_tasks(c, "s", H, nq)));
   CUFLYE_CHECK(cudaEventRecord(c->ev[2], st));
   // 2. groups
@@ -625,9 +649,11 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
   uint64_t* se = buf<uint64_t>(c, "g_se", G);
   uint32_t* glists = buf<uint32_t>(c, "g_lists", 4 * std::max<uint64_t>(G, 1));
   const uint32_t G32 = static_cast<uint32_t>(G);
-  // 3. ext-sorted groups: re-sort by ext pos
-  CUFLYE_CHECK(groups_prepare_ext_sort(ps.keys, ps.vals, groups, ext_list, gcounts, sb, se, st));
-  CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, sb, se, G32, gcounts + 0, glists,
+  // 3. ext-sorted groups: re-sort by ext pos (groups with distinct ext
+  // positions in shared memory, the others by the emulated introsort)
+  CUFLYE_CHECK(group_sort(0, ps.keys, ps.vals, nullptr, groups, ext_list, gcounts + 0, G32, cp.k,
+                          sb, se, ecount, c->num_sms, st));
+  CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, sb, se, G32, ecount, glists,
                                   scounts, c->num_sms, st, sort_tasks(c, "s", H, G32)));
   int32_t* cur = buf<int32_t>(c, "c_cur", H);
   int32_t* ext = buf<int32_t>(c, "c_ext", H);
@@ -638,9 +664,12 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
   CUFLYE_CHECK(cudaEventRecord(c->ev[6], st));
   CUFLYE_CHECK(chain_dp(cur, ext, score, bt, groups, dp_list, gcounts, cp, c->num_sms, st));
   CUFLYE_CHECK(cudaEventRecord(c->ev[7], st));
-  // 5. score order (libstdc++ order of indices by score descending)
-  CUFLYE_CHECK(chain_prepare_order(score, ps.keys, ps.vals, groups, dp_list, gcounts, sb, se, st));
-  CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, sb, se, G32, gcounts + 1, glists,
+  // 5. score order (libstdc++ order of indices by score descending): groups
+  // whose scores above k are distinct in shared memory, the others by the
+  // emulated introsort
+  CUFLYE_CHECK(group_sort(1, ps.keys, ps.vals, score, groups, dp_list, gcounts + 1, G32, cp.k, sb,
+                          se, ecount, c->num_sms, st));
+  CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, sb, se, G32, ecount, glists,
                                   scounts, c->num_sms, st, sort_tasks(c, "s", H, G32)));
   // 6. backtrack, proposals, primary selection; the row pool is sized by the
   // groups that survived the prefilter

@@ -63,8 +63,12 @@ struct alignas(16) TableEntry {
 };
 constexpr uint64_t kEmptyKey = ~0ULL;  // never a standard form (see index.cu)
 constexpr uint64_t kOffsetMask = (1ULL << 40) - 1;
-constexpr uint32_t kCountBits = 23;
+constexpr uint32_t kCountBits = 22;
 constexpr uint64_t kRepetitiveBit = 1ULL << 63;
+// A solid bucket listing one stored target id more than once: a query window
+// that looks it up yields two hits on one target, i.e. two equal
+// (ext id, cur pos) KmerMatch keys.
+constexpr uint64_t kDupIdsBit = 1ULL << 62;
 
 __device__ __forceinline__ uint64_t table_probe(const TableEntry* __restrict__ table,
                                                 uint64_t mask, uint64_t key, bool* found) {

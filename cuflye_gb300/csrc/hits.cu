@@ -53,7 +53,7 @@ __device__ __forceinline__ WindowKmer window_kmer(const QueryBatch& q, uint32_t 
 
 __global__ void count_kernel(DeviceIndex idx, QueryBatch q, uint32_t* __restrict__ cnt,
                              uint32_t* __restrict__ filt, uint64_t* __restrict__ wmeta,
-                             uint8_t* __restrict__ wflags) {
+                             uint8_t* __restrict__ wflags, uint32_t* __restrict__ q_tie) {
   const uint64_t w = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (w >= q.nwin) return;
   const uint32_t qi = query_of(q.win_off, q.nq, w);
@@ -67,6 +67,7 @@ __global__ void count_kernel(DeviceIndex idx, QueryBatch q, uint32_t* __restrict
     fl |= kFlagFiltered;
   } else if (found) {
     c = static_cast<uint32_t>((meta >> 40) & ((1ULL << kCountBits) - 1));
+    if ((meta & kDupIdsBit) && q_tie[qi] == 0) atomicOr(q_tie + qi, 1u);
     const int32_t qdi = q.qdi[qi];
     if (c > 0 && qdi >= 0) {
       // Is the query's own window among the bucket entries?  Stored form of
@@ -161,11 +162,12 @@ __global__ void gather_kernel(const uint64_t* __restrict__ win_off,
 }  // namespace
 
 cudaError_t hits_count(const DeviceIndex& idx, const QueryBatch& q, uint32_t* cnt,
-                       uint32_t* filt, uint64_t* wmeta, uint8_t* wflags, cudaStream_t s) {
+                       uint32_t* filt, uint64_t* wmeta, uint8_t* wflags, uint32_t* q_tie,
+                       cudaStream_t s) {
   if (q.nwin == 0) return cudaSuccess;
   count_launch();
   count_kernel<<<static_cast<unsigned>((q.nwin + 255) / 256), 256, 0, s>>>(idx, q, cnt, filt,
-                                                                          wmeta, wflags);
+                                                                          wmeta, wflags, q_tie);
   return cudaGetLastError();
 }
 

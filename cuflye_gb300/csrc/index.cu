@@ -126,21 +126,32 @@ __device__ bool table_insert(TableEntry* table, uint64_t mask, uint64_t key, uin
   return false;
 }
 
+// vals: the run's entries, (stored id << 32) | stored position.  With
+// sorted_ids the entries of a run are in (id, position) order and a repeated
+// id shows as two neighbours; otherwise (explicit entries in input order)
+// every run of two or more entries is marked.
 __global__ void insert_kernel(const uint64_t* __restrict__ keys,
+                              const uint64_t* __restrict__ vals,
                               const uint64_t* __restrict__ run_start,
                               const uint8_t* __restrict__ cls,
                               const uint64_t* __restrict__ kept_off, uint64_t nruns,
-                              TableEntry* table, uint64_t mask, DeviceStatus* st) {
+                              bool sorted_ids, TableEntry* table, uint64_t mask,
+                              DeviceStatus* st) {
   const uint64_t r = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (r >= nruns || cls[r] == 0) return;
-  const uint64_t key = keys[run_start[r]];
-  const uint64_t freq = run_start[r + 1] - run_start[r];
+  const uint64_t r0 = run_start[r];
+  const uint64_t key = keys[r0];
+  const uint64_t freq = run_start[r + 1] - r0;
   uint64_t meta;
   if (cls[r] == 2) {
     const uint64_t c = freq < ((1ULL << kCountBits) - 1) ? freq : ((1ULL << kCountBits) - 1);
     meta = kRepetitiveBit | (c << 40);
   } else {
     meta = (kept_off[r] & kOffsetMask) | (freq << 40);
+    bool dup = !sorted_ids && freq > 1;
+    for (uint64_t e = 1; sorted_ids && e < freq && !dup; ++e)
+      dup = (vals[r0 + e] >> 32) == (vals[r0 + e - 1] >> 32);
+    if (dup) meta |= kDupIdsBit;
   }
   if (!table_insert(table, mask, key, meta, false)) raise_status(st, kDevTableFull, 0, r);
 }
@@ -204,13 +215,14 @@ cudaError_t index_copy_positions(const uint64_t* vals, const uint64_t* run_id,
   return cudaGetLastError();
 }
 
-cudaError_t index_insert(const uint64_t* keys, const uint64_t* run_start, const uint8_t* cls,
-                         const uint64_t* kept_off, uint64_t nruns, TableEntry* table,
-                         uint64_t mask, DeviceStatus* st, cudaStream_t s) {
+cudaError_t index_insert(const uint64_t* keys, const uint64_t* vals, const uint64_t* run_start,
+                         const uint8_t* cls, const uint64_t* kept_off, uint64_t nruns,
+                         bool sorted_ids, TableEntry* table, uint64_t mask, DeviceStatus* st,
+                         cudaStream_t s) {
   if (nruns == 0) return cudaSuccess;
   count_launch();
-  insert_kernel<<<grid(nruns, 256), 256, 0, s>>>(keys, run_start, cls, kept_off, nruns, table,
-                                                 mask, st);
+  insert_kernel<<<grid(nruns, 256), 256, 0, s>>>(keys, vals, run_start, cls, kept_off, nruns,
+                                                 sorted_ids, table, mask, st);
   return cudaGetLastError();
 }
 

@@ -79,9 +79,13 @@ cudaError_t index_copy_positions(const uint64_t* vals, const uint64_t* run_id,
                                  const uint64_t* run_start, const uint8_t* cls,
                                  const uint64_t* kept_off, uint64_t n, uint64_t* pos,
                                  cudaStream_t s);
-cudaError_t index_insert(const uint64_t* keys, const uint64_t* run_start, const uint8_t* cls,
-                         const uint64_t* kept_off, uint64_t nruns, TableEntry* table,
-                         uint64_t mask, DeviceStatus* st, cudaStream_t s);
+// Table insert of every solid and repetitive run.  Solid buckets that list
+// one stored id twice get kDupIdsBit (sorted_ids: runs are in (id, position)
+// order; otherwise every run of two or more entries is marked).
+cudaError_t index_insert(const uint64_t* keys, const uint64_t* vals, const uint64_t* run_start,
+                         const uint8_t* cls, const uint64_t* kept_off, uint64_t nruns,
+                         bool sorted_ids, TableEntry* table, uint64_t mask, DeviceStatus* st,
+                         cudaStream_t s);
 cudaError_t index_insert_repetitive(const uint64_t* rep_keys, uint64_t n, TableEntry* table,
                                     uint64_t mask, DeviceStatus* st, cudaStream_t s);
 
@@ -95,8 +99,11 @@ struct QueryBatch {
   uint64_t nwin = 0;
 };
 
+// q_tie[i] (zeroed by the caller) becomes nonzero when query i looks up a
+// bucket with kDupIdsBit, i.e. when its KmerMatch keys may repeat.
 cudaError_t hits_count(const DeviceIndex& idx, const QueryBatch& q, uint32_t* cnt,
-                       uint32_t* filt, uint64_t* wmeta, uint8_t* wflags, cudaStream_t s);
+                       uint32_t* filt, uint64_t* wmeta, uint8_t* wflags, uint32_t* q_tie,
+                       cudaStream_t s);
 // keys[j] = (ext dense id << 32) | cur pos, vals[j] = ext pos, kmers (optional).
 cudaError_t hits_emit(const DeviceIndex& idx, const QueryBatch& q, const uint64_t* hit_off,
                       const uint64_t* filt_off, const uint64_t* wmeta, const uint8_t* wflags,
@@ -142,6 +149,42 @@ struct QueryInfo {
   int32_t len;
   int32_t pad;
 };
+
+// ---------------------------------------------------------------- exact fast sorts
+// Sort points whose segments hold no equal keys need no libstdc++-order
+// emulation (fastsort.cu); segments that may hold equal keys are listed in
+// (emu_begin, emu_end, *emu_count) for segmented_std_sort.
+constexpr uint32_t kMatchTile = 4096;  // hits per radix tile (never across queries)
+constexpr uint32_t kGroupCap = 16384;  // largest group sorted in shared memory
+
+struct MatchTile {
+  uint64_t begin;
+  uint32_t n;
+  uint32_t query;
+};
+
+// Per query: flagged (q_tie) queries with two or more hits are listed for the
+// emulated sort; the others get ntiles[q] radix tiles.
+cudaError_t match_plan(const uint64_t* q_off, const uint32_t* q_tie, uint32_t nq, uint32_t* ntiles,
+                       uint64_t* emu_begin, uint64_t* emu_end, uint32_t* emu_count,
+                       cudaStream_t s);
+// tile_off: exclusive scan of ntiles.
+cudaError_t match_tiles(const uint64_t* q_off, const uint32_t* ntiles, const uint64_t* tile_off,
+                        uint32_t nq, MatchTile* tiles, cudaStream_t s);
+// Stable radix sort by the ext id (key bits 32 .. 32 + id_bits) of every
+// tiled query, in place in (keys, vals); alt_* are three word arrays of one
+// word per hit and counts holds 256 words per tile.
+cudaError_t match_radix(uint64_t* keys, uint32_t* vals, uint32_t* alt_hi, uint32_t* alt_lo,
+                        uint32_t* alt_val, const MatchTile* tiles, uint32_t ntile,
+                        const uint64_t* q_off, const uint32_t* ntiles, const uint64_t* tile_off,
+                        uint32_t nq, int id_bits, uint32_t* counts, int num_sms, cudaStream_t s);
+// Groups of list[0 .. *list_count): mode 0 re-sorts ext-sorted groups by ext
+// pos (out: key = ext pos, val = cur pos); mode 1 writes the score order
+// (val[i] = local index of the i-th element by score descending).
+cudaError_t group_sort(int mode, uint64_t* keys, uint32_t* vals, const int32_t* score,
+                       const GroupInfo* groups, const uint32_t* list, const uint32_t* list_count,
+                       uint32_t max_groups, int32_t k, uint64_t* emu_begin, uint64_t* emu_end,
+                       uint32_t* emu_count, int num_sms, cudaStream_t s);
 
 cudaError_t groups_mark(const uint64_t* keys, const uint64_t* q_off, uint32_t nq, uint64_t nhits,
                         uint32_t* flags, cudaStream_t s);
