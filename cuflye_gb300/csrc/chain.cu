@@ -9,7 +9,7 @@
 //   chain_backtrack: score-ordered backtrack (order from the libstdc++-order
 //                    sort of the scores), overlapTest, k-mer divergence,
 //                    proposal sort, primary selection and the divergence
-//                    filter, one thread per group;
+//                    filter, one warp per group;
 //   rows_*         : max_overlaps cutoff per query and order-preserving
 //                    compaction of the rows.
 #include <climits>
@@ -175,15 +175,18 @@ __global__ void split_kernel(const uint64_t* __restrict__ keys, const uint32_t* 
 // max over lanes gives each lane the running maximum before it, a ballot
 // finds the first lane that ends the scan, and the winner is the first lane
 // at or before it that attains the maximum (later equal scores do not update).
-// The 32 most recent elements live in a per-warp ring in shared memory; a
-// one-step fast path handles the common case where j = i-1 itself updates
-// and breaks.
+//
+// Most elements end the scan at j = i-1: it updates (its score is at least 0,
+// and the match adds at least 1) and breaks when 0 < curDelta = extDelta < k
+// (both under maxJump).  That test needs positions only, so the warp marks
+// such "step" elements for 32 elements at once.  Along a run of steps the
+// score is a prefix sum: S[i] = max(S[i-1] + curDelta, k), which is
+// S[i-1] + curDelta whenever S[i-1] >= k (every element but the first has
+// S >= k), and the link is i-1 whenever that sum exceeds k.  The warp scores
+// each run with one prefix sum over lanes and scans predecessors only for the
+// other elements.
 
 constexpr int kDpWarps = 8;
-
-struct DpRing {
-  int32_t c[32], e[32], s[32];
-};
 
 __device__ __forceinline__ void eval_chunk(bool valid, int32_t cj, int32_t ej, int32_t sj,
                                            int32_t j, int32_t ci, int32_t ei, bool es,
@@ -227,10 +230,8 @@ __global__ void __launch_bounds__(kDpWarps * 32) dp_kernel(
     const int32_t* __restrict__ cur, const int32_t* __restrict__ ext, int32_t* score,
     int32_t* bt, const GroupInfo* __restrict__ groups, const uint32_t* __restrict__ list,
     const uint32_t* __restrict__ counts, ChainParams p) {
-  __shared__ DpRing rings[kDpWarps];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  DpRing& ring = rings[wib];
   const uint32_t cnt = counts[1];
   const uint32_t nwarps = gridDim.x * kDpWarps;
   for (uint32_t li = blockIdx.x * kDpWarps + wib; li < cnt; li += nwarps) {
@@ -238,63 +239,67 @@ __global__ void __launch_bounds__(kDpWarps * 32) dp_kernel(
     const uint64_t b = g.start;
     const uint32_t n = g.n;
     const bool es = g.ext_sorted != 0;
-    // prefetched block of 32 consecutive elements: lane L holds element i0 + L
-    uint32_t i0 = 0;
-    int32_t bc = 0, be = 0;
-    if (lane < static_cast<int>(n)) {
-      bc = __ldg(cur + b + lane);
-      be = __ldg(ext + b + lane);
-    }
-    int32_t pc = __shfl_sync(0xffffffffu, bc, 0), pe = __shfl_sync(0xffffffffu, be, 0);
-    int32_t pscore = 0;
-    if (lane == 0) {
-      ring.c[0] = pc;
-      ring.e[0] = pe;
-      ring.s[0] = 0;
-      score[b] = 0;
-      bt[b] = -1;
-    }
-    __syncwarp();
-    for (uint32_t i = 1; i < n; ++i) {
-      if (i - i0 == 32) {
-        i0 = i;
-        if (i0 + lane < n) {
-          bc = __ldg(cur + b + i0 + lane);
-          be = __ldg(ext + b + i0 + lane);
-        }
+    int32_t s_prev = 0;        // score of the element before the next one to score
+    int32_t pc = 0, pe = 0;    // positions of the element before this chunk
+    for (uint32_t i0 = 0; i0 < n; i0 += 32) {
+      const uint32_t i = i0 + lane;
+      const uint32_t len = min(32u, n - i0);
+      int32_t ci = 0, ei = 0;
+      if (i < n) {
+        ci = __ldg(cur + b + i);
+        ei = __ldg(ext + b + i);
       }
-      const int32_t ci = __shfl_sync(0xffffffffu, bc, i - i0);
-      const int32_t ei = __shfl_sync(0xffffffffu, be, i - i0);
-      int32_t best = 0, bestj = 0;
-      // fast path: j = i - 1 updates and breaks
-      {
-        const int32_t cd = ci - pc, ed = ei - pe;
-        const int32_t jd = abs(cd - ed);
-        bool fast = false;
-        if (cd > 0 && cd < p.max_jump && ed > 0 && ed < p.max_jump && jd == 0 && cd < p.k) {
-          const int32_t sc = pscore + min(min(cd, ed), p.k);
-          if (sc > 0) {
-            best = sc;
-            bestj = static_cast<int32_t>(i) - 1;
-            fast = true;
-          }
+      int32_t cp = __shfl_up_sync(0xffffffffu, ci, 1);
+      int32_t ep = __shfl_up_sync(0xffffffffu, ei, 1);
+      if (lane == 0) {
+        cp = pc;
+        ep = pe;
+      }
+      const int32_t cd = ci - cp, ed = ei - ep;
+      const bool step = i < n && i > 0 && cd > 0 && cd < p.max_jump && cd == ed && cd < p.k;
+      const unsigned smask = __ballot_sync(0xffffffffu, step);
+      int32_t s_mine = 0;
+      uint32_t t = 0;
+      if (i0 == 0) {
+        if (lane == 0) {
+          score[b] = 0;
+          bt[b] = -1;
         }
-        if (!fast) {
-          bool done = false;
-          // chunk 0 from the ring
-          {
-            const int32_t j = static_cast<int32_t>(i) - 1 - lane;
-            const bool valid = j >= 0;
-            int32_t cj = 0, ej = 0, sj = 0;
-            if (valid) {
-              const int r = j & 31;
-              cj = ring.c[r];
-              ej = ring.e[r];
-              sj = ring.s[r];
-            }
-            eval_chunk(valid, cj, ej, sj, j, ci, ei, es, p, best, bestj, done);
+        t = 1;
+      }
+      while (t < len) {
+        // run of step elements [t, u)
+        const unsigned rest = ~smask & (0xffffffffu << t);
+        const uint32_t u = min(rest ? static_cast<uint32_t>(__ffs(rest) - 1) : 32u, len);
+        if (u > t) {
+          const bool in = lane >= static_cast<int>(t) && lane < static_cast<int>(u);
+          int32_t x = in ? cd : 0;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const int32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
           }
-          for (int32_t c0 = static_cast<int32_t>(i) - 33; !done && c0 >= 0; c0 -= 32) {
+          const int32_t dt = __shfl_sync(0xffffffffu, cd, t);
+          const int32_t first = max(s_prev + dt, p.k);
+          if (in) {
+            s_mine = first + (x - dt);
+            score[b + i] = s_mine;
+            bt[b + i] = (lane > static_cast<int>(t) || s_prev + dt > p.k)
+                            ? static_cast<int32_t>(i) - 1
+                            : -1;
+          }
+          s_prev = __shfl_sync(0xffffffffu, s_mine, u - 1);
+          t = u;
+        }
+        if (t < len) {
+          // predecessor scan for element i0 + t
+          __syncwarp();
+          const int32_t cit = __shfl_sync(0xffffffffu, ci, t);
+          const int32_t eit = __shfl_sync(0xffffffffu, ei, t);
+          const int32_t it = static_cast<int32_t>(i0 + t);
+          int32_t best = 0, bestj = 0;
+          bool done = false;
+          for (int32_t c0 = it - 1; !done && c0 >= 0; c0 -= 32) {
             const int32_t j = c0 - lane;
             const bool valid = j >= 0;
             int32_t cj = 0, ej = 0, sj = 0;
@@ -303,25 +308,22 @@ __global__ void __launch_bounds__(kDpWarps * 32) dp_kernel(
               ej = __ldg(ext + b + j);
               sj = __ldcg(score + b + j);
             }
-            eval_chunk(valid, cj, ej, sj, j, ci, ei, es, p, best, bestj, done);
+            eval_chunk(valid, cj, ej, sj, j, cit, eit, es, p, best, bestj, done);
           }
+          const int32_t si = max(best, p.k);
+          if (lane == static_cast<int>(t)) {
+            s_mine = si;
+            score[b + it] = si;
+            bt[b + it] = best > p.k ? bestj : -1;
+          }
+          s_prev = si;
+          ++t;
         }
+        __syncwarp();
       }
-      const int32_t si = max(best, p.k);
-      if (lane == 0) {
-        const int r = i & 31;
-        ring.c[r] = ci;
-        ring.e[r] = ei;
-        ring.s[r] = si;
-        score[b + i] = si;
-        bt[b + i] = best > p.k ? bestj : -1;
-      }
-      __syncwarp();
-      pc = ci;
-      pe = ei;
-      pscore = si;
+      pc = __shfl_sync(0xffffffffu, ci, 31);
+      pe = __shfl_sync(0xffffffffu, ei, 31);
     }
-    __syncwarp();
   }
 }
 
@@ -397,8 +399,85 @@ __device__ __forceinline__ uint32_t lower_bound_i32(const int32_t* a, uint32_t n
 // live chain (Flye's serial order) and builds its proposal.  After a walk the
 // remaining starts of the step are tested again, since the walk may have
 // consumed them.
+// Flye walks chains in score order: from each start whose backtrack entry is
+// still set it follows the links, clearing every entry it visits, and the
+// chain ends at the first node whose entry is -1 (never linked, or cleared
+// by an earlier walk).  For groups of up to kBtCap elements a warp keeps
+// three bitmaps in shared memory in place of the table: linked (entry != -1
+// at the start), step (entry == i - 1) and cleared.  A walk crosses a run of
+// step links in one 32-word search per 1,024 nodes (the next node that is not
+// a step or is cleared) and clears the run word by word; only links that are
+// not steps are read from the table, which stays unchanged.  The warp counts
+// linked nodes not yet cleared and ends the score-order loop when none is
+// left: no later start could begin a chain.  Larger groups walk the table in
+// global memory with one lane.
+
 constexpr uint32_t kBtCap = 16384;
-constexpr int kBtWarps = 6;
+constexpr uint32_t kBtWords = kBtCap / 32;
+constexpr int kBtWarps = 8;
+
+struct BtMaps {
+  uint32_t link[kBtWords];
+  uint32_t step[kBtWords];
+  uint32_t done[kBtWords];
+};
+
+__device__ __forceinline__ uint32_t bits_upto(int32_t pos) {
+  const int r = pos & 31;
+  return r == 31 ? 0xffffffffu : ((2u << r) - 1u);
+}
+
+__device__ __forceinline__ uint32_t warp_sum_u32(uint32_t v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Walk from s0 (linked, not cleared) with the whole warp: first node and
+// chain length as Flye's walk counts them; visited nodes become cleared and
+// `remaining` drops by the linked ones among them.
+__device__ void walk_maps(BtMaps& m, const int32_t* __restrict__ btg, int32_t s0, int32_t& first,
+                          int32_t& clen, uint32_t& remaining) {
+  const int lane = threadIdx.x & 31;
+  int32_t pos = s0;
+  clen = 0;
+  for (;;) {
+    // z: the highest node <= pos that is not an uncleared step
+    int32_t z = -1;
+    for (int32_t w0 = pos >> 5; z < 0; w0 -= 32) {
+      const int32_t w = w0 - lane;
+      uint32_t bits = 0;
+      if (w >= 0) {
+        bits = ~m.step[w] | m.done[w];
+        if (w == (pos >> 5)) bits &= bits_upto(pos);
+      }
+      const unsigned bal = __ballot_sync(0xffffffffu, bits != 0);
+      if (bal) {
+        const int l = __ffs(bal) - 1;
+        const uint32_t wb = __shfl_sync(0xffffffffu, bits, l);
+        z = (w0 - l) * 32 + 31 - __clz(wb);
+      }
+    }
+    const bool stop = ((m.done[z >> 5] >> (z & 31)) & 1u) || !((m.link[z >> 5] >> (z & 31)) & 1u);
+    __syncwarp();
+    uint32_t newly = 0;
+    for (int32_t w = (z >> 5) + lane; w <= (pos >> 5); w += 32) {
+      uint32_t mask = 0xffffffffu;
+      if (w == (z >> 5)) mask &= 0xffffffffu << (z & 31);
+      if (w == (pos >> 5)) mask &= bits_upto(pos);
+      newly += __popc(m.link[w] & ~m.done[w] & mask);
+      m.done[w] |= mask;
+    }
+    remaining -= warp_sum_u32(newly);
+    clen += pos - z + 1;
+    __syncwarp();
+    if (stop) {
+      first = z;
+      return;
+    }
+    pos = btg[z];  // a link to a node other than z - 1
+  }
+}
 
 __global__ void __launch_bounds__(kBtWarps * 32) backtrack_kernel(
     const int32_t* __restrict__ cur, const int32_t* __restrict__ ext,
@@ -409,9 +488,9 @@ __global__ void __launch_bounds__(kBtWarps * 32) backtrack_kernel(
     const int64_t* __restrict__ slot_signed, LogfTable logt, ChainParams p,
     OverlapRow* __restrict__ pool, uint64_t pool_cap, uint32_t* __restrict__ pool_count,
     uint32_t* __restrict__ group_rows, DeviceStatus* st) {
-  extern __shared__ uint16_t bt_stage[];
+  extern __shared__ __align__(16) unsigned char bt_raw[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  uint16_t* bts = bt_stage + static_cast<size_t>(wib) * kBtCap;
+  BtMaps& m = reinterpret_cast<BtMaps*>(bt_raw)[wib];
   const uint32_t cnt = counts[1];
   const uint32_t nwarps = gridDim.x * kBtWarps;
   for (uint32_t li = blockIdx.x * kBtWarps + wib; li < cnt; li += nwarps) {
@@ -424,45 +503,52 @@ __global__ void __launch_bounds__(kBtWarps * 32) backtrack_kernel(
                                              : slot_signed[g.ext_di >> 1];
   const int32_t* fq = fpos + f_off[g.query];
   const uint32_t nf = static_cast<uint32_t>(f_off[g.query + 1] - f_off[g.query]);
-  const bool staged = g.n <= kBtCap;
-  if (staged) {
-    for (uint32_t j = lane; j < g.n; j += 32) {
-      const int32_t v = bt[b + j];
-      bts[j] = v < 0 ? 0xFFFFu : static_cast<uint16_t>(v);
+  const bool mapped = g.n <= kBtCap;
+  uint32_t remaining = 0;
+  if (mapped) {
+    const uint32_t nw = (g.n + 31) / 32;
+    for (uint32_t w = 0; w < nw; ++w) {
+      const uint32_t j = w * 32 + lane;
+      const int32_t v = j < g.n ? bt[b + j] : -1;
+      const unsigned lk = __ballot_sync(0xffffffffu, v != -1);
+      const unsigned sp = __ballot_sync(0xffffffffu, j >= 1 && v == static_cast<int32_t>(j) - 1);
+      if (lane == 0) {
+        m.link[w] = lk;
+        m.step[w] = sp;
+        m.done[w] = 0;
+      }
+      remaining += __popc(lk);
     }
+    __syncwarp();
   }
-  __syncwarp();
   Prop props[kMaxProposals];
   int np = 0;
   bool overflow = false;
-  for (uint32_t o0 = 0; o0 < g.n; o0 += 32) {
+  for (uint32_t o0 = 0; o0 < g.n && !(mapped && remaining == 0); o0 += 32) {
     const uint32_t oi = o0 + lane;
     const bool valid = oi < g.n;
     const uint32_t start = valid ? order[b + oi] : 0;
-    unsigned mask = __ballot_sync(0xffffffffu, valid && (staged ? bts[start] != 0xFFFFu
-                                                                 : bt[b + start] != -1));
+    unsigned mask = __ballot_sync(
+        0xffffffffu, valid && (mapped ? (((m.link[start >> 5] & ~m.done[start >> 5]) >>
+                                          (start & 31)) & 1u) != 0
+                                      : bt[b + start] != -1));
     while (mask) {
       const int j = __ffs(mask) - 1;
       const uint32_t s0 = __shfl_sync(0xffffffffu, start, j);
-      if (lane == 0 && !overflow) {
-        int32_t pos = static_cast<int32_t>(s0), first = 0, clen = 0;
-        if (staged) {
-          while (pos != -1) {
-            first = pos;
-            ++clen;
-            const uint16_t nx = bts[pos];
-            bts[pos] = 0xFFFFu;
-            pos = nx == 0xFFFFu ? -1 : static_cast<int32_t>(nx);
-          }
-        } else {
-          while (pos != -1) {
-            first = pos;
-            ++clen;
-            const int32_t nx = bt[b + pos];
-            bt[b + pos] = -1;
-            pos = nx;
-          }
+      int32_t first = 0, clen = 0;
+      if (mapped) {
+        walk_maps(m, bt + b, static_cast<int32_t>(s0), first, clen, remaining);
+      } else if (lane == 0 && !overflow) {
+        int32_t pos = static_cast<int32_t>(s0);
+        while (pos != -1) {
+          first = pos;
+          ++clen;
+          const int32_t nx = bt[b + pos];
+          bt[b + pos] = -1;
+          pos = nx;
         }
+      }
+      if (lane == 0 && !overflow) {
         Prop o;
         o.cb = cur[b + first];
         o.ce = cur[b + s0] + k - 1;
@@ -495,8 +581,12 @@ __global__ void __launch_bounds__(kBtWarps * 32) backtrack_kernel(
         }
       }
       __syncwarp();
-      mask = __ballot_sync(0xffffffffu, valid && lane > j &&
-                                            (staged ? bts[start] != 0xFFFFu : bt[b + start] != -1));
+      if (mapped && remaining == 0) break;
+      mask = __ballot_sync(
+          0xffffffffu,
+          valid && lane > j &&
+              (mapped ? (((m.link[start >> 5] & ~m.done[start >> 5]) >> (start & 31)) & 1u) != 0
+                      : bt[b + start] != -1));
     }
   }
   __syncwarp();
@@ -683,18 +773,15 @@ cudaError_t chain_backtrack(const int32_t* cur, const int32_t* ext, const int32_
                             uint32_t* pool_count, uint32_t* group_rows, DeviceStatus* st,
                             uint32_t max_groups, cudaStream_t s) {
   if (max_groups == 0) return cudaSuccess;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(backtrack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         static_cast<int>(kBtCap * sizeof(uint16_t) * kBtWarps));
-    attr = true;
-  }
+  constexpr size_t smem = sizeof(BtMaps) * kBtWarps;
+  cudaFuncSetAttribute(backtrack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       static_cast<int>(smem));
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (sms <= 0) sms = 1;
   count_launch();
-  backtrack_kernel<<<sms, kBtWarps * 32, kBtCap * sizeof(uint16_t) * kBtWarps, s>>>(
+  backtrack_kernel<<<sms * 4, kBtWarps * 32, smem, s>>>(
       cur, ext, score, bt, order, groups, dp_list, counts, qinfo, f_off, fpos, slot_signed, logt,
       p, pool, pool_cap, pool_count, group_rows, st);
   return cudaGetLastError();
