@@ -133,6 +133,8 @@ def load_library(path: Path | None = None) -> ctypes.CDLL:
     L.cuflye_kernel_launches.argtypes = [_u64p]
     L.cuflye_last_timing.restype = S
     L.cuflye_last_timing.argtypes = [_vp, ctypes.POINTER(ctypes.c_double), _u64p, ctypes.c_size_t]
+    L.cuflye_last_sort_stats.restype = S
+    L.cuflye_last_sort_stats.argtypes = [_vp, _u64p, ctypes.c_size_t]
     _LIB = L
     return L
 
@@ -232,6 +234,15 @@ class CudaBackend:
         by = (ctypes.c_uint64 * 7)()
         self._check(self._L.cuflye_last_timing(self._h, ms, by, 7))
         return list(ms), list(by)
+
+    SORT_STATS = ("match_plain", "match_libstdcxx", "ext_plain", "ext_libstdcxx", "score_plain",
+                  "score_libstdcxx", "backtrack_redo")
+
+    def last_sort_stats(self) -> dict:
+        """How the last overlaps / read-to-graph call's sort points ran (segments per path)."""
+        v = (ctypes.c_uint64 * 7)()
+        self._check(self._L.cuflye_last_sort_stats(self._h, v, 7))
+        return dict(zip(self.SORT_STATS, list(v)))
 
     # -- index
     def build_index(self, targets, k: int, min_freq: int, max_freq: int) -> dict:

@@ -77,11 +77,13 @@ struct cuflye_ctx {
   cudaEvent_t ev[8]{};
   double stage_ms[7]{};
   uint64_t stage_bytes[7]{};
+  uint64_t sort_stats[7]{};  // see cuflye_last_sort_stats
 };
 
 namespace {
 
 constexpr int kStages = 7;
+constexpr int kSortStats = 7;
 
 template <typename T>
 T* buf(cuflye_ctx* c, const std::string& name, uint64_t count) {
@@ -607,6 +609,8 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
   uint32_t* lists = buf<uint32_t>(c, "s_lists", 4ull * std::max<uint64_t>(nq, 1));
   uint32_t* scounts = buf<uint32_t>(c, "s_counts", 8);
   uint32_t* ecount = buf<uint32_t>(c, "s_ecount", 1);
+  uint64_t* sstats = buf<uint64_t>(c, "x_sortstats", kSortStats);
+  CUFLYE_CHECK(cudaMemsetAsync(sstats, 0, kSortStats * 8, st));
   // 1. KmerMatch sort per query by (ext id, cur pos) in libstdc++ order:
   // queries whose keys are distinct by a radix sort on the ext id, the others
   // by the emulated introsort
@@ -621,6 +625,7 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
   while (id_bits < 32 && ((2ull * c->idx.nslots - 1) >> id_bits) != 0) ++id_bits;
   CUFLYE_CHECK(cudaEventRecord(c->ev[1], st));
   CUFLYE_CHECK(match_plan(ps.q_off, ps.q_tie, nq, ntiles, qb, qe, ecount, st));
+  CUFLYE_CHECK(sort_stats_add(sstats, 0, 1, nullptr, nq, ecount, st));
   const uint64_t NT = scan_u32(c, ntiles, tile_off, nq, "m_scan");
   MatchTile* tiles = buf<MatchTile>(c, "m_tiles", NT);
   uint32_t* mcounts = buf<uint32_t>(c, "m_counts", 256 * NT);
@@ -652,7 +657,8 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
   // 3. ext-sorted groups: re-sort by ext pos (groups with distinct ext
   // positions in shared memory, the others by the emulated introsort)
   CUFLYE_CHECK(group_sort(0, ps.keys, ps.vals, nullptr, groups, ext_list, gcounts + 0, G32, cp.k,
-                          sb, se, ecount, c->num_sms, st));
+                          sb, se, ecount, nullptr, c->num_sms, st));
+  CUFLYE_CHECK(sort_stats_add(sstats, 2, 3, gcounts + 0, 0, ecount, st));
   CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, sb, se, G32, ecount, glists,
                                   scounts, c->num_sms, st, sort_tasks(c, "s", H, G32)));
   int32_t* cur = buf<int32_t>(c, "c_cur", H);
@@ -664,11 +670,12 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
   CUFLYE_CHECK(cudaEventRecord(c->ev[6], st));
   CUFLYE_CHECK(chain_dp(cur, ext, score, bt, groups, dp_list, gcounts, cp, c->num_sms, st));
   CUFLYE_CHECK(cudaEventRecord(c->ev[7], st));
-  // 5. score order (libstdc++ order of indices by score descending): groups
-  // whose scores above k are distinct in shared memory, the others by the
-  // emulated introsort
+  // 5. score order (indices by score descending): groups that fit shared
+  // memory by a plain sort, larger ones by the emulated introsort
+  uint8_t* fast_order = buf<uint8_t>(c, "o_fast", G);
   CUFLYE_CHECK(group_sort(1, ps.keys, ps.vals, score, groups, dp_list, gcounts + 1, G32, cp.k, sb,
-                          se, ecount, c->num_sms, st));
+                          se, ecount, fast_order, c->num_sms, st));
+  CUFLYE_CHECK(sort_stats_add(sstats, 4, 5, gcounts + 1, 0, ecount, st));
   CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, sb, se, G32, ecount, glists,
                                   scounts, c->num_sms, st, sort_tasks(c, "s", H, G32)));
   // 6. backtrack, proposals, primary selection; the row pool is sized by the
@@ -680,8 +687,22 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
   uint32_t* group_rows = buf<uint32_t>(c, "o_grows", G);
   CUFLYE_CHECK(cudaMemsetAsync(pool_count, 0, 4, st));
   CUFLYE_CHECK(cudaMemsetAsync(group_rows, 0, std::max<uint64_t>(G, 1) * 4, st));
-  CUFLYE_CHECK(chain_backtrack(cur, ext, score, bt, ps.vals, groups, dp_list, gcounts, ps.qinfo,
-                               ps.f_off, ps.fpos, buf<int64_t>(c, "ix_slot_signed", 1), c->logt,
+  uint32_t* redo = buf<uint32_t>(c, "o_redo", G);
+  uint32_t* redo_count = buf<uint32_t>(c, "o_redocount", 1);
+  CUFLYE_CHECK(cudaMemsetAsync(redo_count, 0, 4, st));
+  const int64_t* slot_signed = buf<int64_t>(c, "ix_slot_signed", 1);
+  CUFLYE_CHECK(chain_backtrack(cur, ext, score, bt, ps.vals, groups, dp_list, gcounts + 1,
+                               fast_order, redo, redo_count, ps.qinfo, ps.f_off, ps.fpos,
+                               slot_signed, c->logt, cp, pool, pool_cap, pool_count, group_rows,
+                               c->status, G32, st));
+  CUFLYE_CHECK(sort_stats_add(sstats, -1, 6, nullptr, 0, redo_count, st));
+  // groups whose result could depend on the order among equal scores: again
+  // with the libstdc++ order
+  CUFLYE_CHECK(chain_prepare_order(score, ps.keys, ps.vals, groups, redo, redo_count, sb, se, st));
+  CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, sb, se, G32, redo_count, glists,
+                                  scounts, c->num_sms, st, sort_tasks(c, "s", H, G32)));
+  CUFLYE_CHECK(chain_backtrack(cur, ext, score, bt, ps.vals, groups, redo, redo_count, nullptr,
+                               nullptr, nullptr, ps.qinfo, ps.f_off, ps.fpos, slot_signed, c->logt,
                                cp, pool, pool_cap, pool_count, group_rows, c->status, G32, st));
   check_device_status(c);
   // 7. max_overlaps + compaction in group order
@@ -715,6 +736,7 @@ void reset_timing(cuflye_ctx* c) {
   for (int i = 0; i < kStages; ++i) {
     c->stage_ms[i] = 0;
     c->stage_bytes[i] = 0;
+    c->sort_stats[i] = 0;
   }
 }
 
@@ -722,6 +744,12 @@ void reset_timing(cuflye_ctx* c) {
 // 4 backtrack + rows, 5 output + D2H, 6 H2D.
 void accumulate_timing(cuflye_ctx* c, bool chained) {
   sync(c);
+  if (chained) {
+    uint64_t st[kSortStats];
+    CUFLYE_CHECK(cudaMemcpy(st, buf<uint64_t>(c, "x_sortstats", kSortStats), sizeof(st),
+                            cudaMemcpyDeviceToHost));
+    for (int i = 0; i < kSortStats; ++i) c->sort_stats[i] += st[i];
+  }
   c->stage_ms[6] += elapsed(c->ev[0], c->ev[5]);
   c->stage_ms[0] += elapsed(c->ev[5], c->ev[1]);
   if (chained) {
@@ -1196,6 +1224,12 @@ cuflye_status cuflye_last_timing(const cuflye_ctx* c, double* stage_ms, uint64_t
     if (stage_ms) stage_ms[i] = c->stage_ms[i];
     if (stage_bytes) stage_bytes[i] = c->stage_bytes[i];
   }
+  return CUFLYE_OK;
+}
+
+cuflye_status cuflye_last_sort_stats(const cuflye_ctx* c, uint64_t* counts, size_t n) {
+  if (!c || (!counts && n)) return CUFLYE_ERR_INVALID;
+  for (size_t i = 0; i < n && i < static_cast<size_t>(kSortStats); ++i) counts[i] = c->sort_stats[i];
   return CUFLYE_OK;
 }
 

@@ -331,9 +331,9 @@ __global__ void prepare_order_kernel(const int32_t* __restrict__ score, uint64_t
                                      uint32_t* __restrict__ vals,
                                      const GroupInfo* __restrict__ groups,
                                      const uint32_t* __restrict__ dp_list,
-                                     const uint32_t* __restrict__ counts,
+                                     const uint32_t* __restrict__ list_count,
                                      uint64_t* __restrict__ sb, uint64_t* __restrict__ se) {
-  const uint32_t cnt = counts[1];
+  const uint32_t cnt = *list_count;
   const int lane = threadIdx.x & 31;
   const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
   for (uint32_t li = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; li < cnt; li += nwarps) {
@@ -414,6 +414,8 @@ __device__ __forceinline__ uint32_t lower_bound_i32(const int32_t* a, uint32_t n
 
 constexpr uint32_t kBtCap = 16384;
 constexpr uint32_t kBtWords = kBtCap / 32;
+// Orders from the plain group sort are checked for ties only with the maps.
+static_assert(kGroupCap <= kBtCap, "group sorts larger than the backtrack maps");
 constexpr int kBtWarps = 8;
 
 struct BtMaps {
@@ -479,11 +481,34 @@ __device__ void walk_maps(BtMaps& m, const int32_t* __restrict__ btg, int32_t s0
   }
 }
 
+// Order position p holds a live start of score sp.  Does a later position of
+// the same score hold another live start?  (Positions are in score order.)
+// If so, Flye's tie order among them can change the result.
+__device__ bool run_has_other_live(const BtMaps& m, const uint32_t* __restrict__ order,
+                                   const int32_t* __restrict__ score, uint32_t n, uint32_t p,
+                                   int32_t sp) {
+  const int lane = threadIdx.x & 31;
+  for (uint32_t q0 = p + 1; q0 < n; q0 += 32) {
+    const uint32_t q = q0 + lane;
+    bool same = false, live = false;
+    if (q < n) {
+      const uint32_t s = order[q];
+      same = score[s] == sp;
+      live = same && (((m.link[s >> 5] & ~m.done[s >> 5]) >> (s & 31)) & 1u);
+    }
+    if (__ballot_sync(0xffffffffu, live)) return true;
+    if (__ballot_sync(0xffffffffu, !same)) return false;
+  }
+  return false;
+}
+
 __global__ void __launch_bounds__(kBtWarps * 32) backtrack_kernel(
     const int32_t* __restrict__ cur, const int32_t* __restrict__ ext,
     const int32_t* __restrict__ score, int32_t* bt, const uint32_t* __restrict__ order,
     const GroupInfo* __restrict__ groups, const uint32_t* __restrict__ dp_list,
-    const uint32_t* __restrict__ counts, const QueryInfo* __restrict__ qinfo,
+    const uint32_t* __restrict__ list_count, const uint8_t* __restrict__ fast_order,
+    uint32_t* __restrict__ redo_list, uint32_t* __restrict__ redo_count,
+    const QueryInfo* __restrict__ qinfo,
     const uint64_t* __restrict__ f_off, const int32_t* __restrict__ fpos,
     const int64_t* __restrict__ slot_signed, LogfTable logt, ChainParams p,
     OverlapRow* __restrict__ pool, uint64_t pool_cap, uint32_t* __restrict__ pool_count,
@@ -491,7 +516,7 @@ __global__ void __launch_bounds__(kBtWarps * 32) backtrack_kernel(
   extern __shared__ __align__(16) unsigned char bt_raw[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   BtMaps& m = reinterpret_cast<BtMaps*>(bt_raw)[wib];
-  const uint32_t cnt = counts[1];
+  const uint32_t cnt = *list_count;
   const uint32_t nwarps = gridDim.x * kBtWarps;
   for (uint32_t li = blockIdx.x * kBtWarps + wib; li < cnt; li += nwarps) {
   const uint32_t gidx = dp_list[li];
@@ -504,6 +529,10 @@ __global__ void __launch_bounds__(kBtWarps * 32) backtrack_kernel(
   const int32_t* fq = fpos + f_off[g.query];
   const uint32_t nf = static_cast<uint32_t>(f_off[g.query + 1] - f_off[g.query]);
   const bool mapped = g.n <= kBtCap;
+  // an order from the plain sort: equal scores may sit in another order
+  // than Flye's (only possible when mapped; larger groups use Flye's order)
+  const bool check = mapped && fast_order && fast_order[gidx];
+  bool ambiguous = false;
   uint32_t remaining = 0;
   if (mapped) {
     const uint32_t nw = (g.n + 31) / 32;
@@ -524,7 +553,7 @@ __global__ void __launch_bounds__(kBtWarps * 32) backtrack_kernel(
   Prop props[kMaxProposals];
   int np = 0;
   bool overflow = false;
-  for (uint32_t o0 = 0; o0 < g.n && !(mapped && remaining == 0); o0 += 32) {
+  for (uint32_t o0 = 0; o0 < g.n && !(mapped && remaining == 0) && !ambiguous; o0 += 32) {
     const uint32_t oi = o0 + lane;
     const bool valid = oi < g.n;
     const uint32_t start = valid ? order[b + oi] : 0;
@@ -535,6 +564,10 @@ __global__ void __launch_bounds__(kBtWarps * 32) backtrack_kernel(
     while (mask) {
       const int j = __ffs(mask) - 1;
       const uint32_t s0 = __shfl_sync(0xffffffffu, start, j);
+      if (check && run_has_other_live(m, order + b, score + b, g.n, o0 + j, score[b + s0])) {
+        ambiguous = true;
+        break;
+      }
       int32_t first = 0, clen = 0;
       if (mapped) {
         walk_maps(m, bt + b, static_cast<int32_t>(s0), first, clen, remaining);
@@ -591,6 +624,10 @@ __global__ void __launch_bounds__(kBtWarps * 32) backtrack_kernel(
   }
   __syncwarp();
   if (lane != 0) continue;
+  if (ambiguous) {
+    redo_list[atomicAdd(redo_count, 1u)] = gidx;
+    continue;
+  }
   if (overflow) {
     group_rows[gidx] = 0;
     continue;
@@ -755,18 +792,19 @@ cudaError_t chain_dp(const int32_t* cur, const int32_t* ext, int32_t* score, int
 }
 
 cudaError_t chain_prepare_order(const int32_t* score, uint64_t* keys, uint32_t* vals,
-                                const GroupInfo* groups, const uint32_t* dp_list,
-                                const uint32_t* counts, uint64_t* seg_begin, uint64_t* seg_end,
-                                cudaStream_t s) {
+                                const GroupInfo* groups, const uint32_t* list,
+                                const uint32_t* list_count, uint64_t* seg_begin,
+                                uint64_t* seg_end, cudaStream_t s) {
   count_launch();
-  prepare_order_kernel<<<2048, 256, 0, s>>>(score, keys, vals, groups, dp_list, counts, seg_begin,
-                                            seg_end);
+  prepare_order_kernel<<<2048, 256, 0, s>>>(score, keys, vals, groups, list, list_count,
+                                            seg_begin, seg_end);
   return cudaGetLastError();
 }
 
 cudaError_t chain_backtrack(const int32_t* cur, const int32_t* ext, const int32_t* score,
                             int32_t* bt, const uint32_t* order, const GroupInfo* groups,
-                            const uint32_t* dp_list, const uint32_t* counts,
+                            const uint32_t* list, const uint32_t* list_count,
+                            const uint8_t* fast_order, uint32_t* redo_list, uint32_t* redo_count,
                             const QueryInfo* qinfo, const uint64_t* f_off, const int32_t* fpos,
                             const int64_t* slot_signed, const LogfTable& logt,
                             const ChainParams& p, OverlapRow* pool, uint64_t pool_cap,
@@ -782,7 +820,8 @@ cudaError_t chain_backtrack(const int32_t* cur, const int32_t* ext, const int32_
   if (sms <= 0) sms = 1;
   count_launch();
   backtrack_kernel<<<sms * 4, kBtWarps * 32, smem, s>>>(
-      cur, ext, score, bt, order, groups, dp_list, counts, qinfo, f_off, fpos, slot_signed, logt,
+      cur, ext, score, bt, order, groups, list, list_count, fast_order, redo_list, redo_count,
+      qinfo, f_off, fpos, slot_signed, logt,
       p, pool, pool_cap, pool_count, group_rows, st);
   return cudaGetLastError();
 }

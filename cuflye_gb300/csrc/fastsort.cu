@@ -20,12 +20,13 @@
 //   the ext-sorted re-sort (tools/replay_read_to_graph_source_pack.py:396-397)
 //   and INT32_MAX - score for the score order of the backtrack
 //   (tools/replay_overlap_chains.py:316).  One block sorts the group in
-//   shared memory (radix sort on (key, index) packed in 32 bits) and compares
-//   neighbours.  The score order only matters among scores above k: every
-//   element with score <= k has no backtrack link and is skipped by the
-//   backtrack, and all of them sort after every score above k.  A group with
-//   equal keys where they matter, or too large for shared memory, is written
-//   out in the layout sort.cu expects and listed for it.
+//   shared memory (radix sort on (key, index) packed in 32 bits).  For the
+//   ext re-sort it compares neighbours, and a group with equal ext positions
+//   is written out in the layout sort.cu expects and listed for it.  The
+//   score order is used as sorted and marked in fast_order: the backtrack
+//   itself detects the rare case where Flye's order among equal scores could
+//   change its result and sends that group back for the libstdc++ order.
+//   Groups too large for shared memory always go to sort.cu.
 #include <algorithm>
 #include <climits>
 #include <cstdint>
@@ -336,16 +337,18 @@ __global__ void __launch_bounds__(kGroupBlock, 1)
                       const int32_t* __restrict__ score, const GroupInfo* __restrict__ groups,
                       const uint32_t* __restrict__ list, const uint32_t* __restrict__ list_count,
                       int32_t k, uint64_t* __restrict__ emu_begin, uint64_t* __restrict__ emu_end,
-                      uint32_t* __restrict__ emu_count) {
+                      uint32_t* __restrict__ emu_count, uint8_t* __restrict__ fast_order) {
   extern __shared__ __align__(16) unsigned char group_raw[];
   GroupSmem& sm = *reinterpret_cast<GroupSmem*>(group_raw);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t lt = (1u << lane) - 1u;
   const uint32_t cnt = *list_count;
   for (uint32_t li = blockIdx.x; li < cnt; li += gridDim.x) {
-    const GroupInfo g = groups[list[li]];
+    const uint32_t gidx = list[li];
+    const GroupInfo g = groups[gidx];
     const uint32_t n = g.n;
     const uint64_t b = g.start;
+    if (MODE == 1 && threadIdx.x == 0) fast_order[gidx] = 0;
     if (n == 0) continue;
     if (n > kGroupCap) {
       group_to_emulation<MODE>(keys, vals, score, g, emu_begin, emu_end, emu_count);
@@ -434,16 +437,10 @@ __global__ void __launch_bounds__(kGroupBlock, 1)
       src = dst;
       dst = tmp;
     }
-    // Equal keys where they matter?
+    // Equal ext positions?  (The score order is checked by the backtrack.)
     bool tie = false;
-    for (uint32_t j = threadIdx.x + 1; j < n && !tie; j += kGroupBlock) {
-      const uint32_t kj = src[j] >> ib, kp = src[j - 1] >> ib;
-      if (kj == kp) {
-        // MODE 1: keys above INT32_MAX - k - 1 are scores <= k, never visited
-        tie = MODE == 0 ||
-              static_cast<uint64_t>(kj) + kmin < static_cast<uint64_t>(INT_MAX - k);
-      }
-    }
+    for (uint32_t j = threadIdx.x + 1; MODE == 0 && j < n && !tie; j += kGroupBlock)
+      tie = (src[j] >> ib) == (src[j - 1] >> ib);
     if (__syncthreads_or(tie)) {
       group_to_emulation<MODE>(keys, vals, score, g, emu_begin, emu_end, emu_count);
       __syncthreads();
@@ -461,9 +458,19 @@ __global__ void __launch_bounds__(kGroupBlock, 1)
       }
     } else {
       for (uint32_t i = threadIdx.x; i < n; i += kGroupBlock) vals[b + i] = src[i] & imask;
+      if (threadIdx.x == 0) fast_order[gidx] = 1;
     }
     __syncthreads();
   }
+}
+
+__global__ void sort_stats_kernel(uint64_t* stats, int i_plain, int i_emul,
+                                  const uint32_t* total_dev, uint32_t total_host,
+                                  const uint32_t* emul) {
+  const uint32_t e = *emul;
+  const uint32_t t = total_dev ? *total_dev : total_host;
+  stats[i_emul] += e;
+  if (i_plain >= 0) stats[i_plain] += t - e;
 }
 
 template <class T>
@@ -534,7 +541,7 @@ cudaError_t match_radix(uint64_t* keys, uint32_t* vals, uint32_t* alt_hi, uint32
 cudaError_t group_sort(int mode, uint64_t* keys, uint32_t* vals, const int32_t* score,
                        const GroupInfo* groups, const uint32_t* list, const uint32_t* list_count,
                        uint32_t max_groups, int32_t k, uint64_t* emu_begin, uint64_t* emu_end,
-                       uint32_t* emu_count, int num_sms, cudaStream_t s) {
+                       uint32_t* emu_count, uint8_t* fast_order, int num_sms, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(emu_count, 0, 4, s);
   if (e != cudaSuccess || max_groups == 0) return e;
   const unsigned grid = static_cast<unsigned>(std::min<uint64_t>(max_groups, num_sms));
@@ -542,12 +549,19 @@ cudaError_t group_sort(int mode, uint64_t* keys, uint32_t* vals, const int32_t* 
   if (mode == 0) {
     allow_smem(group_sort_kernel<0>, sizeof(GroupSmem));
     group_sort_kernel<0><<<grid, kGroupBlock, sizeof(GroupSmem), s>>>(
-        keys, vals, score, groups, list, list_count, k, emu_begin, emu_end, emu_count);
+        keys, vals, score, groups, list, list_count, k, emu_begin, emu_end, emu_count, fast_order);
   } else {
     allow_smem(group_sort_kernel<1>, sizeof(GroupSmem));
     group_sort_kernel<1><<<grid, kGroupBlock, sizeof(GroupSmem), s>>>(
-        keys, vals, score, groups, list, list_count, k, emu_begin, emu_end, emu_count);
+        keys, vals, score, groups, list, list_count, k, emu_begin, emu_end, emu_count, fast_order);
   }
+  return cudaGetLastError();
+}
+
+cudaError_t sort_stats_add(uint64_t* stats, int i_plain, int i_emul, const uint32_t* total_dev,
+                           uint32_t total_host, const uint32_t* emul, cudaStream_t s) {
+  count_launch();
+  sort_stats_kernel<<<1, 1, 0, s>>>(stats, i_plain, i_emul, total_dev, total_host, emul);
   return cudaGetLastError();
 }
 

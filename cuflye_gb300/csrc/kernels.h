@@ -180,11 +180,17 @@ cudaError_t match_radix(uint64_t* keys, uint32_t* vals, uint32_t* alt_hi, uint32
                         uint32_t nq, int id_bits, uint32_t* counts, int num_sms, cudaStream_t s);
 // Groups of list[0 .. *list_count): mode 0 re-sorts ext-sorted groups by ext
 // pos (out: key = ext pos, val = cur pos); mode 1 writes the score order
-// (val[i] = local index of the i-th element by score descending).
+// (val[i] = local index of the i-th element by score descending) and
+// fast_order[group] = 1 where that order came from the plain sort (equal
+// scores in any order), 0 where the group was listed for sort.cu.
+// stats[i_emul] += *emul; stats[i_plain] += total - *emul (total from
+// total_dev when given, else total_host; i_plain < 0 skips it).
+cudaError_t sort_stats_add(uint64_t* stats, int i_plain, int i_emul, const uint32_t* total_dev,
+                           uint32_t total_host, const uint32_t* emul, cudaStream_t s);
 cudaError_t group_sort(int mode, uint64_t* keys, uint32_t* vals, const int32_t* score,
                        const GroupInfo* groups, const uint32_t* list, const uint32_t* list_count,
                        uint32_t max_groups, int32_t k, uint64_t* emu_begin, uint64_t* emu_end,
-                       uint32_t* emu_count, int num_sms, cudaStream_t s);
+                       uint32_t* emu_count, uint8_t* fast_order, int num_sms, cudaStream_t s);
 
 cudaError_t groups_mark(const uint64_t* keys, const uint64_t* q_off, uint32_t nq, uint64_t nhits,
                         uint32_t* flags, cudaStream_t s);
@@ -207,14 +213,20 @@ cudaError_t groups_split(const uint64_t* keys, const uint32_t* vals, const Group
 cudaError_t chain_dp(const int32_t* cur, const int32_t* ext, int32_t* score, int32_t* bt,
                      const GroupInfo* groups, const uint32_t* dp_list, const uint32_t* counts,
                      const ChainParams& p, int num_sms, cudaStream_t s);
-// Score-order sort inputs: key = INT32_MAX - score, val = local index.
+// Score-order sort inputs of the groups list[0 .. *list_count): key =
+// INT32_MAX - score, val = local index, and their segment bounds.
 cudaError_t chain_prepare_order(const int32_t* score, uint64_t* keys, uint32_t* vals,
-                                const GroupInfo* groups, const uint32_t* dp_list,
-                                const uint32_t* counts, uint64_t* seg_begin, uint64_t* seg_end,
-                                cudaStream_t s);
+                                const GroupInfo* groups, const uint32_t* list,
+                                const uint32_t* list_count, uint64_t* seg_begin,
+                                uint64_t* seg_end, cudaStream_t s);
+// Backtrack of the groups list[0 .. *list_count) in the score order `order`.
+// Where fast_order[group] is set the order came from the plain sort; a group
+// whose result could depend on the order among equal scores is not finished
+// but appended to redo_list, to be run again with the libstdc++ order.
 cudaError_t chain_backtrack(const int32_t* cur, const int32_t* ext, const int32_t* score,
                             int32_t* bt, const uint32_t* order, const GroupInfo* groups,
-                            const uint32_t* dp_list, const uint32_t* counts,
+                            const uint32_t* list, const uint32_t* list_count,
+                            const uint8_t* fast_order, uint32_t* redo_list, uint32_t* redo_count,
                             const QueryInfo* qinfo, const uint64_t* f_off, const int32_t* fpos,
                             const int64_t* slot_signed, const LogfTable& logt,
                             const ChainParams& p, OverlapRow* pool, uint64_t pool_cap,

@@ -249,3 +249,23 @@ def small_overlap_case(seed: int, genome_len: int = 60_000, coverage: float = 8.
                          sub, ins, dele)
     return Workload(f"small-{seed}", k, reads, min_freq=2, max_freq=int(5 * coverage),
                     params=dict(OVERLAP_PARAMS, kmer_size=k), seed=seed)
+
+
+def tandem_case(seed: int, genome_len: int = 80_000, coverage: float = 8.0, arrays: int = 3,
+                copy_div: float = 0.04, k: int = 15) -> Workload:
+    """A small genome carrying tandem arrays (200-350 bp units, 10-16 copies, each
+    copy diverged by `copy_div`): a read through an array holds many k-mers two
+    or more times below max_freq, so equal keys reach every sort point."""
+    rng = np.random.default_rng(seed)
+    genome = random_genome(rng, genome_len)
+    for a in range(arrays):
+        unit = random_genome(rng, int(rng.integers(200, 351)))
+        copies = int(rng.integers(10, 17))
+        arr = np.concatenate([mutate(rng, unit, copy_div) for _ in range(copies)])
+        pos = int((a + 0.5) * genome_len / arrays - len(arr) / 2)
+        genome[pos:pos + len(arr)] = arr[:genome_len - pos]
+    reads = sample_reads(rng, genome, coverage,
+                         lambda n: lognormal_lengths(rng, n, 6_000, 3_000, 1_000, 24_000),
+                         0.002, 0.0005, 0.0005)
+    return Workload(f"tandem-{seed}", k, reads, min_freq=2, max_freq=int(5 * coverage),
+                    params=dict(OVERLAP_PARAMS, kmer_size=k), seed=seed)

@@ -102,6 +102,32 @@ def test_overlaps_match_oracle(gpu, oracle_mod, golden_cases, case):
         assert overlap_tuples_gpu(got) == overlap_tuples_oracle(exp), variant
 
 
+@pytest.mark.parametrize("seed", [11, 12])
+def test_equal_keys_take_the_libstdcxx_paths(gpu, oracle_mod, seed):
+    """Tandem arrays put equal keys at every sort point: queries whose KmerMatch
+    keys repeat, ext-sorted groups with equal ext positions and groups whose
+    backtrack depends on Flye's order among equal scores.  Those take the
+    libstdc++-order paths, the rest the plain sorts, and the rows still match
+    the oracle bit for bit."""
+    from cuflye_gb300 import synth
+    from cuflye_gb300.backend import OverlapParams
+    oracle_mod.set_stable(False)
+    wl = synth.tandem_case(seed)
+    idx, b = oracle_index(oracle_mod, wl.reads, wl.k, wl.min_freq, wl.max_freq)
+    gpu.build_index(wl.reads, wl.k, wl.min_freq, wl.max_freq)
+    seen = dict.fromkeys(gpu.SORT_STATS, 0)
+    for variant in ({}, {"only_max_ext": 0}, {"only_max_ext": 0, "check_overhang": 0}):
+        params = dict(wl.params, **variant)
+        got = gpu.overlaps(wl.reads, OverlapParams.make(**params))
+        for key, v in gpu.last_sort_stats().items():
+            seen[key] += v
+        exp = oracle_mod.overlaps(idx, b, oracle_mod.default_params(**params))
+        assert overlap_tuples_gpu(got) == overlap_tuples_oracle(exp), variant
+    for key in ("match_plain", "match_libstdcxx", "ext_plain", "ext_libstdcxx", "score_plain",
+                "backtrack_redo"):
+        assert seen[key] > 0, seen
+
+
 @pytest.mark.parametrize("case", ["ovl-a", "ovl-d"])
 def test_overlaps_match_reference_tool_output(gpu, golden_cases, case):
     """Against tools/replay_read_to_graph_source_pack.py's rows (committed)."""
