@@ -657,7 +657,8 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
   // 3. ext-sorted groups: re-sort by ext pos (groups with distinct ext
   // positions in shared memory, the others by the emulated introsort)
   CUFLYE_CHECK(group_sort(0, ps.keys, ps.vals, nullptr, groups, ext_list, gcounts + 0, G32, cp.k,
-                          sb, se, ecount, nullptr, c->num_sms, st));
+                          sb, se, ecount, nullptr, buf<uint32_t>(c, "c_work", 1),
+                          c->num_sms, st));
   CUFLYE_CHECK(sort_stats_add(sstats, 2, 3, gcounts + 0, 0, ecount, st));
   CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, sb, se, G32, ecount, glists,
                                   scounts, c->num_sms, st, sort_tasks(c, "s", H, G32)));
@@ -668,13 +669,15 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
   int32_t* score = buf<int32_t>(c, "c_score", H);
   int32_t* bt = buf<int32_t>(c, "c_bt", H);
   CUFLYE_CHECK(cudaEventRecord(c->ev[6], st));
-  CUFLYE_CHECK(chain_dp(cur, ext, score, bt, groups, dp_list, gcounts, cp, c->num_sms, st));
+  CUFLYE_CHECK(chain_dp(cur, ext, score, bt, groups, dp_list, gcounts, cp,
+                        buf<uint32_t>(c, "c_work", 1), c->num_sms, st));
   CUFLYE_CHECK(cudaEventRecord(c->ev[7], st));
   // 5. score order (indices by score descending): groups that fit shared
   // memory by a plain sort, larger ones by the emulated introsort
   uint8_t* fast_order = buf<uint8_t>(c, "o_fast", G);
   CUFLYE_CHECK(group_sort(1, ps.keys, ps.vals, score, groups, dp_list, gcounts + 1, G32, cp.k, sb,
-                          se, ecount, fast_order, c->num_sms, st));
+                          se, ecount, fast_order, buf<uint32_t>(c, "c_work", 1),
+                          c->num_sms, st));
   CUFLYE_CHECK(sort_stats_add(sstats, 4, 5, gcounts + 1, 0, ecount, st));
   CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, sb, se, G32, ecount, glists,
                                   scounts, c->num_sms, st, sort_tasks(c, "s", H, G32)));
@@ -694,7 +697,7 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
   CUFLYE_CHECK(chain_backtrack(cur, ext, score, bt, ps.vals, groups, dp_list, gcounts + 1,
                                fast_order, redo, redo_count, ps.qinfo, ps.f_off, ps.fpos,
                                slot_signed, c->logt, cp, pool, pool_cap, pool_count, group_rows,
-                               c->status, G32, st));
+                               c->status, G32, buf<uint32_t>(c, "c_work", 1), st));
   CUFLYE_CHECK(sort_stats_add(sstats, -1, 6, nullptr, 0, redo_count, st));
   // groups whose result could depend on the order among equal scores: again
   // with the libstdc++ order
@@ -703,7 +706,7 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
                                   scounts, c->num_sms, st, sort_tasks(c, "s", H, G32)));
   CUFLYE_CHECK(chain_backtrack(cur, ext, score, bt, ps.vals, groups, redo, redo_count, nullptr,
                                nullptr, nullptr, ps.qinfo, ps.f_off, ps.fpos, slot_signed, c->logt,
-                               cp, pool, pool_cap, pool_count, group_rows, c->status, G32, st));
+                               cp, pool, pool_cap, pool_count, group_rows, c->status, G32, buf<uint32_t>(c, "c_work", 1), st));
   check_device_status(c);
   // 7. max_overlaps + compaction in group order
   uint64_t* qg = buf<uint64_t>(c, "o_qg", nq + 1);

@@ -12,6 +12,7 @@
 //                    filter, one warp per group;
 //   rows_*         : max_overlaps cutoff per query and order-preserving
 //                    compaction of the rows.
+#include <algorithm>
 #include <climits>
 #include <cstdint>
 
@@ -226,15 +227,20 @@ __device__ __forceinline__ void eval_chunk(bool valid, int32_t cj, int32_t ej, i
   done = bm != 0;
 }
 
+// Warps take groups from a shared counter (groups differ a lot in length).
+__device__ __forceinline__ uint32_t next_item(uint32_t* counter) {
+  uint32_t v = 0;
+  if ((threadIdx.x & 31) == 0) v = atomicAdd(counter, 1u);
+  return __shfl_sync(0xffffffffu, v, 0);
+}
+
 __global__ void __launch_bounds__(kDpWarps * 32) dp_kernel(
     const int32_t* __restrict__ cur, const int32_t* __restrict__ ext, int32_t* score,
     int32_t* bt, const GroupInfo* __restrict__ groups, const uint32_t* __restrict__ list,
-    const uint32_t* __restrict__ counts, ChainParams p) {
+    const uint32_t* __restrict__ counts, ChainParams p, uint32_t* __restrict__ work) {
   const int lane = threadIdx.x & 31;
-  const int wib = threadIdx.x >> 5;
   const uint32_t cnt = counts[1];
-  const uint32_t nwarps = gridDim.x * kDpWarps;
-  for (uint32_t li = blockIdx.x * kDpWarps + wib; li < cnt; li += nwarps) {
+  for (uint32_t li = next_item(work); li < cnt; li = next_item(work)) {
     const GroupInfo g = groups[list[li]];
     const uint64_t b = g.start;
     const uint32_t n = g.n;
@@ -512,13 +518,12 @@ __global__ void __launch_bounds__(kBtWarps * 32) backtrack_kernel(
     const uint64_t* __restrict__ f_off, const int32_t* __restrict__ fpos,
     const int64_t* __restrict__ slot_signed, LogfTable logt, ChainParams p,
     OverlapRow* __restrict__ pool, uint64_t pool_cap, uint32_t* __restrict__ pool_count,
-    uint32_t* __restrict__ group_rows, DeviceStatus* st) {
+    uint32_t* __restrict__ group_rows, DeviceStatus* st, uint32_t* __restrict__ work) {
   extern __shared__ __align__(16) unsigned char bt_raw[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   BtMaps& m = reinterpret_cast<BtMaps*>(bt_raw)[wib];
   const uint32_t cnt = *list_count;
-  const uint32_t nwarps = gridDim.x * kBtWarps;
-  for (uint32_t li = blockIdx.x * kBtWarps + wib; li < cnt; li += nwarps) {
+  for (uint32_t li = next_item(work); li < cnt; li = next_item(work)) {
   const uint32_t gidx = dp_list[li];
   const GroupInfo g = groups[gidx];
   const uint64_t b = g.start;
@@ -785,9 +790,15 @@ cudaError_t groups_split(const uint64_t* keys, const uint32_t* vals, const Group
 
 cudaError_t chain_dp(const int32_t* cur, const int32_t* ext, int32_t* score, int32_t* bt,
                      const GroupInfo* groups, const uint32_t* dp_list, const uint32_t* counts,
-                     const ChainParams& p, int num_sms, cudaStream_t s) {
+                     const ChainParams& p, uint32_t* work, int num_sms, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(work, 0, 4, s);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dp_kernel, kDpWarps * 32, 0);
+  if (e != cudaSuccess) return e;
   count_launch();
-  dp_kernel<<<num_sms * 8, kDpWarps * 32, 0, s>>>(cur, ext, score, bt, groups, dp_list, counts, p);
+  dp_kernel<<<num_sms * std::max(per_sm, 1), kDpWarps * 32, 0, s>>>(cur, ext, score, bt, groups,
+                                                                   dp_list, counts, p, work);
   return cudaGetLastError();
 }
 
@@ -809,8 +820,10 @@ cudaError_t chain_backtrack(const int32_t* cur, const int32_t* ext, const int32_
                             const int64_t* slot_signed, const LogfTable& logt,
                             const ChainParams& p, OverlapRow* pool, uint64_t pool_cap,
                             uint32_t* pool_count, uint32_t* group_rows, DeviceStatus* st,
-                            uint32_t max_groups, cudaStream_t s) {
+                            uint32_t max_groups, uint32_t* work, cudaStream_t s) {
   if (max_groups == 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(work, 0, 4, s);
+  if (e != cudaSuccess) return e;
   constexpr size_t smem = sizeof(BtMaps) * kBtWarps;
   cudaFuncSetAttribute(backtrack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        static_cast<int>(smem));
@@ -822,7 +835,7 @@ cudaError_t chain_backtrack(const int32_t* cur, const int32_t* ext, const int32_
   backtrack_kernel<<<sms * 4, kBtWarps * 32, smem, s>>>(
       cur, ext, score, bt, order, groups, list, list_count, fast_order, redo_list, redo_count,
       qinfo, f_off, fpos, slot_signed, logt,
-      p, pool, pool_cap, pool_count, group_rows, st);
+      p, pool, pool_cap, pool_count, group_rows, st, work);
   return cudaGetLastError();
 }
 

@@ -302,6 +302,7 @@ struct GroupSmem {
   uint32_t dbase[256];
   uint32_t ws[kGroupWarps];
   uint32_t kmin, kmax;
+  uint32_t item;
 };
 
 // Rewrites the group for sort.cu and lists it there.
@@ -337,13 +338,20 @@ __global__ void __launch_bounds__(kGroupBlock, 1)
                       const int32_t* __restrict__ score, const GroupInfo* __restrict__ groups,
                       const uint32_t* __restrict__ list, const uint32_t* __restrict__ list_count,
                       int32_t k, uint64_t* __restrict__ emu_begin, uint64_t* __restrict__ emu_end,
-                      uint32_t* __restrict__ emu_count, uint8_t* __restrict__ fast_order) {
+                      uint32_t* __restrict__ emu_count, uint8_t* __restrict__ fast_order,
+                      uint32_t* __restrict__ work) {
   extern __shared__ __align__(16) unsigned char group_raw[];
   GroupSmem& sm = *reinterpret_cast<GroupSmem*>(group_raw);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t lt = (1u << lane) - 1u;
   const uint32_t cnt = *list_count;
-  for (uint32_t li = blockIdx.x; li < cnt; li += gridDim.x) {
+  for (;;) {
+    // blocks take groups from a shared counter (group lengths vary widely)
+    __syncthreads();
+    if (threadIdx.x == 0) sm.item = atomicAdd(work, 1u);
+    __syncthreads();
+    const uint32_t li = sm.item;
+    if (li >= cnt) break;
     const uint32_t gidx = list[li];
     const GroupInfo g = groups[gidx];
     const uint32_t n = g.n;
@@ -541,19 +549,23 @@ cudaError_t match_radix(uint64_t* keys, uint32_t* vals, uint32_t* alt_hi, uint32
 cudaError_t group_sort(int mode, uint64_t* keys, uint32_t* vals, const int32_t* score,
                        const GroupInfo* groups, const uint32_t* list, const uint32_t* list_count,
                        uint32_t max_groups, int32_t k, uint64_t* emu_begin, uint64_t* emu_end,
-                       uint32_t* emu_count, uint8_t* fast_order, int num_sms, cudaStream_t s) {
+                       uint32_t* emu_count, uint8_t* fast_order, uint32_t* work, int num_sms,
+                       cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(emu_count, 0, 4, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(work, 0, 4, s);
   if (e != cudaSuccess || max_groups == 0) return e;
   const unsigned grid = static_cast<unsigned>(std::min<uint64_t>(max_groups, num_sms));
   count_launch();
   if (mode == 0) {
     allow_smem(group_sort_kernel<0>, sizeof(GroupSmem));
     group_sort_kernel<0><<<grid, kGroupBlock, sizeof(GroupSmem), s>>>(
-        keys, vals, score, groups, list, list_count, k, emu_begin, emu_end, emu_count, fast_order);
+        keys, vals, score, groups, list, list_count, k, emu_begin, emu_end, emu_count, fast_order,
+        work);
   } else {
     allow_smem(group_sort_kernel<1>, sizeof(GroupSmem));
     group_sort_kernel<1><<<grid, kGroupBlock, sizeof(GroupSmem), s>>>(
-        keys, vals, score, groups, list, list_count, k, emu_begin, emu_end, emu_count, fast_order);
+        keys, vals, score, groups, list, list_count, k, emu_begin, emu_end, emu_count, fast_order,
+        work);
   }
   return cudaGetLastError();
 }

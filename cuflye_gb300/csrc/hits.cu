@@ -110,44 +110,73 @@ __global__ void count_kernel(DeviceIndex idx, QueryBatch q, uint32_t* __restrict
   wflags[w] = fl;
 }
 
+// A warp owns 32 consecutive windows (lane L <-> window w0 + L) and writes
+// their hits one window at a time with all lanes, so that each store covers
+// up to 32 consecutive records of one window.
 __global__ void emit_kernel(DeviceIndex idx, QueryBatch q, const uint64_t* __restrict__ hit_off,
                             const uint64_t* __restrict__ filt_off,
                             const uint64_t* __restrict__ wmeta,
                             const uint8_t* __restrict__ wflags, uint64_t* __restrict__ keys,
                             uint32_t* __restrict__ vals, uint64_t* __restrict__ kmers,
                             int32_t* __restrict__ fpos) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t lt = (1u << lane) - 1u;
   const uint64_t w = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (w >= q.nwin) return;
-  const uint8_t fl = wflags[w];
-  const uint32_t qi = query_of(q.win_off, q.nq, w);
-  const uint64_t p = w - q.win_off[qi];
-  if (fl & kFlagFiltered) {
-    fpos[filt_off[w]] = static_cast<int32_t>(p);
-    return;
-  }
-  uint64_t o = hit_off[w];
-  const uint64_t end = hit_off[w + 1];
-  if (o == end) return;
-  const uint64_t meta = wmeta[w];
-  const uint64_t off = meta & kOffsetMask;
-  const uint32_t c = static_cast<uint32_t>((meta >> 40) & ((1ULL << kCountBits) - 1));
-  const bool flip = idx.transform && (fl & kFlagRev);
-  const int32_t qdi = q.qdi[qi];
-  uint64_t x = 0;
-  if (kmers) x = kmer_at(q.words, q.base_off[qi] + p, idx.k);
-  for (uint32_t e = 0; e < c; ++e) {
-    const uint64_t sv = __ldg(idx.pos + off + e);
-    uint32_t id = static_cast<uint32_t>(sv >> 32);
-    int32_t pos = static_cast<int32_t>(sv & 0xffffffffu);
-    if (flip) {
-      pos = idx.slot_len[id >> 1] - pos - idx.k;
-      id ^= 1u;
+  uint8_t fl = 0;
+  uint32_t qi = 0, p = 0;
+  uint64_t o = 0, end = 0, meta = 0;
+  if (w < q.nwin) {
+    fl = wflags[w];
+    qi = query_of(q.win_off, q.nq, w);
+    p = static_cast<uint32_t>(w - q.win_off[qi]);
+    if (fl & kFlagFiltered) {
+      fpos[filt_off[w]] = static_cast<int32_t>(p);
+    } else {
+      o = hit_off[w];
+      end = hit_off[w + 1];
+      meta = wmeta[w];
     }
-    if (static_cast<int32_t>(id) == qdi && pos == static_cast<int32_t>(p)) continue;
-    keys[o] = (static_cast<uint64_t>(id) << 32) | static_cast<uint32_t>(p);
-    vals[o] = static_cast<uint32_t>(pos);
-    if (kmers) kmers[o] = x;
-    ++o;
+  }
+  unsigned todo = __ballot_sync(0xffffffffu, end > o);
+  while (todo) {
+    const int src = __ffs(todo) - 1;
+    todo &= todo - 1;
+    const uint64_t wo = __shfl_sync(0xffffffffu, o, src);
+    const uint64_t wm = __shfl_sync(0xffffffffu, meta, src);
+    const uint32_t wq = __shfl_sync(0xffffffffu, qi, src);
+    const uint32_t wp = __shfl_sync(0xffffffffu, p, src);
+    const uint32_t wf = __shfl_sync(0xffffffffu, static_cast<uint32_t>(fl), src);
+    const uint64_t off = wm & kOffsetMask;
+    const uint32_t c = static_cast<uint32_t>((wm >> 40) & ((1ULL << kCountBits) - 1));
+    const bool flip = idx.transform && (wf & kFlagRev);
+    const int32_t qdi = q.qdi[wq];
+    uint64_t x = 0;
+    if (kmers) x = kmer_at(q.words, q.base_off[wq] + wp, idx.k);
+    uint64_t out = wo;
+    for (uint32_t e0 = 0; e0 < c; e0 += 32) {
+      const uint32_t e = e0 + lane;
+      bool keep = e < c;
+      uint32_t id = 0;
+      int32_t pos = 0;
+      if (keep) {
+        const uint64_t sv = __ldg(idx.pos + off + e);
+        id = static_cast<uint32_t>(sv >> 32);
+        pos = static_cast<int32_t>(sv & 0xffffffffu);
+        if (flip) {
+          pos = idx.slot_len[id >> 1] - pos - idx.k;
+          id ^= 1u;
+        }
+        keep = !(static_cast<int32_t>(id) == qdi && pos == static_cast<int32_t>(wp));
+      }
+      const unsigned km = __ballot_sync(0xffffffffu, keep);
+      if (keep) {
+        const uint64_t d = out + __popc(km & lt);
+        keys[d] = (static_cast<uint64_t>(id) << 32) | wp;
+        vals[d] = static_cast<uint32_t>(pos);
+        if (kmers) kmers[d] = x;
+      }
+      out += __popc(km);
+    }
   }
 }
 

@@ -190,7 +190,8 @@ cudaError_t sort_stats_add(uint64_t* stats, int i_plain, int i_emul, const uint3
 cudaError_t group_sort(int mode, uint64_t* keys, uint32_t* vals, const int32_t* score,
                        const GroupInfo* groups, const uint32_t* list, const uint32_t* list_count,
                        uint32_t max_groups, int32_t k, uint64_t* emu_begin, uint64_t* emu_end,
-                       uint32_t* emu_count, uint8_t* fast_order, int num_sms, cudaStream_t s);
+                       uint32_t* emu_count, uint8_t* fast_order, uint32_t* work, int num_sms,
+                       cudaStream_t s);
 
 cudaError_t groups_mark(const uint64_t* keys, const uint64_t* q_off, uint32_t nq, uint64_t nhits,
                         uint32_t* flags, cudaStream_t s);
@@ -210,9 +211,10 @@ cudaError_t groups_prepare_ext_sort(uint64_t* keys, uint32_t* vals, const GroupI
 cudaError_t groups_split(const uint64_t* keys, const uint32_t* vals, const GroupInfo* groups,
                          const uint32_t* dp_list, const uint32_t* counts, int32_t* cur,
                          int32_t* ext, cudaStream_t s);
+// work: one word of device scratch (the group counter of the launch).
 cudaError_t chain_dp(const int32_t* cur, const int32_t* ext, int32_t* score, int32_t* bt,
                      const GroupInfo* groups, const uint32_t* dp_list, const uint32_t* counts,
-                     const ChainParams& p, int num_sms, cudaStream_t s);
+                     const ChainParams& p, uint32_t* work, int num_sms, cudaStream_t s);
 // Score-order sort inputs of the groups list[0 .. *list_count): key =
 // INT32_MAX - score, val = local index, and their segment bounds.
 cudaError_t chain_prepare_order(const int32_t* score, uint64_t* keys, uint32_t* vals,
@@ -231,7 +233,7 @@ cudaError_t chain_backtrack(const int32_t* cur, const int32_t* ext, const int32_
                             const int64_t* slot_signed, const LogfTable& logt,
                             const ChainParams& p, OverlapRow* pool, uint64_t pool_cap,
                             uint32_t* pool_count, uint32_t* group_rows, DeviceStatus* st,
-                            uint32_t max_groups, cudaStream_t s);
+                            uint32_t max_groups, uint32_t* work, cudaStream_t s);
 // max_overlaps cutoff and group-order compaction of the pooled rows.
 cudaError_t rows_limit(const uint32_t* group_rows, const uint64_t* q_group_off, uint32_t nq,
                        int32_t max_overlaps, uint32_t* kept_rows, cudaStream_t s);
