@@ -654,11 +654,15 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
   uint64_t* se = buf<uint64_t>(c, "g_se", G);
   uint32_t* glists = buf<uint32_t>(c, "g_lists", 4 * std::max<uint64_t>(G, 1));
   const uint32_t G32 = static_cast<uint32_t>(G);
-  // 3. ext-sorted groups: re-sort by ext pos (groups with distinct ext
-  // positions in shared memory, the others by the emulated introsort)
-  CUFLYE_CHECK(group_sort(0, ps.keys, ps.vals, nullptr, groups, ext_list, gcounts + 0, G32, cp.k,
-                          sb, se, ecount, nullptr, buf<uint32_t>(c, "c_work", 1),
-                          c->num_sms, st));
+  // 3. ext-sorted groups in ext-pos order: most already are (checked, read in
+  // place); the rest are re-sorted in shared memory, or by the emulated
+  // introsort where ext positions repeat
+  uint32_t* work = buf<uint32_t>(c, "c_work", 1);
+  uint32_t* resort = buf<uint32_t>(c, "g_resort", G);
+  uint32_t* resort_count = buf<uint32_t>(c, "g_resortcount", 1);
+  CUFLYE_CHECK(groups_ext_presorted(ps.vals, groups, ext_list, gcounts, resort, resort_count, st));
+  CUFLYE_CHECK(group_ext_sort(ps.keys, ps.vals, groups, resort, resort_count, G32, sb, se, ecount,
+                              work, c->num_sms, st));
   CUFLYE_CHECK(sort_stats_add(sstats, 2, 3, gcounts + 0, 0, ecount, st));
   CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, sb, se, G32, ecount, glists,
                                   scounts, c->num_sms, st, sort_tasks(c, "s", H, G32)));
@@ -668,18 +672,21 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
   // 4. DP
   int32_t* score = buf<int32_t>(c, "c_score", H);
   int32_t* bt = buf<int32_t>(c, "c_bt", H);
+  GroupTop* top = buf<GroupTop>(c, "c_top", G);
   CUFLYE_CHECK(cudaEventRecord(c->ev[6], st));
-  CUFLYE_CHECK(chain_dp(cur, ext, score, bt, groups, dp_list, gcounts, cp,
-                        buf<uint32_t>(c, "c_work", 1), c->num_sms, st));
+  CUFLYE_CHECK(chain_dp(cur, ext, score, bt, groups, dp_list, gcounts, cp, top, work, c->num_sms,
+                        st));
   CUFLYE_CHECK(cudaEventRecord(c->ev[7], st));
-  // 5. score order (indices by score descending): groups that fit shared
-  // memory by a plain sort, larger ones by the emulated introsort
-  uint8_t* fast_order = buf<uint8_t>(c, "o_fast", G);
-  CUFLYE_CHECK(group_sort(1, ps.keys, ps.vals, score, groups, dp_list, gcounts + 1, G32, cp.k, sb,
-                          se, ecount, fast_order, buf<uint32_t>(c, "c_work", 1),
-                          c->num_sms, st));
-  CUFLYE_CHECK(sort_stats_add(sstats, 4, 5, gcounts + 1, 0, ecount, st));
-  CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, sb, se, G32, ecount, glists,
+  // 5. score order (indices by score descending, libstdc++ order) only for
+  // groups above the backtrack's shared-memory maps; the backtrack picks the
+  // starts of the others itself
+  uint32_t* big = buf<uint32_t>(c, "o_big", G);
+  uint32_t* big_count = buf<uint32_t>(c, "o_bigcount", 1);
+  CUFLYE_CHECK(list_large_groups(groups, dp_list, gcounts + 1, G32, kBacktrackCap, big, big_count,
+                                 st));
+  CUFLYE_CHECK(sort_stats_add(sstats, 4, 5, gcounts + 1, 0, big_count, st));
+  CUFLYE_CHECK(chain_prepare_order(score, ps.keys, ps.vals, groups, big, big_count, sb, se, st));
+  CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, sb, se, G32, big_count, glists,
                                   scounts, c->num_sms, st, sort_tasks(c, "s", H, G32)));
   // 6. backtrack, proposals, primary selection; the row pool is sized by the
   // groups that survived the prefilter
@@ -694,10 +701,10 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
   uint32_t* redo_count = buf<uint32_t>(c, "o_redocount", 1);
   CUFLYE_CHECK(cudaMemsetAsync(redo_count, 0, 4, st));
   const int64_t* slot_signed = buf<int64_t>(c, "ix_slot_signed", 1);
-  CUFLYE_CHECK(chain_backtrack(cur, ext, score, bt, ps.vals, groups, dp_list, gcounts + 1,
-                               fast_order, redo, redo_count, ps.qinfo, ps.f_off, ps.fpos,
-                               slot_signed, c->logt, cp, pool, pool_cap, pool_count, group_rows,
-                               c->status, G32, buf<uint32_t>(c, "c_work", 1), st));
+  CUFLYE_CHECK(chain_backtrack(cur, ext, score, bt, ps.vals, groups, dp_list, gcounts + 1, top,
+                               redo, redo_count, ps.qinfo, ps.f_off, ps.fpos, slot_signed, c->logt,
+                               cp, pool, pool_cap, pool_count, group_rows, c->status, G32, work,
+                               st));
   CUFLYE_CHECK(sort_stats_add(sstats, -1, 6, nullptr, 0, redo_count, st));
   // groups whose result could depend on the order among equal scores: again
   // with the libstdc++ order
@@ -706,7 +713,8 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
                                   scounts, c->num_sms, st, sort_tasks(c, "s", H, G32)));
   CUFLYE_CHECK(chain_backtrack(cur, ext, score, bt, ps.vals, groups, redo, redo_count, nullptr,
                                nullptr, nullptr, ps.qinfo, ps.f_off, ps.fpos, slot_signed, c->logt,
-                               cp, pool, pool_cap, pool_count, group_rows, c->status, G32, buf<uint32_t>(c, "c_work", 1), st));
+                               cp, pool, pool_cap, pool_count, group_rows, c->status, G32, work,
+                               st));
   check_device_status(c);
   // 7. max_overlaps + compaction in group order
   uint64_t* qg = buf<uint64_t>(c, "o_qg", nq + 1);

@@ -143,6 +143,33 @@ __global__ void prepare_ext_sort_kernel(uint64_t* __restrict__ keys, uint32_t* _
   }
 }
 
+// An ext-sorted group whose ext positions already increase strictly in
+// cur-pos order is in its only ext-pos order: it is marked ext_sorted = 2 and
+// read in place; the others are listed for the re-sort.
+__global__ void ext_presorted_kernel(const uint32_t* __restrict__ vals,
+                                     GroupInfo* __restrict__ groups,
+                                     const uint32_t* __restrict__ ext_list,
+                                     const uint32_t* __restrict__ counts,
+                                     uint32_t* __restrict__ out, uint32_t* __restrict__ out_count) {
+  const uint32_t cnt = counts[0];
+  const int lane = threadIdx.x & 31;
+  const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t li = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; li < cnt; li += nwarps) {
+    const uint32_t gid = ext_list[li];
+    const GroupInfo g = groups[gid];
+    bool up = true;
+    for (uint32_t j = lane + 1; j < g.n && up; j += 32)
+      up = vals[g.start + j] > vals[g.start + j - 1];
+    up = __all_sync(0xffffffffu, up);
+    if (lane == 0) {
+      if (up)
+        groups[gid].ext_sorted = 2;
+      else
+        out[atomicAdd(out_count, 1u)] = gid;
+    }
+  }
+}
+
 __global__ void split_kernel(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ vals,
                              const GroupInfo* __restrict__ groups,
                              const uint32_t* __restrict__ dp_list,
@@ -155,7 +182,7 @@ __global__ void split_kernel(const uint64_t* __restrict__ keys, const uint32_t* 
     const GroupInfo g = groups[dp_list[li]];
     for (uint32_t j = lane; j < g.n; j += 32) {
       const uint64_t i = g.start + j;
-      if (g.ext_sorted) {
+      if (g.ext_sorted == 1) {  // re-sorted: key = ext pos, val = cur pos
         cur[i] = static_cast<int32_t>(vals[i]);
         ext[i] = static_cast<int32_t>(keys[i] & 0xffffffffu);
       } else {
@@ -237,11 +264,16 @@ __device__ __forceinline__ uint32_t next_item(uint32_t* counter) {
 __global__ void __launch_bounds__(kDpWarps * 32) dp_kernel(
     const int32_t* __restrict__ cur, const int32_t* __restrict__ ext, int32_t* score,
     int32_t* bt, const GroupInfo* __restrict__ groups, const uint32_t* __restrict__ list,
-    const uint32_t* __restrict__ counts, ChainParams p, uint32_t* __restrict__ work) {
+    const uint32_t* __restrict__ counts, ChainParams p, GroupTop* __restrict__ top,
+    uint32_t* __restrict__ work) {
   const int lane = threadIdx.x & 31;
   const uint32_t cnt = counts[1];
   for (uint32_t li = next_item(work); li < cnt; li = next_item(work)) {
-    const GroupInfo g = groups[list[li]];
+    const uint32_t gidx = list[li];
+    const GroupInfo g = groups[gidx];
+    // this lane's highest score, its first element and how many elements have it
+    int32_t top_s = INT_MIN;
+    uint32_t top_i = 0, top_c = 0;
     const uint64_t b = g.start;
     const uint32_t n = g.n;
     const bool es = g.ext_sorted != 0;
@@ -270,6 +302,9 @@ __global__ void __launch_bounds__(kDpWarps * 32) dp_kernel(
         if (lane == 0) {
           score[b] = 0;
           bt[b] = -1;
+          top_s = 0;
+          top_i = 0;
+          top_c = 1;
         }
         t = 1;
       }
@@ -290,6 +325,13 @@ __global__ void __launch_bounds__(kDpWarps * 32) dp_kernel(
           if (in) {
             s_mine = first + (x - dt);
             score[b + i] = s_mine;
+            if (s_mine > top_s) {
+              top_s = s_mine;
+              top_i = i;
+              top_c = 1;
+            } else if (s_mine == top_s) {
+              ++top_c;
+            }
             bt[b + i] = (lane > static_cast<int>(t) || s_prev + dt > p.k)
                             ? static_cast<int32_t>(i) - 1
                             : -1;
@@ -321,6 +363,13 @@ __global__ void __launch_bounds__(kDpWarps * 32) dp_kernel(
             s_mine = si;
             score[b + it] = si;
             bt[b + it] = best > p.k ? bestj : -1;
+            if (si > top_s) {
+              top_s = si;
+              top_i = static_cast<uint32_t>(it);
+              top_c = 1;
+            } else if (si == top_s) {
+              ++top_c;
+            }
           }
           s_prev = si;
           ++t;
@@ -330,6 +379,17 @@ __global__ void __launch_bounds__(kDpWarps * 32) dp_kernel(
       pc = __shfl_sync(0xffffffffu, ci, 31);
       pe = __shfl_sync(0xffffffffu, ei, 31);
     }
+    int32_t ms = top_s;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) ms = max(ms, __shfl_xor_sync(0xffffffffu, ms, o));
+    uint32_t mc = top_s == ms ? top_c : 0u;
+    uint32_t mi = top_s == ms ? top_i : 0xffffffffu;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      mc += __shfl_xor_sync(0xffffffffu, mc, o);
+      mi = min(mi, __shfl_xor_sync(0xffffffffu, mi, o));
+    }
+    if (lane == 0) top[gidx] = GroupTop{ms, mi, mc, 0u};
   }
 }
 
@@ -418,10 +478,8 @@ __device__ __forceinline__ uint32_t lower_bound_i32(const int32_t* a, uint32_t n
 // left: no later start could begin a chain.  Larger groups walk the table in
 // global memory with one lane.
 
-constexpr uint32_t kBtCap = 16384;
+constexpr uint32_t kBtCap = kBacktrackCap;
 constexpr uint32_t kBtWords = kBtCap / 32;
-// Orders from the plain group sort are checked for ties only with the maps.
-static_assert(kGroupCap <= kBtCap, "group sorts larger than the backtrack maps");
 constexpr int kBtWarps = 8;
 
 struct BtMaps {
@@ -487,32 +545,51 @@ __device__ void walk_maps(BtMaps& m, const int32_t* __restrict__ btg, int32_t s0
   }
 }
 
-// Order position p holds a live start of score sp.  Does a later position of
-// the same score hold another live start?  (Positions are in score order.)
-// If so, Flye's tie order among them can change the result.
-__device__ bool run_has_other_live(const BtMaps& m, const uint32_t* __restrict__ order,
-                                   const int32_t* __restrict__ score, uint32_t n, uint32_t p,
-                                   int32_t sp) {
-  const int lane = threadIdx.x & 31;
-  for (uint32_t q0 = p + 1; q0 < n; q0 += 32) {
-    const uint32_t q = q0 + lane;
-    bool same = false, live = false;
-    if (q < n) {
-      const uint32_t s = order[q];
-      same = score[s] == sp;
-      live = same && (((m.link[s >> 5] & ~m.done[s >> 5]) >> (s & 31)) & 1u);
+// The overlap of one walked chain (start s0 back to first): overlapTest,
+// then the k-mer divergence; kept proposals are appended to props.
+__device__ __forceinline__ void add_proposal(
+    const int32_t* __restrict__ cur, const int32_t* __restrict__ ext,
+    const int32_t* __restrict__ score, uint64_t b, uint32_t s0, int32_t first, int32_t clen,
+    const QueryInfo& qi, int64_t ext_signed, const GroupInfo& g, const int32_t* fq, uint32_t nf,
+    const LogfTable& logt, const ChainParams& p, DeviceStatus* st, uint32_t gidx, Prop* props,
+    int& np, bool& overflow) {
+  const int32_t k = p.k;
+  Prop o;
+  o.cb = cur[b + first];
+  o.ce = cur[b + s0] + k - 1;
+  o.eb = ext[b + first];
+  o.ee = ext[b + s0] + k - 1;
+  o.score = score[b + s0] - score[b + first] + k - 1;
+  o.clen = clen;
+  bool keep = overlap_test(o, qi.signed_id, ext_signed, qi.len, g.ext_len, p);
+  if (keep) {
+    const uint32_t lo = lower_bound_i32(fq, nf, o.cb);
+    const uint32_t hi = lower_bound_i32(fq, nf, o.ce + 1);
+    const int32_t norm = max(o.ce - o.cb, o.ee - o.eb) - static_cast<int32_t>(hi - lo);
+    keep = norm > 0;
+    if (keep) {
+      float rate = fdiv(fmul(static_cast<float>(clen), p.sample_rate), static_cast<float>(norm));
+      rate = rate < 1.0f ? rate : 1.0f;
+      const float x = fdiv(1.0f, rate);
+      if (!(x < 16777216.0f)) raise_status(st, kDevLogDomain, 0, static_cast<int64_t>(gidx));
+      o.div = fdiv(flye_logf(x, logt), static_cast<float>(k));
     }
-    if (__ballot_sync(0xffffffffu, live)) return true;
-    if (__ballot_sync(0xffffffffu, !same)) return false;
   }
-  return false;
+  if (keep) {
+    if (np == kMaxProposals) {
+      raise_status(st, kDevProposalOverflow, 0, static_cast<int64_t>(gidx));
+      overflow = true;
+    } else {
+      props[np++] = o;
+    }
+  }
 }
 
 __global__ void __launch_bounds__(kBtWarps * 32) backtrack_kernel(
     const int32_t* __restrict__ cur, const int32_t* __restrict__ ext,
     const int32_t* __restrict__ score, int32_t* bt, const uint32_t* __restrict__ order,
     const GroupInfo* __restrict__ groups, const uint32_t* __restrict__ dp_list,
-    const uint32_t* __restrict__ list_count, const uint8_t* __restrict__ fast_order,
+    const uint32_t* __restrict__ list_count, const GroupTop* __restrict__ top,
     uint32_t* __restrict__ redo_list, uint32_t* __restrict__ redo_count,
     const QueryInfo* __restrict__ qinfo,
     const uint64_t* __restrict__ f_off, const int32_t* __restrict__ fpos,
@@ -534,9 +611,9 @@ __global__ void __launch_bounds__(kBtWarps * 32) backtrack_kernel(
   const int32_t* fq = fpos + f_off[g.query];
   const uint32_t nf = static_cast<uint32_t>(f_off[g.query + 1] - f_off[g.query]);
   const bool mapped = g.n <= kBtCap;
-  // an order from the plain sort: equal scores may sit in another order
-  // than Flye's (only possible when mapped; larger groups use Flye's order)
-  const bool check = mapped && fast_order && fast_order[gidx];
+  // mapped groups of the first run pick their starts themselves; the others
+  // follow `order` (Flye's order)
+  const bool pick = mapped && top != nullptr;
   bool ambiguous = false;
   uint32_t remaining = 0;
   if (mapped) {
@@ -558,7 +635,59 @@ __global__ void __launch_bounds__(kBtWarps * 32) backtrack_kernel(
   Prop props[kMaxProposals];
   int np = 0;
   bool overflow = false;
-  for (uint32_t o0 = 0; o0 < g.n && !(mapped && remaining == 0) && !ambiguous; o0 += 32) {
+  // Starts by score: the live node of the highest score next (the DP's top
+  // first).  Two live nodes sharing that score: Flye's order between them
+  // could matter, and the group goes back for that order.
+  for (bool first_pick = true; pick && remaining > 0; first_pick = false) {
+    int32_t ms;
+    uint32_t mi, mc;
+    if (first_pick) {
+      const GroupTop t = top[gidx];
+      ms = t.score;
+      mi = t.first;
+      mc = t.count;
+    } else {
+      int32_t bs = INT_MIN;
+      uint32_t bi = 0xffffffffu, bc = 0;
+      const uint32_t nw = (g.n + 31) / 32;
+      for (uint32_t w = 0; w < nw; ++w) {
+        const uint32_t lv = m.link[w] & ~m.done[w];
+        if (!lv) continue;
+        if ((lv >> lane) & 1u) {
+          const int32_t sv = score[b + w * 32 + lane];
+          if (sv > bs) {
+            bs = sv;
+            bi = w * 32 + lane;
+            bc = 1;
+          } else if (sv == bs) {
+            ++bc;
+          }
+        }
+      }
+      ms = bs;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) ms = max(ms, __shfl_xor_sync(0xffffffffu, ms, o));
+      mc = bs == ms ? bc : 0u;
+      mi = bs == ms ? bi : 0xffffffffu;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        mc += __shfl_xor_sync(0xffffffffu, mc, o);
+        mi = min(mi, __shfl_xor_sync(0xffffffffu, mi, o));
+      }
+    }
+    if (mc > 1) {
+      ambiguous = true;
+      break;
+    }
+    const uint32_t s0 = mi;
+    int32_t first = 0, clen = 0;
+    walk_maps(m, bt + b, static_cast<int32_t>(s0), first, clen, remaining);
+    if (lane == 0 && !overflow)
+      add_proposal(cur, ext, score, b, s0, first, clen, qi, ext_signed, g, fq, nf, logt, p, st,
+                   gidx, props, np, overflow);
+    __syncwarp();
+  }
+  for (uint32_t o0 = 0; !pick && o0 < g.n && !(mapped && remaining == 0); o0 += 32) {
     const uint32_t oi = o0 + lane;
     const bool valid = oi < g.n;
     const uint32_t start = valid ? order[b + oi] : 0;
@@ -569,10 +698,6 @@ __global__ void __launch_bounds__(kBtWarps * 32) backtrack_kernel(
     while (mask) {
       const int j = __ffs(mask) - 1;
       const uint32_t s0 = __shfl_sync(0xffffffffu, start, j);
-      if (check && run_has_other_live(m, order + b, score + b, g.n, o0 + j, score[b + s0])) {
-        ambiguous = true;
-        break;
-      }
       int32_t first = 0, clen = 0;
       if (mapped) {
         walk_maps(m, bt + b, static_cast<int32_t>(s0), first, clen, remaining);
@@ -586,38 +711,9 @@ __global__ void __launch_bounds__(kBtWarps * 32) backtrack_kernel(
           pos = nx;
         }
       }
-      if (lane == 0 && !overflow) {
-        Prop o;
-        o.cb = cur[b + first];
-        o.ce = cur[b + s0] + k - 1;
-        o.eb = ext[b + first];
-        o.ee = ext[b + s0] + k - 1;
-        o.score = score[b + s0] - score[b + first] + k - 1;
-        o.clen = clen;
-        bool keep = overlap_test(o, qi.signed_id, ext_signed, qi.len, g.ext_len, p);
-        if (keep) {
-          const uint32_t lo = lower_bound_i32(fq, nf, o.cb);
-          const uint32_t hi = lower_bound_i32(fq, nf, o.ce + 1);
-          const int32_t norm = max(o.ce - o.cb, o.ee - o.eb) - static_cast<int32_t>(hi - lo);
-          keep = norm > 0;
-          if (keep) {
-            float rate =
-                fdiv(fmul(static_cast<float>(clen), p.sample_rate), static_cast<float>(norm));
-            rate = rate < 1.0f ? rate : 1.0f;
-            const float x = fdiv(1.0f, rate);
-            if (!(x < 16777216.0f)) raise_status(st, kDevLogDomain, 0, static_cast<int64_t>(gidx));
-            o.div = fdiv(flye_logf(x, logt), static_cast<float>(k));
-          }
-        }
-        if (keep) {
-          if (np == kMaxProposals) {
-            raise_status(st, kDevProposalOverflow, 0, static_cast<int64_t>(gidx));
-            overflow = true;
-          } else {
-            props[np++] = o;
-          }
-        }
-      }
+      if (lane == 0 && !overflow)
+        add_proposal(cur, ext, score, b, s0, first, clen, qi, ext_signed, g, fq, nf, logt, p, st,
+                     gidx, props, np, overflow);
       __syncwarp();
       if (mapped && remaining == 0) break;
       mask = __ballot_sync(
@@ -780,6 +876,16 @@ cudaError_t groups_prepare_ext_sort(uint64_t* keys, uint32_t* vals, const GroupI
   return cudaGetLastError();
 }
 
+cudaError_t groups_ext_presorted(const uint32_t* vals, GroupInfo* groups, const uint32_t* ext_list,
+                                 const uint32_t* counts, uint32_t* out, uint32_t* out_count,
+                                 cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(out_count, 0, 4, s);
+  if (e != cudaSuccess) return e;
+  count_launch();
+  ext_presorted_kernel<<<2048, 256, 0, s>>>(vals, groups, ext_list, counts, out, out_count);
+  return cudaGetLastError();
+}
+
 cudaError_t groups_split(const uint64_t* keys, const uint32_t* vals, const GroupInfo* groups,
                          const uint32_t* dp_list, const uint32_t* counts, int32_t* cur,
                          int32_t* ext, cudaStream_t s) {
@@ -790,7 +896,8 @@ cudaError_t groups_split(const uint64_t* keys, const uint32_t* vals, const Group
 
 cudaError_t chain_dp(const int32_t* cur, const int32_t* ext, int32_t* score, int32_t* bt,
                      const GroupInfo* groups, const uint32_t* dp_list, const uint32_t* counts,
-                     const ChainParams& p, uint32_t* work, int num_sms, cudaStream_t s) {
+                     const ChainParams& p, GroupTop* top, uint32_t* work, int num_sms,
+                     cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(work, 0, 4, s);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
@@ -798,7 +905,35 @@ cudaError_t chain_dp(const int32_t* cur, const int32_t* ext, int32_t* score, int
   if (e != cudaSuccess) return e;
   count_launch();
   dp_kernel<<<num_sms * std::max(per_sm, 1), kDpWarps * 32, 0, s>>>(cur, ext, score, bt, groups,
-                                                                   dp_list, counts, p, work);
+                                                                   dp_list, counts, p, top,
+                                                                   work);
+  return cudaGetLastError();
+}
+
+namespace {
+
+__global__ void large_groups_kernel(const GroupInfo* __restrict__ groups,
+                                    const uint32_t* __restrict__ list,
+                                    const uint32_t* __restrict__ list_count, uint32_t min_n,
+                                    uint32_t* __restrict__ out, uint32_t* __restrict__ out_count) {
+  const uint32_t cnt = *list_count;
+  for (uint32_t li = blockIdx.x * blockDim.x + threadIdx.x; li < cnt;
+       li += gridDim.x * blockDim.x) {
+    const uint32_t g = list[li];
+    if (groups[g].n > min_n) out[atomicAdd(out_count, 1u)] = g;
+  }
+}
+
+}  // namespace
+
+cudaError_t list_large_groups(const GroupInfo* groups, const uint32_t* list,
+                              const uint32_t* list_count, uint32_t max_groups, uint32_t min_n,
+                              uint32_t* out, uint32_t* out_count, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(out_count, 0, 4, s);
+  if (e != cudaSuccess || max_groups == 0) return e;
+  count_launch();
+  large_groups_kernel<<<grid(max_groups, 256) < 1024 ? grid(max_groups, 256) : 1024, 256, 0, s>>>(
+      groups, list, list_count, min_n, out, out_count);
   return cudaGetLastError();
 }
 
@@ -815,7 +950,7 @@ cudaError_t chain_prepare_order(const int32_t* score, uint64_t* keys, uint32_t* 
 cudaError_t chain_backtrack(const int32_t* cur, const int32_t* ext, const int32_t* score,
                             int32_t* bt, const uint32_t* order, const GroupInfo* groups,
                             const uint32_t* list, const uint32_t* list_count,
-                            const uint8_t* fast_order, uint32_t* redo_list, uint32_t* redo_count,
+                            const GroupTop* top, uint32_t* redo_list, uint32_t* redo_count,
                             const QueryInfo* qinfo, const uint64_t* f_off, const int32_t* fpos,
                             const int64_t* slot_signed, const LogfTable& logt,
                             const ChainParams& p, OverlapRow* pool, uint64_t pool_cap,
@@ -833,7 +968,7 @@ cudaError_t chain_backtrack(const int32_t* cur, const int32_t* ext, const int32_
   if (sms <= 0) sms = 1;
   count_launch();
   backtrack_kernel<<<sms * 4, kBtWarps * 32, smem, s>>>(
-      cur, ext, score, bt, order, groups, list, list_count, fast_order, redo_list, redo_count,
+      cur, ext, score, bt, order, groups, list, list_count, top, redo_list, redo_count,
       qinfo, f_off, fpos, slot_signed, logt,
       p, pool, pool_cap, pool_count, group_rows, st, work);
   return cudaGetLastError();

@@ -16,17 +16,12 @@
 //   query's keys are distinct, and its sort is a stable sort by ext id: a
 //   least-significant-digit radix sort over the ext id bits, 8 bits per pass,
 //   in tiles of kMatchTile hits that never straddle two queries.
-// * Per-group sorts of at most kGroupCap elements by a 32-bit key: ext pos for
-//   the ext-sorted re-sort (tools/replay_read_to_graph_source_pack.py:396-397)
-//   and INT32_MAX - score for the score order of the backtrack
-//   (tools/replay_overlap_chains.py:316).  One block sorts the group in
-//   shared memory (radix sort on (key, index) packed in 32 bits).  For the
-//   ext re-sort it compares neighbours, and a group with equal ext positions
-//   is written out in the layout sort.cu expects and listed for it.  The
-//   score order is used as sorted and marked in fast_order: the backtrack
-//   itself detects the rare case where Flye's order among equal scores could
-//   change its result and sends that group back for the libstdc++ order.
-//   Groups too large for shared memory always go to sort.cu.
+// * Ext-pos re-sort of ext-sorted groups of at most kGroupCap elements
+//   (tools/replay_read_to_graph_source_pack.py:396-397) that are not already
+//   in strict ext-pos order.  One block sorts the group in shared memory
+//   (radix sort on (ext pos, index) packed in 32 bits) and compares
+//   neighbours; a group with equal ext positions, or too large for shared
+//   memory, is written out in the layout sort.cu expects and listed for it.
 #include <algorithm>
 #include <climits>
 #include <cstdint>
@@ -305,21 +300,14 @@ struct GroupSmem {
   uint32_t item;
 };
 
-// Rewrites the group for sort.cu and lists it there.
-template <int MODE>
-__device__ void group_to_emulation(uint64_t* keys, uint32_t* vals, const int32_t* score,
-                                   const GroupInfo& g, uint64_t* emu_begin, uint64_t* emu_end,
-                                   uint32_t* emu_count) {
+// Rewrites the group as (key = ext pos, val = cur pos) for sort.cu and lists it there.
+__device__ void group_to_emulation(uint64_t* keys, uint32_t* vals, const GroupInfo& g,
+                                   uint64_t* emu_begin, uint64_t* emu_end, uint32_t* emu_count) {
   for (uint32_t j = threadIdx.x; j < g.n; j += blockDim.x) {
     const uint64_t i = g.start + j;
-    if (MODE == 0) {
-      const uint64_t kk = keys[i];
-      keys[i] = static_cast<uint64_t>(vals[i]);
-      vals[i] = static_cast<uint32_t>(kk & 0xffffffffu);
-    } else {
-      keys[i] = static_cast<uint64_t>(static_cast<uint32_t>(INT_MAX - score[i]));
-      vals[i] = j;
-    }
+    const uint64_t kk = keys[i];
+    keys[i] = static_cast<uint64_t>(vals[i]);
+    vals[i] = static_cast<uint32_t>(kk & 0xffffffffu);
   }
   if (threadIdx.x == 0) {
     const uint32_t s = atomicAdd(emu_count, 1u);
@@ -328,17 +316,13 @@ __device__ void group_to_emulation(uint64_t* keys, uint32_t* vals, const int32_t
   }
 }
 
-// MODE 0, ext re-sort: in (key = (ext id << 32) | cur pos, val = ext pos),
-//   out (key = ext pos, val = cur pos) in ext-pos order.
-// MODE 1, score order: out val[i] = local index of the i-th element by
-//   score descending (keys untouched).
-template <int MODE>
+// In (key = (ext id << 32) | cur pos, val = ext pos), out (key = ext pos,
+// val = cur pos) in ext-pos order.
 __global__ void __launch_bounds__(kGroupBlock, 1)
     group_sort_kernel(uint64_t* __restrict__ keys, uint32_t* __restrict__ vals,
-                      const int32_t* __restrict__ score, const GroupInfo* __restrict__ groups,
-                      const uint32_t* __restrict__ list, const uint32_t* __restrict__ list_count,
-                      int32_t k, uint64_t* __restrict__ emu_begin, uint64_t* __restrict__ emu_end,
-                      uint32_t* __restrict__ emu_count, uint8_t* __restrict__ fast_order,
+                      const GroupInfo* __restrict__ groups, const uint32_t* __restrict__ list,
+                      const uint32_t* __restrict__ list_count, uint64_t* __restrict__ emu_begin,
+                      uint64_t* __restrict__ emu_end, uint32_t* __restrict__ emu_count,
                       uint32_t* __restrict__ work) {
   extern __shared__ __align__(16) unsigned char group_raw[];
   GroupSmem& sm = *reinterpret_cast<GroupSmem*>(group_raw);
@@ -356,10 +340,9 @@ __global__ void __launch_bounds__(kGroupBlock, 1)
     const GroupInfo g = groups[gidx];
     const uint32_t n = g.n;
     const uint64_t b = g.start;
-    if (MODE == 1 && threadIdx.x == 0) fast_order[gidx] = 0;
     if (n == 0) continue;
     if (n > kGroupCap) {
-      group_to_emulation<MODE>(keys, vals, score, g, emu_begin, emu_end, emu_count);
+      group_to_emulation(keys, vals, g, emu_begin, emu_end, emu_count);
       __syncthreads();
       continue;
     }
@@ -370,7 +353,7 @@ __global__ void __launch_bounds__(kGroupBlock, 1)
     __syncthreads();
     uint32_t lmin = 0xffffffffu, lmax = 0;
     for (uint32_t j = threadIdx.x; j < n; j += kGroupBlock) {
-      const uint32_t key = MODE == 0 ? vals[b + j] : static_cast<uint32_t>(INT_MAX - score[b + j]);
+      const uint32_t key = vals[b + j];
       sm.a[j] = key;
       lmin = min(lmin, key);
       lmax = max(lmax, key);
@@ -382,7 +365,7 @@ __global__ void __launch_bounds__(kGroupBlock, 1)
     const int kb = range ? 32 - __clz(range) : 0;
     const int ib = n > 1 ? 32 - __clz(n - 1) : 0;
     if (kb + ib > 32) {  // the packed form does not fit: leave it to sort.cu
-      group_to_emulation<MODE>(keys, vals, score, g, emu_begin, emu_end, emu_count);
+      group_to_emulation(keys, vals, g, emu_begin, emu_end, emu_count);
       __syncthreads();
       continue;
     }
@@ -445,28 +428,23 @@ __global__ void __launch_bounds__(kGroupBlock, 1)
       src = dst;
       dst = tmp;
     }
-    // Equal ext positions?  (The score order is checked by the backtrack.)
+    // Equal ext positions?
     bool tie = false;
-    for (uint32_t j = threadIdx.x + 1; MODE == 0 && j < n && !tie; j += kGroupBlock)
+    for (uint32_t j = threadIdx.x + 1; j < n && !tie; j += kGroupBlock)
       tie = (src[j] >> ib) == (src[j - 1] >> ib);
     if (__syncthreads_or(tie)) {
-      group_to_emulation<MODE>(keys, vals, score, g, emu_begin, emu_end, emu_count);
+      group_to_emulation(keys, vals, g, emu_begin, emu_end, emu_count);
       __syncthreads();
       continue;
     }
     const uint32_t imask = ib ? ((1u << ib) - 1u) : 0u;
-    if (MODE == 0) {
-      // gather the cur positions before any write: the group is rewritten in place
-      for (uint32_t i = threadIdx.x; i < n; i += kGroupBlock)
-        dst[i] = static_cast<uint32_t>(keys[b + (src[i] & imask)] & 0xffffffffu);
-      __syncthreads();
-      for (uint32_t i = threadIdx.x; i < n; i += kGroupBlock) {
-        keys[b + i] = static_cast<uint64_t>((ib ? (src[i] >> ib) : 0u) + kmin);
-        vals[b + i] = dst[i];
-      }
-    } else {
-      for (uint32_t i = threadIdx.x; i < n; i += kGroupBlock) vals[b + i] = src[i] & imask;
-      if (threadIdx.x == 0) fast_order[gidx] = 1;
+    // gather the cur positions before any write: the group is rewritten in place
+    for (uint32_t i = threadIdx.x; i < n; i += kGroupBlock)
+      dst[i] = static_cast<uint32_t>(keys[b + (src[i] & imask)] & 0xffffffffu);
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < n; i += kGroupBlock) {
+      keys[b + i] = static_cast<uint64_t>((ib ? (src[i] >> ib) : 0u) + kmin);
+      vals[b + i] = dst[i];
     }
     __syncthreads();
   }
@@ -546,27 +524,18 @@ cudaError_t match_radix(uint64_t* keys, uint32_t* vals, uint32_t* alt_hi, uint32
   return cudaGetLastError();
 }
 
-cudaError_t group_sort(int mode, uint64_t* keys, uint32_t* vals, const int32_t* score,
-                       const GroupInfo* groups, const uint32_t* list, const uint32_t* list_count,
-                       uint32_t max_groups, int32_t k, uint64_t* emu_begin, uint64_t* emu_end,
-                       uint32_t* emu_count, uint8_t* fast_order, uint32_t* work, int num_sms,
-                       cudaStream_t s) {
+cudaError_t group_ext_sort(uint64_t* keys, uint32_t* vals, const GroupInfo* groups,
+                           const uint32_t* list, const uint32_t* list_count, uint32_t max_groups,
+                           uint64_t* emu_begin, uint64_t* emu_end, uint32_t* emu_count,
+                           uint32_t* work, int num_sms, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(emu_count, 0, 4, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(work, 0, 4, s);
   if (e != cudaSuccess || max_groups == 0) return e;
   const unsigned grid = static_cast<unsigned>(std::min<uint64_t>(max_groups, num_sms));
+  allow_smem(group_sort_kernel, sizeof(GroupSmem));
   count_launch();
-  if (mode == 0) {
-    allow_smem(group_sort_kernel<0>, sizeof(GroupSmem));
-    group_sort_kernel<0><<<grid, kGroupBlock, sizeof(GroupSmem), s>>>(
-        keys, vals, score, groups, list, list_count, k, emu_begin, emu_end, emu_count, fast_order,
-        work);
-  } else {
-    allow_smem(group_sort_kernel<1>, sizeof(GroupSmem));
-    group_sort_kernel<1><<<grid, kGroupBlock, sizeof(GroupSmem), s>>>(
-        keys, vals, score, groups, list, list_count, k, emu_begin, emu_end, emu_count, fast_order,
-        work);
-  }
+  group_sort_kernel<<<grid, kGroupBlock, sizeof(GroupSmem), s>>>(
+      keys, vals, groups, list, list_count, emu_begin, emu_end, emu_count, work);
   return cudaGetLastError();
 }
 

@@ -128,7 +128,7 @@ struct GroupInfo {
   uint32_t ext_di;
   int32_t ext_len;
   int32_t survive;
-  int32_t ext_sorted;
+  int32_t ext_sorted;  // 0: cur-pos order; 1: re-sorted by ext pos; 2: ext order already
 };
 
 // Device-side overlap row before the final ABI conversion.
@@ -155,7 +155,8 @@ struct QueryInfo {
 // emulation (fastsort.cu); segments that may hold equal keys are listed in
 // (emu_begin, emu_end, *emu_count) for segmented_std_sort.
 constexpr uint32_t kMatchTile = 4096;  // hits per radix tile (never across queries)
-constexpr uint32_t kGroupCap = 16384;  // largest group sorted in shared memory
+constexpr uint32_t kGroupCap = 16384;      // largest group re-sorted in shared memory
+constexpr uint32_t kBacktrackCap = 16384;  // largest group backtracked over shared-memory maps
 
 struct MatchTile {
   uint64_t begin;
@@ -178,20 +179,17 @@ cudaError_t match_radix(uint64_t* keys, uint32_t* vals, uint32_t* alt_hi, uint32
                         uint32_t* alt_val, const MatchTile* tiles, uint32_t ntile,
                         const uint64_t* q_off, const uint32_t* ntiles, const uint64_t* tile_off,
                         uint32_t nq, int id_bits, uint32_t* counts, int num_sms, cudaStream_t s);
-// Groups of list[0 .. *list_count): mode 0 re-sorts ext-sorted groups by ext
-// pos (out: key = ext pos, val = cur pos); mode 1 writes the score order
-// (val[i] = local index of the i-th element by score descending) and
-// fast_order[group] = 1 where that order came from the plain sort (equal
-// scores in any order), 0 where the group was listed for sort.cu.
 // stats[i_emul] += *emul; stats[i_plain] += total - *emul (total from
 // total_dev when given, else total_host; i_plain < 0 skips it).
 cudaError_t sort_stats_add(uint64_t* stats, int i_plain, int i_emul, const uint32_t* total_dev,
                            uint32_t total_host, const uint32_t* emul, cudaStream_t s);
-cudaError_t group_sort(int mode, uint64_t* keys, uint32_t* vals, const int32_t* score,
-                       const GroupInfo* groups, const uint32_t* list, const uint32_t* list_count,
-                       uint32_t max_groups, int32_t k, uint64_t* emu_begin, uint64_t* emu_end,
-                       uint32_t* emu_count, uint8_t* fast_order, uint32_t* work, int num_sms,
-                       cudaStream_t s);
+// Ext-pos re-sort of the groups list[0 .. *list_count) (out: key = ext pos,
+// val = cur pos); groups with equal ext positions or over kGroupCap elements
+// are listed for segmented_std_sort instead.
+cudaError_t group_ext_sort(uint64_t* keys, uint32_t* vals, const GroupInfo* groups,
+                           const uint32_t* list, const uint32_t* list_count, uint32_t max_groups,
+                           uint64_t* emu_begin, uint64_t* emu_end, uint32_t* emu_count,
+                           uint32_t* work, int num_sms, cudaStream_t s);
 
 cudaError_t groups_mark(const uint64_t* keys, const uint64_t* q_off, uint32_t nq, uint64_t nhits,
                         uint32_t* flags, cudaStream_t s);
@@ -207,28 +205,51 @@ cudaError_t groups_prefilter_n(const uint64_t* keys, const uint32_t* vals, Group
 cudaError_t groups_prepare_ext_sort(uint64_t* keys, uint32_t* vals, const GroupInfo* groups,
                                     const uint32_t* ext_list, const uint32_t* counts,
                                     uint64_t* seg_begin, uint64_t* seg_end, cudaStream_t s);
-// Split (key, val) into CUR / EXT arrays for the DP.
+// Ext-sorted groups already in strict ext-pos order get ext_sorted = 2 (read
+// in place); the others are appended to out / *out_count (zeroed here).
+cudaError_t groups_ext_presorted(const uint32_t* vals, GroupInfo* groups, const uint32_t* ext_list,
+                                 const uint32_t* counts, uint32_t* out, uint32_t* out_count,
+                                 cudaStream_t s);
+// Split (key, val) into CUR / EXT arrays for the DP (ext_sorted == 1 groups
+// hold key = ext pos, val = cur pos after their re-sort).
 cudaError_t groups_split(const uint64_t* keys, const uint32_t* vals, const GroupInfo* groups,
                          const uint32_t* dp_list, const uint32_t* counts, int32_t* cur,
                          int32_t* ext, cudaStream_t s);
-// work: one word of device scratch (the group counter of the launch).
+// Highest score of a group, its first element and how many elements have it.
+struct GroupTop {
+  int32_t score;
+  uint32_t first;
+  uint32_t count;
+  uint32_t pad;
+};
+
+// work: one word of device scratch (the group counter of the launch); top
+// (indexed by group) receives each group's GroupTop.
 cudaError_t chain_dp(const int32_t* cur, const int32_t* ext, int32_t* score, int32_t* bt,
                      const GroupInfo* groups, const uint32_t* dp_list, const uint32_t* counts,
-                     const ChainParams& p, uint32_t* work, int num_sms, cudaStream_t s);
+                     const ChainParams& p, GroupTop* top, uint32_t* work, int num_sms,
+                     cudaStream_t s);
+// Groups of list[0 .. *list_count) with more than min_n elements, appended
+// to out / *out_count (zeroed here).
+cudaError_t list_large_groups(const GroupInfo* groups, const uint32_t* list,
+                              const uint32_t* list_count, uint32_t max_groups, uint32_t min_n,
+                              uint32_t* out, uint32_t* out_count, cudaStream_t s);
 // Score-order sort inputs of the groups list[0 .. *list_count): key =
 // INT32_MAX - score, val = local index, and their segment bounds.
 cudaError_t chain_prepare_order(const int32_t* score, uint64_t* keys, uint32_t* vals,
                                 const GroupInfo* groups, const uint32_t* list,
                                 const uint32_t* list_count, uint64_t* seg_begin,
                                 uint64_t* seg_end, cudaStream_t s);
-// Backtrack of the groups list[0 .. *list_count) in the score order `order`.
-// Where fast_order[group] is set the order came from the plain sort; a group
-// whose result could depend on the order among equal scores is not finished
-// but appended to redo_list, to be run again with the libstdc++ order.
+// Backtrack of the groups list[0 .. *list_count).  With `top` (the DP's
+// GroupTop per group), groups of up to 16,384 elements pick their starts in
+// score order themselves, and a group whose result could depend on the order
+// among equal scores is not finished but appended to redo_list, to be run
+// again with Flye's order; larger groups, and every group when top is null,
+// follow the score order in `order` (local indices, libstdc++ order).
 cudaError_t chain_backtrack(const int32_t* cur, const int32_t* ext, const int32_t* score,
                             int32_t* bt, const uint32_t* order, const GroupInfo* groups,
                             const uint32_t* list, const uint32_t* list_count,
-                            const uint8_t* fast_order, uint32_t* redo_list, uint32_t* redo_count,
+                            const GroupTop* top, uint32_t* redo_list, uint32_t* redo_count,
                             const QueryInfo* qinfo, const uint64_t* f_off, const int32_t* fpos,
                             const int64_t* slot_signed, const LogfTable& logt,
                             const ChainParams& p, OverlapRow* pool, uint64_t pool_cap,

@@ -269,12 +269,14 @@ cuflye_status cuflye_last_timing(const cuflye_ctx* ctx, double* stage_ms, uint64
 
 /* Diagnostics of the last overlaps / read-to-graph call (no counterpart in
  * the reference): how its sort points ran.  Segments whose keys are all
- * distinct have one sorted order and take plain sorts; the others take the
- * libstdc++-order sort.  counts[0] / [1]: queries whose KmerMatch sort ran
- * plain / libstdc++-order; [2] / [3]: ext-sorted groups re-sorted plain /
- * libstdc++-order; [4] / [5]: score orders plain / libstdc++-order (groups
- * over 16,384 elements); [6]: groups whose backtrack ran again in the
- * libstdc++ order because equal scores could change their result. */
+ * distinct have one sorted order and need no emulation of libstdc++'s
+ * std::sort; the others take the libstdc++-order sort.  counts[0] / [1]:
+ * queries whose KmerMatch sort ran plain / libstdc++-order; [2] / [3]:
+ * ext-sorted groups put in ext-pos order plain (most already are) /
+ * libstdc++-order; [4] / [5]: groups whose backtrack picked its starts by
+ * score itself / followed the libstdc++-order score sort (groups over
+ * 16,384 elements); [6]: groups whose backtrack ran again in the libstdc++
+ * order because equal scores could change their result. */
 cuflye_status cuflye_last_sort_stats(const cuflye_ctx* ctx, uint64_t* counts, size_t n);
 
 /* Kernel launches issued by the library in this process so far. */
