@@ -674,8 +674,9 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
   int32_t* bt = buf<int32_t>(c, "c_bt", H);
   GroupTop* top = buf<GroupTop>(c, "c_top", G);
   CUFLYE_CHECK(cudaEventRecord(c->ev[6], st));
-  CUFLYE_CHECK(chain_dp(cur, ext, score, bt, groups, dp_list, gcounts, cp, top, work, c->num_sms,
-                        st));
+  int32_t* pmc = buf<int32_t>(c, "c_pmc", chain_dp_pmc_words(H, G));
+  CUFLYE_CHECK(chain_dp(cur, ext, score, bt, groups, dp_list, gcounts, cp, top, pmc, work,
+                        c->num_sms, st));
   CUFLYE_CHECK(cudaEventRecord(c->ev[7], st));
   // 5. score order (indices by score descending, libstdc++ order) only for
   // groups above the backtrack's shared-memory maps; the backtrack picks the

@@ -233,6 +233,10 @@ __device__ __forceinline__ void eval_chunk(bool valid, int32_t cj, int32_t ej, i
     sc = sj + ms - gc;
   }
   const bool stop = !valid || (es ? ed > p.max_jump : cd > p.max_jump);
+  if (__ballot_sync(0xffffffffu, acc) == 0) {  // no candidate: only a stop matters
+    done = __ballot_sync(0xffffffffu, stop) != 0;
+    return;
+  }
   int32_t incl = sc;
 #pragma unroll
   for (int d = 1; d < 32; d <<= 1) {
@@ -265,7 +269,7 @@ __global__ void __launch_bounds__(kDpWarps * 32) dp_kernel(
     const int32_t* __restrict__ cur, const int32_t* __restrict__ ext, int32_t* score,
     int32_t* bt, const GroupInfo* __restrict__ groups, const uint32_t* __restrict__ list,
     const uint32_t* __restrict__ counts, ChainParams p, GroupTop* __restrict__ top,
-    uint32_t* __restrict__ work) {
+    int32_t* pmc, uint32_t* __restrict__ work) {
   const int lane = threadIdx.x & 31;
   const uint32_t cnt = counts[1];
   for (uint32_t li = next_item(work); li < cnt; li = next_item(work)) {
@@ -279,6 +283,12 @@ __global__ void __launch_bounds__(kDpWarps * 32) dp_kernel(
     const bool es = g.ext_sorted != 0;
     int32_t s_prev = 0;        // score of the element before the next one to score
     int32_t pc = 0, pe = 0;    // positions of the element before this chunk
+    // Highest score so far, and per 32-element chunk t of the group the
+    // highest score over elements [0, 32t + 31] in pmc[pbase + t].  A
+    // predecessor j scores at most S[j] + k, so a scan stops once that bound
+    // over every j still to visit cannot beat the best found.
+    int32_t run_max = 0;
+    const uint64_t pbase = (b >> 5) + gidx;
     for (uint32_t i0 = 0; i0 < n; i0 += 32) {
       const uint32_t i = i0 + lane;
       const uint32_t len = min(32u, n - i0);
@@ -337,6 +347,7 @@ __global__ void __launch_bounds__(kDpWarps * 32) dp_kernel(
                             : -1;
           }
           s_prev = __shfl_sync(0xffffffffu, s_mine, u - 1);
+          run_max = max(run_max, s_prev);  // scores rise along a run
           t = u;
         }
         if (t < len) {
@@ -348,6 +359,9 @@ __global__ void __launch_bounds__(kDpWarps * 32) dp_kernel(
           int32_t best = 0, bestj = 0;
           bool done = false;
           for (int32_t c0 = it - 1; !done && c0 >= 0; c0 -= 32) {
+            const int32_t bound =
+                c0 >= static_cast<int32_t>(i0) ? run_max : __ldcg(pmc + pbase + (c0 >> 5));
+            if (bound + p.k <= best) break;
             const int32_t j = c0 - lane;
             const bool valid = j >= 0;
             int32_t cj = 0, ej = 0, sj = 0;
@@ -372,10 +386,13 @@ __global__ void __launch_bounds__(kDpWarps * 32) dp_kernel(
             }
           }
           s_prev = si;
+          run_max = max(run_max, si);
           ++t;
         }
         __syncwarp();
       }
+      if (lane == 0) pmc[pbase + (i0 >> 5)] = run_max;
+      __syncwarp();
       pc = __shfl_sync(0xffffffffu, ci, 31);
       pe = __shfl_sync(0xffffffffu, ei, 31);
     }
@@ -896,8 +913,8 @@ cudaError_t groups_split(const uint64_t* keys, const uint32_t* vals, const Group
 
 cudaError_t chain_dp(const int32_t* cur, const int32_t* ext, int32_t* score, int32_t* bt,
                      const GroupInfo* groups, const uint32_t* dp_list, const uint32_t* counts,
-                     const ChainParams& p, GroupTop* top, uint32_t* work, int num_sms,
-                     cudaStream_t s) {
+                     const ChainParams& p, GroupTop* top, int32_t* pmc, uint32_t* work,
+                     int num_sms, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(work, 0, 4, s);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
@@ -906,7 +923,7 @@ cudaError_t chain_dp(const int32_t* cur, const int32_t* ext, int32_t* score, int
   count_launch();
   dp_kernel<<<num_sms * std::max(per_sm, 1), kDpWarps * 32, 0, s>>>(cur, ext, score, bt, groups,
                                                                    dp_list, counts, p, top,
-                                                                   work);
+                                                                   pmc, work);
   return cudaGetLastError();
 }
 

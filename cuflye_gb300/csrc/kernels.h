@@ -224,11 +224,15 @@ struct GroupTop {
 };
 
 // work: one word of device scratch (the group counter of the launch); top
-// (indexed by group) receives each group's GroupTop.
+// (indexed by group) receives each group's GroupTop; pmc: chain_dp_pmc_words
+// words of scratch (running score maxima per 32 elements).
 cudaError_t chain_dp(const int32_t* cur, const int32_t* ext, int32_t* score, int32_t* bt,
                      const GroupInfo* groups, const uint32_t* dp_list, const uint32_t* counts,
-                     const ChainParams& p, GroupTop* top, uint32_t* work, int num_sms,
-                     cudaStream_t s);
+                     const ChainParams& p, GroupTop* top, int32_t* pmc, uint32_t* work,
+                     int num_sms, cudaStream_t s);
+inline uint64_t chain_dp_pmc_words(uint64_t nhits, uint64_t ngroups) {
+  return (nhits >> 5) + ngroups + 2;
+}
 // Groups of list[0 .. *list_count) with more than min_n elements, appended
 // to out / *out_count (zeroed here).
 cudaError_t list_large_groups(const GroupInfo* groups, const uint32_t* list,
