@@ -666,28 +666,28 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
   CUFLYE_CHECK(sort_stats_add(sstats, 2, 3, gcounts + 0, 0, ecount, st));
   CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, sb, se, G32, ecount, glists,
                                   scounts, c->num_sms, st, sort_tasks(c, "s", H, G32)));
-  int32_t* cur = buf<int32_t>(c, "c_cur", H);
-  int32_t* ext = buf<int32_t>(c, "c_ext", H);
-  CUFLYE_CHECK(groups_split(ps.keys, ps.vals, groups, dp_list, gcounts, cur, ext, st));
-  // 4. DP
+  // 4. DP over the sorted pairs
   int32_t* score = buf<int32_t>(c, "c_score", H);
   int32_t* bt = buf<int32_t>(c, "c_bt", H);
   GroupTop* top = buf<GroupTop>(c, "c_top", G);
   CUFLYE_CHECK(cudaEventRecord(c->ev[6], st));
   int32_t* pmc = buf<int32_t>(c, "c_pmc", chain_dp_pmc_words(H, G));
-  CUFLYE_CHECK(chain_dp(cur, ext, score, bt, groups, dp_list, gcounts, cp, top, pmc, work,
+  CUFLYE_CHECK(chain_dp(ps.keys, ps.vals, score, bt, groups, dp_list, gcounts, cp, top, pmc, work,
                         c->num_sms, st));
   CUFLYE_CHECK(cudaEventRecord(c->ev[7], st));
   // 5. score order (indices by score descending, libstdc++ order) only for
   // groups above the backtrack's shared-memory maps; the backtrack picks the
-  // starts of the others itself
+  // starts of the others itself.  The (key, index) pairs of the order live in
+  // the group-building buffers, free by now.
+  uint64_t* okeys = gid;
+  uint32_t* order = gflags;
   uint32_t* big = buf<uint32_t>(c, "o_big", G);
   uint32_t* big_count = buf<uint32_t>(c, "o_bigcount", 1);
   CUFLYE_CHECK(list_large_groups(groups, dp_list, gcounts + 1, G32, kBacktrackCap, big, big_count,
                                  st));
   CUFLYE_CHECK(sort_stats_add(sstats, 4, 5, gcounts + 1, 0, big_count, st));
-  CUFLYE_CHECK(chain_prepare_order(score, ps.keys, ps.vals, groups, big, big_count, sb, se, st));
-  CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, sb, se, G32, big_count, glists,
+  CUFLYE_CHECK(chain_prepare_order(score, okeys, order, groups, big, big_count, sb, se, st));
+  CUFLYE_CHECK(segmented_std_sort(okeys, order, lscr, rscr, sb, se, G32, big_count, glists,
                                   scounts, c->num_sms, st, sort_tasks(c, "s", H, G32)));
   // 6. backtrack, proposals, primary selection; the row pool is sized by the
   // groups that survived the prefilter
@@ -702,17 +702,17 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
   uint32_t* redo_count = buf<uint32_t>(c, "o_redocount", 1);
   CUFLYE_CHECK(cudaMemsetAsync(redo_count, 0, 4, st));
   const int64_t* slot_signed = buf<int64_t>(c, "ix_slot_signed", 1);
-  CUFLYE_CHECK(chain_backtrack(cur, ext, score, bt, ps.vals, groups, dp_list, gcounts + 1, top,
+  CUFLYE_CHECK(chain_backtrack(ps.keys, ps.vals, score, bt, order, groups, dp_list, gcounts + 1, top,
                                redo, redo_count, ps.qinfo, ps.f_off, ps.fpos, slot_signed, c->logt,
                                cp, pool, pool_cap, pool_count, group_rows, c->status, G32, work,
                                st));
   CUFLYE_CHECK(sort_stats_add(sstats, -1, 6, nullptr, 0, redo_count, st));
   // groups whose result could depend on the order among equal scores: again
   // with the libstdc++ order
-  CUFLYE_CHECK(chain_prepare_order(score, ps.keys, ps.vals, groups, redo, redo_count, sb, se, st));
-  CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, sb, se, G32, redo_count, glists,
+  CUFLYE_CHECK(chain_prepare_order(score, okeys, order, groups, redo, redo_count, sb, se, st));
+  CUFLYE_CHECK(segmented_std_sort(okeys, order, lscr, rscr, sb, se, G32, redo_count, glists,
                                   scounts, c->num_sms, st, sort_tasks(c, "s", H, G32)));
-  CUFLYE_CHECK(chain_backtrack(cur, ext, score, bt, ps.vals, groups, redo, redo_count, nullptr,
+  CUFLYE_CHECK(chain_backtrack(ps.keys, ps.vals, score, bt, order, groups, redo, redo_count, nullptr,
                                nullptr, nullptr, ps.qinfo, ps.f_off, ps.fpos, slot_signed, c->logt,
                                cp, pool, pool_cap, pool_count, group_rows, c->status, G32, work,
                                st));

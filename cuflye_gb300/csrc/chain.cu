@@ -4,12 +4,13 @@
 //
 // A group is a run of equal ext ids inside one query's sorted matches.
 //   groups_*       : group bounds, the survival / span / overhang prefilter,
-//                    and the ext-sorted re-sort (via the libstdc++-order sort);
-//   chain_dp       : the O(n * window) DP, one warp per group (see dp_kernel);
-//   chain_backtrack: score-ordered backtrack (order from the libstdc++-order
-//                    sort of the scores), overlapTest, k-mer divergence,
-//                    proposal sort, primary selection and the divergence
-//                    filter, one warp per group;
+//                    and which ext-sorted groups are already in ext order;
+//   chain_dp       : the DP over the sorted pairs, one warp per group (see
+//                    dp_kernel);
+//   chain_backtrack: score-ordered backtrack (starts picked by score, or the
+//                    libstdc++-order sort of the scores), overlapTest, k-mer
+//                    divergence, proposal sort, primary selection and the
+//                    divergence filter, one warp per group;
 //   rows_*         : max_overlaps cutoff per query and order-preserving
 //                    compaction of the rows.
 #include <algorithm>
@@ -170,29 +171,6 @@ __global__ void ext_presorted_kernel(const uint32_t* __restrict__ vals,
   }
 }
 
-__global__ void split_kernel(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ vals,
-                             const GroupInfo* __restrict__ groups,
-                             const uint32_t* __restrict__ dp_list,
-                             const uint32_t* __restrict__ counts, int32_t* __restrict__ cur,
-                             int32_t* __restrict__ ext) {
-  const uint32_t cnt = counts[1];
-  const int lane = threadIdx.x & 31;
-  const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
-  for (uint32_t li = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; li < cnt; li += nwarps) {
-    const GroupInfo g = groups[dp_list[li]];
-    for (uint32_t j = lane; j < g.n; j += 32) {
-      const uint64_t i = g.start + j;
-      if (g.ext_sorted == 1) {  // re-sorted: key = ext pos, val = cur pos
-        cur[i] = static_cast<int32_t>(vals[i]);
-        ext[i] = static_cast<int32_t>(keys[i] & 0xffffffffu);
-      } else {
-        cur[i] = static_cast<int32_t>(keys[i] & 0xffffffffu);
-        ext[i] = static_cast<int32_t>(vals[i]);
-      }
-    }
-  }
-}
-
 // ---------------------------------------------------------------- DP
 //
 // Flye's DP visits predecessors j = i-1, i-2, ... and keeps the first j (in
@@ -265,8 +243,20 @@ __device__ __forceinline__ uint32_t next_item(uint32_t* counter) {
   return __shfl_sync(0xffffffffu, v, 0);
 }
 
+// Positions of match i of a group: the sorted pairs hold key = (ext id << 32)
+// | cur pos, val = ext pos, or key = ext pos, val = cur pos in groups
+// re-sorted by ext pos (swapped).
+__device__ __forceinline__ void load_match(const uint64_t* __restrict__ keys,
+                                           const uint32_t* __restrict__ vals, bool swapped,
+                                           uint64_t i, int32_t& c, int32_t& e) {
+  const uint32_t lo = static_cast<uint32_t>(__ldg(keys + i));
+  const uint32_t v = __ldg(vals + i);
+  c = static_cast<int32_t>(swapped ? v : lo);
+  e = static_cast<int32_t>(swapped ? lo : v);
+}
+
 __global__ void __launch_bounds__(kDpWarps * 32) dp_kernel(
-    const int32_t* __restrict__ cur, const int32_t* __restrict__ ext, int32_t* score,
+    const uint64_t* __restrict__ keys, const uint32_t* __restrict__ vals, int32_t* score,
     int32_t* bt, const GroupInfo* __restrict__ groups, const uint32_t* __restrict__ list,
     const uint32_t* __restrict__ counts, ChainParams p, GroupTop* __restrict__ top,
     int32_t* pmc, uint32_t* __restrict__ work) {
@@ -281,6 +271,7 @@ __global__ void __launch_bounds__(kDpWarps * 32) dp_kernel(
     const uint64_t b = g.start;
     const uint32_t n = g.n;
     const bool es = g.ext_sorted != 0;
+    const bool swapped = g.ext_sorted == 1;
     int32_t s_prev = 0;        // score of the element before the next one to score
     int32_t pc = 0, pe = 0;    // positions of the element before this chunk
     // Highest score so far, and per 32-element chunk t of the group the
@@ -293,10 +284,7 @@ __global__ void __launch_bounds__(kDpWarps * 32) dp_kernel(
       const uint32_t i = i0 + lane;
       const uint32_t len = min(32u, n - i0);
       int32_t ci = 0, ei = 0;
-      if (i < n) {
-        ci = __ldg(cur + b + i);
-        ei = __ldg(ext + b + i);
-      }
+      if (i < n) load_match(keys, vals, swapped, b + i, ci, ei);
       int32_t cp = __shfl_up_sync(0xffffffffu, ci, 1);
       int32_t ep = __shfl_up_sync(0xffffffffu, ei, 1);
       if (lane == 0) {
@@ -366,8 +354,7 @@ __global__ void __launch_bounds__(kDpWarps * 32) dp_kernel(
             const bool valid = j >= 0;
             int32_t cj = 0, ej = 0, sj = 0;
             if (valid) {
-              cj = __ldg(cur + b + j);
-              ej = __ldg(ext + b + j);
+              load_match(keys, vals, swapped, b + j, cj, ej);
               sj = __ldcg(score + b + j);
             }
             eval_chunk(valid, cj, ej, sj, j, cit, eit, es, p, best, bestj, done);
@@ -565,17 +552,21 @@ __device__ void walk_maps(BtMaps& m, const int32_t* __restrict__ btg, int32_t s0
 // The overlap of one walked chain (start s0 back to first): overlapTest,
 // then the k-mer divergence; kept proposals are appended to props.
 __device__ __forceinline__ void add_proposal(
-    const int32_t* __restrict__ cur, const int32_t* __restrict__ ext,
+    const uint64_t* __restrict__ keys, const uint32_t* __restrict__ vals,
     const int32_t* __restrict__ score, uint64_t b, uint32_t s0, int32_t first, int32_t clen,
     const QueryInfo& qi, int64_t ext_signed, const GroupInfo& g, const int32_t* fq, uint32_t nf,
     const LogfTable& logt, const ChainParams& p, DeviceStatus* st, uint32_t gidx, Prop* props,
     int& np, bool& overflow) {
   const int32_t k = p.k;
+  const bool swapped = g.ext_sorted == 1;
+  int32_t c0, e0, c1, e1;
+  load_match(keys, vals, swapped, b + first, c0, e0);
+  load_match(keys, vals, swapped, b + s0, c1, e1);
   Prop o;
-  o.cb = cur[b + first];
-  o.ce = cur[b + s0] + k - 1;
-  o.eb = ext[b + first];
-  o.ee = ext[b + s0] + k - 1;
+  o.cb = c0;
+  o.ce = c1 + k - 1;
+  o.eb = e0;
+  o.ee = e1 + k - 1;
   o.score = score[b + s0] - score[b + first] + k - 1;
   o.clen = clen;
   bool keep = overlap_test(o, qi.signed_id, ext_signed, qi.len, g.ext_len, p);
@@ -603,7 +594,7 @@ __device__ __forceinline__ void add_proposal(
 }
 
 __global__ void __launch_bounds__(kBtWarps * 32) backtrack_kernel(
-    const int32_t* __restrict__ cur, const int32_t* __restrict__ ext,
+    const uint64_t* __restrict__ keys, const uint32_t* __restrict__ vals,
     const int32_t* __restrict__ score, int32_t* bt, const uint32_t* __restrict__ order,
     const GroupInfo* __restrict__ groups, const uint32_t* __restrict__ dp_list,
     const uint32_t* __restrict__ list_count, const GroupTop* __restrict__ top,
@@ -700,7 +691,7 @@ __global__ void __launch_bounds__(kBtWarps * 32) backtrack_kernel(
     int32_t first = 0, clen = 0;
     walk_maps(m, bt + b, static_cast<int32_t>(s0), first, clen, remaining);
     if (lane == 0 && !overflow)
-      add_proposal(cur, ext, score, b, s0, first, clen, qi, ext_signed, g, fq, nf, logt, p, st,
+      add_proposal(keys, vals, score, b, s0, first, clen, qi, ext_signed, g, fq, nf, logt, p, st,
                    gidx, props, np, overflow);
     __syncwarp();
   }
@@ -729,7 +720,7 @@ __global__ void __launch_bounds__(kBtWarps * 32) backtrack_kernel(
         }
       }
       if (lane == 0 && !overflow)
-        add_proposal(cur, ext, score, b, s0, first, clen, qi, ext_signed, g, fq, nf, logt, p, st,
+        add_proposal(keys, vals, score, b, s0, first, clen, qi, ext_signed, g, fq, nf, logt, p, st,
                      gidx, props, np, overflow);
       __syncwarp();
       if (mapped && remaining == 0) break;
@@ -903,15 +894,7 @@ cudaError_t groups_ext_presorted(const uint32_t* vals, GroupInfo* groups, const 
   return cudaGetLastError();
 }
 
-cudaError_t groups_split(const uint64_t* keys, const uint32_t* vals, const GroupInfo* groups,
-                         const uint32_t* dp_list, const uint32_t* counts, int32_t* cur,
-                         int32_t* ext, cudaStream_t s) {
-  count_launch();
-  split_kernel<<<2048, 256, 0, s>>>(keys, vals, groups, dp_list, counts, cur, ext);
-  return cudaGetLastError();
-}
-
-cudaError_t chain_dp(const int32_t* cur, const int32_t* ext, int32_t* score, int32_t* bt,
+cudaError_t chain_dp(const uint64_t* keys, const uint32_t* vals, int32_t* score, int32_t* bt,
                      const GroupInfo* groups, const uint32_t* dp_list, const uint32_t* counts,
                      const ChainParams& p, GroupTop* top, int32_t* pmc, uint32_t* work,
                      int num_sms, cudaStream_t s) {
@@ -921,7 +904,7 @@ cudaError_t chain_dp(const int32_t* cur, const int32_t* ext, int32_t* score, int
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dp_kernel, kDpWarps * 32, 0);
   if (e != cudaSuccess) return e;
   count_launch();
-  dp_kernel<<<num_sms * std::max(per_sm, 1), kDpWarps * 32, 0, s>>>(cur, ext, score, bt, groups,
+  dp_kernel<<<num_sms * std::max(per_sm, 1), kDpWarps * 32, 0, s>>>(keys, vals, score, bt, groups,
                                                                    dp_list, counts, p, top,
                                                                    pmc, work);
   return cudaGetLastError();
@@ -964,7 +947,7 @@ cudaError_t chain_prepare_order(const int32_t* score, uint64_t* keys, uint32_t* 
   return cudaGetLastError();
 }
 
-cudaError_t chain_backtrack(const int32_t* cur, const int32_t* ext, const int32_t* score,
+cudaError_t chain_backtrack(const uint64_t* keys, const uint32_t* vals, const int32_t* score,
                             int32_t* bt, const uint32_t* order, const GroupInfo* groups,
                             const uint32_t* list, const uint32_t* list_count,
                             const GroupTop* top, uint32_t* redo_list, uint32_t* redo_count,
@@ -985,7 +968,7 @@ cudaError_t chain_backtrack(const int32_t* cur, const int32_t* ext, const int32_
   if (sms <= 0) sms = 1;
   count_launch();
   backtrack_kernel<<<sms * 4, kBtWarps * 32, smem, s>>>(
-      cur, ext, score, bt, order, groups, list, list_count, top, redo_list, redo_count,
+      keys, vals, score, bt, order, groups, list, list_count, top, redo_list, redo_count,
       qinfo, f_off, fpos, slot_signed, logt,
       p, pool, pool_cap, pool_count, group_rows, st, work);
   return cudaGetLastError();

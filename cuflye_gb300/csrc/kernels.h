@@ -210,11 +210,6 @@ cudaError_t groups_prepare_ext_sort(uint64_t* keys, uint32_t* vals, const GroupI
 cudaError_t groups_ext_presorted(const uint32_t* vals, GroupInfo* groups, const uint32_t* ext_list,
                                  const uint32_t* counts, uint32_t* out, uint32_t* out_count,
                                  cudaStream_t s);
-// Split (key, val) into CUR / EXT arrays for the DP (ext_sorted == 1 groups
-// hold key = ext pos, val = cur pos after their re-sort).
-cudaError_t groups_split(const uint64_t* keys, const uint32_t* vals, const GroupInfo* groups,
-                         const uint32_t* dp_list, const uint32_t* counts, int32_t* cur,
-                         int32_t* ext, cudaStream_t s);
 // Highest score of a group, its first element and how many elements have it.
 struct GroupTop {
   int32_t score;
@@ -223,10 +218,12 @@ struct GroupTop {
   uint32_t pad;
 };
 
+// keys / vals: the sorted matches (key = (ext id << 32) | cur pos, val = ext
+// pos; groups with ext_sorted == 1 hold key = ext pos, val = cur pos).
 // work: one word of device scratch (the group counter of the launch); top
 // (indexed by group) receives each group's GroupTop; pmc: chain_dp_pmc_words
 // words of scratch (running score maxima per 32 elements).
-cudaError_t chain_dp(const int32_t* cur, const int32_t* ext, int32_t* score, int32_t* bt,
+cudaError_t chain_dp(const uint64_t* keys, const uint32_t* vals, int32_t* score, int32_t* bt,
                      const GroupInfo* groups, const uint32_t* dp_list, const uint32_t* counts,
                      const ChainParams& p, GroupTop* top, int32_t* pmc, uint32_t* work,
                      int num_sms, cudaStream_t s);
@@ -250,7 +247,7 @@ cudaError_t chain_prepare_order(const int32_t* score, uint64_t* keys, uint32_t* 
 // among equal scores is not finished but appended to redo_list, to be run
 // again with Flye's order; larger groups, and every group when top is null,
 // follow the score order in `order` (local indices, libstdc++ order).
-cudaError_t chain_backtrack(const int32_t* cur, const int32_t* ext, const int32_t* score,
+cudaError_t chain_backtrack(const uint64_t* keys, const uint32_t* vals, const int32_t* score,
                             int32_t* bt, const uint32_t* order, const GroupInfo* groups,
                             const uint32_t* list, const uint32_t* list_count,
                             const GroupTop* top, uint32_t* redo_list, uint32_t* redo_count,
