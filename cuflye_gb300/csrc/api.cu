@@ -443,12 +443,19 @@ struct PassState {
   uint64_t* f_off = nullptr;  // nq + 1 filtered offsets
   QueryInfo* qinfo = nullptr;
   uint32_t* q_tie = nullptr;  // per query: its KmerMatch keys may repeat
+  bool presorted = false;     // distinct-key queries written in KmerMatch order
 };
+
+// Passes of at least this many queries write distinct-key queries directly
+// in KmerMatch order (one block per query); smaller ones, the one-read plain
+// path above all, spread each query's sort over many blocks instead.
+constexpr uint32_t kPresortMinQueries = 64;
 
 // Buffers sized by the hit count of a pass (reused by the next pass).
 const char* const kPerHitBuffers[] = {"h_keys",  "h_vals", "h_kmers", "s_l",     "s_r",
                                       "g_flags", "g_id",   "c_cur",   "c_ext",   "c_score",
-                                      "c_bt",    "a_cand", "m_tiles", "m_counts"};
+                                      "c_bt",    "a_cand", "m_tiles", "m_counts", "c_pmc",
+                                      "o_maps"};
 
 // The memory budget, or the device's memory less a 4 GiB margin when unbounded.
 uint64_t effective_budget(cuflye_ctx* c) {
@@ -566,8 +573,25 @@ bool run_hits(cuflye_ctx* c, const Queries& Q, size_t q0, size_t q1, bool want_k
   ps.vals = buf<uint32_t>(c, "h_vals", ps.nhits);
   ps.kmers = want_kmers ? buf<uint64_t>(c, "h_kmers", ps.nhits) : nullptr;
   ps.fpos = buf<int32_t>(c, "h_fpos", ps.nfilt);
-  CUFLYE_CHECK(hits_emit(c->idx, qb, hit_off, filt_off, wmeta, wflags, ps.keys, ps.vals, ps.kmers,
-                         ps.fpos, st));
+  if (want_kmers) {
+    // candidate records: every hit in generation order
+    CUFLYE_CHECK(hits_emit(c->idx, qb, hit_off, filt_off, wmeta, wflags, ps.keys, ps.vals,
+                           ps.kmers, ps.fpos, nullptr, st));
+  } else if (ps.nq >= kPresortMinQueries) {
+    // for chaining, a batch of many queries: queries whose KmerMatch keys are
+    // distinct straight in sorted order (one block per query), the others
+    // (q_tie = 1) in generation order for the emulated sort
+    ps.presorted = true;
+    CUFLYE_CHECK(hits_emit_sorted(c->idx, qb, hit_off, wmeta, wflags, ps.q_tie, ps.keys, ps.vals,
+                                  buf<uint32_t>(c, "c_work", 1), c->num_sms, st));
+    CUFLYE_CHECK(hits_emit(c->idx, qb, hit_off, filt_off, wmeta, wflags, ps.keys, ps.vals, nullptr,
+                           ps.fpos, ps.q_tie, st));
+  } else {
+    // smaller batches: generation order, sorted by radix tiles spread over
+    // the device
+    CUFLYE_CHECK(hits_emit(c->idx, qb, hit_off, filt_off, wmeta, wflags, ps.keys, ps.vals, nullptr,
+                           ps.fpos, nullptr, st));
+  }
   return true;
 }
 
@@ -624,7 +648,7 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
   int id_bits = 0;
   while (id_bits < 32 && ((2ull * c->idx.nslots - 1) >> id_bits) != 0) ++id_bits;
   CUFLYE_CHECK(cudaEventRecord(c->ev[1], st));
-  CUFLYE_CHECK(match_plan(ps.q_off, ps.q_tie, nq, ntiles, qb, qe, ecount, st));
+  CUFLYE_CHECK(match_plan(ps.q_off, ps.q_tie, nq, ps.presorted, ntiles, qb, qe, ecount, st));
   CUFLYE_CHECK(sort_stats_add(sstats, 0, 1, nullptr, nq, ecount, st));
   const uint64_t NT = scan_u32(c, ntiles, tile_off, nq, "m_scan");
   MatchTile* tiles = buf<MatchTile>(c, "m_tiles", NT);
@@ -675,20 +699,14 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
   CUFLYE_CHECK(chain_dp(ps.keys, ps.vals, score, bt, groups, dp_list, gcounts, cp, top, pmc, work,
                         c->num_sms, st));
   CUFLYE_CHECK(cudaEventRecord(c->ev[7], st));
-  // 5. score order (indices by score descending, libstdc++ order) only for
-  // groups above the backtrack's shared-memory maps; the backtrack picks the
-  // starts of the others itself.  The (key, index) pairs of the order live in
-  // the group-building buffers, free by now.
+  // 5. the backtrack picks its chain starts by score itself; groups where
+  // Flye's order among equal scores could matter get that order (libstdc++
+  // order of indices by score descending) and run again.  The (key, index)
+  // pairs of the order live in the group-building buffers, free by now.
   uint64_t* okeys = gid;
   uint32_t* order = gflags;
-  uint32_t* big = buf<uint32_t>(c, "o_big", G);
-  uint32_t* big_count = buf<uint32_t>(c, "o_bigcount", 1);
-  CUFLYE_CHECK(list_large_groups(groups, dp_list, gcounts + 1, G32, kBacktrackCap, big, big_count,
-                                 st));
-  CUFLYE_CHECK(sort_stats_add(sstats, 4, 5, gcounts + 1, 0, big_count, st));
-  CUFLYE_CHECK(chain_prepare_order(score, okeys, order, groups, big, big_count, sb, se, st));
-  CUFLYE_CHECK(segmented_std_sort(okeys, order, lscr, rscr, sb, se, G32, big_count, glists,
-                                  scounts, c->num_sms, st, sort_tasks(c, "s", H, G32)));
+  const uint64_t gmap_words = chain_dp_pmc_words(H, G);
+  uint32_t* gmaps = buf<uint32_t>(c, "o_maps", 3 * gmap_words);
   // 6. backtrack, proposals, primary selection; the row pool is sized by the
   // groups that survived the prefilter
   const uint32_t survivors = read_scalar(c, gcounts + 1);
@@ -704,9 +722,9 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
   const int64_t* slot_signed = buf<int64_t>(c, "ix_slot_signed", 1);
   CUFLYE_CHECK(chain_backtrack(ps.keys, ps.vals, score, bt, order, groups, dp_list, gcounts + 1, top,
                                redo, redo_count, ps.qinfo, ps.f_off, ps.fpos, slot_signed, c->logt,
-                               cp, pool, pool_cap, pool_count, group_rows, c->status, G32, work,
-                               st));
-  CUFLYE_CHECK(sort_stats_add(sstats, -1, 6, nullptr, 0, redo_count, st));
+                               cp, pool, pool_cap, pool_count, group_rows, c->status, G32, gmaps,
+                               gmap_words, work, st));
+  CUFLYE_CHECK(sort_stats_add(sstats, 4, 6, gcounts + 1, 0, redo_count, st));
   // groups whose result could depend on the order among equal scores: again
   // with the libstdc++ order
   CUFLYE_CHECK(chain_prepare_order(score, okeys, order, groups, redo, redo_count, sb, se, st));
@@ -714,8 +732,8 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
                                   scounts, c->num_sms, st, sort_tasks(c, "s", H, G32)));
   CUFLYE_CHECK(chain_backtrack(ps.keys, ps.vals, score, bt, order, groups, redo, redo_count, nullptr,
                                nullptr, nullptr, ps.qinfo, ps.f_off, ps.fpos, slot_signed, c->logt,
-                               cp, pool, pool_cap, pool_count, group_rows, c->status, G32, work,
-                               st));
+                               cp, pool, pool_cap, pool_count, group_rows, c->status, G32, gmaps,
+                               gmap_words, work, st));
   check_device_status(c);
   // 7. max_overlaps + compaction in group order
   uint64_t* qg = buf<uint64_t>(c, "o_qg", nq + 1);

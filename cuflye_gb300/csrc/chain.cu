@@ -463,24 +463,17 @@ __device__ __forceinline__ uint32_t lower_bound_i32(const int32_t* a, uint32_t n
   return lo;
 }
 
-// One warp per group.  The group's backtrack array is staged in shared memory
-// as 16-bit indices (0xFFFF = -1) when it fits kBtCap; the warp tests 32
-// score-ordered chain starts per step with a ballot, and lane 0 walks each
-// live chain (Flye's serial order) and builds its proposal.  After a walk the
-// remaining starts of the step are tested again, since the walk may have
-// consumed them.
 // Flye walks chains in score order: from each start whose backtrack entry is
 // still set it follows the links, clearing every entry it visits, and the
 // chain ends at the first node whose entry is -1 (never linked, or cleared
-// by an earlier walk).  For groups of up to kBtCap elements a warp keeps
-// three bitmaps in shared memory in place of the table: linked (entry != -1
-// at the start), step (entry == i - 1) and cleared.  A walk crosses a run of
-// step links in one 32-word search per 1,024 nodes (the next node that is not
-// a step or is cleared) and clears the run word by word; only links that are
-// not steps are read from the table, which stays unchanged.  The warp counts
-// linked nodes not yet cleared and ends the score-order loop when none is
-// left: no later start could begin a chain.  Larger groups walk the table in
-// global memory with one lane.
+// by an earlier walk).  One warp per group keeps three bitmaps in place of
+// the table: linked (entry != -1 at the start), step (entry == i - 1) and
+// cleared; in shared memory for groups of up to kBtCap elements, else in
+// device memory.  A walk crosses a run of step links in one 32-word search
+// per 1,024 nodes (the next node that is not a step or is cleared) and
+// clears the run word by word; only links that are not steps are read from
+// the table, which stays unchanged.  The warp counts linked nodes not yet
+// cleared and stops when none is left: no later start could begin a chain.
 
 constexpr uint32_t kBtCap = kBacktrackCap;
 constexpr uint32_t kBtWords = kBtCap / 32;
@@ -506,7 +499,8 @@ __device__ __forceinline__ uint32_t warp_sum_u32(uint32_t v) {
 // Walk from s0 (linked, not cleared) with the whole warp: first node and
 // chain length as Flye's walk counts them; visited nodes become cleared and
 // `remaining` drops by the linked ones among them.
-__device__ void walk_maps(BtMaps& m, const int32_t* __restrict__ btg, int32_t s0, int32_t& first,
+__device__ void walk_maps(const uint32_t* link, const uint32_t* step, uint32_t* done,
+                          const int32_t* __restrict__ btg, int32_t s0, int32_t& first,
                           int32_t& clen, uint32_t& remaining) {
   const int lane = threadIdx.x & 31;
   int32_t pos = s0;
@@ -518,7 +512,7 @@ __device__ void walk_maps(BtMaps& m, const int32_t* __restrict__ btg, int32_t s0
       const int32_t w = w0 - lane;
       uint32_t bits = 0;
       if (w >= 0) {
-        bits = ~m.step[w] | m.done[w];
+        bits = ~step[w] | done[w];
         if (w == (pos >> 5)) bits &= bits_upto(pos);
       }
       const unsigned bal = __ballot_sync(0xffffffffu, bits != 0);
@@ -528,15 +522,15 @@ __device__ void walk_maps(BtMaps& m, const int32_t* __restrict__ btg, int32_t s0
         z = (w0 - l) * 32 + 31 - __clz(wb);
       }
     }
-    const bool stop = ((m.done[z >> 5] >> (z & 31)) & 1u) || !((m.link[z >> 5] >> (z & 31)) & 1u);
+    const bool stop = ((done[z >> 5] >> (z & 31)) & 1u) || !((link[z >> 5] >> (z & 31)) & 1u);
     __syncwarp();
     uint32_t newly = 0;
     for (int32_t w = (z >> 5) + lane; w <= (pos >> 5); w += 32) {
       uint32_t mask = 0xffffffffu;
       if (w == (z >> 5)) mask &= 0xffffffffu << (z & 31);
       if (w == (pos >> 5)) mask &= bits_upto(pos);
-      newly += __popc(m.link[w] & ~m.done[w] & mask);
-      m.done[w] |= mask;
+      newly += __popc(link[w] & ~done[w] & mask);
+      done[w] |= mask;
     }
     remaining -= warp_sum_u32(newly);
     clen += pos - z + 1;
@@ -603,7 +597,8 @@ __global__ void __launch_bounds__(kBtWarps * 32) backtrack_kernel(
     const uint64_t* __restrict__ f_off, const int32_t* __restrict__ fpos,
     const int64_t* __restrict__ slot_signed, LogfTable logt, ChainParams p,
     OverlapRow* __restrict__ pool, uint64_t pool_cap, uint32_t* __restrict__ pool_count,
-    uint32_t* __restrict__ group_rows, DeviceStatus* st, uint32_t* __restrict__ work) {
+    uint32_t* __restrict__ group_rows, DeviceStatus* st, uint32_t* gmaps, uint64_t gmap_words,
+    uint32_t* __restrict__ work) {
   extern __shared__ __align__(16) unsigned char bt_raw[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   BtMaps& m = reinterpret_cast<BtMaps*>(bt_raw)[wib];
@@ -618,28 +613,34 @@ __global__ void __launch_bounds__(kBtWarps * 32) backtrack_kernel(
                                              : slot_signed[g.ext_di >> 1];
   const int32_t* fq = fpos + f_off[g.query];
   const uint32_t nf = static_cast<uint32_t>(f_off[g.query + 1] - f_off[g.query]);
-  const bool mapped = g.n <= kBtCap;
-  // mapped groups of the first run pick their starts themselves; the others
-  // follow `order` (Flye's order)
-  const bool pick = mapped && top != nullptr;
+  // the maps: shared memory up to kBtCap nodes, else device memory at the
+  // group's own word range
+  uint32_t *lk = m.link, *sp = m.step, *dn = m.done;
+  if (g.n > kBtCap) {
+    const uint64_t pb = (b >> 5) + gidx;
+    lk = gmaps + pb;
+    sp = gmaps + gmap_words + pb;
+    dn = gmaps + 2 * gmap_words + pb;
+  }
+  // the first run picks its starts itself; the second follows `order`
+  // (Flye's order)
+  const bool pick = top != nullptr;
   bool ambiguous = false;
   uint32_t remaining = 0;
-  if (mapped) {
-    const uint32_t nw = (g.n + 31) / 32;
-    for (uint32_t w = 0; w < nw; ++w) {
-      const uint32_t j = w * 32 + lane;
-      const int32_t v = j < g.n ? bt[b + j] : -1;
-      const unsigned lk = __ballot_sync(0xffffffffu, v != -1);
-      const unsigned sp = __ballot_sync(0xffffffffu, j >= 1 && v == static_cast<int32_t>(j) - 1);
-      if (lane == 0) {
-        m.link[w] = lk;
-        m.step[w] = sp;
-        m.done[w] = 0;
-      }
-      remaining += __popc(lk);
+  const uint32_t nw = (g.n + 31) / 32;
+  for (uint32_t w = 0; w < nw; ++w) {
+    const uint32_t j = w * 32 + lane;
+    const int32_t v = j < g.n ? bt[b + j] : -1;
+    const unsigned lkw = __ballot_sync(0xffffffffu, v != -1);
+    const unsigned spw = __ballot_sync(0xffffffffu, j >= 1 && v == static_cast<int32_t>(j) - 1);
+    if (lane == 0) {
+      lk[w] = lkw;
+      sp[w] = spw;
+      dn[w] = 0;
     }
-    __syncwarp();
+    remaining += __popc(lkw);
   }
+  __syncwarp();
   Prop props[kMaxProposals];
   int np = 0;
   bool overflow = false;
@@ -657,9 +658,8 @@ __global__ void __launch_bounds__(kBtWarps * 32) backtrack_kernel(
     } else {
       int32_t bs = INT_MIN;
       uint32_t bi = 0xffffffffu, bc = 0;
-      const uint32_t nw = (g.n + 31) / 32;
       for (uint32_t w = 0; w < nw; ++w) {
-        const uint32_t lv = m.link[w] & ~m.done[w];
+        const uint32_t lv = lk[w] & ~dn[w];
         if (!lv) continue;
         if ((lv >> lane) & 1u) {
           const int32_t sv = score[b + w * 32 + lane];
@@ -689,46 +689,33 @@ __global__ void __launch_bounds__(kBtWarps * 32) backtrack_kernel(
     }
     const uint32_t s0 = mi;
     int32_t first = 0, clen = 0;
-    walk_maps(m, bt + b, static_cast<int32_t>(s0), first, clen, remaining);
+    walk_maps(lk, sp, dn, bt + b, static_cast<int32_t>(s0), first, clen, remaining);
     if (lane == 0 && !overflow)
       add_proposal(keys, vals, score, b, s0, first, clen, qi, ext_signed, g, fq, nf, logt, p, st,
                    gidx, props, np, overflow);
     __syncwarp();
   }
-  for (uint32_t o0 = 0; !pick && o0 < g.n && !(mapped && remaining == 0); o0 += 32) {
+  for (uint32_t o0 = 0; !pick && o0 < g.n && remaining > 0; o0 += 32) {
     const uint32_t oi = o0 + lane;
     const bool valid = oi < g.n;
     const uint32_t start = valid ? order[b + oi] : 0;
     unsigned mask = __ballot_sync(
-        0xffffffffu, valid && (mapped ? (((m.link[start >> 5] & ~m.done[start >> 5]) >>
-                                          (start & 31)) & 1u) != 0
-                                      : bt[b + start] != -1));
+        0xffffffffu,
+        valid && (((lk[start >> 5] & ~dn[start >> 5]) >> (start & 31)) & 1u) != 0);
     while (mask) {
       const int j = __ffs(mask) - 1;
       const uint32_t s0 = __shfl_sync(0xffffffffu, start, j);
       int32_t first = 0, clen = 0;
-      if (mapped) {
-        walk_maps(m, bt + b, static_cast<int32_t>(s0), first, clen, remaining);
-      } else if (lane == 0 && !overflow) {
-        int32_t pos = static_cast<int32_t>(s0);
-        while (pos != -1) {
-          first = pos;
-          ++clen;
-          const int32_t nx = bt[b + pos];
-          bt[b + pos] = -1;
-          pos = nx;
-        }
-      }
+      walk_maps(lk, sp, dn, bt + b, static_cast<int32_t>(s0), first, clen, remaining);
       if (lane == 0 && !overflow)
         add_proposal(keys, vals, score, b, s0, first, clen, qi, ext_signed, g, fq, nf, logt, p, st,
                      gidx, props, np, overflow);
       __syncwarp();
-      if (mapped && remaining == 0) break;
+      if (remaining == 0) break;
       mask = __ballot_sync(
           0xffffffffu,
           valid && lane > j &&
-              (mapped ? (((m.link[start >> 5] & ~m.done[start >> 5]) >> (start & 31)) & 1u) != 0
-                      : bt[b + start] != -1));
+              (((lk[start >> 5] & ~dn[start >> 5]) >> (start & 31)) & 1u) != 0);
     }
   }
   __syncwarp();
@@ -910,33 +897,6 @@ cudaError_t chain_dp(const uint64_t* keys, const uint32_t* vals, int32_t* score,
   return cudaGetLastError();
 }
 
-namespace {
-
-__global__ void large_groups_kernel(const GroupInfo* __restrict__ groups,
-                                    const uint32_t* __restrict__ list,
-                                    const uint32_t* __restrict__ list_count, uint32_t min_n,
-                                    uint32_t* __restrict__ out, uint32_t* __restrict__ out_count) {
-  const uint32_t cnt = *list_count;
-  for (uint32_t li = blockIdx.x * blockDim.x + threadIdx.x; li < cnt;
-       li += gridDim.x * blockDim.x) {
-    const uint32_t g = list[li];
-    if (groups[g].n > min_n) out[atomicAdd(out_count, 1u)] = g;
-  }
-}
-
-}  // namespace
-
-cudaError_t list_large_groups(const GroupInfo* groups, const uint32_t* list,
-                              const uint32_t* list_count, uint32_t max_groups, uint32_t min_n,
-                              uint32_t* out, uint32_t* out_count, cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(out_count, 0, 4, s);
-  if (e != cudaSuccess || max_groups == 0) return e;
-  count_launch();
-  large_groups_kernel<<<grid(max_groups, 256) < 1024 ? grid(max_groups, 256) : 1024, 256, 0, s>>>(
-      groups, list, list_count, min_n, out, out_count);
-  return cudaGetLastError();
-}
-
 cudaError_t chain_prepare_order(const int32_t* score, uint64_t* keys, uint32_t* vals,
                                 const GroupInfo* groups, const uint32_t* list,
                                 const uint32_t* list_count, uint64_t* seg_begin,
@@ -955,7 +915,8 @@ cudaError_t chain_backtrack(const uint64_t* keys, const uint32_t* vals, const in
                             const int64_t* slot_signed, const LogfTable& logt,
                             const ChainParams& p, OverlapRow* pool, uint64_t pool_cap,
                             uint32_t* pool_count, uint32_t* group_rows, DeviceStatus* st,
-                            uint32_t max_groups, uint32_t* work, cudaStream_t s) {
+                            uint32_t max_groups, uint32_t* gmaps, uint64_t gmap_words,
+                            uint32_t* work, cudaStream_t s) {
   if (max_groups == 0) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(work, 0, 4, s);
   if (e != cudaSuccess) return e;
@@ -970,7 +931,7 @@ cudaError_t chain_backtrack(const uint64_t* keys, const uint32_t* vals, const in
   backtrack_kernel<<<sms * 4, kBtWarps * 32, smem, s>>>(
       keys, vals, score, bt, order, groups, list, list_count, top, redo_list, redo_count,
       qinfo, f_off, fpos, slot_signed, logt,
-      p, pool, pool_cap, pool_count, group_rows, st, work);
+      p, pool, pool_cap, pool_count, group_rows, st, gmaps, gmap_words, work);
   return cudaGetLastError();
 }
 

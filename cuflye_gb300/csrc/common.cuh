@@ -56,7 +56,8 @@ __host__ __device__ __forceinline__ uint64_t mix64(uint64_t x) {
 }
 
 // Open-addressing table entry: 16 bytes, one sector-aligned 128-bit load.
-// meta: bits 0-39 bucket offset, 40-62 bucket count, 63 repetitive.
+// meta: bits 0-39 bucket offset, 40-61 bucket count, 62 repeated stored id,
+// 63 repetitive.
 struct alignas(16) TableEntry {
   uint64_t key;
   uint64_t meta;
@@ -69,6 +70,11 @@ constexpr uint64_t kRepetitiveBit = 1ULL << 63;
 // that looks it up yields two hits on one target, i.e. two equal
 // (ext id, cur pos) KmerMatch keys.
 constexpr uint64_t kDupIdsBit = 1ULL << 62;
+
+// Per-window flags of hit counting.
+constexpr uint8_t kWinRev = 1;       // the window k-mer is not in standard form
+constexpr uint8_t kWinFiltered = 2;  // repetitive: a filtered position
+constexpr uint8_t kWinTrivial = 4;   // the bucket held the window's own position
 
 __device__ __forceinline__ uint64_t table_probe(const TableEntry* __restrict__ table,
                                                 uint64_t mask, uint64_t key, bool* found) {

@@ -12,10 +12,12 @@
 //   are generated window by window, so the hits on one ext id already come
 //   in cur-pos order.  Two hits share (ext id, cur pos) only when one window's
 //   bucket lists a target id twice; the index marks such buckets (kDupIdsBit)
-//   and hit counting flags the queries that look one up.  An unflagged
-//   query's keys are distinct, and its sort is a stable sort by ext id: a
-//   least-significant-digit radix sort over the ext id bits, 8 bits per pass,
-//   in tiles of kMatchTile hits that never straddle two queries.
+//   and hit counting flags the queries that look one up (q_tie = 1).  An
+//   unflagged query's keys are distinct, and its sort is a stable sort by ext
+//   id.  Most unflagged queries are written in that order directly
+//   (bucket.cu); the rest (q_tie = 2) take a least-significant-digit radix
+//   sort over the ext id bits, 8 bits per pass, in tiles of kMatchTile hits
+//   that never straddle two queries.
 // * Ext-pos re-sort of ext-sorted groups of at most kGroupCap elements
 //   (tools/replay_read_to_graph_source_pack.py:396-397) that are not already
 //   in strict ext-pos order.  One block sorts the group in shared memory
@@ -77,18 +79,18 @@ struct PairsSoA {
 };
 
 __global__ void match_plan_kernel(const uint64_t* __restrict__ q_off,
-                                  const uint32_t* __restrict__ q_tie, uint32_t nq,
+                                  const uint32_t* __restrict__ q_tie, uint32_t nq, bool presorted,
                                   uint32_t* __restrict__ ntiles, uint64_t* __restrict__ emu_begin,
                                   uint64_t* __restrict__ emu_end, uint32_t* __restrict__ emu_count) {
   for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
     const uint64_t b = q_off[q], e = q_off[q + 1];
     uint32_t t = 0;
     if (e - b > 1) {
-      if (q_tie[q]) {
+      if (q_tie[q] == 1) {
         const uint32_t s = atomicAdd(emu_count, 1u);
         emu_begin[s] = b;
         emu_end[s] = e;
-      } else {
+      } else if (q_tie[q] == 2 || !presorted) {
         t = static_cast<uint32_t>((e - b + kMatchTile - 1) / kMatchTile);
       }
     }
@@ -467,14 +469,14 @@ void allow_smem(T* kernel, size_t bytes) {
 
 }  // namespace
 
-cudaError_t match_plan(const uint64_t* q_off, const uint32_t* q_tie, uint32_t nq, uint32_t* ntiles,
-                       uint64_t* emu_begin, uint64_t* emu_end, uint32_t* emu_count,
-                       cudaStream_t s) {
+cudaError_t match_plan(const uint64_t* q_off, const uint32_t* q_tie, uint32_t nq, bool presorted,
+                       uint32_t* ntiles, uint64_t* emu_begin, uint64_t* emu_end,
+                       uint32_t* emu_count, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(emu_count, 0, 4, s);
   if (e != cudaSuccess || nq == 0) return e;
   count_launch();
-  match_plan_kernel<<<(nq + 255) / 256, 256, 0, s>>>(q_off, q_tie, nq, ntiles, emu_begin, emu_end,
-                                                     emu_count);
+  match_plan_kernel<<<(nq + 255) / 256, 256, 0, s>>>(q_off, q_tie, nq, presorted, ntiles,
+                                                     emu_begin, emu_end, emu_count);
   return cudaGetLastError();
 }
 

@@ -18,9 +18,6 @@
 namespace cuflye {
 namespace {
 
-constexpr uint8_t kFlagRev = 1;
-constexpr uint8_t kFlagFiltered = 2;
-constexpr uint8_t kFlagTrivial = 4;
 
 __device__ __forceinline__ uint32_t query_of(const uint64_t* __restrict__ win_off, uint32_t nq,
                                              uint64_t w) {
@@ -62,9 +59,9 @@ __global__ void count_kernel(DeviceIndex idx, QueryBatch q, uint32_t* __restrict
   bool found;
   const uint64_t meta = table_probe(idx.table, idx.mask, km.key, &found);
   uint32_t c = 0;
-  uint8_t fl = km.rev ? kFlagRev : 0;
+  uint8_t fl = km.rev ? kWinRev : 0;
   if (found && (meta & kRepetitiveBit)) {
-    fl |= kFlagFiltered;
+    fl |= kWinFiltered;
   } else if (found) {
     c = static_cast<uint32_t>((meta >> 40) & ((1ULL << kCountBits) - 1));
     if ((meta & kDupIdsBit) && q_tie[qi] == 0) atomicOr(q_tie + qi, 1u);
@@ -100,12 +97,12 @@ __global__ void count_kernel(DeviceIndex idx, QueryBatch q, uint32_t* __restrict
       }
       if (self_hits) {
         c -= self_hits;
-        fl |= kFlagTrivial;
+        fl |= kWinTrivial;
       }
     }
   }
   cnt[w] = c;
-  filt[w] = (fl & kFlagFiltered) ? 1u : 0u;
+  filt[w] = (fl & kWinFiltered) ? 1u : 0u;
   wmeta[w] = meta;
   wflags[w] = fl;
 }
@@ -118,7 +115,7 @@ __global__ void emit_kernel(DeviceIndex idx, QueryBatch q, const uint64_t* __res
                             const uint64_t* __restrict__ wmeta,
                             const uint8_t* __restrict__ wflags, uint64_t* __restrict__ keys,
                             uint32_t* __restrict__ vals, uint64_t* __restrict__ kmers,
-                            int32_t* __restrict__ fpos) {
+                            int32_t* __restrict__ fpos, const uint32_t* __restrict__ only_tie) {
   const int lane = threadIdx.x & 31;
   const uint32_t lt = (1u << lane) - 1u;
   const uint64_t w = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -129,9 +126,9 @@ __global__ void emit_kernel(DeviceIndex idx, QueryBatch q, const uint64_t* __res
     fl = wflags[w];
     qi = query_of(q.win_off, q.nq, w);
     p = static_cast<uint32_t>(w - q.win_off[qi]);
-    if (fl & kFlagFiltered) {
+    if (fl & kWinFiltered) {
       fpos[filt_off[w]] = static_cast<int32_t>(p);
-    } else {
+    } else if (!only_tie || only_tie[qi] == 1) {
       o = hit_off[w];
       end = hit_off[w + 1];
       meta = wmeta[w];
@@ -148,7 +145,7 @@ __global__ void emit_kernel(DeviceIndex idx, QueryBatch q, const uint64_t* __res
     const uint32_t wf = __shfl_sync(0xffffffffu, static_cast<uint32_t>(fl), src);
     const uint64_t off = wm & kOffsetMask;
     const uint32_t c = static_cast<uint32_t>((wm >> 40) & ((1ULL << kCountBits) - 1));
-    const bool flip = idx.transform && (wf & kFlagRev);
+    const bool flip = idx.transform && (wf & kWinRev);
     const int32_t qdi = q.qdi[wq];
     uint64_t x = 0;
     if (kmers) x = kmer_at(q.words, q.base_off[wq] + wp, idx.k);
@@ -203,11 +200,11 @@ cudaError_t hits_count(const DeviceIndex& idx, const QueryBatch& q, uint32_t* cn
 cudaError_t hits_emit(const DeviceIndex& idx, const QueryBatch& q, const uint64_t* hit_off,
                       const uint64_t* filt_off, const uint64_t* wmeta, const uint8_t* wflags,
                       uint64_t* keys, uint32_t* vals, uint64_t* kmers, int32_t* fpos,
-                      cudaStream_t s) {
+                      const uint32_t* only_tie, cudaStream_t s) {
   if (q.nwin == 0) return cudaSuccess;
   count_launch();
   emit_kernel<<<static_cast<unsigned>((q.nwin + 255) / 256), 256, 0, s>>>(
-      idx, q, hit_off, filt_off, wmeta, wflags, keys, vals, kmers, fpos);
+      idx, q, hit_off, filt_off, wmeta, wflags, keys, vals, kmers, fpos, only_tie);
   return cudaGetLastError();
 }
 

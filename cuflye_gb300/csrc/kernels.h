@@ -104,11 +104,20 @@ struct QueryBatch {
 cudaError_t hits_count(const DeviceIndex& idx, const QueryBatch& q, uint32_t* cnt,
                        uint32_t* filt, uint64_t* wmeta, uint8_t* wflags, uint32_t* q_tie,
                        cudaStream_t s);
-// keys[j] = (ext dense id << 32) | cur pos, vals[j] = ext pos, kmers (optional).
+// keys[j] = (ext dense id << 32) | cur pos, vals[j] = ext pos, kmers
+// (optional), in generation order; filtered positions into fpos.  With
+// only_tie, hits are written only for queries with only_tie[q] == 1.
 cudaError_t hits_emit(const DeviceIndex& idx, const QueryBatch& q, const uint64_t* hit_off,
                       const uint64_t* filt_off, const uint64_t* wmeta, const uint8_t* wflags,
                       uint64_t* keys, uint32_t* vals, uint64_t* kmers, int32_t* fpos,
-                      cudaStream_t s);
+                      const uint32_t* only_tie, cudaStream_t s);
+// Hits of every query with q_tie[q] == 0 written directly in KmerMatch order
+// ((ext id, cur pos) ascending); a query with too many distinct ext ids is
+// written in generation order instead and gets q_tie[q] = 2 (bucket.cu).
+cudaError_t hits_emit_sorted(const DeviceIndex& idx, const QueryBatch& q, const uint64_t* hit_off,
+                             const uint64_t* wmeta, const uint8_t* wflags, uint32_t* q_tie,
+                             uint64_t* keys, uint32_t* vals, uint32_t* work, int num_sms,
+                             cudaStream_t s);
 // Gather per-query segment bounds from window-level offsets.
 cudaError_t gather_query_offsets(const uint64_t* win_off, const uint64_t* wl_off, uint32_t nq,
                                  uint64_t* q_off, cudaStream_t s);
@@ -164,11 +173,13 @@ struct MatchTile {
   uint32_t query;
 };
 
-// Per query: flagged (q_tie) queries with two or more hits are listed for the
-// emulated sort; the others get ntiles[q] radix tiles.
-cudaError_t match_plan(const uint64_t* q_off, const uint32_t* q_tie, uint32_t nq, uint32_t* ntiles,
-                       uint64_t* emu_begin, uint64_t* emu_end, uint32_t* emu_count,
-                       cudaStream_t s);
+// Per query with two or more hits: q_tie = 1 (keys may repeat) is listed for
+// the emulated sort, q_tie = 2 (in generation order, keys distinct) gets
+// ntiles[q] radix tiles; q_tie = 0 queries are sorted already when
+// `presorted` (hits_emit_sorted ran), else they get radix tiles too.
+cudaError_t match_plan(const uint64_t* q_off, const uint32_t* q_tie, uint32_t nq, bool presorted,
+                       uint32_t* ntiles, uint64_t* emu_begin, uint64_t* emu_end,
+                       uint32_t* emu_count, cudaStream_t s);
 // tile_off: exclusive scan of ntiles.
 cudaError_t match_tiles(const uint64_t* q_off, const uint32_t* ntiles, const uint64_t* tile_off,
                         uint32_t nq, MatchTile* tiles, cudaStream_t s);
@@ -230,11 +241,6 @@ cudaError_t chain_dp(const uint64_t* keys, const uint32_t* vals, int32_t* score,
 inline uint64_t chain_dp_pmc_words(uint64_t nhits, uint64_t ngroups) {
   return (nhits >> 5) + ngroups + 2;
 }
-// Groups of list[0 .. *list_count) with more than min_n elements, appended
-// to out / *out_count (zeroed here).
-cudaError_t list_large_groups(const GroupInfo* groups, const uint32_t* list,
-                              const uint32_t* list_count, uint32_t max_groups, uint32_t min_n,
-                              uint32_t* out, uint32_t* out_count, cudaStream_t s);
 // Score-order sort inputs of the groups list[0 .. *list_count): key =
 // INT32_MAX - score, val = local index, and their segment bounds.
 cudaError_t chain_prepare_order(const int32_t* score, uint64_t* keys, uint32_t* vals,
@@ -242,11 +248,13 @@ cudaError_t chain_prepare_order(const int32_t* score, uint64_t* keys, uint32_t* 
                                 const uint32_t* list_count, uint64_t* seg_begin,
                                 uint64_t* seg_end, cudaStream_t s);
 // Backtrack of the groups list[0 .. *list_count).  With `top` (the DP's
-// GroupTop per group), groups of up to 16,384 elements pick their starts in
-// score order themselves, and a group whose result could depend on the order
-// among equal scores is not finished but appended to redo_list, to be run
-// again with Flye's order; larger groups, and every group when top is null,
-// follow the score order in `order` (local indices, libstdc++ order).
+// GroupTop per group) every group picks its starts in score order itself,
+// and a group whose result could depend on the order among equal scores is
+// not finished but appended to redo_list, to be run again with Flye's order;
+// with top null every group follows the score order in `order` (local
+// indices, libstdc++ order).  gmaps: 3 * gmap_words words of device scratch
+// (the walk bitmaps of groups over 16,384 elements), gmap_words =
+// chain_dp_pmc_words(nhits, ngroups).
 cudaError_t chain_backtrack(const uint64_t* keys, const uint32_t* vals, const int32_t* score,
                             int32_t* bt, const uint32_t* order, const GroupInfo* groups,
                             const uint32_t* list, const uint32_t* list_count,
@@ -255,7 +263,8 @@ cudaError_t chain_backtrack(const uint64_t* keys, const uint32_t* vals, const in
                             const int64_t* slot_signed, const LogfTable& logt,
                             const ChainParams& p, OverlapRow* pool, uint64_t pool_cap,
                             uint32_t* pool_count, uint32_t* group_rows, DeviceStatus* st,
-                            uint32_t max_groups, uint32_t* work, cudaStream_t s);
+                            uint32_t max_groups, uint32_t* gmaps, uint64_t gmap_words,
+                            uint32_t* work, cudaStream_t s);
 // max_overlaps cutoff and group-order compaction of the pooled rows.
 cudaError_t rows_limit(const uint32_t* group_rows, const uint64_t* q_group_off, uint32_t nq,
                        int32_t max_overlaps, uint32_t* kept_rows, cudaStream_t s);

@@ -273,10 +273,10 @@ cuflye_status cuflye_last_timing(const cuflye_ctx* ctx, double* stage_ms, uint64
  * std::sort; the others take the libstdc++-order sort.  counts[0] / [1]:
  * queries whose KmerMatch sort ran plain / libstdc++-order; [2] / [3]:
  * ext-sorted groups put in ext-pos order plain (most already are) /
- * libstdc++-order; [4] / [5]: groups whose backtrack picked its starts by
- * score itself / followed the libstdc++-order score sort (groups over
- * 16,384 elements); [6]: groups whose backtrack ran again in the libstdc++
- * order because equal scores could change their result. */
+ * libstdc++-order; [4]: groups whose backtrack picked its starts by score
+ * itself; [5]: 0 (no score order is sorted ahead of the backtrack); [6]:
+ * groups whose backtrack ran again in the libstdc++ order because equal
+ * scores could change their result. */
 cuflye_status cuflye_last_sort_stats(const cuflye_ctx* ctx, uint64_t* counts, size_t n);
 
 /* Kernel launches issued by the library in this process so far. */
