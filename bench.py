@@ -233,6 +233,7 @@ def run_ours(args, world, rank, local) -> None:
         rows = gpu.overlaps(seqs, params, out=out)
         wall_s.append(time.perf_counter() - t)
         ms, by = gpu.last_timing()
+        sort_paths = gpu.last_sort_stats()
         ms = np.array(ms)
         stage_tot += ms
         bytes_tot += np.array(by, dtype=np.float64)
@@ -310,6 +311,7 @@ def run_ours(args, world, rank, local) -> None:
         "gpu_launches": int(round(launches_step * args.steps)),
         "stages_ms_per_step": {n: round(float(stage_tot[i]) / args.steps, 3)
                                for i, n in enumerate(names + ["output + D2H", "H2D"])},
+        "sort_paths_per_step": sort_paths,
         "roofline": {"bound": "hbm", "stage": names[dom], "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": (achieved / peak) if peak else None,
                      "traffic": traffic, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"

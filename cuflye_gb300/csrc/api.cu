@@ -443,19 +443,13 @@ struct PassState {
   uint64_t* f_off = nullptr;  // nq + 1 filtered offsets
   QueryInfo* qinfo = nullptr;
   uint32_t* q_tie = nullptr;  // per query: its KmerMatch keys may repeat
-  bool presorted = false;     // distinct-key queries written in KmerMatch order
 };
 
-// Passes of at least this many queries write distinct-key queries directly
-// in KmerMatch order (one block per query); smaller ones, the one-read plain
-// path above all, spread each query's sort over many blocks instead.
-constexpr uint32_t kPresortMinQueries = 64;
-
 // Buffers sized by the hit count of a pass (reused by the next pass).
-const char* const kPerHitBuffers[] = {"h_keys",  "h_vals", "h_kmers", "s_l",     "s_r",
-                                      "g_flags", "g_id",   "c_cur",   "c_ext",   "c_score",
-                                      "c_bt",    "a_cand", "m_tiles", "m_counts", "c_pmc",
-                                      "o_maps"};
+const char* const kPerHitBuffers[] = {"h_keys",  "h_vals",   "h_kmers", "s_l",     "s_r",
+                                      "c_akeys", "c_avals",  "c_score", "c_bt",    "a_cand",
+                                      "m_tiles", "m_counts", "c_pmc",   "o_maps",  "g_tcount",
+                                      "g_toff"};
 
 // The memory budget, or the device's memory less a 4 GiB margin when unbounded.
 uint64_t effective_budget(cuflye_ctx* c) {
@@ -573,25 +567,8 @@ bool run_hits(cuflye_ctx* c, const Queries& Q, size_t q0, size_t q1, bool want_k
   ps.vals = buf<uint32_t>(c, "h_vals", ps.nhits);
   ps.kmers = want_kmers ? buf<uint64_t>(c, "h_kmers", ps.nhits) : nullptr;
   ps.fpos = buf<int32_t>(c, "h_fpos", ps.nfilt);
-  if (want_kmers) {
-    // candidate records: every hit in generation order
-    CUFLYE_CHECK(hits_emit(c->idx, qb, hit_off, filt_off, wmeta, wflags, ps.keys, ps.vals,
-                           ps.kmers, ps.fpos, nullptr, st));
-  } else if (ps.nq >= kPresortMinQueries) {
-    // for chaining, a batch of many queries: queries whose KmerMatch keys are
-    // distinct straight in sorted order (one block per query), the others
-    // (q_tie = 1) in generation order for the emulated sort
-    ps.presorted = true;
-    CUFLYE_CHECK(hits_emit_sorted(c->idx, qb, hit_off, wmeta, wflags, ps.q_tie, ps.keys, ps.vals,
-                                  buf<uint32_t>(c, "c_work", 1), c->num_sms, st));
-    CUFLYE_CHECK(hits_emit(c->idx, qb, hit_off, filt_off, wmeta, wflags, ps.keys, ps.vals, nullptr,
-                           ps.fpos, ps.q_tie, st));
-  } else {
-    // smaller batches: generation order, sorted by radix tiles spread over
-    // the device
-    CUFLYE_CHECK(hits_emit(c->idx, qb, hit_off, filt_off, wmeta, wflags, ps.keys, ps.vals, nullptr,
-                           ps.fpos, nullptr, st));
-  }
+  CUFLYE_CHECK(hits_emit(c->idx, qb, hit_off, filt_off, wmeta, wflags, ps.keys, ps.vals, ps.kmers,
+                         ps.fpos, st));
   return true;
 }
 
@@ -642,32 +619,33 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
   uint64_t* qe = buf<uint64_t>(c, "s_qe", nq);
   uint32_t* ntiles = buf<uint32_t>(c, "m_ntiles", nq);
   uint64_t* tile_off = buf<uint64_t>(c, "m_tileoff", nq + 1);
-  uint32_t* alt_h = reinterpret_cast<uint32_t*>(buf<int32_t>(c, "c_score", H));
-  uint32_t* alt_l = reinterpret_cast<uint32_t*>(buf<int32_t>(c, "c_cur", H));
-  uint32_t* alt_v = reinterpret_cast<uint32_t*>(buf<int32_t>(c, "c_ext", H));
+  // second buffer of the radix passes; later the exact score orders
+  uint64_t* alt_keys = buf<uint64_t>(c, "c_akeys", H + 1);
+  uint32_t* alt_vals = buf<uint32_t>(c, "c_avals", H + 1);
   int id_bits = 0;
   while (id_bits < 32 && ((2ull * c->idx.nslots - 1) >> id_bits) != 0) ++id_bits;
   CUFLYE_CHECK(cudaEventRecord(c->ev[1], st));
-  CUFLYE_CHECK(match_plan(ps.q_off, ps.q_tie, nq, ps.presorted, ntiles, qb, qe, ecount, st));
+  CUFLYE_CHECK(match_plan(ps.q_off, ps.q_tie, nq, ntiles, qb, qe, ecount, st));
   CUFLYE_CHECK(sort_stats_add(sstats, 0, 1, nullptr, nq, ecount, st));
   const uint64_t NT = scan_u32(c, ntiles, tile_off, nq, "m_scan");
   MatchTile* tiles = buf<MatchTile>(c, "m_tiles", NT);
   uint32_t* mcounts = buf<uint32_t>(c, "m_counts", 256 * NT);
   CUFLYE_CHECK(match_tiles(ps.q_off, ntiles, tile_off, nq, tiles, st));
-  CUFLYE_CHECK(match_radix(ps.keys, ps.vals, alt_h, alt_l, alt_v, tiles,
+  CUFLYE_CHECK(match_radix(ps.keys, ps.vals, alt_keys, alt_vals, tiles,
                            static_cast<uint32_t>(NT), ps.q_off, ntiles, tile_off, nq, id_bits,
                            mcounts, c->num_sms, st));
   CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, qb, qe, nq, ecount, lists,
                                   scounts, c->num_sms, st, sort_tasks(c, "s", H, nq)));
   CUFLYE_CHECK(cudaEventRecord(c->ev[2], st));
-  // 2. groups
-  uint32_t* gflags = buf<uint32_t>(c, "g_flags", H);
-  uint64_t* gid = buf<uint64_t>(c, "g_id", H + 1);
-  CUFLYE_CHECK(groups_mark(ps.keys, ps.q_off, nq, H, gflags, st));
-  const uint64_t G = scan_u32(c, gflags, gid, H, "g_scan");
+  // 2. groups: runs of one ext id within a query
+  const uint64_t gtiles = (H + kGroupTile - 1) / kGroupTile;
+  uint32_t* gtcount = buf<uint32_t>(c, "g_tcount", gtiles);
+  uint64_t* gtoff = buf<uint64_t>(c, "g_toff", gtiles + 1);
+  CUFLYE_CHECK(groups_count(ps.keys, ps.q_off, nq, H, gtcount, st));
+  const uint64_t G = scan_u32(c, gtcount, gtoff, gtiles, "g_scan");
   if (G >= (1ull << 32)) throw Error(CUFLYE_ERR_UNSUPPORTED, "more than 2^32 target groups");
   GroupInfo* groups = buf<GroupInfo>(c, "g_info", G);
-  CUFLYE_CHECK(groups_build(ps.keys, gflags, gid, ps.q_off, nq, H, G, groups, st));
+  CUFLYE_CHECK(groups_write(ps.keys, ps.q_off, nq, H, gtoff, groups, st));
   uint32_t* ext_list = buf<uint32_t>(c, "g_extlist", G);
   uint32_t* dp_list = buf<uint32_t>(c, "g_dplist", G);
   uint32_t* gcounts = buf<uint32_t>(c, "g_counts", 4);
@@ -702,9 +680,9 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
   // 5. the backtrack picks its chain starts by score itself; groups where
   // Flye's order among equal scores could matter get that order (libstdc++
   // order of indices by score descending) and run again.  The (key, index)
-  // pairs of the order live in the group-building buffers, free by now.
-  uint64_t* okeys = gid;
-  uint32_t* order = gflags;
+  // pairs of the order live in the radix sort's second buffer, free by now.
+  uint64_t* okeys = alt_keys;
+  uint32_t* order = alt_vals;
   const uint64_t gmap_words = chain_dp_pmc_words(H, G);
   uint32_t* gmaps = buf<uint32_t>(c, "o_maps", 3 * gmap_words);
   // 6. backtrack, proposals, primary selection; the row pool is sized by the
@@ -814,10 +792,10 @@ void for_each_pass(cuflye_ctx* c, const Queries& Q, bool kmers, uint64_t bytes_p
   }
 }
 
-// Device bytes per hit of one pass: keys, values, the two rank maps, group
-// flags and ids, cur / ext / score / backtrack, plus about 2 bytes for the
-// per-group tables and the sort's task list.
-constexpr uint64_t kChainBytesPerHit = 8 + 4 + 4 + 4 + 4 + 8 + 4 + 4 + 4 + 4 + 2;
+// Device bytes per hit of one pass: keys, values, the two rank maps, the
+// radix sort's second key / value buffer, score and backtrack, plus about 2
+// bytes for the per-group tables, tiles, bitmaps and the sort's task list.
+constexpr uint64_t kChainBytesPerHit = 8 + 4 + 4 + 4 + 8 + 4 + 4 + 4 + 2;
 
 void require_index(cuflye_ctx* c) {
   if (!c->has_index) throw Error(CUFLYE_ERR_NO_INDEX, "no k-mer index: call cuflye_index_build");

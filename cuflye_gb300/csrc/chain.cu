@@ -42,30 +42,72 @@ __device__ __forceinline__ uint32_t upper_query(const uint64_t* __restrict__ q_o
   return lo;
 }
 
-__global__ void mark_ext_changes(const uint64_t* __restrict__ keys, uint64_t n,
-                                 uint32_t* __restrict__ flags) {
-  const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  flags[i] = (i == 0 || (keys[i] >> 32) != (keys[i - 1] >> 32)) ? 1u : 0u;
-}
+// Thread t of a tile owns hits [tile * kGroupTile + t * kGroupItems, ...);
+// a group starts where the ext id changes or a query starts.
+constexpr int kGroupBlock = 256;
+constexpr int kGroupItems = static_cast<int>(kGroupTile / kGroupBlock);
 
-__global__ void mark_query_starts(const uint64_t* __restrict__ q_off, uint32_t nq,
-                                  uint32_t* __restrict__ flags) {
-  const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= nq) return;
-  if (q_off[q] < q_off[q + 1]) flags[q_off[q]] = 1u;
-}
-
-__global__ void build_groups(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ flags,
-                             const uint64_t* __restrict__ gid, const uint64_t* __restrict__ q_off,
-                             uint32_t nq, uint64_t n, GroupInfo* __restrict__ groups) {
-  const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= n || !flags[i]) return;
-  GroupInfo g{};
-  g.start = i;
-  g.ext_di = static_cast<uint32_t>(keys[i] >> 32);
-  g.query = upper_query(q_off, nq, i);
-  groups[gid[i]] = g;
+template <bool WRITE>
+__global__ void __launch_bounds__(kGroupBlock) group_tiles_kernel(
+    const uint64_t* __restrict__ keys, const uint64_t* __restrict__ q_off, uint32_t nq,
+    uint64_t n, uint32_t* __restrict__ tile_counts, const uint64_t* __restrict__ tile_off,
+    GroupInfo* __restrict__ groups) {
+  __shared__ uint32_t part[kGroupBlock / 32];
+  const uint64_t i0 = static_cast<uint64_t>(blockIdx.x) * kGroupTile +
+                      static_cast<uint64_t>(threadIdx.x) * kGroupItems;
+  const uint64_t i1 = i0 + kGroupItems < n ? i0 + kGroupItems : n;
+  uint32_t q = 0, cnt = 0;
+  uint64_t qnext = 0;
+  uint32_t prev = 0;
+  if (i0 < n) {
+    q = upper_query(q_off, nq, i0);
+    qnext = q_off[q + 1];
+    prev = i0 ? static_cast<uint32_t>(keys[i0 - 1] >> 32) : 0u;
+  }
+  uint32_t starts = 0;  // bit j: hit i0 + j starts a group
+  for (uint64_t i = i0; i < i1; ++i) {
+    while (i >= qnext) qnext = q_off[++q + 1];
+    const uint32_t e = static_cast<uint32_t>(keys[i] >> 32);
+    if (i == 0 || i == q_off[q] || e != prev) {
+      starts |= 1u << (i - i0);
+      ++cnt;
+    }
+    prev = e;
+  }
+  // block-wide exclusive scan of the per-thread counts
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t inc = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += u;
+  }
+  if (lane == 31) part[warp] = inc;
+  __syncthreads();
+  if (!WRITE) {
+    if (threadIdx.x == 0) {
+      uint32_t tot = 0;
+      for (int w = 0; w < kGroupBlock / 32; ++w) tot += part[w];
+      tile_counts[blockIdx.x] = tot;
+    }
+    return;
+  }
+  uint32_t before = 0;
+  for (int w = 0; w < warp; ++w) before += part[w];
+  uint64_t g = tile_off[blockIdx.x] + before + inc - cnt;
+  if (i0 >= n) return;
+  q = upper_query(q_off, nq, i0);
+  qnext = q_off[q + 1];
+  for (uint64_t i = i0; i < i1; ++i) {
+    while (i >= qnext) qnext = q_off[++q + 1];
+    if ((starts >> (i - i0)) & 1u) {
+      GroupInfo gi{};
+      gi.start = i;
+      gi.ext_di = static_cast<uint32_t>(keys[i] >> 32);
+      gi.query = q;
+      groups[g++] = gi;
+    }
+  }
 }
 
 __global__ void prefilter_kernel(const uint64_t* __restrict__ keys,
@@ -828,23 +870,23 @@ __global__ void rows_scatter_kernel(const OverlapRow* __restrict__ pool, uint32_
 
 }  // namespace
 
-cudaError_t groups_mark(const uint64_t* keys, const uint64_t* q_off, uint32_t nq, uint64_t nhits,
-                        uint32_t* flags, cudaStream_t s) {
+cudaError_t groups_count(const uint64_t* keys, const uint64_t* q_off, uint32_t nq, uint64_t nhits,
+                         uint32_t* tile_counts, cudaStream_t s) {
   if (nhits == 0) return cudaSuccess;
   count_launch();
-  mark_ext_changes<<<grid(nhits, 256), 256, 0, s>>>(keys, nhits, flags);
-  count_launch();
-  mark_query_starts<<<grid(nq, 256), 256, 0, s>>>(q_off, nq, flags);
+  group_tiles_kernel<false><<<static_cast<unsigned>((nhits + kGroupTile - 1) / kGroupTile),
+                              kGroupBlock, 0, s>>>(keys, q_off, nq, nhits, tile_counts, nullptr,
+                                                   nullptr);
   return cudaGetLastError();
 }
 
-cudaError_t groups_build(const uint64_t* keys, const uint32_t* flags, const uint64_t* gid,
-                         const uint64_t* q_off, uint32_t nq, uint64_t nhits, uint64_t ngroups,
-                         GroupInfo* groups, cudaStream_t s) {
+cudaError_t groups_write(const uint64_t* keys, const uint64_t* q_off, uint32_t nq, uint64_t nhits,
+                         const uint64_t* tile_off, GroupInfo* groups, cudaStream_t s) {
   if (nhits == 0) return cudaSuccess;
-  (void)ngroups;
   count_launch();
-  build_groups<<<grid(nhits, 256), 256, 0, s>>>(keys, flags, gid, q_off, nq, nhits, groups);
+  group_tiles_kernel<true><<<static_cast<unsigned>((nhits + kGroupTile - 1) / kGroupTile),
+                             kGroupBlock, 0, s>>>(keys, q_off, nq, nhits, nullptr, tile_off,
+                                                  groups);
   return cudaGetLastError();
 }
 

@@ -12,12 +12,10 @@
 //   are generated window by window, so the hits on one ext id already come
 //   in cur-pos order.  Two hits share (ext id, cur pos) only when one window's
 //   bucket lists a target id twice; the index marks such buckets (kDupIdsBit)
-//   and hit counting flags the queries that look one up (q_tie = 1).  An
+//   and hit counting flags the queries that look one up (q_tie).  An
 //   unflagged query's keys are distinct, and its sort is a stable sort by ext
-//   id.  Most unflagged queries are written in that order directly
-//   (bucket.cu); the rest (q_tie = 2) take a least-significant-digit radix
-//   sort over the ext id bits, 8 bits per pass, in tiles of kMatchTile hits
-//   that never straddle two queries.
+//   id: a least-significant-digit radix sort over the ext id bits, 8 bits per
+//   pass, in tiles of kMatchTile hits that never straddle two queries.
 // * Ext-pos re-sort of ext-sorted groups of at most kGroupCap elements
 //   (tools/replay_read_to_graph_source_pack.py:396-397) that are not already
 //   in strict ext-pos order.  One block sorts the group in shared memory
@@ -60,37 +58,19 @@ struct PairsAoS {
   }
 };
 
-// The same pairs as three word arrays (the other buffer of the radix passes).
-struct PairsSoA {
-  uint32_t* h;
-  uint32_t* l;
-  uint32_t* v;
-  __device__ __forceinline__ uint32_t hi(uint64_t i) const { return h[i]; }
-  __device__ __forceinline__ void load(uint64_t i, uint32_t& hh, uint32_t& ll, uint32_t& x) const {
-    hh = h[i];
-    ll = l[i];
-    x = v[i];
-  }
-  __device__ __forceinline__ void store(uint64_t i, uint32_t hh, uint32_t ll, uint32_t x) const {
-    h[i] = hh;
-    l[i] = ll;
-    v[i] = x;
-  }
-};
-
 __global__ void match_plan_kernel(const uint64_t* __restrict__ q_off,
-                                  const uint32_t* __restrict__ q_tie, uint32_t nq, bool presorted,
+                                  const uint32_t* __restrict__ q_tie, uint32_t nq,
                                   uint32_t* __restrict__ ntiles, uint64_t* __restrict__ emu_begin,
                                   uint64_t* __restrict__ emu_end, uint32_t* __restrict__ emu_count) {
   for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
     const uint64_t b = q_off[q], e = q_off[q + 1];
     uint32_t t = 0;
     if (e - b > 1) {
-      if (q_tie[q] == 1) {
+      if (q_tie[q]) {
         const uint32_t s = atomicAdd(emu_count, 1u);
         emu_begin[s] = b;
         emu_end[s] = e;
-      } else if (q_tie[q] == 2 || !presorted) {
+      } else {
         t = static_cast<uint32_t>((e - b + kMatchTile - 1) / kMatchTile);
       }
     }
@@ -469,14 +449,14 @@ void allow_smem(T* kernel, size_t bytes) {
 
 }  // namespace
 
-cudaError_t match_plan(const uint64_t* q_off, const uint32_t* q_tie, uint32_t nq, bool presorted,
-                       uint32_t* ntiles, uint64_t* emu_begin, uint64_t* emu_end,
-                       uint32_t* emu_count, cudaStream_t s) {
+cudaError_t match_plan(const uint64_t* q_off, const uint32_t* q_tie, uint32_t nq, uint32_t* ntiles,
+                       uint64_t* emu_begin, uint64_t* emu_end, uint32_t* emu_count,
+                       cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(emu_count, 0, 4, s);
   if (e != cudaSuccess || nq == 0) return e;
   count_launch();
-  match_plan_kernel<<<(nq + 255) / 256, 256, 0, s>>>(q_off, q_tie, nq, presorted, ntiles,
-                                                     emu_begin, emu_end, emu_count);
+  match_plan_kernel<<<(nq + 255) / 256, 256, 0, s>>>(q_off, q_tie, nq, ntiles, emu_begin, emu_end,
+                                                     emu_count);
   return cudaGetLastError();
 }
 
@@ -488,40 +468,33 @@ cudaError_t match_tiles(const uint64_t* q_off, const uint32_t* ntiles, const uin
   return cudaGetLastError();
 }
 
-cudaError_t match_radix(uint64_t* keys, uint32_t* vals, uint32_t* alt_hi, uint32_t* alt_lo,
-                        uint32_t* alt_val, const MatchTile* tiles, uint32_t ntile,
+cudaError_t match_radix(uint64_t* keys, uint32_t* vals, uint64_t* alt_keys, uint32_t* alt_vals,
+                        const MatchTile* tiles, uint32_t ntile,
                         const uint64_t* q_off, const uint32_t* ntiles, const uint64_t* tile_off,
                         uint32_t nq, int id_bits, uint32_t* counts, int num_sms,
                         cudaStream_t s) {
   if (ntile == 0 || id_bits <= 0) return cudaSuccess;
   const PairsAoS aos{keys, vals};
-  const PairsSoA soa{alt_hi, alt_lo, alt_val};
-  allow_smem(match_scatter_kernel<PairsAoS, PairsSoA>, sizeof(TileSmem));
-  allow_smem(match_scatter_kernel<PairsSoA, PairsAoS>, sizeof(TileSmem));
+  const PairsAoS alt{alt_keys, alt_vals};
+  allow_smem(match_scatter_kernel<PairsAoS, PairsAoS>, sizeof(TileSmem));
   const unsigned tgrid = static_cast<unsigned>(std::min<uint64_t>(ntile, 2ull * num_sms * 8));
   const unsigned sgrid = static_cast<unsigned>(std::min<uint64_t>(ntile, 2ull * num_sms));
   const unsigned qgrid = static_cast<unsigned>(std::min<uint64_t>(nq, 4ull * num_sms));
   bool in_aos = true;
   for (int sh = 0; sh < id_bits; sh += 8) {
+    const PairsAoS src = in_aos ? aos : alt, dst = in_aos ? alt : aos;
     count_launch();
-    if (in_aos)
-      match_hist_kernel<<<tgrid, 256, 0, s>>>(aos, tiles, ntile, sh, counts);
-    else
-      match_hist_kernel<<<tgrid, 256, 0, s>>>(soa, tiles, ntile, sh, counts);
+    match_hist_kernel<<<tgrid, 256, 0, s>>>(src, tiles, ntile, sh, counts);
     count_launch();
     match_offsets_kernel<<<qgrid, 256, 0, s>>>(ntiles, tile_off, nq, counts);
     count_launch();
-    if (in_aos)
-      match_scatter_kernel<<<sgrid, kTileBlock, sizeof(TileSmem), s>>>(aos, soa, tiles, ntile,
-                                                                       q_off, sh, counts);
-    else
-      match_scatter_kernel<<<sgrid, kTileBlock, sizeof(TileSmem), s>>>(soa, aos, tiles, ntile,
-                                                                       q_off, sh, counts);
+    match_scatter_kernel<<<sgrid, kTileBlock, sizeof(TileSmem), s>>>(src, dst, tiles, ntile, q_off,
+                                                                     sh, counts);
     in_aos = !in_aos;
   }
   if (!in_aos) {
     count_launch();
-    match_copy_kernel<<<tgrid, 256, 0, s>>>(soa, aos, tiles, ntile);
+    match_copy_kernel<<<tgrid, 256, 0, s>>>(alt, aos, tiles, ntile);
   }
   return cudaGetLastError();
 }

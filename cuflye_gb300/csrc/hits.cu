@@ -115,7 +115,7 @@ __global__ void emit_kernel(DeviceIndex idx, QueryBatch q, const uint64_t* __res
                             const uint64_t* __restrict__ wmeta,
                             const uint8_t* __restrict__ wflags, uint64_t* __restrict__ keys,
                             uint32_t* __restrict__ vals, uint64_t* __restrict__ kmers,
-                            int32_t* __restrict__ fpos, const uint32_t* __restrict__ only_tie) {
+                            int32_t* __restrict__ fpos) {
   const int lane = threadIdx.x & 31;
   const uint32_t lt = (1u << lane) - 1u;
   const uint64_t w = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -128,7 +128,7 @@ __global__ void emit_kernel(DeviceIndex idx, QueryBatch q, const uint64_t* __res
     p = static_cast<uint32_t>(w - q.win_off[qi]);
     if (fl & kWinFiltered) {
       fpos[filt_off[w]] = static_cast<int32_t>(p);
-    } else if (!only_tie || only_tie[qi] == 1) {
+    } else {
       o = hit_off[w];
       end = hit_off[w + 1];
       meta = wmeta[w];
@@ -200,11 +200,11 @@ cudaError_t hits_count(const DeviceIndex& idx, const QueryBatch& q, uint32_t* cn
 cudaError_t hits_emit(const DeviceIndex& idx, const QueryBatch& q, const uint64_t* hit_off,
                       const uint64_t* filt_off, const uint64_t* wmeta, const uint8_t* wflags,
                       uint64_t* keys, uint32_t* vals, uint64_t* kmers, int32_t* fpos,
-                      const uint32_t* only_tie, cudaStream_t s) {
+                      cudaStream_t s) {
   if (q.nwin == 0) return cudaSuccess;
   count_launch();
   emit_kernel<<<static_cast<unsigned>((q.nwin + 255) / 256), 256, 0, s>>>(
-      idx, q, hit_off, filt_off, wmeta, wflags, keys, vals, kmers, fpos, only_tie);
+      idx, q, hit_off, filt_off, wmeta, wflags, keys, vals, kmers, fpos);
   return cudaGetLastError();
 }
 

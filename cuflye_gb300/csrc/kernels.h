@@ -105,19 +105,11 @@ cudaError_t hits_count(const DeviceIndex& idx, const QueryBatch& q, uint32_t* cn
                        uint32_t* filt, uint64_t* wmeta, uint8_t* wflags, uint32_t* q_tie,
                        cudaStream_t s);
 // keys[j] = (ext dense id << 32) | cur pos, vals[j] = ext pos, kmers
-// (optional), in generation order; filtered positions into fpos.  With
-// only_tie, hits are written only for queries with only_tie[q] == 1.
+// (optional), in generation order; filtered positions into fpos.
 cudaError_t hits_emit(const DeviceIndex& idx, const QueryBatch& q, const uint64_t* hit_off,
                       const uint64_t* filt_off, const uint64_t* wmeta, const uint8_t* wflags,
                       uint64_t* keys, uint32_t* vals, uint64_t* kmers, int32_t* fpos,
-                      const uint32_t* only_tie, cudaStream_t s);
-// Hits of every query with q_tie[q] == 0 written directly in KmerMatch order
-// ((ext id, cur pos) ascending); a query with too many distinct ext ids is
-// written in generation order instead and gets q_tie[q] = 2 (bucket.cu).
-cudaError_t hits_emit_sorted(const DeviceIndex& idx, const QueryBatch& q, const uint64_t* hit_off,
-                             const uint64_t* wmeta, const uint8_t* wflags, uint32_t* q_tie,
-                             uint64_t* keys, uint32_t* vals, uint32_t* work, int num_sms,
-                             cudaStream_t s);
+                      cudaStream_t s);
 // Gather per-query segment bounds from window-level offsets.
 cudaError_t gather_query_offsets(const uint64_t* win_off, const uint64_t* wl_off, uint32_t nq,
                                  uint64_t* q_off, cudaStream_t s);
@@ -173,21 +165,19 @@ struct MatchTile {
   uint32_t query;
 };
 
-// Per query with two or more hits: q_tie = 1 (keys may repeat) is listed for
-// the emulated sort, q_tie = 2 (in generation order, keys distinct) gets
-// ntiles[q] radix tiles; q_tie = 0 queries are sorted already when
-// `presorted` (hits_emit_sorted ran), else they get radix tiles too.
-cudaError_t match_plan(const uint64_t* q_off, const uint32_t* q_tie, uint32_t nq, bool presorted,
-                       uint32_t* ntiles, uint64_t* emu_begin, uint64_t* emu_end,
-                       uint32_t* emu_count, cudaStream_t s);
+// Per query with two or more hits: flagged queries (q_tie, keys may repeat)
+// are listed for the emulated sort; the others get ntiles[q] radix tiles.
+cudaError_t match_plan(const uint64_t* q_off, const uint32_t* q_tie, uint32_t nq, uint32_t* ntiles,
+                       uint64_t* emu_begin, uint64_t* emu_end, uint32_t* emu_count,
+                       cudaStream_t s);
 // tile_off: exclusive scan of ntiles.
 cudaError_t match_tiles(const uint64_t* q_off, const uint32_t* ntiles, const uint64_t* tile_off,
                         uint32_t nq, MatchTile* tiles, cudaStream_t s);
 // Stable radix sort by the ext id (key bits 32 .. 32 + id_bits) of every
-// tiled query, in place in (keys, vals); alt_* are three word arrays of one
-// word per hit and counts holds 256 words per tile.
-cudaError_t match_radix(uint64_t* keys, uint32_t* vals, uint32_t* alt_hi, uint32_t* alt_lo,
-                        uint32_t* alt_val, const MatchTile* tiles, uint32_t ntile,
+// tiled query, in place in (keys, vals); (alt_keys, alt_vals) is a second
+// buffer of the same shape and counts holds 256 words per tile.
+cudaError_t match_radix(uint64_t* keys, uint32_t* vals, uint64_t* alt_keys, uint32_t* alt_vals,
+                        const MatchTile* tiles, uint32_t ntile,
                         const uint64_t* q_off, const uint32_t* ntiles, const uint64_t* tile_off,
                         uint32_t nq, int id_bits, uint32_t* counts, int num_sms, cudaStream_t s);
 // stats[i_emul] += *emul; stats[i_plain] += total - *emul (total from
@@ -202,11 +192,14 @@ cudaError_t group_ext_sort(uint64_t* keys, uint32_t* vals, const GroupInfo* grou
                            uint64_t* emu_begin, uint64_t* emu_end, uint32_t* emu_count,
                            uint32_t* work, int num_sms, cudaStream_t s);
 
-cudaError_t groups_mark(const uint64_t* keys, const uint64_t* q_off, uint32_t nq, uint64_t nhits,
-                        uint32_t* flags, cudaStream_t s);
-cudaError_t groups_build(const uint64_t* keys, const uint32_t* flags, const uint64_t* gid,
-                         const uint64_t* q_off, uint32_t nq, uint64_t nhits, uint64_t ngroups,
-                         GroupInfo* groups, cudaStream_t s);
+// Groups (runs of one ext id within a query's sorted hits) in two passes
+// over tiles of kGroupTile hits: counts per tile, then (after an exclusive
+// scan of the counts into tile_off) each group's start, query and ext id.
+constexpr uint32_t kGroupTile = 4096;
+cudaError_t groups_count(const uint64_t* keys, const uint64_t* q_off, uint32_t nq, uint64_t nhits,
+                         uint32_t* tile_counts, cudaStream_t s);
+cudaError_t groups_write(const uint64_t* keys, const uint64_t* q_off, uint32_t nq, uint64_t nhits,
+                         const uint64_t* tile_off, GroupInfo* groups, cudaStream_t s);
 cudaError_t groups_prefilter_n(const uint64_t* keys, const uint32_t* vals, GroupInfo* groups,
                                uint64_t ngroups, uint64_t nhits, const QueryInfo* qinfo,
                                const int32_t* slot_len, const ChainParams& p,
