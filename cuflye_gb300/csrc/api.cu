@@ -1029,14 +1029,17 @@ cuflye_status cuflye_overlaps(cuflye_ctx* c, size_t n, const int64_t* ids, const
     accumulate_timing(c, true);
   });
   // algorithmic bytes per stage: packed bases + one 32-byte sector per window
-  // probe + bucket entries read (8 B) + hit records written (12 B); a read and a
-  // write of every 12-byte record per sort; the DP reads (cur, ext) and writes
-  // (score, backtrack)
+  // Compulsory traffic per stage: the bases and one probe sector per window,
+  // bucket entries read (8 B) and hit records written (12 B); a read and a
+  // write of every 12-byte record for the KmerMatch sort; the group stage
+  // reads the sorted records (12 B) and the ext positions of ext-sorted
+  // groups (counted as 8 B on average); the DP reads (cur, ext) and writes
+  // (score, backtrack); the backtrack reads its table once.
   c->stage_bytes[0] = bases_total / 4 + windows_total * 32 + hits_total * 20;
   c->stage_bytes[1] = hits_total * 24;
   c->stage_bytes[2] = hits_total * 20;
   c->stage_bytes[3] = hits_total * 16;
-  c->stage_bytes[4] = hits_total * 28;
+  c->stage_bytes[4] = hits_total * 4;
   if (n_out) *n_out = total;
   if (overflow)
     throw Error(CUFLYE_ERR_CAPACITY,

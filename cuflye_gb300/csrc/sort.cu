@@ -599,9 +599,14 @@ __global__ void __launch_bounds__(kBigBlock, 4) sort_big(uint64_t* K, uint32_t* 
         continue;
       }
       if (d == 0) {
+        // depth exhausted: libstdc++ heap-sorts the range; sort_heaps does it
+        // in shared memory (a task longer than kCap)
         if (threadIdx.x == 0) {
-          isort::heap_sort(Ks, Vs, f, l);
           sm.gn = nt - 1;
+          const uint32_t slot = atomicAdd(task_count, 1u);
+          task_f[slot] = b + f;
+          task_n[slot] = l - f;
+          task_d[slot] = 0;
         }
         __syncthreads();
         continue;
@@ -631,7 +636,67 @@ __global__ void __launch_bounds__(kBlock, 3) sort_tasks(uint64_t* K, uint32_t* V
   CtaSmem& sm = *reinterpret_cast<CtaSmem*>(smem_raw);
   const uint32_t cnt = *task_count;
   for (uint32_t i = blockIdx.x; i < cnt; i += gridDim.x)
-    cta_load_sort_store(K, V, task_f[i], task_n[i], task_d[i], sm);
+    if (task_n[i] <= kCap) cta_load_sort_store(K, V, task_f[i], task_n[i], task_d[i], sm);
+}
+
+// Heapsorts the tasks longer than kCap (ranges whose introsort depth ran out
+// in the global phase), one CTA per task: the range is loaded into shared
+// memory, the heap is built level by level (sibling subtrees are disjoint, so
+// building a level in parallel equals libstdc++'s right-to-left order), then
+// one thread pops it.  Ranges beyond kHeapCap are heap-sorted in place.
+constexpr uint32_t kHeapCap = 18432;
+constexpr int kHeapBlock = 256;
+constexpr size_t kHeapSmem = kHeapCap * (sizeof(uint64_t) + sizeof(uint32_t));
+
+__global__ void __launch_bounds__(kHeapBlock, 1) sort_heaps(uint64_t* K, uint32_t* V,
+                                                         const uint64_t* __restrict__ task_f,
+                                                         const uint32_t* __restrict__ task_n,
+                                                         const uint32_t* __restrict__ task_count) {
+  extern __shared__ __align__(16) unsigned char heap_raw[];
+  uint64_t* hk = reinterpret_cast<uint64_t*>(heap_raw);
+  uint32_t* hv = reinterpret_cast<uint32_t*>(hk + kHeapCap);
+  const uint32_t cnt = *task_count;
+  for (uint32_t i = blockIdx.x; i < cnt; i += gridDim.x) {
+    const uint32_t n = task_n[i];
+    if (n <= kCap) continue;
+    const uint64_t f = task_f[i];
+    if (n > kHeapCap) {
+      if (threadIdx.x == 0) isort::heap_sort(K + f, V + f, 0, n);
+      __syncthreads();
+      continue;
+    }
+    for (uint32_t j = threadIdx.x; j < n; j += kHeapBlock) {
+      hk[j] = K[f + j];
+      hv[j] = V[f + j];
+    }
+    __syncthreads();
+    // parents 0 .. (n - 2) / 2, deepest level first
+    const uint32_t last_parent = (n - 2) / 2;
+    int top_level = 31 - __clz(last_parent + 1);
+    for (int lv = top_level; lv >= 0; --lv) {
+      const uint32_t lo = (1u << lv) - 1u;
+      const uint32_t hi = min((2u << lv) - 2u, last_parent);
+      for (uint32_t p = lo + threadIdx.x; p <= hi; p += kHeapBlock)
+        isort::heap_adjust(hk, hv, 0, p, n, hk[p], hv[p]);
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      for (uint32_t last = n; last > 1;) {
+        --last;
+        const uint64_t vk = hk[last];
+        const uint32_t vv = hv[last];
+        hk[last] = hk[0];
+        hv[last] = hv[0];
+        isort::heap_adjust(hk, hv, 0, 0, last, vk, vv);
+      }
+    }
+    __syncthreads();
+    for (uint32_t j = threadIdx.x; j < n; j += kHeapBlock) {
+      K[f + j] = hk[j];
+      V[f + j] = hv[j];
+    }
+    __syncthreads();
+  }
 }
 
 }  // namespace
@@ -657,6 +722,8 @@ cudaError_t segmented_std_sort(uint64_t* keys, uint32_t* vals, uint32_t* lscratc
                          static_cast<int>(sizeof(CtaSmem)));
     cudaFuncSetAttribute(sort_warp, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          static_cast<int>(sizeof(WarpSlice) * kWarpSegWarps));
+    cudaFuncSetAttribute(sort_heaps, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         static_cast<int>(kHeapSmem));
     attr = true;
   }
   if (nseg == 0) return cudaSuccess;
@@ -680,6 +747,8 @@ cudaError_t segmented_std_sort(uint64_t* keys, uint32_t* vals, uint32_t* lscratc
   count_launch();
   sort_tasks<<<num_sms * 3, kBlock, sizeof(CtaSmem), stream>>>(keys, vals, tasks.f, tasks.n, tasks.d,
                                                            counts + 4);
+  count_launch();
+  sort_heaps<<<num_sms, kHeapBlock, kHeapSmem, stream>>>(keys, vals, tasks.f, tasks.n, counts + 4);
   return cudaGetLastError();
 }
 
