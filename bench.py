@@ -314,7 +314,10 @@ def run_ours(args, world, rank, local) -> None:
         "sort_paths_per_step": sort_paths,
         "roofline": {"bound": "hbm", "stage": names[dom], "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": (achieved / peak) if peak else None,
-                     "traffic": traffic, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"
+                     "traffic": traffic,
+                     "traffic_unit": "DRAM bytes per step of the stage's kernels (ncu bytes per "
+                                     "hit from profiles/ncu_traffic.json x hits per step)",
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"
                      if peak else "missing"},
         "clocks": clocks,
     }
