@@ -42,72 +42,78 @@ __device__ __forceinline__ uint32_t upper_query(const uint64_t* __restrict__ q_o
   return lo;
 }
 
-// Thread t of a tile owns hits [tile * kGroupTile + t * kGroupItems, ...);
-// a group starts where the ext id changes or a query starts.
+// A tile's hits are visited in kGroupTile / kGroupBlock rounds of
+// consecutive hits (coalesced); a group starts where the ext id changes or a
+// query starts (the tile's query starts are marked in a bitmap first).
 constexpr int kGroupBlock = 256;
-constexpr int kGroupItems = static_cast<int>(kGroupTile / kGroupBlock);
+constexpr int kGroupRounds = static_cast<int>(kGroupTile / kGroupBlock);
 
 template <bool WRITE>
 __global__ void __launch_bounds__(kGroupBlock) group_tiles_kernel(
     const uint64_t* __restrict__ keys, const uint64_t* __restrict__ q_off, uint32_t nq,
     uint64_t n, uint32_t* __restrict__ tile_counts, const uint64_t* __restrict__ tile_off,
     GroupInfo* __restrict__ groups) {
-  __shared__ uint32_t part[kGroupBlock / 32];
-  const uint64_t i0 = static_cast<uint64_t>(blockIdx.x) * kGroupTile +
-                      static_cast<uint64_t>(threadIdx.x) * kGroupItems;
-  const uint64_t i1 = i0 + kGroupItems < n ? i0 + kGroupItems : n;
-  uint32_t q = 0, cnt = 0;
-  uint64_t qnext = 0;
-  uint32_t prev = 0;
-  if (i0 < n) {
-    q = upper_query(q_off, nq, i0);
-    qnext = q_off[q + 1];
-    prev = i0 ? static_cast<uint32_t>(keys[i0 - 1] >> 32) : 0u;
-  }
-  uint32_t starts = 0;  // bit j: hit i0 + j starts a group
-  for (uint64_t i = i0; i < i1; ++i) {
-    while (i >= qnext) qnext = q_off[++q + 1];
-    const uint32_t e = static_cast<uint32_t>(keys[i] >> 32);
-    if (i == 0 || i == q_off[q] || e != prev) {
-      starts |= 1u << (i - i0);
-      ++cnt;
-    }
-    prev = e;
-  }
-  // block-wide exclusive scan of the per-thread counts
+  __shared__ uint32_t qbits[kGroupTile / 32];
+  __shared__ uint32_t wsum[kGroupBlock / 32];
+  __shared__ uint32_t qfirst;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint32_t inc = cnt;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
-    if (lane >= o) inc += u;
-  }
-  if (lane == 31) part[warp] = inc;
-  __syncthreads();
-  if (!WRITE) {
-    if (threadIdx.x == 0) {
-      uint32_t tot = 0;
-      for (int w = 0; w < kGroupBlock / 32; ++w) tot += part[w];
-      tile_counts[blockIdx.x] = tot;
+  const uint64_t t0 = static_cast<uint64_t>(blockIdx.x) * kGroupTile;
+  const uint32_t tn = static_cast<uint32_t>(n - t0 < kGroupTile ? n - t0 : kGroupTile);
+  for (uint32_t w = threadIdx.x; w < kGroupTile / 32; w += kGroupBlock) qbits[w] = 0;
+  if (threadIdx.x == 0) {
+    // first query starting at or after t0
+    uint32_t lo = 0, hi = nq;
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (q_off[mid] < t0)
+        lo = mid + 1;
+      else
+        hi = mid;
     }
-    return;
+    qfirst = lo;
   }
-  uint32_t before = 0;
-  for (int w = 0; w < warp; ++w) before += part[w];
-  uint64_t g = tile_off[blockIdx.x] + before + inc - cnt;
-  if (i0 >= n) return;
-  q = upper_query(q_off, nq, i0);
-  qnext = q_off[q + 1];
-  for (uint64_t i = i0; i < i1; ++i) {
-    while (i >= qnext) qnext = q_off[++q + 1];
-    if ((starts >> (i - i0)) & 1u) {
+  __syncthreads();
+  for (uint32_t q = qfirst + threadIdx.x; q < nq && q_off[q] < t0 + tn; q += kGroupBlock) {
+    const uint32_t j = static_cast<uint32_t>(q_off[q] - t0);
+    atomicOr(&qbits[j >> 5], 1u << (j & 31));
+  }
+  __syncthreads();
+  uint64_t g = WRITE ? tile_off[blockIdx.x] : 0;
+  uint32_t total = 0;
+  for (int r = 0; r < kGroupRounds; ++r) {
+    const uint32_t j = static_cast<uint32_t>(r) * kGroupBlock + threadIdx.x;
+    const uint64_t i = t0 + j;
+    bool start = false;
+    uint32_t e = 0;
+    if (j < tn) {
+      e = static_cast<uint32_t>(keys[i] >> 32);
+      start = i == 0 || ((qbits[j >> 5] >> (j & 31)) & 1u) ||
+              e != static_cast<uint32_t>(keys[i - 1] >> 32);
+    }
+    if (!WRITE) {
+      total += __syncthreads_count(start);
+      continue;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, start);
+    if (lane == 0) wsum[warp] = __popc(m);
+    __syncthreads();
+    uint32_t before = 0, round_total = 0;
+    for (int w = 0; w < kGroupBlock / 32; ++w) {
+      const uint32_t c = wsum[w];
+      if (w < warp) before += c;
+      round_total += c;
+    }
+    if (start) {
       GroupInfo gi{};
       gi.start = i;
-      gi.ext_di = static_cast<uint32_t>(keys[i] >> 32);
-      gi.query = q;
-      groups[g++] = gi;
+      gi.ext_di = e;
+      gi.query = upper_query(q_off, nq, i);
+      groups[g + before + __popc(m & ((1u << lane) - 1u))] = gi;
     }
+    g += round_total;
+    __syncthreads();
   }
+  if (!WRITE && threadIdx.x == 0) tile_counts[blockIdx.x] = total;
 }
 
 __global__ void prefilter_kernel(const uint64_t* __restrict__ keys,
