@@ -200,6 +200,103 @@ def pinned_like(a: np.ndarray) -> np.ndarray:
     return v
 
 
+def serving_run(args, device: int) -> dict:
+    """Continuous batching (cuflye_submit / cuflye_poll) on the serving
+    workload: single-read requests arriving by a Poisson process at each
+    offered rate, p50/p99 latency from submit to rows, throughput, and the
+    plain one-read-per-call path on the same queries."""
+    import queue
+    import threading
+    from cuflye_gb300 import synth
+    from cuflye_gb300.backend import CudaBackend, CudaServer, OverlapParams, Sequences
+    sw = synth.serving_workload(seed=4)
+    q = sw.queries
+    pool = [Sequences(q.ids[i:i + 1].copy(), np.array([0, q.offsets[i + 1] - q.offsets[i]],
+                                                         dtype=np.int64),
+                      np.ascontiguousarray(q.bases[q.offsets[i]:q.offsets[i + 1]]))
+            for i in range(q.n)]
+    out = {"workload": "100 Mb genome, 5% interspersed repeats (2-8 kb families, 1-3% div) "
+                       "indexed as 1 Mb pieces, k=15; single-read requests, lengths log-uniform "
+                       "1-100 kb, 1% or 8% error 50/50, Poisson arrivals",
+           "budget_bytes": 40 << 30, "workers": args.serve_workers,
+           "max_batch_bases": args.serve_batch_bases, "rates": []}
+    with CudaBackend(device=device, memory_budget_bytes=40 << 30) as be:
+        t = time.perf_counter()
+        be.build_index(sw.targets, sw.k, sw.min_freq, sw.max_freq)
+        out["index_build_s"] = round(time.perf_counter() - t, 3)
+        p = OverlapParams.make(**sw.params)
+        # plain path: one read per call
+        lat = []
+        for s in pool[:5]:
+            be.overlaps(s, p)
+        t = time.perf_counter()
+        nb = 0
+        for s in pool[:args.plain_sample or 100]:
+            t1 = time.perf_counter()
+            be.overlaps(s, p)
+            lat.append(time.perf_counter() - t1)
+            nb += int(s.offsets[-1])
+        plain_s = time.perf_counter() - t
+        lat_ms = sorted(1000 * x for x in lat)
+        out["plain"] = {"read_bases_per_s": nb / plain_s, "p50_ms": lat_ms[len(lat_ms) // 2],
+                        "p99_ms": lat_ms[min(len(lat_ms) - 1, int(0.99 * len(lat_ms)))]}
+        best = 0.0
+        with CudaServer(be, p, workers=args.serve_workers,
+                        max_batch_bases=args.serve_batch_bases) as srv:
+            for s in pool[:20]:
+                srv.poll(srv.submit(s), -1)
+            for rate in args.serve_rates:
+                n = max(10, min(int(rate * args.serve_seconds), 50_000))
+                rng = np.random.default_rng(int(rate))
+                arrive = np.cumsum(rng.exponential(1.0 / rate, n))
+                t_sub = np.zeros(n)
+                t_done = np.zeros(n)
+                nbases = np.zeros(n)
+                tq: queue.Queue = queue.Queue()
+                b0 = srv.stats()
+
+                failed: list = []
+
+                def poller():
+                    for _ in range(n):
+                        i, tk = tq.get()
+                        try:
+                            srv.poll(tk, -1)
+                        except Exception as e:  # recorded; the rate reports it
+                            failed.append(f"request {i}: {e}")
+                        t_done[i] = time.perf_counter()
+
+                th = threading.Thread(target=poller)
+                th.start()
+                t0 = time.perf_counter()
+                for i in range(n):
+                    wait = arrive[i] - (time.perf_counter() - t0)
+                    if wait > 0:
+                        time.sleep(wait)
+                    s = pool[i % len(pool)]
+                    t_sub[i] = time.perf_counter()
+                    tq.put((i, srv.submit(s)))
+                    nbases[i] = s.offsets[-1]
+                th.join()
+                b1 = srv.stats()
+                if failed:
+                    out["rates"].append({"offered_reads_per_s": rate, "requests": n,
+                                         "failed": len(failed), "first_error": failed[0]})
+                    continue
+                lat = np.sort(1000 * (t_done - t_sub))
+                span = t_done.max() - t_sub[0]
+                thr = float(nbases.sum() / span)
+                best = max(best, thr)
+                out["rates"].append({
+                    "offered_reads_per_s": rate, "requests": n,
+                    "submitted_reads_per_s": round(n / max(t_sub[-1] - t_sub[0], 1e-9), 1),
+                    "p50_ms": float(lat[n // 2]), "p99_ms": float(lat[min(n - 1, int(0.99 * n))]),
+                    "read_bases_per_s": thr,
+                    "batches": b1["batches"] - b0["batches"]})
+        out["served_over_plain"] = best / out["plain"]["read_bases_per_s"]
+    return out
+
+
 def run_ours(args, world, rank, local) -> None:
     from cuflye_gb300 import abi
     from cuflye_gb300.backend import CudaBackend, OverlapParams, Sequences, load_library
@@ -329,8 +426,10 @@ def run_ours(args, world, rank, local) -> None:
                               "mode": "plain path, one read per call through the C ABI"}
     if cpu:
         line["cpu_baseline"] = cpu
-    print(json.dumps(line), flush=True)
     gpu.close()
+    if args.serve_rates and world == 1:
+        line["serving"] = serving_run(args, local)
+    print(json.dumps(line), flush=True)
 
 
 def main() -> int:
@@ -345,6 +444,13 @@ def main() -> int:
     ap.add_argument("--plain-sample", type=int, default=200)
     ap.add_argument("--cpu-sample", type=int, default=384)
     ap.add_argument("--reference-sample", type=int, default=256)
+    ap.add_argument("--serve-rates", type=lambda v: [float(x) for x in v.split(",") if x],
+                    default=[1000.0, 10000.0, 50000.0],
+                    help="offered request rates (reads/s) of the serving run; empty skips it")
+    ap.add_argument("--serve-seconds", type=float, default=1.0)
+    ap.add_argument("--serve-workers", type=int, default=2)
+    ap.add_argument("--serve-batch-bases", type=int, default=32_000_000,
+                    help="most read bases one served batch takes")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":

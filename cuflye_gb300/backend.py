@@ -26,8 +26,9 @@ LIB_PATH = Path(__file__).resolve().parent / "_build" / "libcuflye_gb300.so"
 
 STATUS = {0: "CUFLYE_OK", 1: "CUFLYE_ERR_INVALID", 2: "CUFLYE_ERR_UNSUPPORTED",
           3: "CUFLYE_ERR_BUDGET", 4: "CUFLYE_ERR_CUDA", 5: "CUFLYE_ERR_CAPACITY",
-          6: "CUFLYE_ERR_TIMEOUT", 7: "CUFLYE_ERR_NO_INDEX"}
+          6: "CUFLYE_ERR_TIMEOUT", 7: "CUFLYE_ERR_NO_INDEX", 8: "CUFLYE_PENDING"}
 ERR_CAPACITY = 5
+PENDING = 8
 
 
 class CuflyeError(RuntimeError):
@@ -135,6 +136,18 @@ def load_library(path: Path | None = None) -> ctypes.CDLL:
     L.cuflye_last_timing.argtypes = [_vp, ctypes.POINTER(ctypes.c_double), _u64p, ctypes.c_size_t]
     L.cuflye_last_sort_stats.restype = S
     L.cuflye_last_sort_stats.argtypes = [_vp, _u64p, ctypes.c_size_t]
+    L.cuflye_server_open.restype = S
+    L.cuflye_server_open.argtypes = [_vp, ctypes.c_int, ctypes.POINTER(OverlapParams),
+                                     ctypes.c_uint64, ctypes.POINTER(_vp)]
+    L.cuflye_submit.restype = S
+    L.cuflye_submit.argtypes = [_vp, ctypes.c_size_t, _i64p, _i64p, ctypes.c_char_p, _u64p]
+    L.cuflye_poll.restype = S
+    L.cuflye_poll.argtypes = [_vp, ctypes.c_uint64, ctypes.c_int, _vp, ctypes.c_size_t, _szp]
+    L.cuflye_server_stats.restype = S
+    L.cuflye_server_stats.argtypes = [_vp, _u64p, _u64p, _u64p]
+    L.cuflye_server_last_error.restype = ctypes.c_char_p
+    L.cuflye_server_last_error.argtypes = [_vp]
+    L.cuflye_server_close.argtypes = [_vp]
     _LIB = L
     return L
 
@@ -348,6 +361,75 @@ class CudaBackend:
         self._check(self._L.cuflye_std_sort_segments(self._h, _ptr(k, _u64p), _ptr(v, _u32p),
                                                      _ptr(o, _u64p), len(o) - 1))
         return k, v
+
+
+class CudaServer:
+    """Continuous batching of overlap requests (cuflye_server_*): requests
+    are submitted as they arrive, and each worker context takes every request
+    waiting when it falls idle, so batches overlap on the device."""
+
+    def __init__(self, backend: CudaBackend, params: OverlapParams, workers: int = 2,
+                 max_batch_bases: int = 0):
+        self._L = backend._L
+        self._backend = backend  # keeps the owner (and its index) alive
+        self._params = params
+        h = _vp()
+        st = self._L.cuflye_server_open(backend._h, int(workers), ctypes.byref(params),
+                                        int(max_batch_bases), ctypes.byref(h))
+        if st != 0:
+            raise CuflyeError(st, self._L.cuflye_last_error(backend._h).decode())
+        self._h = h
+
+    def _err(self, st: int):
+        raise CuflyeError(st, self._L.cuflye_server_last_error(self._h).decode())
+
+    def submit(self, queries) -> int:
+        q = Sequences.of(queries)
+        t = ctypes.c_uint64()
+        st = self._L.cuflye_submit(self._h, q.n, _ptr(q.ids, _i64p), _ptr(q.offsets, _i64p),
+                                   q.bases.ctypes.data_as(ctypes.c_char_p), ctypes.byref(t))
+        if st != 0:
+            self._err(st)
+        return t.value
+
+    def poll(self, ticket: int, wait_ms: int = -1, capacity: int = 4096):
+        """Rows of a finished request, or None while it is pending."""
+        cap = capacity
+        while True:
+            out = np.empty(cap, dtype=abi.OVERLAP_DTYPE)
+            n = ctypes.c_size_t()
+            st = self._L.cuflye_poll(self._h, int(ticket), int(wait_ms), out.ctypes.data, cap,
+                                     ctypes.byref(n))
+            if st == PENDING:
+                return None
+            if st == ERR_CAPACITY:
+                cap = n.value
+                continue
+            if st != 0:
+                self._err(st)
+            return out[:n.value]
+
+    def stats(self) -> dict:
+        a, b, c = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        self._L.cuflye_server_stats(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+        return {"batches": a.value, "requests": b.value, "pending": c.value}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._L.cuflye_server_close(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def collect_candidate_matches_cuda(backend: CudaBackend, query_id: int, sequence: bytes):

@@ -8,13 +8,17 @@
 // for a contiguous run of queries, then the libstdc++-order match sort and
 // the chaining stages, all on the context's stream; the host only reads back
 // the sizes it needs to size the next stage's buffers.  A pass that would
-// exceed the memory budget is split in half; a single query that does not
-// fit fails with CUFLYE_ERR_BUDGET (records are never truncated,
-// docs/abi/candidate-record-v1.md:105-118).
+// exceed the memory budget keeps the longest prefix of its queries whose hits
+// fit, and a pass whose later stages do not fit runs again on half of its
+// queries; a single query that does not fit fails with CUFLYE_ERR_BUDGET
+// (records are never truncated, docs/abi/candidate-record-v1.md:105-118).
 #include <dlfcn.h>
 
 #include <algorithm>
 #include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <thread>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -325,6 +329,7 @@ void build_index(cuflye_ctx* c, int k, size_t n, const int64_t* ids, const int64
   c->idx.pos = pos;
   c->idx.npos = npos;
   c->idx.slot_len = d_len;
+  c->idx.slot_signed = d_signed;
   c->idx.nslots = static_cast<uint32_t>(n);
   c->idx.nkeys = nsolid + nrep;
   c->idx.nrep = nrep;
@@ -417,6 +422,7 @@ void build_index_entries(cuflye_ctx* c, int k, size_t n, const int64_t* tids, co
   c->idx.pos = pos;
   c->idx.npos = npos;
   c->idx.slot_len = d_len;
+  c->idx.slot_signed = d_signed;
   c->idx.nslots = nslots;
   c->idx.nkeys = nruns + nrep;
   c->idx.nrep = nrep;
@@ -601,7 +607,8 @@ SortTasks sort_tasks(cuflye_ctx* c, const std::string& prefix, uint64_t nelems, 
 
 // Sort + chaining of the pass's hits; returns the number of overlap rows left
 // on the device in "o_rows" (OverlapRow, query order, Flye emission order).
-uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
+uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp,
+                   uint64_t* rows_per_query = nullptr) {
   cudaStream_t st = c->stream;
   const uint64_t H = ps.nhits;
   const uint32_t nq = ps.nq;
@@ -664,7 +671,8 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
   uint32_t* resort_count = buf<uint32_t>(c, "g_resortcount", 1);
   CUFLYE_CHECK(groups_ext_presorted(ps.vals, groups, ext_list, gcounts, resort, resort_count, st));
   CUFLYE_CHECK(group_ext_sort(ps.keys, ps.vals, groups, resort, resort_count, G32, sb, se, ecount,
-                              work, c->num_sms, st));
+                              lscr, rscr, reinterpret_cast<uint32_t*>(alt_keys), H, work,
+                              c->num_sms, st));
   CUFLYE_CHECK(sort_stats_add(sstats, 2, 3, gcounts + 0, 0, ecount, st));
   CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, sb, se, G32, ecount, glists,
                                   scounts, c->num_sms, st, sort_tasks(c, "s", H, G32)));
@@ -684,7 +692,7 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
   uint64_t* okeys = alt_keys;
   uint32_t* order = alt_vals;
   const uint64_t gmap_words = chain_dp_pmc_words(H, G);
-  uint32_t* gmaps = buf<uint32_t>(c, "o_maps", 3 * gmap_words);
+  uint32_t* gmaps = buf<uint32_t>(c, "o_maps", 4 * gmap_words);
   // 6. backtrack, proposals, primary selection; the row pool is sized by the
   // groups that survived the prefilter
   const uint32_t survivors = read_scalar(c, gcounts + 1);
@@ -697,7 +705,7 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
   uint32_t* redo = buf<uint32_t>(c, "o_redo", G);
   uint32_t* redo_count = buf<uint32_t>(c, "o_redocount", 1);
   CUFLYE_CHECK(cudaMemsetAsync(redo_count, 0, 4, st));
-  const int64_t* slot_signed = buf<int64_t>(c, "ix_slot_signed", 1);
+  const int64_t* slot_signed = c->idx.slot_signed;
   CUFLYE_CHECK(chain_backtrack(ps.keys, ps.vals, score, bt, order, groups, dp_list, gcounts + 1, top,
                                redo, redo_count, ps.qinfo, ps.f_off, ps.fpos, slot_signed, c->logt,
                                cp, pool, pool_cap, pool_count, group_rows, c->status, G32, gmaps,
@@ -727,6 +735,12 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp) {
   const uint32_t npool = read_scalar(c, pool_count);
   OverlapRow* rows = buf<OverlapRow>(c, "o_rows", R);
   CUFLYE_CHECK(rows_scatter(pool, npool, kept, kept_off, rows, st));
+  if (rows_per_query) {
+    uint64_t* qrows = buf<uint64_t>(c, "o_qrows", nq);
+    CUFLYE_CHECK(query_row_counts(qg, kept_off, nq, qrows, st));
+    CUFLYE_CHECK(cudaMemcpyAsync(rows_per_query, qrows, nq * sizeof(uint64_t),
+                                 cudaMemcpyDeviceToHost, st));
+  }
   CUFLYE_CHECK(cudaEventRecord(c->ev[3], st));
   return R;
 }
@@ -774,7 +788,11 @@ size_t pass_size(cuflye_ctx* c, size_t n) {
   return n;
 }
 
-// Runs passes over [0, n): `body(q0, q1, ps)` consumes each pass.
+// Runs passes over [0, n): `body(q0, q1, ps)` consumes each pass.  A body
+// whose later buffers (per-group tables, the row pool) do not fit the budget
+// runs again on the first half of the pass's queries; bodies make their
+// results visible only after their last allocation, so the retry repeats no
+// output.
 template <typename Body>
 void for_each_pass(cuflye_ctx* c, const Queries& Q, bool kmers, uint64_t bytes_per_hit,
                    Body body) {
@@ -787,7 +805,14 @@ void for_each_pass(cuflye_ctx* c, const Queries& Q, bool kmers, uint64_t bytes_p
     run_hits(c, Q, q0, q1, kmers, bytes_per_hit, ps);
     q1 = q0 + ps.nq;
     CUFLYE_CHECK(cudaEventRecord(c->ev[1], c->stream));
-    body(q0, q1, ps);
+    try {
+      body(q0, q1, ps);
+    } catch (const Error& e) {
+      if (e.code != CUFLYE_ERR_BUDGET || ps.nq <= 1) throw;
+      sync(c);
+      step = std::max<size_t>(ps.nq / 2, 1);
+      continue;
+    }
     q0 = q1;
   }
 }
@@ -969,7 +994,7 @@ cuflye_status cuflye_candidates(cuflye_ctx* c, size_t n, const int64_t* ids,
       cuflye_candidate* d_out = buf<cuflye_candidate>(c, "a_cand", ps.nhits);
       cuflye_filtered_pos* d_f = buf<cuflye_filtered_pos>(c, "a_filt", ps.nfilt);
       CUFLYE_CHECK(hits_to_abi(ps.keys, ps.vals, ps.kmers, ps.nhits, ps.q_off, ps.nq, ps.qinfo,
-                               buf<int64_t>(c, "ix_slot_signed", 1), d_out, c->stream));
+                               c->idx.slot_signed, d_out, c->stream));
       CUFLYE_CHECK(filtered_to_abi(ps.fpos, ps.nfilt, ps.f_off, ps.nq, ps.qinfo, d_f, c->stream));
       if (ps.nhits)
         CUFLYE_CHECK(cudaMemcpyAsync(out + total, d_out, ps.nhits * sizeof(cuflye_candidate),
@@ -1010,20 +1035,20 @@ cuflye_status cuflye_overlaps(cuflye_ctx* c, size_t n, const int64_t* ids, const
   bool overflow = false;
   uint64_t hits_total = 0, windows_total = 0, bases_total = 0;
   for_each_pass(c, Q, false, kChainBytesPerHit, [&](size_t q0, size_t q1, PassState& ps) {
-    hits_total += ps.nhits;
-    windows_total += ps.nwin;
-    bases_total += static_cast<uint64_t>(offsets[q1] - offsets[q0]);
     const uint64_t R = run_chain(c, ps, cp);
     if (!overflow && total + R <= out_cap) {
       cuflye_overlap_range* d_out = buf<cuflye_overlap_range>(c, "a_ovl", R);
       CUFLYE_CHECK(rows_to_abi(buf<OverlapRow>(c, "o_rows", R), R, ps.qinfo,
-                               buf<int64_t>(c, "ix_slot_signed", 1), d_out, c->stream));
+                               c->idx.slot_signed, d_out, c->stream));
       if (R)
         CUFLYE_CHECK(cudaMemcpyAsync(out + total, d_out, R * sizeof(cuflye_overlap_range),
                                      cudaMemcpyDeviceToHost, c->stream));
     } else {
       overflow = true;
     }
+    hits_total += ps.nhits;
+    windows_total += ps.nwin;
+    bases_total += static_cast<uint64_t>(offsets[q1] - offsets[q0]);
     CUFLYE_CHECK(cudaEventRecord(c->ev[4], c->stream));
     total += R;
     accumulate_timing(c, true);
@@ -1101,7 +1126,7 @@ cuflye_status cuflye_read_to_graph(cuflye_ctx* c, size_t n, const int64_t* ids,
                r2g->max_chain_divergence};
   const uint32_t ns = c->idx.nslots;
   R2GGraph g{buf<int64_t>(c, "gr_edge", ns), buf<int32_t>(c, "gr_left", ns),
-             buf<int32_t>(c, "gr_right", ns), buf<int64_t>(c, "ix_slot_signed", ns)};
+             buf<int32_t>(c, "gr_right", ns), c->idx.slot_signed};
   Queries Q{n, ids, offsets, bases};
   size_t total = 0;
   uint64_t chain_base = 0;
@@ -1248,6 +1273,291 @@ cuflye_status cuflye_kernel_launches(uint64_t* total) {
   if (!total) return CUFLYE_ERR_INVALID;
   *total = launches_total();
   return CUFLYE_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- serving
+//
+// Continuous batching on one device.  A server borrows the owner context's
+// resident index and runs `workers` worker contexts, each with its own
+// stream and device arena, on one host thread each.  A worker that falls
+// idle takes every request that has arrived (up to max_batch_bases of
+// query bases) and runs them as one batch through the overlap stage, so
+// requests that arrive while a batch is on the GPU are admitted into the
+// next free worker's batch and their work overlaps on the device.  Each
+// batch is split back into its requests by the per-query row counts; a
+// request's rows are exactly what cuflye_overlaps returns for its queries
+// alone.
+
+namespace {
+
+struct ServeRequest {
+  uint64_t ticket = 0;
+  std::vector<int64_t> ids, offsets;
+  std::vector<char> bases;
+};
+
+struct ServeResult {
+  bool done = false;
+  cuflye_status status = CUFLYE_OK;
+  std::string err;
+  std::vector<cuflye_overlap_range> rows;
+};
+
+// Overlap rows of Q (every pass) with the rows of each query.
+void overlaps_collect(cuflye_ctx* c, const Queries& Q, const ChainParams& cp,
+                      std::vector<cuflye_overlap_range>& rows, std::vector<uint64_t>& per_query) {
+  rows.clear();
+  per_query.assign(Q.n, 0);
+  reset_timing(c);
+  for_each_pass(c, Q, false, kChainBytesPerHit, [&](size_t q0, size_t, PassState& ps) {
+    const uint64_t R = run_chain(c, ps, cp, per_query.data() + q0);
+    cuflye_overlap_range* d_out = buf<cuflye_overlap_range>(c, "a_ovl", R);
+    const size_t base = rows.size();
+    rows.resize(base + R);
+    CUFLYE_CHECK(rows_to_abi(buf<OverlapRow>(c, "o_rows", R), R, ps.qinfo, c->idx.slot_signed, d_out,
+                             c->stream));
+    if (R)
+      CUFLYE_CHECK(cudaMemcpyAsync(rows.data() + base, d_out, R * sizeof(cuflye_overlap_range),
+                                   cudaMemcpyDeviceToHost, c->stream));
+    CUFLYE_CHECK(cudaEventRecord(c->ev[4], c->stream));
+    accumulate_timing(c, true);  // synchronises the pass
+  });
+}
+
+}  // namespace
+
+struct cuflye_server {
+  cuflye_ctx* owner = nullptr;
+  cuflye_overlap_params params{};
+  uint64_t max_batch_bases = 0;
+  std::vector<cuflye_ctx*> workers;
+  std::vector<std::thread> threads;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<ServeRequest> pending;
+  std::unordered_map<uint64_t, ServeResult> results;
+  uint64_t next_ticket = 1;
+  bool stop = false;
+  uint64_t batches = 0, batched_requests = 0;
+  std::string err;
+};
+
+namespace {
+
+void serve_worker(cuflye_server* s, cuflye_ctx* c) {
+  cudaSetDevice(c->device);
+  const ChainParams cp = to_chain_params(&s->params);
+  for (;;) {
+    std::vector<ServeRequest> batch;
+    {
+      std::unique_lock<std::mutex> lk(s->mu);
+      s->cv_work.wait(lk, [&] { return s->stop || !s->pending.empty(); });
+      if (s->pending.empty()) return;
+      uint64_t taken = 0;
+      while (!s->pending.empty()) {
+        const uint64_t b = s->pending.front().bases.size();
+        if (!batch.empty() && s->max_batch_bases && taken + b > s->max_batch_bases) break;
+        taken += b;
+        batch.push_back(std::move(s->pending.front()));
+        s->pending.pop_front();
+      }
+    }
+    std::vector<int64_t> ids, offs{0};
+    std::vector<char> bases;
+    for (const ServeRequest& r : batch) {
+      ids.insert(ids.end(), r.ids.begin(), r.ids.end());
+      for (size_t i = 0; i + 1 < r.offsets.size(); ++i)
+        offs.push_back(offs.back() + (r.offsets[i + 1] - r.offsets[i]));
+      bases.insert(bases.end(), r.bases.begin(), r.bases.end());
+    }
+    std::vector<cuflye_overlap_range> rows;
+    std::vector<uint64_t> per_query;
+    cuflye_status st = CUFLYE_OK;
+    std::string msg;
+    try {
+      std::lock_guard<std::mutex> g(c->mu);
+      const Queries Q{ids.size(), ids.data(), offs.data(), bases.data()};
+      overlaps_collect(c, Q, cp, rows, per_query);
+    } catch (const Error& e) {
+      st = e.code;
+      msg = e.what();
+    } catch (const std::exception& e) {
+      st = CUFLYE_ERR_CUDA;
+      msg = e.what();
+    }
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      size_t q = 0, r = 0;
+      for (const ServeRequest& req : batch) {
+        ServeResult& res = s->results[req.ticket];
+        res.done = true;
+        res.status = st;
+        res.err = msg;
+        if (st == CUFLYE_OK) {
+          size_t nr = 0;
+          for (size_t i = 0; i < req.ids.size(); ++i) nr += per_query[q + i];
+          res.rows.assign(rows.begin() + r, rows.begin() + r + nr);
+          r += nr;
+        }
+        q += req.ids.size();
+      }
+      ++s->batches;
+      s->batched_requests += batch.size();
+    }
+    s->cv_done.notify_all();
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+cuflye_status cuflye_server_open(cuflye_ctx* owner, int workers,
+                                 const cuflye_overlap_params* params, uint64_t max_batch_bases,
+                                 cuflye_server** out) {
+  if (!out) return CUFLYE_ERR_INVALID;
+  *out = nullptr;
+  cuflye_server* s = nullptr;
+  CUFLYE_API_BEGIN(owner)
+  require_index(owner);
+  check_params(owner, params);
+  if (workers < 1 || workers > 8) throw Error(CUFLYE_ERR_INVALID, "workers must be in [1, 8]");
+  CUFLYE_CHECK(cudaSetDevice(owner->device));
+  // the workers share what is left of the budget (or of the free memory)
+  uint64_t avail = 0;
+  if (owner->budget) {
+    avail = owner->budget > owner->in_use ? owner->budget - owner->in_use : 0;
+  } else {
+    size_t free_b = 0, total_b = 0;
+    CUFLYE_CHECK(cudaMemGetInfo(&free_b, &total_b));
+    const uint64_t margin = 8ull << 30;
+    avail = free_b > margin ? free_b - margin : free_b / 2;
+  }
+  const uint64_t per = avail / static_cast<uint64_t>(workers);
+  if (per < (64ull << 20))
+    throw Error(CUFLYE_ERR_BUDGET, "memory budget leaves under 64 MiB per serving worker");
+  s = new cuflye_server();
+  s->owner = owner;
+  s->params = *params;
+  s->max_batch_bases = max_batch_bases;
+  for (int w = 0; w < workers; ++w) {
+    cuflye_ctx* c = nullptr;
+    const cuflye_status st = cuflye_open(owner->device, per, &c);
+    if (st != CUFLYE_OK) {
+      for (cuflye_ctx* x : s->workers) cuflye_close(x);
+      delete s;
+      s = nullptr;
+      throw Error(st, "cannot open a serving worker context");
+    }
+    // borrow the owner's resident index (device buffers stay the owner's)
+    c->idx = owner->idx;
+    c->slot_of = owner->slot_of;
+    c->slot_signed_h = owner->slot_signed_h;
+    c->has_index = true;
+    s->workers.push_back(c);
+  }
+  for (cuflye_ctx* c : s->workers) s->threads.emplace_back(serve_worker, s, c);
+  *out = s;
+  CUFLYE_API_END(owner)
+}
+
+cuflye_status cuflye_submit(cuflye_server* s, size_t n, const int64_t* ids, const int64_t* offsets,
+                            const char* bases, uint64_t* ticket) {
+  if (!s || !ticket || (n && (!ids || !offsets || !bases))) return CUFLYE_ERR_INVALID;
+  ServeRequest r;
+  r.ids.assign(ids, ids + n);
+  r.offsets.assign(offsets, offsets + n + 1);
+  for (size_t i = 0; i < n; ++i)
+    if (ids[i] == 0 || offsets[i + 1] < offsets[i]) {
+      std::lock_guard<std::mutex> lk(s->mu);
+      s->err = "query ids must not be zero and offsets must not decrease";
+      return CUFLYE_ERR_INVALID;
+    }
+  const int64_t b0 = n ? offsets[0] : 0, b1 = n ? offsets[n] : 0;
+  r.bases.assign(bases + b0, bases + b1);
+  for (int64_t& o : r.offsets) o -= b0;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    r.ticket = s->next_ticket++;
+    *ticket = r.ticket;
+    s->results[r.ticket];
+    s->pending.push_back(std::move(r));
+  }
+  s->cv_work.notify_one();
+  return CUFLYE_OK;
+}
+
+cuflye_status cuflye_poll(cuflye_server* s, uint64_t ticket, int wait_ms, cuflye_overlap_range* out,
+                          size_t out_cap, size_t* n_out) {
+  if (!s) return CUFLYE_ERR_INVALID;
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->results.find(ticket);
+  if (it == s->results.end()) {
+    s->err = "unknown ticket " + std::to_string(ticket);
+    return CUFLYE_ERR_INVALID;
+  }
+  if (!it->second.done && wait_ms != 0) {
+    auto ready = [&] {
+      auto f = s->results.find(ticket);
+      return f == s->results.end() || f->second.done;
+    };
+    if (wait_ms < 0)
+      s->cv_done.wait(lk, ready);
+    else
+      s->cv_done.wait_for(lk, std::chrono::milliseconds(wait_ms), ready);
+    it = s->results.find(ticket);
+    if (it == s->results.end()) {
+      s->err = "ticket " + std::to_string(ticket) + " was consumed by another poll";
+      return CUFLYE_ERR_INVALID;
+    }
+  }
+  ServeResult& res = it->second;
+  if (!res.done) return CUFLYE_PENDING;
+  if (res.status != CUFLYE_OK) {
+    const cuflye_status st = res.status;
+    s->err = res.err;
+    s->results.erase(it);
+    return st;
+  }
+  if (n_out) *n_out = res.rows.size();
+  if (res.rows.size() > out_cap) {
+    s->err = "output capacity too small: need " + std::to_string(res.rows.size()) +
+             " overlap rows";
+    return CUFLYE_ERR_CAPACITY;
+  }
+  if (!res.rows.empty()) std::memcpy(out, res.rows.data(), res.rows.size() * sizeof(res.rows[0]));
+  s->results.erase(it);
+  return CUFLYE_OK;
+}
+
+cuflye_status cuflye_server_stats(cuflye_server* s, uint64_t* batches, uint64_t* requests,
+                                  uint64_t* pending) {
+  if (!s) return CUFLYE_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (batches) *batches = s->batches;
+  if (requests) *requests = s->batched_requests;
+  if (pending) *pending = s->pending.size();
+  return CUFLYE_OK;
+}
+
+const char* cuflye_server_last_error(cuflye_server* s) {
+  if (!s) return "null server";
+  std::lock_guard<std::mutex> lk(s->mu);
+  return s->err.c_str();
+}
+
+void cuflye_server_close(cuflye_server* s) {
+  if (!s) return;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+  }
+  s->cv_work.notify_all();
+  for (std::thread& t : s->threads) t.join();
+  for (cuflye_ctx* c : s->workers) cuflye_close(c);
+  delete s;
 }
 
 }  // extern "C"

@@ -522,6 +522,8 @@ __device__ __forceinline__ uint32_t lower_bound_i32(const int32_t* a, uint32_t n
 // clears the run word by word; only links that are not steps are read from
 // the table, which stays unchanged.  The warp counts linked nodes not yet
 // cleared and stops when none is left: no later start could begin a chain.
+// A fourth map marks the nodes cleared while several starts share the top
+// score (a tie round), to tell whether their walks touch one another.
 
 constexpr uint32_t kBtCap = kBacktrackCap;
 constexpr uint32_t kBtWords = kBtCap / 32;
@@ -531,6 +533,7 @@ struct BtMaps {
   uint32_t link[kBtWords];
   uint32_t step[kBtWords];
   uint32_t done[kBtWords];
+  uint32_t round[kBtWords];
 };
 
 __device__ __forceinline__ uint32_t bits_upto(int32_t pos) {
@@ -546,10 +549,12 @@ __device__ __forceinline__ uint32_t warp_sum_u32(uint32_t v) {
 
 // Walk from s0 (linked, not cleared) with the whole warp: first node and
 // chain length as Flye's walk counts them; visited nodes become cleared and
-// `remaining` drops by the linked ones among them.
+// `remaining` drops by the linked ones among them.  With `round`, visited
+// nodes are marked there too, and `met` tells whether the walk ended on a
+// linked node marked earlier.
 __device__ void walk_maps(const uint32_t* link, const uint32_t* step, uint32_t* done,
                           const int32_t* __restrict__ btg, int32_t s0, int32_t& first,
-                          int32_t& clen, uint32_t& remaining) {
+                          int32_t& clen, uint32_t& remaining, uint32_t* round, bool& met) {
   const int lane = threadIdx.x & 31;
   int32_t pos = s0;
   clen = 0;
@@ -571,6 +576,8 @@ __device__ void walk_maps(const uint32_t* link, const uint32_t* step, uint32_t* 
       }
     }
     const bool stop = ((done[z >> 5] >> (z & 31)) & 1u) || !((link[z >> 5] >> (z & 31)) & 1u);
+    // an unlinked node ends every walk that reaches it, whichever comes first
+    if (round && stop) met = ((round[z >> 5] & link[z >> 5]) >> (z & 31)) & 1u;
     __syncwarp();
     uint32_t newly = 0;
     for (int32_t w = (z >> 5) + lane; w <= (pos >> 5); w += 32) {
@@ -579,6 +586,7 @@ __device__ void walk_maps(const uint32_t* link, const uint32_t* step, uint32_t* 
       if (w == (pos >> 5)) mask &= bits_upto(pos);
       newly += __popc(link[w] & ~done[w] & mask);
       done[w] |= mask;
+      if (round) round[w] |= mask;
     }
     remaining -= warp_sum_u32(newly);
     clen += pos - z + 1;
@@ -663,12 +671,13 @@ __global__ void __launch_bounds__(kBtWarps * 32) backtrack_kernel(
   const uint32_t nf = static_cast<uint32_t>(f_off[g.query + 1] - f_off[g.query]);
   // the maps: shared memory up to kBtCap nodes, else device memory at the
   // group's own word range
-  uint32_t *lk = m.link, *sp = m.step, *dn = m.done;
+  uint32_t *lk = m.link, *sp = m.step, *dn = m.done, *rn = m.round;
   if (g.n > kBtCap) {
     const uint64_t pb = (b >> 5) + gidx;
     lk = gmaps + pb;
     sp = gmaps + gmap_words + pb;
     dn = gmaps + 2 * gmap_words + pb;
+    rn = gmaps + 3 * gmap_words + pb;
   }
   // the first run picks its starts itself; the second follows `order`
   // (Flye's order)
@@ -685,6 +694,7 @@ __global__ void __launch_bounds__(kBtWarps * 32) backtrack_kernel(
       lk[w] = lkw;
       sp[w] = spw;
       dn[w] = 0;
+      rn[w] = 0;
     }
     remaining += __popc(lkw);
   }
@@ -693,17 +703,28 @@ __global__ void __launch_bounds__(kBtWarps * 32) backtrack_kernel(
   int np = 0;
   bool overflow = false;
   // Starts by score: the live node of the highest score next (the DP's top
-  // first).  Two live nodes sharing that score: Flye's order between them
-  // could matter, and the group goes back for that order.
+  // first, when it is linked and no other node shares its score).  Live
+  // nodes sharing the top score are walked in index order; Flye's order
+  // among them (libstdc++'s) gives the same result unless a walk clears
+  // another tied start or ends on a node another tied walk cleared, two
+  // proposals they keep share a score, or they keep two or more proposals
+  // and the group's proposals end up more than 16 (libstdc++ then sorts them
+  // unstably).  In those cases the group goes back for Flye's order.
+  bool multi = false;
   for (bool first_pick = true; pick && remaining > 0; first_pick = false) {
-    int32_t ms;
-    uint32_t mi, mc;
+    int32_t ms = INT_MIN;
+    uint32_t mi = 0xffffffffu, mc = 0;
+    bool scan = true;
     if (first_pick) {
       const GroupTop t = top[gidx];
-      ms = t.score;
-      mi = t.first;
-      mc = t.count;
-    } else {
+      if (t.count == 1 && ((lk[t.first >> 5] >> (t.first & 31)) & 1u)) {
+        ms = t.score;
+        mi = t.first;
+        mc = 1;
+        scan = false;
+      }
+    }
+    if (scan) {
       int32_t bs = INT_MIN;
       uint32_t bi = 0xffffffffu, bc = 0;
       for (uint32_t w = 0; w < nw; ++w) {
@@ -731,18 +752,65 @@ __global__ void __launch_bounds__(kBtWarps * 32) backtrack_kernel(
         mi = min(mi, __shfl_xor_sync(0xffffffffu, mi, o));
       }
     }
-    if (mc > 1) {
+    if (mc == 0) break;  // no live node (remaining counts them; kept as a guard)
+    if (mc == 1) {
+      int32_t first = 0, clen = 0;
+      bool met = false;
+      walk_maps(lk, sp, dn, bt + b, static_cast<int32_t>(mi), first, clen, remaining, nullptr,
+                met);
+      if (lane == 0 && !overflow)
+        add_proposal(keys, vals, score, b, mi, first, clen, qi, ext_signed, g, fq, nf, logt, p, st,
+                     gidx, props, np, overflow);
+      __syncwarp();
+      continue;
+    }
+    // a tie round over the mc live nodes of score ms
+    const int np0 = np;
+    bool clash = false;
+    uint32_t left = mc;
+    for (uint32_t w = mi >> 5; w < nw && left > 0 && !clash; ++w) {
+      const uint32_t lv = lk[w] & ~dn[w];
+      unsigned tied = __ballot_sync(0xffffffffu,
+                                    ((lv >> lane) & 1u) && score[b + w * 32 + lane] == ms);
+      while (tied && !clash) {
+        const int j = __ffs(tied) - 1;
+        tied &= tied - 1;
+        --left;
+        if ((dn[w] >> j) & 1u) {  // cleared by an earlier walk of this round
+          clash = true;
+          break;
+        }
+        int32_t first = 0, clen = 0;
+        bool met = false;
+        const uint32_t s0 = w * 32 + j;
+        walk_maps(lk, sp, dn, bt + b, static_cast<int32_t>(s0), first, clen, remaining, rn, met);
+        if (met) {
+          clash = true;
+          break;
+        }
+        if (lane == 0 && !overflow)
+          add_proposal(keys, vals, score, b, s0, first, clen, qi, ext_signed, g, fq, nf, logt, p,
+                       st, gidx, props, np, overflow);
+        __syncwarp();
+      }
+    }
+    // a tied start cleared before its word was reached is never met above
+    if (left > 0) clash = true;
+    if (lane == 0 && !clash) {
+      for (int i = np0; i < np && !clash; ++i)
+        for (int j = i + 1; j < np; ++j)
+          if (props[i].score == props[j].score) clash = true;
+      if (np - np0 >= 2) multi = true;
+    }
+    clash = __shfl_sync(0xffffffffu, clash, 0);
+    if (clash) {
       ambiguous = true;
       break;
     }
-    const uint32_t s0 = mi;
-    int32_t first = 0, clen = 0;
-    walk_maps(lk, sp, dn, bt + b, static_cast<int32_t>(s0), first, clen, remaining);
-    if (lane == 0 && !overflow)
-      add_proposal(keys, vals, score, b, s0, first, clen, qi, ext_signed, g, fq, nf, logt, p, st,
-                   gidx, props, np, overflow);
+    for (uint32_t w = lane; w < nw; w += 32) rn[w] = 0;
     __syncwarp();
   }
+  if (multi && np > 16) ambiguous = true;
   for (uint32_t o0 = 0; !pick && o0 < g.n && remaining > 0; o0 += 32) {
     const uint32_t oi = o0 + lane;
     const bool valid = oi < g.n;
@@ -754,7 +822,9 @@ __global__ void __launch_bounds__(kBtWarps * 32) backtrack_kernel(
       const int j = __ffs(mask) - 1;
       const uint32_t s0 = __shfl_sync(0xffffffffu, start, j);
       int32_t first = 0, clen = 0;
-      walk_maps(lk, sp, dn, bt + b, static_cast<int32_t>(s0), first, clen, remaining);
+      bool met = false;
+      walk_maps(lk, sp, dn, bt + b, static_cast<int32_t>(s0), first, clen, remaining, nullptr,
+                met);
       if (lane == 0 && !overflow)
         add_proposal(keys, vals, score, b, s0, first, clen, qi, ext_signed, g, fq, nf, logt, p, st,
                      gidx, props, np, overflow);
@@ -942,6 +1012,23 @@ cudaError_t chain_dp(const uint64_t* keys, const uint32_t* vals, int32_t* score,
   dp_kernel<<<num_sms * std::max(per_sm, 1), kDpWarps * 32, 0, s>>>(keys, vals, score, bt, groups,
                                                                    dp_list, counts, p, top,
                                                                    pmc, work);
+  return cudaGetLastError();
+}
+
+namespace {
+__global__ void query_rows_kernel(const uint64_t* __restrict__ q_group_off,
+                                  const uint64_t* __restrict__ kept_off, uint32_t nq,
+                                  uint64_t* __restrict__ out) {
+  const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < nq) out[q] = kept_off[q_group_off[q + 1]] - kept_off[q_group_off[q]];
+}
+}  // namespace
+
+cudaError_t query_row_counts(const uint64_t* q_group_off, const uint64_t* kept_off, uint32_t nq,
+                             uint64_t* out, cudaStream_t s) {
+  if (nq == 0) return cudaSuccess;
+  count_launch();
+  query_rows_kernel<<<grid(nq, 256), 256, 0, s>>>(q_group_off, kept_off, nq, out);
   return cudaGetLastError();
 }
 

@@ -16,12 +16,13 @@
 //   unflagged query's keys are distinct, and its sort is a stable sort by ext
 //   id: a least-significant-digit radix sort over the ext id bits, 8 bits per
 //   pass, in tiles of kMatchTile hits that never straddle two queries.
-// * Ext-pos re-sort of ext-sorted groups of at most kGroupCap elements
+// * Ext-pos re-sort of ext-sorted groups
 //   (tools/replay_read_to_graph_source_pack.py:396-397) that are not already
-//   in strict ext-pos order.  One block sorts the group in shared memory
-//   (radix sort on (ext pos, index) packed in 32 bits) and compares
-//   neighbours; a group with equal ext positions, or too large for shared
-//   memory, is written out in the layout sort.cu expects and listed for it.
+//   in strict ext-pos order.  One block sorts the group, in shared memory up
+//   to kGroupCap elements (radix sort on (ext pos, index) packed in 32 bits),
+//   beyond that in device scratch (the same radix sort on separate key and
+//   index arrays), and compares neighbours; a group with equal ext positions
+//   is written out in the layout sort.cu expects and listed for it.
 #include <algorithm>
 #include <climits>
 #include <cstdint>
@@ -298,6 +299,134 @@ __device__ void group_to_emulation(uint64_t* keys, uint32_t* vals, const GroupIn
   }
 }
 
+// Turns the per-warp digit counts in sm.wc into each warp's first output slot
+// per digit: digits in order, warps in order within a digit.
+__device__ void group_digit_bases(GroupSmem& sm) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t tot = 0;
+  if (threadIdx.x < 256) {
+    for (int w = 0; w < kGroupWarps; ++w) {
+      const uint32_t c = sm.wc[w][threadIdx.x];
+      sm.wc[w][threadIdx.x] = tot;
+      tot += c;
+    }
+  }
+  uint32_t inc = tot;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += u;
+  }
+  if (lane == 31 && warp < 8) sm.ws[warp] = inc;
+  __syncthreads();
+  if (threadIdx.x < 256) {
+    uint32_t before = 0;
+    for (int w = 0; w < warp; ++w) before += sm.ws[w];
+    sm.dbase[threadIdx.x] = before + inc - tot;
+  }
+  __syncthreads();
+}
+
+// Key and index arrays of the device-scratch sort, indexed like the hits.
+struct GroupScratch {
+  uint32_t* k0;
+  uint32_t* i0;
+  uint32_t* k1;
+  uint32_t* i1;
+};
+
+// A group beyond shared memory: LSD radix sort of (ext pos - min, index) by
+// 8-bit digits in device scratch; each warp owns a contiguous slice, counts
+// its digits, then scatters the slice in order (stable).  Equal ext
+// positions send the group to sort.cu untouched; otherwise the group is
+// rewritten as (key = ext pos, val = cur pos) in ext-pos order.
+__device__ void group_sort_global(uint64_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                                  const GroupInfo& g, GroupScratch sc, GroupSmem& sm,
+                                  uint64_t* emu_begin, uint64_t* emu_end, uint32_t* emu_count) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t lt = (1u << lane) - 1u;
+  const uint32_t n = g.n;
+  const uint64_t b = g.start;
+  if (threadIdx.x == 0) {
+    sm.kmin = 0xffffffffu;
+    sm.kmax = 0;
+  }
+  __syncthreads();
+  uint32_t lmin = 0xffffffffu, lmax = 0;
+  for (uint32_t j = threadIdx.x; j < n; j += kGroupBlock) {
+    const uint32_t key = vals[b + j];
+    lmin = min(lmin, key);
+    lmax = max(lmax, key);
+  }
+  atomicMin(&sm.kmin, lmin);
+  atomicMax(&sm.kmax, lmax);
+  __syncthreads();
+  const uint32_t kmin = sm.kmin, range = sm.kmax - sm.kmin;
+  const int kb = range ? 32 - __clz(range) : 0;
+  uint32_t* sk = sc.k0 + b;
+  uint32_t* si = sc.i0 + b;
+  uint32_t* dk = sc.k1 + b;
+  uint32_t* di = sc.i1 + b;
+  for (uint32_t j = threadIdx.x; j < n; j += kGroupBlock) {
+    sk[j] = vals[b + j] - kmin;
+    si[j] = j;
+  }
+  const uint32_t per_warp = (((n + 31) / 32 + kGroupWarps - 1) / kGroupWarps) * 32;
+  const uint32_t w0 = min(n, warp * per_warp);
+  const uint32_t w1 = min(n, w0 + per_warp);
+  for (int shift = 0; shift < kb; shift += 8) {
+    for (int i = threadIdx.x; i < kGroupWarps * 256; i += kGroupBlock) (&sm.wc[0][0])[i] = 0;
+    __syncthreads();
+    for (uint32_t r0 = w0; r0 < w1; r0 += 32) {
+      const uint32_t j = r0 + lane;
+      const bool valid = j < w1;
+      const uint32_t d = valid ? (sk[j] >> shift) & 0xffu : 256u;
+      const uint32_t peers = __match_any_sync(0xffffffffu, d);
+      if (valid && lane == __ffs(peers) - 1) sm.wc[warp][d] += __popc(peers);
+      __syncwarp();
+    }
+    __syncthreads();
+    group_digit_bases(sm);
+    for (uint32_t r0 = w0; r0 < w1; r0 += 32) {
+      const uint32_t j = r0 + lane;
+      const bool valid = j < w1;
+      const uint32_t x = valid ? sk[j] : 0u;
+      const uint32_t d = valid ? (x >> shift) & 0xffu : 256u;
+      const uint32_t peers = __match_any_sync(0xffffffffu, d);
+      const uint32_t base = valid ? sm.dbase[d] + sm.wc[warp][d] : 0u;
+      __syncwarp();
+      if (valid && lane == __ffs(peers) - 1) sm.wc[warp][d] += __popc(peers);
+      __syncwarp();
+      if (valid) {
+        const uint32_t o = base + __popc(peers & lt);
+        dk[o] = x;
+        di[o] = si[j];
+      }
+    }
+    __syncthreads();
+    uint32_t* t = sk;
+    sk = dk;
+    dk = t;
+    t = si;
+    si = di;
+    di = t;
+  }
+  bool tie = false;
+  for (uint32_t j = threadIdx.x + 1; j < n && !tie; j += kGroupBlock) tie = sk[j] == sk[j - 1];
+  if (__syncthreads_or(tie)) {
+    group_to_emulation(keys, vals, g, emu_begin, emu_end, emu_count);
+    return;
+  }
+  // gather the cur positions before any write: the group is rewritten in place
+  for (uint32_t i = threadIdx.x; i < n; i += kGroupBlock)
+    dk[i] = static_cast<uint32_t>(keys[b + si[i]] & 0xffffffffu);
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < n; i += kGroupBlock) {
+    keys[b + i] = static_cast<uint64_t>(sk[i] + kmin);
+    vals[b + i] = dk[i];
+  }
+}
+
 // In (key = (ext id << 32) | cur pos, val = ext pos), out (key = ext pos,
 // val = cur pos) in ext-pos order.
 __global__ void __launch_bounds__(kGroupBlock, 1)
@@ -305,7 +434,7 @@ __global__ void __launch_bounds__(kGroupBlock, 1)
                       const GroupInfo* __restrict__ groups, const uint32_t* __restrict__ list,
                       const uint32_t* __restrict__ list_count, uint64_t* __restrict__ emu_begin,
                       uint64_t* __restrict__ emu_end, uint32_t* __restrict__ emu_count,
-                      uint32_t* __restrict__ work) {
+                      GroupScratch sc, uint32_t* __restrict__ work) {
   extern __shared__ __align__(16) unsigned char group_raw[];
   GroupSmem& sm = *reinterpret_cast<GroupSmem*>(group_raw);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -324,7 +453,7 @@ __global__ void __launch_bounds__(kGroupBlock, 1)
     const uint64_t b = g.start;
     if (n == 0) continue;
     if (n > kGroupCap) {
-      group_to_emulation(keys, vals, g, emu_begin, emu_end, emu_count);
+      group_sort_global(keys, vals, g, sc, sm, emu_begin, emu_end, emu_count);
       __syncthreads();
       continue;
     }
@@ -378,28 +507,7 @@ __global__ void __launch_bounds__(kGroupBlock, 1)
         if (valid) sm.rank[j] = static_cast<uint16_t>(base + __popc(peers & lt));
       }
       __syncthreads();
-      uint32_t tot = 0;
-      if (threadIdx.x < 256) {
-        for (int w = 0; w < kGroupWarps; ++w) {
-          const uint32_t c = sm.wc[w][threadIdx.x];
-          sm.wc[w][threadIdx.x] = tot;
-          tot += c;
-        }
-      }
-      uint32_t inc = tot;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
-        if (lane >= o) inc += u;
-      }
-      if (lane == 31 && warp < 8) sm.ws[warp] = inc;
-      __syncthreads();
-      if (threadIdx.x < 256) {
-        uint32_t before = 0;
-        for (int w = 0; w < warp; ++w) before += sm.ws[w];
-        sm.dbase[threadIdx.x] = before + inc - tot;
-      }
-      __syncthreads();
+      group_digit_bases(sm);
       for (uint32_t j = w0 + lane; j < w1; j += 32) {
         const uint32_t x = src[j];
         const uint32_t d = (x >> shift) & 0xffu;
@@ -502,7 +610,8 @@ cudaError_t match_radix(uint64_t* keys, uint32_t* vals, uint64_t* alt_keys, uint
 cudaError_t group_ext_sort(uint64_t* keys, uint32_t* vals, const GroupInfo* groups,
                            const uint32_t* list, const uint32_t* list_count, uint32_t max_groups,
                            uint64_t* emu_begin, uint64_t* emu_end, uint32_t* emu_count,
-                           uint32_t* work, int num_sms, cudaStream_t s) {
+                           uint32_t* scratch_a, uint32_t* scratch_b, uint32_t* scratch_c,
+                           uint64_t nhits, uint32_t* work, int num_sms, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(emu_count, 0, 4, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(work, 0, 4, s);
   if (e != cudaSuccess || max_groups == 0) return e;
@@ -510,7 +619,8 @@ cudaError_t group_ext_sort(uint64_t* keys, uint32_t* vals, const GroupInfo* grou
   allow_smem(group_sort_kernel, sizeof(GroupSmem));
   count_launch();
   group_sort_kernel<<<grid, kGroupBlock, sizeof(GroupSmem), s>>>(
-      keys, vals, groups, list, list_count, emu_begin, emu_end, emu_count, work);
+      keys, vals, groups, list, list_count, emu_begin, emu_end, emu_count,
+      GroupScratch{scratch_a, scratch_b, scratch_c, scratch_c + nhits}, work);
   return cudaGetLastError();
 }
 

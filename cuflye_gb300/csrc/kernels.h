@@ -56,6 +56,7 @@ struct DeviceIndex {
   uint64_t* pos = nullptr;       // (dense id << 32) | stored position, bucket order
   uint64_t npos = 0;
   int32_t* slot_len = nullptr;   // target length per dense slot
+  int64_t* slot_signed = nullptr;  // signed id per dense slot
   uint32_t nslots = 0;
   uint64_t nkeys = 0, nrep = 0;
 };
@@ -187,10 +188,13 @@ cudaError_t sort_stats_add(uint64_t* stats, int i_plain, int i_emul, const uint3
 // Ext-pos re-sort of the groups list[0 .. *list_count) (out: key = ext pos,
 // val = cur pos); groups with equal ext positions or over kGroupCap elements
 // are listed for segmented_std_sort instead.
+// scratch_a and scratch_b hold nhits words each, scratch_c 2 * nhits (groups
+// beyond shared memory sort there).
 cudaError_t group_ext_sort(uint64_t* keys, uint32_t* vals, const GroupInfo* groups,
                            const uint32_t* list, const uint32_t* list_count, uint32_t max_groups,
                            uint64_t* emu_begin, uint64_t* emu_end, uint32_t* emu_count,
-                           uint32_t* work, int num_sms, cudaStream_t s);
+                           uint32_t* scratch_a, uint32_t* scratch_b, uint32_t* scratch_c,
+                           uint64_t nhits, uint32_t* work, int num_sms, cudaStream_t s);
 
 // Groups (runs of one ext id within a query's sorted hits) in two passes
 // over tiles of kGroupTile hits: counts per tile, then (after an exclusive
@@ -265,5 +269,8 @@ cudaError_t rows_scatter(const OverlapRow* pool, uint32_t npool, const uint32_t*
                          const uint64_t* kept_off, OverlapRow* rows, cudaStream_t s);
 cudaError_t query_group_offsets(const GroupInfo* groups, uint64_t ngroups, uint32_t nq,
                                 uint64_t* q_group_off, cudaStream_t s);
+// Rows of each query after compaction: out[q] = kept_off[qg[q + 1]] - kept_off[qg[q]].
+cudaError_t query_row_counts(const uint64_t* q_group_off, const uint64_t* kept_off, uint32_t nq,
+                             uint64_t* out, cudaStream_t s);
 
 }  // namespace cuflye

@@ -14,6 +14,7 @@
 // Every partition is a single pass: L stoppers get ranks from the left, R
 // stoppers left ranks too (the k-th R stopper from the right is the
 // (TR - k)-th from the left), so a partition reads its keys once.
+#include <algorithm>
 #include <cstdint>
 
 #include "common.cuh"
@@ -425,14 +426,9 @@ __device__ void cta_sort(CtaSmem& sm, uint32_t n, int depth0) {
     if (lane == 0) t = atomicAdd(&sm.next, 1);
     t = __shfl_sync(0xffffffffu, t, 0);
     if (t >= nt) break;
-    const uint32_t f = sm.tf[t], l = sm.tl[t];
-    const int d = sm.td[t];
-    if (d == 0) {
-      if (lane == 0) isort::heap_sort(sm.K, sm.V, f, l);
-      __syncwarp();
-    } else {
-      warp_subtree_sort(sm.K, sm.V, sm.Lr, sm.Rr, f, l, d, sm.leaves[warp]);
-    }
+    // a spent budget heap-sorts only ranges above 16 elements; shorter ones
+    // are leaves, as in libstdc++'s loop (warp_subtree_sort checks in that order)
+    warp_subtree_sort(sm.K, sm.V, sm.Lr, sm.Rr, sm.tf[t], sm.tl[t], sm.td[t], sm.leaves[warp]);
   }
   __syncthreads();
 }
@@ -640,26 +636,252 @@ __global__ void __launch_bounds__(kBlock, 3) sort_tasks(uint64_t* K, uint32_t* V
 }
 
 // Heapsorts the tasks longer than kCap (ranges whose introsort depth ran out
-// in the global phase), one CTA per task: the range is loaded into shared
-// memory, the heap is built level by level (sibling subtrees are disjoint, so
-// building a level in parallel equals libstdc++'s right-to-left order), then
-// one thread pops it.  Ranges beyond kHeapCap are heap-sorted in place.
+// in the global phase), one CTA per task, as libstdc++'s make_heap and
+// sort_heap do: the heap is built level by level (sibling subtrees are
+// disjoint, so building a level in parallel equals libstdc++'s right-to-left
+// order), then one thread pops it.
+//
+// Packed form (ranges of up to kPackCap elements whose keys span at most 47
+// bits): the heap only compares keys, so each key is replaced by its dense
+// rank among the range's keys (found by an LSD radix sort of
+// (key - min) << 16 | position, in the range's own key slots and the two
+// scratch maps), and the heap holds 4-byte words rank << 16 | position in
+// shared memory, a node's two children in one 8-byte word.  The sorted keys
+// are the radix sort's; the heap gives the order of the positions, so the
+// values are gathered by it.  Other ranges: 12-byte entries in shared memory
+// up to kHeapCap, beyond that in place in device memory.
 constexpr uint32_t kHeapCap = 18432;
-constexpr int kHeapBlock = 256;
-constexpr size_t kHeapSmem = kHeapCap * (sizeof(uint64_t) + sizeof(uint32_t));
+constexpr uint32_t kPackCap = 57344;
+constexpr int kHeapBlock = 512;
+constexpr int kHeapWarps = kHeapBlock / 32;
+constexpr size_t kHeapSmem =
+    std::max<size_t>(kHeapCap * (sizeof(uint64_t) + sizeof(uint32_t)), (kPackCap + 2) * 4);
+
+// key(a) < key(b) for packed words rank << 16 | position
+__device__ __forceinline__ bool rank_less(uint32_t a, uint32_t b) {
+  return (a | 0xffffu) < (b & 0xffff0000u);
+}
+
+// libstdc++ __adjust_heap on packed words; node x lives at E[x + 1], so the
+// children 2x + 1 and 2x + 2 of x share one 8-byte word.
+__device__ __forceinline__ void packed_adjust(uint32_t* E, uint32_t hole, uint32_t len,
+                                              uint32_t v) {
+  const uint32_t top = hole;
+  uint32_t child = hole;
+  const uint32_t lim = len > 2 ? (len - 1) / 2 : 0;
+  while (child < lim) {
+    child = 2 * (child + 1);
+    const uint2 pr = *reinterpret_cast<const uint2*>(E + child);  // nodes child - 1, child
+    uint32_t c = pr.y;
+    if (rank_less(pr.y, pr.x)) {
+      --child;
+      c = pr.x;
+    }
+    E[hole + 1] = c;
+    hole = child;
+  }
+  if ((len & 1u) == 0 && len >= 2 && child == (len - 2) / 2) {
+    child = 2 * (child + 1);
+    E[hole + 1] = E[child];
+    hole = child - 1;
+  }
+  while (hole > top) {
+    const uint32_t parent = (hole - 1) / 2;
+    const uint32_t pv = E[parent + 1];
+    if (!rank_less(pv, v)) break;
+    E[hole + 1] = pv;
+    hole = parent;
+  }
+  E[hole + 1] = v;
+}
+
+struct HeapShared {
+  uint32_t kmin_hi, kmin_lo, kmax_hi, kmax_lo;
+  uint32_t carry;
+  uint32_t ws[kHeapWarps];
+};
+
+__device__ __forceinline__ uint64_t heap_pair_load(const uint64_t* K, const uint32_t* hi,
+                                                   const uint32_t* lo, bool in_keys, uint64_t i) {
+  return in_keys ? K[i] : ((static_cast<uint64_t>(hi[i]) << 32) | lo[i]);
+}
+
+__device__ __forceinline__ void heap_pair_store(uint64_t* K, uint32_t* hi, uint32_t* lo,
+                                                bool in_keys, uint64_t i, uint64_t x) {
+  if (in_keys) {
+    K[i] = x;
+  } else {
+    hi[i] = static_cast<uint32_t>(x >> 32);
+    lo[i] = static_cast<uint32_t>(x);
+  }
+}
+
+// The packed heapsort of K/V[f, f + n); Lg and Rg are free at f.. f + n.
+__device__ void packed_heap_sort(uint64_t* K, uint32_t* V, uint32_t* Lg, uint32_t* Rg, uint64_t f,
+                                 uint32_t n, uint64_t kmin, int kb, uint32_t* E, HeapShared& hs) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t lt = (1u << lane) - 1u;
+  for (uint32_t j = threadIdx.x; j < n; j += kHeapBlock)
+    K[f + j] = ((K[f + j] - kmin) << 16) | j;
+  // LSD radix sort on the key bits; counters in the heap's space until the heap
+  uint32_t (*wc)[256] = reinterpret_cast<uint32_t (*)[256]>(E);
+  uint32_t* dbase = E + kHeapWarps * 256;
+  uint32_t* dws = dbase + 256;
+  const uint32_t per_warp = (((n + 31) / 32 + kHeapWarps - 1) / kHeapWarps) * 32;
+  const uint32_t w0 = min(n, warp * per_warp);
+  const uint32_t w1 = min(n, w0 + per_warp);
+  bool in_keys = true;
+  for (int shift = 16; shift < 16 + kb; shift += 8) {
+    for (int i = threadIdx.x; i < kHeapWarps * 256; i += kHeapBlock) (&wc[0][0])[i] = 0;
+    __syncthreads();
+    for (uint32_t r0 = w0; r0 < w1; r0 += 32) {
+      const uint32_t j = r0 + lane;
+      const bool valid = j < w1;
+      const uint32_t d =
+          valid ? static_cast<uint32_t>(heap_pair_load(K, Rg, Lg, in_keys, f + j) >> shift) & 0xffu
+                : 256u;
+      const uint32_t peers = __match_any_sync(0xffffffffu, d);
+      if (valid && lane == __ffs(peers) - 1) wc[warp][d] += __popc(peers);
+      __syncwarp();
+    }
+    __syncthreads();
+    // warp-major prefix within each digit, then digit bases
+    uint32_t tot = 0;
+    if (threadIdx.x < 256) {
+      for (int w = 0; w < kHeapWarps; ++w) {
+        const uint32_t c = wc[w][threadIdx.x];
+        wc[w][threadIdx.x] = tot;
+        tot += c;
+      }
+    }
+    uint32_t inc = tot;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += u;
+    }
+    if (lane == 31 && warp < 8) dws[warp] = inc;
+    __syncthreads();
+    if (threadIdx.x < 256) {
+      uint32_t before = 0;
+      for (int w = 0; w < warp; ++w) before += dws[w];
+      dbase[threadIdx.x] = before + inc - tot;
+    }
+    __syncthreads();
+    for (uint32_t r0 = w0; r0 < w1; r0 += 32) {
+      const uint32_t j = r0 + lane;
+      const bool valid = j < w1;
+      const uint64_t x = valid ? heap_pair_load(K, Rg, Lg, in_keys, f + j) : 0;
+      const uint32_t d = valid ? static_cast<uint32_t>(x >> shift) & 0xffu : 256u;
+      const uint32_t peers = __match_any_sync(0xffffffffu, d);
+      const uint32_t base = valid ? dbase[d] + wc[warp][d] : 0u;
+      __syncwarp();
+      if (valid && lane == __ffs(peers) - 1) wc[warp][d] += __popc(peers);
+      __syncwarp();
+      if (valid) heap_pair_store(K, Rg, Lg, !in_keys, f + base + __popc(peers & lt), x);
+    }
+    __syncthreads();
+    in_keys = !in_keys;
+  }
+  if (!in_keys) {
+    for (uint32_t j = threadIdx.x; j < n; j += kHeapBlock)
+      K[f + j] = heap_pair_load(K, Rg, Lg, false, f + j);
+    __syncthreads();
+  }
+  // dense ranks in sorted order, stored at each element's position
+  if (threadIdx.x == 0) hs.carry = 0;
+  __syncthreads();
+  for (uint32_t c0 = 0; c0 < n; c0 += kHeapBlock) {
+    const uint32_t i = c0 + threadIdx.x;
+    const bool valid = i < n;
+    const uint64_t sv = valid ? K[f + i] : 0;
+    const bool step = valid && i > 0 && (sv >> 16) != (K[f + i - 1] >> 16);
+    const unsigned bal = __ballot_sync(0xffffffffu, step);
+    if (lane == 0) hs.ws[warp] = __popc(bal);
+    __syncthreads();
+    uint32_t before = hs.carry;
+    for (int w = 0; w < warp; ++w) before += hs.ws[w];
+    const uint32_t rank = before + __popc(bal & (lt | (1u << lane)));
+    if (valid) {
+      const uint32_t pos = static_cast<uint32_t>(sv & 0xffffu);
+      E[pos + 1] = (rank << 16) | pos;
+    }
+    __syncthreads();
+    if (threadIdx.x == kHeapBlock - 1) hs.carry = rank;
+    __syncthreads();
+  }
+  // make_heap, deepest level of parents first
+  const uint32_t last_parent = (n - 2) / 2;
+  for (int lv = 31 - __clz(last_parent + 1); lv >= 0; --lv) {
+    const uint32_t lo = (1u << lv) - 1u;
+    const uint32_t hi = min((2u << lv) - 2u, last_parent);
+    for (uint32_t p = lo + threadIdx.x; p <= hi; p += kHeapBlock)
+      packed_adjust(E, p, n, E[p + 1]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    for (uint32_t last = n - 1; last >= 1; --last) {
+      const uint32_t v = E[last + 1];
+      E[last + 1] = E[1];
+      packed_adjust(E, 0, last, v);
+    }
+  }
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < n; i += kHeapBlock) {
+    K[f + i] = kmin + (K[f + i] >> 16);
+    Lg[f + i] = V[f + (E[i + 1] & 0xffffu)];
+  }
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < n; i += kHeapBlock) V[f + i] = Lg[f + i];
+  __syncthreads();
+}
 
 __global__ void __launch_bounds__(kHeapBlock, 1) sort_heaps(uint64_t* K, uint32_t* V,
+                                                         uint32_t* Lg, uint32_t* Rg,
                                                          const uint64_t* __restrict__ task_f,
                                                          const uint32_t* __restrict__ task_n,
                                                          const uint32_t* __restrict__ task_count) {
   extern __shared__ __align__(16) unsigned char heap_raw[];
+  __shared__ HeapShared hs;
   uint64_t* hk = reinterpret_cast<uint64_t*>(heap_raw);
   uint32_t* hv = reinterpret_cast<uint32_t*>(hk + kHeapCap);
+  uint32_t* E = reinterpret_cast<uint32_t*>(heap_raw);
   const uint32_t cnt = *task_count;
   for (uint32_t i = blockIdx.x; i < cnt; i += gridDim.x) {
     const uint32_t n = task_n[i];
     if (n <= kCap) continue;
     const uint64_t f = task_f[i];
+    // key span
+    if (threadIdx.x == 0) {
+      hs.kmin_hi = hs.kmin_lo = 0xffffffffu;
+      hs.kmax_hi = hs.kmax_lo = 0;
+    }
+    __syncthreads();
+    uint64_t lmin = ~0ull, lmax = 0;
+    for (uint32_t j = threadIdx.x; j < n; j += kHeapBlock) {
+      const uint64_t k = K[f + j];
+      lmin = min(lmin, k);
+      lmax = max(lmax, k);
+    }
+    // 64-bit min / max as (hi, lo) under one lock-free pass: hi first, then lo
+    // among the threads holding the extreme hi
+    atomicMin(&hs.kmin_hi, static_cast<uint32_t>(lmin >> 32));
+    atomicMax(&hs.kmax_hi, static_cast<uint32_t>(lmax >> 32));
+    __syncthreads();
+    if (static_cast<uint32_t>(lmin >> 32) == hs.kmin_hi)
+      atomicMin(&hs.kmin_lo, static_cast<uint32_t>(lmin));
+    if (static_cast<uint32_t>(lmax >> 32) == hs.kmax_hi)
+      atomicMax(&hs.kmax_lo, static_cast<uint32_t>(lmax));
+    __syncthreads();
+    const uint64_t kmin = (static_cast<uint64_t>(hs.kmin_hi) << 32) | hs.kmin_lo;
+    const uint64_t kmax = (static_cast<uint64_t>(hs.kmax_hi) << 32) | hs.kmax_lo;
+    const uint64_t span = kmax - kmin;
+    const int kb = span ? 64 - __clzll(span) : 0;
+    __syncthreads();
+    if (n <= kPackCap && kb <= 47) {
+      packed_heap_sort(K, V, Lg, Rg, f, n, kmin, kb, E, hs);
+      continue;
+    }
     if (n > kHeapCap) {
       if (threadIdx.x == 0) isort::heap_sort(K + f, V + f, 0, n);
       __syncthreads();
@@ -748,7 +970,8 @@ cudaError_t segmented_std_sort(uint64_t* keys, uint32_t* vals, uint32_t* lscratc
   sort_tasks<<<num_sms * 3, kBlock, sizeof(CtaSmem), stream>>>(keys, vals, tasks.f, tasks.n, tasks.d,
                                                            counts + 4);
   count_launch();
-  sort_heaps<<<num_sms, kHeapBlock, kHeapSmem, stream>>>(keys, vals, tasks.f, tasks.n, counts + 4);
+  sort_heaps<<<num_sms, kHeapBlock, kHeapSmem, stream>>>(keys, vals, lscratch, rscratch, tasks.f,
+                                                        tasks.n, counts + 4);
   return cudaGetLastError();
 }
 

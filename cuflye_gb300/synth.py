@@ -269,3 +269,52 @@ def tandem_case(seed: int, genome_len: int = 80_000, coverage: float = 8.0, arra
                          0.002, 0.0005, 0.0005)
     return Workload(f"tandem-{seed}", k, reads, min_freq=2, max_freq=int(5 * coverage),
                     params=dict(OVERLAP_PARAMS, kmer_size=k), seed=seed)
+
+
+@dataclass
+class ServingWorkload:
+    k: int
+    targets: ReadSet  # the genome in 1 Mb pieces (ids 1..n), the served index
+    queries: ReadSet  # query pool, ids from 1,000,001
+    min_freq: int
+    max_freq: int
+    params: dict
+
+
+def serving_workload(seed: int = 4, genome_len: int = 100_000_000, n_queries: int = 2000,
+                     piece: int = 1_000_000, k: int = 15) -> ServingWorkload:
+    """100 Mb genome with 5 % interspersed repeats (families of 2-8 kb, copies at
+    1-3 % divergence), indexed as 1 Mb pieces; queries log-uniform 1-100 kb, half
+    HiFi-like (1 % error) and half ONT-like (8 %), from random positions and
+    strands."""
+    rng = np.random.default_rng(seed)
+    genome = random_genome(rng, genome_len)
+    placed = 0
+    while placed < 0.05 * genome_len:
+        fam = random_genome(rng, int(rng.integers(2_000, 8_001)))
+        for _ in range(int(rng.integers(3, 12))):
+            pos = int(rng.integers(0, genome_len - len(fam)))
+            copy = mutate(rng, fam, float(rng.uniform(0.01, 0.03)))[:genome_len - pos]
+            genome[pos:pos + len(copy)] = copy
+            placed += len(copy)
+    npieces = (genome_len + piece - 1) // piece
+    targets = ReadSet.from_strings(np.arange(1, npieces + 1),
+                                   [genome[i * piece:(i + 1) * piece].tobytes()
+                                    for i in range(npieces)])
+    lens = np.exp(rng.uniform(np.log(1_000), np.log(100_000), n_queries)).astype(np.int64)
+    seqs = []
+    for i in range(n_queries):
+        ln = int(min(lens[i], genome_len))
+        s = int(rng.integers(0, genome_len - ln + 1))
+        q = genome[s:s + ln]
+        if rng.random() < 0.5:
+            q = revcomp(q)
+        if rng.random() < 0.5:
+            q = mutate(rng, q, 0.005, 0.0025, 0.0025)
+        else:
+            q = mutate(rng, q, 0.03, 0.025, 0.025)
+        seqs.append(q.tobytes())
+    queries = ReadSet.from_strings(np.arange(1_000_001, 1_000_001 + n_queries), seqs)
+    return ServingWorkload(k, targets, queries, min_freq=1, max_freq=32,
+                           params=dict(OVERLAP_PARAMS, kmer_size=k, check_overhang=0,
+                                       only_max_ext=0))

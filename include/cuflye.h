@@ -39,7 +39,8 @@ typedef enum cuflye_status {
   CUFLYE_ERR_CUDA = 4,        /* CUDA runtime error                          */
   CUFLYE_ERR_CAPACITY = 5,    /* caller buffer too small; counts written     */
   CUFLYE_ERR_TIMEOUT = 6,     /* a bounded device wait expired               */
-  CUFLYE_ERR_NO_INDEX = 7     /* call needs an index; none built             */
+  CUFLYE_ERR_NO_INDEX = 7,    /* call needs an index; none built             */
+  CUFLYE_PENDING = 8          /* serving: the request is not finished yet    */
 } cuflye_status;
 
 typedef struct cuflye_ctx cuflye_ctx;
@@ -255,6 +256,45 @@ cuflye_status cuflye_std_sort_segments(cuflye_ctx* ctx, uint64_t* keys, uint32_t
 cuflye_status cuflye_std_sort_segments_noalloc(uint64_t* keys, uint32_t* values,
                                                const uint64_t* seg_offsets, size_t n_segments,
                                                size_t n_elements, void* stream);
+
+/* --------------------------------------------------------------------------
+ * Serving: continuous batching of overlap requests on the owner's device.
+ * The cuflye_submit / cuflye_poll pair of the C-ABI the reference's worker
+ * protocol stands in for (docs/abi/cuda-overlap-worker-protocol-v0.md:30-142,
+ * file-backed requests and responses); no in-process counterpart exists in
+ * the reference.
+ *
+ * cuflye_server_open borrows `owner`'s resident index (the owner must keep it
+ * and stay open until cuflye_server_close) and starts `workers` (1-8) worker
+ * contexts, each with its own stream and device arena; the owner's budget
+ * left over (or the free device memory less 8 GiB when unbounded) is split
+ * between them.  A worker that falls idle takes every request that has
+ * arrived, up to max_batch_bases query bases (0 = no limit), and runs them
+ * as one batch with `params`; requests arriving meanwhile go to the next
+ * idle worker, so batches overlap on the device.  A request's rows are the
+ * rows cuflye_overlaps gives for its queries alone, in the same order.
+ *
+ * cuflye_submit copies the request (queries as for cuflye_overlaps) and
+ * returns a ticket.  cuflye_poll waits up to wait_ms (negative: until done,
+ * 0: no wait) and returns CUFLYE_PENDING, the request's error, or its rows;
+ * with too small a capacity it returns CUFLYE_ERR_CAPACITY and the row count,
+ * and keeps the result for a retry.  A finished ticket is consumed by the
+ * poll that returns its rows or its error.
+ * ------------------------------------------------------------------------ */
+typedef struct cuflye_server cuflye_server;
+
+cuflye_status cuflye_server_open(cuflye_ctx* owner, int workers,
+                                 const cuflye_overlap_params* params, uint64_t max_batch_bases,
+                                 cuflye_server** out);
+cuflye_status cuflye_submit(cuflye_server* server, size_t n, const int64_t* query_ids,
+                            const int64_t* offsets, const char* bases, uint64_t* ticket);
+cuflye_status cuflye_poll(cuflye_server* server, uint64_t ticket, int wait_ms,
+                          cuflye_overlap_range* out, size_t out_cap, size_t* n_out);
+/* Batches run so far, requests they carried, requests waiting. */
+cuflye_status cuflye_server_stats(cuflye_server* server, uint64_t* batches, uint64_t* requests,
+                                  uint64_t* pending);
+const char* cuflye_server_last_error(cuflye_server* server);
+void cuflye_server_close(cuflye_server* server);
 
 /* --------------------------------------------------------------------------
  * Timing of the last call's device work (CUDA events on the context's

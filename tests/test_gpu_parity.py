@@ -128,6 +128,32 @@ def test_equal_keys_take_the_libstdcxx_paths(gpu, oracle_mod, seed):
         assert seen[key] > 0, seen
 
 
+def test_long_reads_against_long_targets(gpu, oracle_mod):
+    """Reads of up to 100 kb against 1 Mb target pieces with interspersed
+    repeats: a read's group on its own piece holds tens of thousands of hits,
+    out of ext-pos order (repeat and random hits), which takes the device-scratch
+    ext re-sort, or the heap ranges of the emulated introsort where ext
+    positions repeat; singletons and short chains tie on score in every group.
+    Rows bit-exact with the oracle."""
+    from cuflye_gb300 import synth
+    from cuflye_gb300.backend import OverlapParams
+    oracle_mod.set_stable(False)
+    sw = synth.serving_workload(seed=5, genome_len=2_000_000, n_queries=60)
+    lens = np.diff(sw.queries.offsets)
+    q = sw.queries.subset(np.sort(np.argsort(lens)[-8:]))
+    assert int(np.diff(q.offsets).min()) > 40_000
+    idx, _ = oracle_index(oracle_mod, sw.targets, sw.k, sw.min_freq, sw.max_freq)
+    gpu.build_index(sw.targets, sw.k, sw.min_freq, sw.max_freq)
+    b = oracle_mod.SeqBatch(q.ids, q.offsets, q.bases.tobytes())
+    for variant in ({}, {"only_max_ext": 1}):
+        params = dict(sw.params, **variant)
+        got = gpu.overlaps(q, OverlapParams.make(**params))
+        exp = oracle_mod.overlaps(idx, b, oracle_mod.default_params(**params))
+        assert overlap_tuples_gpu(got) == overlap_tuples_oracle(exp), variant
+        assert len(got) > 0
+        assert gpu.last_sort_stats()["ext_plain"] > 0
+
+
 @pytest.mark.parametrize("case", ["ovl-a", "ovl-d"])
 def test_overlaps_match_reference_tool_output(gpu, golden_cases, case):
     """Against tools/replay_read_to_graph_source_pack.py's rows (committed)."""
@@ -182,6 +208,26 @@ def test_std_sort_many_segments(gpu, oracle_mod):
         a, b = int(offs[s]), int(offs[s + 1])
         ek, ev = oracle_mod.std_sort_u64(keys[a:b], vals[a:b])
         assert np.array_equal(k2[a:b], ek) and np.array_equal(v2[a:b], ev), s
+
+
+@pytest.mark.parametrize("n,scale", [(20_000, 1), (200_000, 1), (200_000, 1 << 41),
+                                     (300_000, 1)])
+def test_heap_fallback_ranges_match_libstdcxx(gpu, oracle_mod, n, scale):
+    """Organ-pipe keys (every value twice) drive libstdc++'s introsort into
+    heapsort on ranges of 4k-95k elements: n = 200,000 gives heap ranges of
+    47,105, 42,183, 21,505 and 12,089 elements, n = 300,000 one of 95,233.
+    The heap's order among equal keys must match; keys spanning more than 47
+    bits (scale 2**41) take the 12-byte heap instead of the rank-packed one.
+    n = 20,000 spends its recursion budget inside a block-wide partition of a
+    shared-memory task, leaving leaves of 12 and 16 elements at depth 0 that
+    libstdc++ insertion-sorts rather than heap-sorts."""
+    i = np.arange(n, dtype=np.uint64)
+    keys = np.where(i < n // 2, i, n - i).astype(np.uint64) * np.uint64(scale)
+    vals = np.random.default_rng(n).permutation(n).astype(np.uint32)
+    k2, v2 = gpu.std_sort_segments(keys, vals, [0, n])
+    ek, ev = oracle_mod.std_sort_u64(keys, vals)
+    assert np.array_equal(k2, ek)
+    assert np.array_equal(v2, ev)
 
 
 def test_sorted_and_presorted_inputs(gpu, oracle_mod):
