@@ -602,7 +602,8 @@ ChainParams to_chain_params(const cuflye_overlap_params* p) {
 SortTasks sort_tasks(cuflye_ctx* c, const std::string& prefix, uint64_t nelems, uint32_t nseg) {
   const uint64_t w = segsort_task_words(nelems, nseg);
   return SortTasks{buf<uint64_t>(c, prefix + "_tf", w), buf<uint32_t>(c, prefix + "_tn", w),
-                   buf<int>(c, prefix + "_td", w)};
+                   buf<int>(c, prefix + "_td", w), static_cast<uint32_t>(w),
+                   segsort_pair_reserve(nelems)};
 }
 
 // Sort + chaining of the pass's hits; returns the number of overlap rows left
@@ -615,7 +616,7 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp,
   uint32_t* lscr = buf<uint32_t>(c, "s_l", H + 1);
   uint32_t* rscr = buf<uint32_t>(c, "s_r", H + 1);
   uint32_t* lists = buf<uint32_t>(c, "s_lists", 4ull * std::max<uint64_t>(nq, 1));
-  uint32_t* scounts = buf<uint32_t>(c, "s_counts", 8);
+  uint32_t* scounts = buf<uint32_t>(c, "s_counts", 16);
   uint32_t* ecount = buf<uint32_t>(c, "s_ecount", 1);
   uint64_t* sstats = buf<uint64_t>(c, "x_sortstats", kSortStats);
   CUFLYE_CHECK(cudaMemsetAsync(sstats, 0, kSortStats * 8, st));
@@ -1165,7 +1166,7 @@ cuflye_status cuflye_read_to_graph(cuflye_ctx* c, size_t n, const int64_t* ids,
     uint32_t* sl = buf<uint32_t>(c, "r_sl", A + 1);
     uint32_t* sr = buf<uint32_t>(c, "r_sr", A + 1);
     uint32_t* slists = buf<uint32_t>(c, "r_slists", 4ull * nq);
-    uint32_t* scounts = buf<uint32_t>(c, "r_scounts", 8);
+    uint32_t* scounts = buf<uint32_t>(c, "r_scounts", 16);
     CUFLYE_CHECK(segmented_std_sort(skeys, svals, sl, sr, d_aoff, d_aoff + 1, nq, nullptr, slists,
                                     scounts, c->num_sms, st, sort_tasks(c, "r", A, nq)));
     OverlapRow* sorted = buf<OverlapRow>(c, "r_sorted", A);
@@ -1237,7 +1238,7 @@ cuflye_status cuflye_std_sort_segments(cuflye_ctx* c, uint64_t* keys, uint32_t* 
   uint32_t* dr = buf<uint32_t>(c, "t_r", m + 1);
   uint64_t* off = buf<uint64_t>(c, "t_off", n_segments + 1);
   uint32_t* lists = buf<uint32_t>(c, "t_lists", 4 * n_segments);
-  uint32_t* counts = buf<uint32_t>(c, "t_counts", 8);
+  uint32_t* counts = buf<uint32_t>(c, "t_counts", 16);
   std::vector<uint64_t> rel(n_segments + 1);
   for (size_t s = 0; s <= n_segments; ++s) rel[s] = seg_offsets[s] - base;
   CUFLYE_CHECK(cudaMemcpyAsync(dk, keys + base, m * 8, cudaMemcpyHostToDevice, st));

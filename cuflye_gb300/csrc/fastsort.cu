@@ -19,10 +19,10 @@
 // * Ext-pos re-sort of ext-sorted groups
 //   (tools/replay_read_to_graph_source_pack.py:396-397) that are not already
 //   in strict ext-pos order.  One block sorts the group, in shared memory up
-//   to kGroupCap elements (radix sort on (ext pos, index) packed in 32 bits),
-//   beyond that in device scratch (the same radix sort on separate key and
-//   index arrays), and compares neighbours; a group with equal ext positions
-//   is written out in the layout sort.cu expects and listed for it.
+//   to kGroupCap elements when (ext pos - min, index) packs in 32 bits, else in
+//   device scratch (the same radix sort on separate key and index arrays),
+//   and compares neighbours; a group with equal ext positions is written out
+//   in the layout sort.cu expects and listed for it.
 #include <algorithm>
 #include <climits>
 #include <cstdint>
@@ -475,8 +475,9 @@ __global__ void __launch_bounds__(kGroupBlock, 1)
     const uint32_t kmin = sm.kmin, range = sm.kmax - sm.kmin;
     const int kb = range ? 32 - __clz(range) : 0;
     const int ib = n > 1 ? 32 - __clz(n - 1) : 0;
-    if (kb + ib > 32) {  // the packed form does not fit: leave it to sort.cu
-      group_to_emulation(keys, vals, g, emu_begin, emu_end, emu_count);
+    if (kb + ib > 32) {  // the packed form does not fit: separate keys and indices
+      __syncthreads();     // every thread has read kmin / kmax before they are reset
+      group_sort_global(keys, vals, g, sc, sm, emu_begin, emu_end, emu_count);
       __syncthreads();
       continue;
     }

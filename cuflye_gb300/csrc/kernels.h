@@ -25,13 +25,19 @@ cudaError_t exclusive_scan_u64(const uint64_t* in, uint64_t* out, uint64_t n, ui
 size_t segsort_smem_bytes();
 // Task list handed from the global phase of large segments to the
 // shared-memory phase: segsort_task_words(n, nseg) entries each.
+// Longest heap range one block sorts in its own shared memory; longer ones
+// take a block pair.
+constexpr uint32_t kHeapPackCap = 57344;
 struct SortTasks {
   uint64_t* f;
   uint32_t* n;
   int* d;
+  uint32_t cap;           // entries of f, n and d (segsort_task_words)
+  uint32_t pair_reserve;  // top entries kept for heap ranges beyond kHeapPackCap
 };
+uint32_t segsort_pair_reserve(uint64_t nelems);
 size_t segsort_task_words(uint64_t nelems, uint32_t nseg);
-// lists: 4 * nseg words; counts: 5 words.  l/r scratch: one word per element.
+// lists: 4 * nseg words; counts: 16 words.  l/r scratch: one word per element.
 // nseg_dev (optional) holds the live segment count on the device (<= nseg).
 cudaError_t segmented_std_sort(uint64_t* keys, uint32_t* vals, uint32_t* lscratch,
                                uint32_t* rscratch, const uint64_t* begin, const uint64_t* end,

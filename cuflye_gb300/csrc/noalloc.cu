@@ -42,7 +42,7 @@ constexpr size_t kOffL = 0;
 constexpr size_t kOffR = align256(kOffL + 4 * (kMaxElems + 1));
 constexpr size_t kOffLists = align256(kOffR + 4 * (kMaxElems + 1));
 constexpr size_t kOffCounts = align256(kOffLists + 4 * 4 * kMaxSegs);
-constexpr size_t kOffSegs = align256(kOffCounts + 4 * 8);
+constexpr size_t kOffSegs = align256(kOffCounts + 4 * 16);
 constexpr size_t kOffTf = align256(kOffSegs + 8 * (kMaxSegs + 1));
 constexpr size_t kOffTn = align256(kOffTf + 8 * kTaskCap);
 constexpr size_t kOffTd = align256(kOffTn + 4 * kTaskCap);
@@ -117,7 +117,8 @@ extern "C" cuflye_status cuflye_std_sort_segments_noalloc(uint64_t* keys, uint32
     return CUFLYE_ERR_CUDA;
   }
   SortTasks tasks{reinterpret_cast<uint64_t*>(base + kOffTf),
-                  reinterpret_cast<uint32_t*>(base + kOffTn), reinterpret_cast<int*>(base + kOffTd)};
+                  reinterpret_cast<uint32_t*>(base + kOffTn), reinterpret_cast<int*>(base + kOffTd),
+                  static_cast<uint32_t>(kTaskCap), segsort_pair_reserve(n_elements)};
   // segmented_std_sort clears its counters (the task count included) itself
   const cudaError_t e = segmented_std_sort(
       keys, values, reinterpret_cast<uint32_t*>(base + kOffL),

@@ -14,6 +14,8 @@
 // Every partition is a single pass: L stoppers get ranks from the left, R
 // stoppers left ranks too (the k-th R stopper from the right is the
 // (TR - k)-th from the left), so a partition reads its keys once.
+#include <cooperative_groups.h>
+
 #include <algorithm>
 #include <cstdint>
 
@@ -557,7 +559,9 @@ __global__ void __launch_bounds__(kBigBlock, 4) sort_big(uint64_t* K, uint32_t* 
                                                       const uint32_t* __restrict__ list,
                                                       const uint32_t* __restrict__ counts,
                                                       uint64_t* task_f, uint32_t* task_n,
-                                                      int* task_d, uint32_t* task_count) {
+                                                      int* task_d, uint32_t* task_count,
+                                                      uint32_t* heap_count, uint32_t* pair_count,
+                                                      uint32_t task_cap, uint32_t pair_reserve) {
   __shared__ BigSmem sm;
   const uint32_t cnt = counts[3];
   for (uint32_t i = blockIdx.x; i < cnt; i += gridDim.x) {
@@ -596,10 +600,13 @@ __global__ void __launch_bounds__(kBigBlock, 4) sort_big(uint64_t* K, uint32_t* 
       }
       if (d == 0) {
         // depth exhausted: libstdc++ heap-sorts the range; sort_heaps does it
-        // in shared memory (a task longer than kCap)
+        // (a task longer than kCap, listed from the top of the task arrays:
+        // ranges beyond one block's shared memory first, then the others)
         if (threadIdx.x == 0) {
           sm.gn = nt - 1;
-          const uint32_t slot = atomicAdd(task_count, 1u);
+          const uint32_t slot = l - f > kHeapPackCap
+                                    ? task_cap - 1u - atomicAdd(pair_count, 1u)
+                                    : task_cap - 1u - pair_reserve - atomicAdd(heap_count, 1u);
           task_f[slot] = b + f;
           task_n[slot] = l - f;
           task_d[slot] = 0;
@@ -636,69 +643,138 @@ __global__ void __launch_bounds__(kBlock, 3) sort_tasks(uint64_t* K, uint32_t* V
 }
 
 // Heapsorts the tasks longer than kCap (ranges whose introsort depth ran out
-// in the global phase), one CTA per task, as libstdc++'s make_heap and
-// sort_heap do: the heap is built level by level (sibling subtrees are
-// disjoint, so building a level in parallel equals libstdc++'s right-to-left
-// order), then one thread pops it.
+// in the global phase), as libstdc++'s make_heap and sort_heap do: the heap is
+// built level by level (sibling subtrees are disjoint, so building a level in
+// parallel equals libstdc++'s right-to-left order), then one thread pops it.
 //
-// Packed form (ranges of up to kPackCap elements whose keys span at most 47
-// bits): the heap only compares keys, so each key is replaced by its dense
-// rank among the range's keys (found by an LSD radix sort of
-// (key - min) << 16 | position, in the range's own key slots and the two
-// scratch maps), and the heap holds 4-byte words rank << 16 | position in
-// shared memory, a node's two children in one 8-byte word.  The sorted keys
-// are the radix sort's; the heap gives the order of the positions, so the
-// values are gathered by it.  Other ranges: 12-byte entries in shared memory
-// up to kHeapCap, beyond that in place in device memory.
+// The heap only compares keys, so each key is replaced by its dense rank among
+// the range's keys, found by an LSD radix sort of (key - min) << s | position
+// in the range's own key slots and the two scratch maps.  Heap entries are
+// 4-byte words holding the rank in the high bits:
+//   * own form (ranges of up to kPackCap elements): rank << 16 | position, in
+//     the block's shared memory;
+//   * pair form (up to kPairCap elements): rank << 15 | index within the run
+//     of equal keys, in the shared memory of a block pair (a cluster of two;
+//     the second block lends its shared memory for the deeper nodes); a run's
+//     start in sorted order maps an entry back to its position.
+// A node's two children are one 8-byte word, its four grandchildren one
+// 16-byte word.  The sorted keys are the radix sort's; the heap gives the
+// order of the positions, so the values are gathered by it.  Ranges whose
+// keys span too many bits: 12-byte entries in shared memory up to kHeapCap,
+// beyond that in place in device memory.
 constexpr uint32_t kHeapCap = 18432;
-constexpr uint32_t kPackCap = 57344;
+constexpr uint32_t kPackCap = kHeapPackCap;
+constexpr uint32_t kPairCap = 2 * kPackCap - 1;
 constexpr int kHeapBlock = 512;
 constexpr int kHeapWarps = kHeapBlock / 32;
 constexpr size_t kHeapSmem =
     std::max<size_t>(kHeapCap * (sizeof(uint64_t) + sizeof(uint32_t)), (kPackCap + 2) * 4);
 
-// key(a) < key(b) for packed words rank << 16 | position
+// key(a) < key(b) for entries rank << SH | low bits
+template <int SH>
 __device__ __forceinline__ bool rank_less(uint32_t a, uint32_t b) {
-  return (a | 0xffffu) < (b & 0xffff0000u);
+  constexpr uint32_t lo = (1u << SH) - 1u;
+  return (a | lo) < (b & ~lo);
 }
 
-// libstdc++ __adjust_heap on packed words; node x lives at E[x + 1], so the
-// children 2x + 1 and 2x + 2 of x share one 8-byte word.
-__device__ __forceinline__ void packed_adjust(uint32_t* E, uint32_t hole, uint32_t len,
-                                              uint32_t v) {
+// Node x lives at word x + 1, so the children 2x + 1 and 2x + 2 of x share
+// one 8-byte word and the grandchildren one 16-byte word.
+struct OwnHeap {
+  uint32_t* E;
+  __device__ __forceinline__ uint32_t* at(uint32_t i) const { return E + i; }
+};
+// Words from kPackCap on live in the partner block (a multiple of 8, so no
+// aligned 8- or 16-byte word straddles the two).
+struct PairHeap {
+  uint32_t* E;
+  uint32_t* E1;
+  __device__ __forceinline__ uint32_t* at(uint32_t i) const {
+    return i < kPackCap ? E + i : E1 + (i - kPackCap);
+  }
+};
+
+// libstdc++ __adjust_heap on packed entries.
+template <int SH, class H>
+__device__ __forceinline__ void packed_adjust(H h, uint32_t hole, uint32_t len, uint32_t v) {
   const uint32_t top = hole;
   uint32_t child = hole;
   const uint32_t lim = len > 2 ? (len - 1) / 2 : 0;
+  // three of libstdc++'s steps at once while every node two levels below the
+  // hole has two children: the 2 + 4 + 8 candidate nodes load together
+  while (4 * child + 6 < lim) {
+    const uint2 a = *reinterpret_cast<const uint2*>(h.at(2 * (child + 1)));
+    const uint4 b = *reinterpret_cast<const uint4*>(h.at(4 * (child + 1)));
+    const uint4 c0 = *reinterpret_cast<const uint4*>(h.at(8 * (child + 1)));
+    const uint4 c1 = *reinterpret_cast<const uint4*>(h.at(8 * (child + 1) + 4));
+    const bool s1 = !rank_less<SH>(a.y, a.x);  // the right child unless right < left
+    const uint32_t v1 = s1 ? a.y : a.x;
+    const uint32_t l2 = s1 ? b.z : b.x, r2 = s1 ? b.w : b.y;
+    const bool s2 = !rank_less<SH>(r2, l2);
+    const uint32_t v2 = s2 ? r2 : l2;
+    const uint4 cc = s1 ? c1 : c0;
+    const uint32_t l3 = s2 ? cc.z : cc.x, r3 = s2 ? cc.w : cc.y;
+    const bool s3 = !rank_less<SH>(r3, l3);
+    const uint32_t v3 = s3 ? r3 : l3;
+    const uint32_t n1 = 2 * child + 1 + s1;
+    const uint32_t n2 = 2 * n1 + 1 + s2;
+    *h.at(child + 1) = v1;
+    *h.at(n1 + 1) = v2;
+    *h.at(n2 + 1) = v3;
+    child = 2 * n2 + 1 + s3;
+  }
+  hole = child;
   while (child < lim) {
     child = 2 * (child + 1);
-    const uint2 pr = *reinterpret_cast<const uint2*>(E + child);  // nodes child - 1, child
+    const uint2 pr = *reinterpret_cast<const uint2*>(h.at(child));  // nodes child - 1, child
     uint32_t c = pr.y;
-    if (rank_less(pr.y, pr.x)) {
+    if (rank_less<SH>(pr.y, pr.x)) {
       --child;
       c = pr.x;
     }
-    E[hole + 1] = c;
+    *h.at(hole + 1) = c;
     hole = child;
   }
   if ((len & 1u) == 0 && len >= 2 && child == (len - 2) / 2) {
     child = 2 * (child + 1);
-    E[hole + 1] = E[child];
+    *h.at(hole + 1) = *h.at(child);
     hole = child - 1;
   }
   while (hole > top) {
     const uint32_t parent = (hole - 1) / 2;
-    const uint32_t pv = E[parent + 1];
-    if (!rank_less(pv, v)) break;
-    E[hole + 1] = pv;
+    const uint32_t pv = *h.at(parent + 1);
+    if (!rank_less<SH>(pv, v)) break;
+    *h.at(hole + 1) = pv;
     hole = parent;
   }
-  E[hole + 1] = v;
+  *h.at(hole + 1) = v;
+}
+
+// make_heap by levels (all threads), then sort_heap (thread 0).
+template <int SH, class H>
+__device__ void packed_heap_run(H h, uint32_t n) {
+  const uint32_t last_parent = (n - 2) / 2;
+  for (int lv = 31 - __clz(last_parent + 1); lv >= 0; --lv) {
+    const uint32_t lo = (1u << lv) - 1u;
+    const uint32_t hi = min((2u << lv) - 2u, last_parent);
+    for (uint32_t p = lo + threadIdx.x; p <= hi; p += kHeapBlock)
+      packed_adjust<SH>(h, p, n, *h.at(p + 1));
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    for (uint32_t last = n - 1; last >= 1; --last) {
+      const uint32_t v = *h.at(last + 1);
+      *h.at(last + 1) = *h.at(1);
+      packed_adjust<SH>(h, 0, last, v);
+    }
+  }
+  __syncthreads();
 }
 
 struct HeapShared {
   uint32_t kmin_hi, kmin_lo, kmax_hi, kmax_lo;
-  uint32_t carry;
+  uint32_t carry, cstart, item;
   uint32_t ws[kHeapWarps];
+  uint32_t wm[kHeapWarps];
 };
 
 __device__ __forceinline__ uint64_t heap_pair_load(const uint64_t* K, const uint32_t* hi,
@@ -716,22 +792,55 @@ __device__ __forceinline__ void heap_pair_store(uint64_t* K, uint32_t* hi, uint3
   }
 }
 
-// The packed heapsort of K/V[f, f + n); Lg and Rg are free at f.. f + n.
-__device__ void packed_heap_sort(uint64_t* K, uint32_t* V, uint32_t* Lg, uint32_t* Rg, uint64_t f,
-                                 uint32_t n, uint64_t kmin, int kb, uint32_t* E, HeapShared& hs) {
+// Smallest key and the bit span of (key - smallest) over K[f, f + n).
+__device__ void heap_key_span(const uint64_t* K, uint64_t f, uint32_t n, HeapShared& hs,
+                              uint64_t& kmin, int& kb) {
+  if (threadIdx.x == 0) {
+    hs.kmin_hi = hs.kmin_lo = 0xffffffffu;
+    hs.kmax_hi = hs.kmax_lo = 0;
+  }
+  __syncthreads();
+  uint64_t lmin = ~0ull, lmax = 0;
+  for (uint32_t j = threadIdx.x; j < n; j += kHeapBlock) {
+    const uint64_t k = K[f + j];
+    lmin = min(lmin, k);
+    lmax = max(lmax, k);
+  }
+  // 64-bit min / max as (hi, lo): hi first, then lo among the threads holding
+  // the extreme hi
+  atomicMin(&hs.kmin_hi, static_cast<uint32_t>(lmin >> 32));
+  atomicMax(&hs.kmax_hi, static_cast<uint32_t>(lmax >> 32));
+  __syncthreads();
+  if (static_cast<uint32_t>(lmin >> 32) == hs.kmin_hi)
+    atomicMin(&hs.kmin_lo, static_cast<uint32_t>(lmin));
+  if (static_cast<uint32_t>(lmax >> 32) == hs.kmax_hi)
+    atomicMax(&hs.kmax_lo, static_cast<uint32_t>(lmax));
+  __syncthreads();
+  kmin = (static_cast<uint64_t>(hs.kmin_hi) << 32) | hs.kmin_lo;
+  const uint64_t kmax = (static_cast<uint64_t>(hs.kmax_hi) << 32) | hs.kmax_lo;
+  const uint64_t span = kmax - kmin;
+  kb = span ? 64 - __clzll(span) : 0;
+  __syncthreads();
+}
+
+// K[f + j] = (K[f + j] - kmin) << sh | j, then an LSD radix sort on the key
+// bits [sh, sh + kb) (8 per pass, stable), ping-ponging with the (Rg, Lg)
+// pairs; ends with the sorted words in K.  Counters live in `scratch` (the
+// heap's shared memory, unused until the heap is built).
+__device__ void heap_radix(uint64_t* K, uint32_t* Lg, uint32_t* Rg, uint64_t f, uint32_t n,
+                           uint64_t kmin, int sh, int kb, uint32_t* scratch) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t lt = (1u << lane) - 1u;
   for (uint32_t j = threadIdx.x; j < n; j += kHeapBlock)
-    K[f + j] = ((K[f + j] - kmin) << 16) | j;
-  // LSD radix sort on the key bits; counters in the heap's space until the heap
-  uint32_t (*wc)[256] = reinterpret_cast<uint32_t (*)[256]>(E);
-  uint32_t* dbase = E + kHeapWarps * 256;
+    K[f + j] = ((K[f + j] - kmin) << sh) | j;
+  uint32_t (*wc)[256] = reinterpret_cast<uint32_t (*)[256]>(scratch);
+  uint32_t* dbase = scratch + kHeapWarps * 256;
   uint32_t* dws = dbase + 256;
   const uint32_t per_warp = (((n + 31) / 32 + kHeapWarps - 1) / kHeapWarps) * 32;
   const uint32_t w0 = min(n, warp * per_warp);
   const uint32_t w1 = min(n, w0 + per_warp);
   bool in_keys = true;
-  for (int shift = 16; shift < 16 + kb; shift += 8) {
+  for (int shift = sh; shift < sh + kb; shift += 8) {
     for (int i = threadIdx.x; i < kHeapWarps * 256; i += kHeapBlock) (&wc[0][0])[i] = 0;
     __syncthreads();
     for (uint32_t r0 = w0; r0 < w1; r0 += 32) {
@@ -786,138 +895,215 @@ __device__ void packed_heap_sort(uint64_t* K, uint32_t* V, uint32_t* Lg, uint32_
   if (!in_keys) {
     for (uint32_t j = threadIdx.x; j < n; j += kHeapBlock)
       K[f + j] = heap_pair_load(K, Rg, Lg, false, f + j);
-    __syncthreads();
   }
-  // dense ranks in sorted order, stored at each element's position
-  if (threadIdx.x == 0) hs.carry = 0;
+  __syncthreads();
+}
+
+// Runs of equal keys over the sorted words K[f, f + n) (key bits from sh
+// up): for each sorted index i its dense rank and the index where its run
+// starts; `act(i, word, rank, start, first)` is called for every i.
+template <class Act>
+__device__ void heap_runs(const uint64_t* K, uint64_t f, uint32_t n, int sh, HeapShared& hs,
+                          Act act) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t le = (2u << lane) - 1u;
+  if (threadIdx.x == 0) {
+    hs.carry = 0;
+    hs.cstart = 0;
+  }
   __syncthreads();
   for (uint32_t c0 = 0; c0 < n; c0 += kHeapBlock) {
     const uint32_t i = c0 + threadIdx.x;
     const bool valid = i < n;
-    const uint64_t sv = valid ? K[f + i] : 0;
-    const bool step = valid && i > 0 && (sv >> 16) != (K[f + i - 1] >> 16);
-    const unsigned bal = __ballot_sync(0xffffffffu, step);
-    if (lane == 0) hs.ws[warp] = __popc(bal);
-    __syncthreads();
-    uint32_t before = hs.carry;
-    for (int w = 0; w < warp; ++w) before += hs.ws[w];
-    const uint32_t rank = before + __popc(bal & (lt | (1u << lane)));
-    if (valid) {
-      const uint32_t pos = static_cast<uint32_t>(sv & 0xffffu);
-      E[pos + 1] = (rank << 16) | pos;
+    const uint64_t w = valid ? K[f + i] : 0;
+    const bool first = valid && (i == 0 || (w >> sh) != (K[f + i - 1] >> sh));
+    const unsigned bal = __ballot_sync(0xffffffffu, first);
+    uint32_t st = first ? i : 0u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, st, o);
+      if (lane >= o) st = max(st, y);
+    }
+    if (lane == 31) {
+      hs.ws[warp] = __popc(bal);
+      hs.wm[warp] = st;
     }
     __syncthreads();
-    if (threadIdx.x == kHeapBlock - 1) hs.carry = rank;
-    __syncthreads();
-  }
-  // make_heap, deepest level of parents first
-  const uint32_t last_parent = (n - 2) / 2;
-  for (int lv = 31 - __clz(last_parent + 1); lv >= 0; --lv) {
-    const uint32_t lo = (1u << lv) - 1u;
-    const uint32_t hi = min((2u << lv) - 2u, last_parent);
-    for (uint32_t p = lo + threadIdx.x; p <= hi; p += kHeapBlock)
-      packed_adjust(E, p, n, E[p + 1]);
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    for (uint32_t last = n - 1; last >= 1; --last) {
-      const uint32_t v = E[last + 1];
-      E[last + 1] = E[1];
-      packed_adjust(E, 0, last, v);
+    uint32_t count = hs.carry, start = max(hs.cstart, st);
+    for (int v = 0; v < warp; ++v) {
+      count += hs.ws[v];
+      start = max(start, hs.wm[v]);
     }
+    count += __popc(bal & le);
+    if (valid) act(i, w, count - 1u, start, first);
+    __syncthreads();
+    if (threadIdx.x == kHeapBlock - 1) {
+      hs.carry = count;
+      hs.cstart = start;
+    }
+    __syncthreads();
   }
-  __syncthreads();
+}
+
+// Own form: ranges of up to kPackCap elements whose keys span at most 47 bits.
+__device__ void own_heap_sort(uint64_t* K, uint32_t* V, uint32_t* Lg, uint32_t* Rg, uint64_t f,
+                              uint32_t n, uint64_t kmin, int kb, uint32_t* E, HeapShared& hs) {
+  heap_radix(K, Lg, Rg, f, n, kmin, 16, kb, E);
+  const OwnHeap h{E};
+  heap_runs(K, f, n, 16, hs, [&](uint32_t, uint64_t w, uint32_t rank, uint32_t, bool) {
+    const uint32_t pos = static_cast<uint32_t>(w & 0xffffu);
+    *h.at(pos + 1) = (rank << 16) | pos;
+  });
+  packed_heap_run<16>(h, n);
   for (uint32_t i = threadIdx.x; i < n; i += kHeapBlock) {
     K[f + i] = kmin + (K[f + i] >> 16);
-    Lg[f + i] = V[f + (E[i + 1] & 0xffffu)];
+    Lg[f + i] = V[f + (*h.at(i + 1) & 0xffffu)];
   }
   __syncthreads();
   for (uint32_t i = threadIdx.x; i < n; i += kHeapBlock) V[f + i] = Lg[f + i];
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(kHeapBlock, 1) sort_heaps(uint64_t* K, uint32_t* V,
-                                                         uint32_t* Lg, uint32_t* Rg,
-                                                         const uint64_t* __restrict__ task_f,
-                                                         const uint32_t* __restrict__ task_n,
-                                                         const uint32_t* __restrict__ task_count) {
+// Pair form: ranges of up to kPairCap elements whose keys span at most 46
+// bits and whose runs of equal keys are shorter than 32,768.  Returns false,
+// with K as it was, when a run is longer.
+__device__ bool pair_heap_sort(uint64_t* K, uint32_t* V, uint32_t* Lg, uint32_t* Rg, uint64_t f,
+                               uint32_t n, uint64_t kmin, int kb, PairHeap h, HeapShared& hs) {
+  heap_radix(K, Lg, Rg, f, n, kmin, 17, kb, h.E);
+  bool long_run = false;
+  heap_runs(K, f, n, 17, hs, [&](uint32_t i, uint64_t, uint32_t, uint32_t start, bool) {
+    long_run |= i - start >= 32768u;
+  });
+  if (__syncthreads_or(long_run)) {
+    // put the keys back in position order
+    for (uint32_t i = threadIdx.x; i < n; i += kHeapBlock) {
+      const uint64_t w = K[f + i];
+      heap_pair_store(K, Rg, Lg, false, f + (w & 0x1ffffu), kmin + (w >> 17));
+    }
+    __syncthreads();
+    for (uint32_t j = threadIdx.x; j < n; j += kHeapBlock)
+      K[f + j] = heap_pair_load(K, Rg, Lg, false, f + j);
+    __syncthreads();
+    return false;
+  }
+  heap_runs(K, f, n, 17, hs, [&](uint32_t i, uint64_t w, uint32_t rank, uint32_t start, bool first) {
+    if (first) Rg[f + rank] = i;
+    *h.at(static_cast<uint32_t>(w & 0x1ffffu) + 1) = (rank << 15) | (i - start);
+  });
+  packed_heap_run<15>(h, n);
+  for (uint32_t i = threadIdx.x; i < n; i += kHeapBlock) {
+    const uint32_t e = *h.at(i + 1);
+    const uint32_t s = Rg[f + (e >> 15)] + (e & 0x7fffu);
+    Lg[f + i] = V[f + static_cast<uint32_t>(K[f + s] & 0x1ffffu)];
+  }
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < n; i += kHeapBlock) K[f + i] = kmin + (K[f + i] >> 17);
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < n; i += kHeapBlock) V[f + i] = Lg[f + i];
+  __syncthreads();
+  return true;
+}
+
+// 12-byte entries in shared memory (ranges of up to kHeapCap elements).
+__device__ void wide_heap_sort(uint64_t* K, uint32_t* V, uint64_t f, uint32_t n,
+                               unsigned char* raw) {
+  uint64_t* hk = reinterpret_cast<uint64_t*>(raw);
+  uint32_t* hv = reinterpret_cast<uint32_t*>(hk + kHeapCap);
+  for (uint32_t j = threadIdx.x; j < n; j += kHeapBlock) {
+    hk[j] = K[f + j];
+    hv[j] = V[f + j];
+  }
+  __syncthreads();
+  const uint32_t last_parent = (n - 2) / 2;
+  for (int lv = 31 - __clz(last_parent + 1); lv >= 0; --lv) {
+    const uint32_t lo = (1u << lv) - 1u;
+    const uint32_t hi = min((2u << lv) - 2u, last_parent);
+    for (uint32_t p = lo + threadIdx.x; p <= hi; p += kHeapBlock)
+      isort::heap_adjust(hk, hv, 0, p, n, hk[p], hv[p]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    for (uint32_t last = n; last > 1;) {
+      --last;
+      const uint64_t vk = hk[last];
+      const uint32_t vv = hv[last];
+      hk[last] = hk[0];
+      hv[last] = hv[0];
+      isort::heap_adjust(hk, hv, 0, 0, last, vk, vv);
+    }
+  }
+  __syncthreads();
+  for (uint32_t j = threadIdx.x; j < n; j += kHeapBlock) {
+    K[f + j] = hk[j];
+    V[f + j] = hv[j];
+  }
+  __syncthreads();
+}
+
+// Heap tasks sit at the top of the task arrays: tasks longer than kPackCap
+// (pair tasks) at slot task_cap - 1 - j, the others below the pair reserve.
+// Each block pair first takes pair tasks together (the first block works,
+// the second lends its shared memory), then both blocks take the other tasks
+// one at a time from a counter (their lengths vary).
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kHeapBlock, 1)
+    sort_heaps(uint64_t* K, uint32_t* V, uint32_t* Lg, uint32_t* Rg,
+               const uint64_t* __restrict__ task_f, const uint32_t* __restrict__ task_n,
+               const uint32_t* __restrict__ heap_count, uint32_t* heap_work,
+               const uint32_t* __restrict__ pair_count, uint32_t* pair_work, uint32_t task_cap,
+               uint32_t pair_reserve) {
   extern __shared__ __align__(16) unsigned char heap_raw[];
   __shared__ HeapShared hs;
-  uint64_t* hk = reinterpret_cast<uint64_t*>(heap_raw);
-  uint32_t* hv = reinterpret_cast<uint32_t*>(hk + kHeapCap);
   uint32_t* E = reinterpret_cast<uint32_t*>(heap_raw);
-  const uint32_t cnt = *task_count;
-  for (uint32_t i = blockIdx.x; i < cnt; i += gridDim.x) {
-    const uint32_t n = task_n[i];
-    if (n <= kCap) continue;
-    const uint64_t f = task_f[i];
-    // key span
-    if (threadIdx.x == 0) {
-      hs.kmin_hi = hs.kmin_lo = 0xffffffffu;
-      hs.kmax_hi = hs.kmax_lo = 0;
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  const unsigned crank = cluster.block_rank();
+  const uint32_t npair = *pair_count;
+  for (;;) {
+    if (crank == 0 && threadIdx.x == 0) {
+      const uint32_t it = atomicAdd(pair_work, 1u);
+      hs.item = it;
+      *cluster.map_shared_rank(&hs.item, 1) = it;
     }
-    __syncthreads();
-    uint64_t lmin = ~0ull, lmax = 0;
-    for (uint32_t j = threadIdx.x; j < n; j += kHeapBlock) {
-      const uint64_t k = K[f + j];
-      lmin = min(lmin, k);
-      lmax = max(lmax, k);
-    }
-    // 64-bit min / max as (hi, lo) under one lock-free pass: hi first, then lo
-    // among the threads holding the extreme hi
-    atomicMin(&hs.kmin_hi, static_cast<uint32_t>(lmin >> 32));
-    atomicMax(&hs.kmax_hi, static_cast<uint32_t>(lmax >> 32));
-    __syncthreads();
-    if (static_cast<uint32_t>(lmin >> 32) == hs.kmin_hi)
-      atomicMin(&hs.kmin_lo, static_cast<uint32_t>(lmin));
-    if (static_cast<uint32_t>(lmax >> 32) == hs.kmax_hi)
-      atomicMax(&hs.kmax_lo, static_cast<uint32_t>(lmax));
-    __syncthreads();
-    const uint64_t kmin = (static_cast<uint64_t>(hs.kmin_hi) << 32) | hs.kmin_lo;
-    const uint64_t kmax = (static_cast<uint64_t>(hs.kmax_hi) << 32) | hs.kmax_lo;
-    const uint64_t span = kmax - kmin;
-    const int kb = span ? 64 - __clzll(span) : 0;
-    __syncthreads();
-    if (n <= kPackCap && kb <= 47) {
-      packed_heap_sort(K, V, Lg, Rg, f, n, kmin, kb, E, hs);
-      continue;
-    }
-    if (n > kHeapCap) {
-      if (threadIdx.x == 0) isort::heap_sort(K + f, V + f, 0, n);
-      __syncthreads();
-      continue;
-    }
-    for (uint32_t j = threadIdx.x; j < n; j += kHeapBlock) {
-      hk[j] = K[f + j];
-      hv[j] = V[f + j];
-    }
-    __syncthreads();
-    // parents 0 .. (n - 2) / 2, deepest level first
-    const uint32_t last_parent = (n - 2) / 2;
-    int top_level = 31 - __clz(last_parent + 1);
-    for (int lv = top_level; lv >= 0; --lv) {
-      const uint32_t lo = (1u << lv) - 1u;
-      const uint32_t hi = min((2u << lv) - 2u, last_parent);
-      for (uint32_t p = lo + threadIdx.x; p <= hi; p += kHeapBlock)
-        isort::heap_adjust(hk, hv, 0, p, n, hk[p], hv[p]);
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-      for (uint32_t last = n; last > 1;) {
-        --last;
-        const uint64_t vk = hk[last];
-        const uint32_t vv = hv[last];
-        hk[last] = hk[0];
-        hv[last] = hv[0];
-        isort::heap_adjust(hk, hv, 0, 0, last, vk, vv);
+    cluster.sync();
+    const uint32_t item = hs.item;
+    if (item >= npair) break;
+    if (crank == 0) {
+      const uint32_t i = task_cap - 1u - item;
+      const uint32_t n = task_n[i];
+      const uint64_t f = task_f[i];
+      uint64_t kmin = 0;
+      int kb = 0;
+      heap_key_span(K, f, n, hs, kmin, kb);
+      const PairHeap h{E, cluster.map_shared_rank(E, 1)};
+      const bool done = n <= kPairCap && kb <= 46 && pair_heap_sort(K, V, Lg, Rg, f, n, kmin, kb, h, hs);
+      if (!done) {
+        if (threadIdx.x == 0) isort::heap_sort(K + f, V + f, 0, n);
+        __syncthreads();
       }
     }
+    cluster.sync();
+  }
+  const uint32_t cnt = *heap_count;
+  for (;;) {
     __syncthreads();
-    for (uint32_t j = threadIdx.x; j < n; j += kHeapBlock) {
-      K[f + j] = hk[j];
-      V[f + j] = hv[j];
+    if (threadIdx.x == 0) hs.item = atomicAdd(heap_work, 1u);
+    __syncthreads();
+    const uint32_t item = hs.item;
+    if (item >= cnt) break;
+    const uint32_t i = task_cap - 1u - pair_reserve - item;
+    const uint32_t n = task_n[i];
+    const uint64_t f = task_f[i];
+    uint64_t kmin = 0;
+    int kb = 0;
+    heap_key_span(K, f, n, hs, kmin, kb);
+    if (kb <= 47) {
+      own_heap_sort(K, V, Lg, Rg, f, n, kmin, kb, E, hs);
+    } else if (n <= kHeapCap) {
+      wide_heap_sort(K, V, f, n, heap_raw);
+    } else {
+      if (threadIdx.x == 0) isort::heap_sort(K + f, V + f, 0, n);
+      __syncthreads();
     }
-    __syncthreads();
   }
 }
 
@@ -925,10 +1111,15 @@ __global__ void __launch_bounds__(kHeapBlock, 1) sort_heaps(uint64_t* K, uint32_
 
 size_t segsort_smem_bytes() { return sizeof(CtaSmem); }
 
+uint32_t segsort_pair_reserve(uint64_t nelems) {
+  return static_cast<uint32_t>(nelems / kHeapPackCap + 1);
+}
+
 size_t segsort_task_words(uint64_t nelems, uint32_t nseg) {
   // final tasks of the global phase are disjoint and come from partitions of
-  // tasks larger than kCap (at most depth_limit levels of them)
-  return nseg + 2 * (nelems / kCap + 1) * 64;
+  // tasks larger than kCap (at most depth_limit levels of them); heap tasks
+  // beyond kHeapPackCap get a reserve of their own at the top
+  return nseg + 2 * (nelems / kCap + 1) * 64 + segsort_pair_reserve(nelems);
 }
 
 cudaError_t segmented_std_sort(uint64_t* keys, uint32_t* vals, uint32_t* lscratch,
@@ -949,7 +1140,7 @@ cudaError_t segmented_std_sort(uint64_t* keys, uint32_t* vals, uint32_t* lscratc
     attr = true;
   }
   if (nseg == 0) return cudaSuccess;
-  cudaMemsetAsync(counts, 0, 5 * sizeof(uint32_t), stream);
+  cudaMemsetAsync(counts, 0, 9 * sizeof(uint32_t), stream);
   count_launch();
   classify_segments<<<(nseg + 255) / 256, 256, 0, stream>>>(begin, end, nseg, nseg_dev, lists,
                                                             counts);
@@ -965,13 +1156,16 @@ cudaError_t segmented_std_sort(uint64_t* keys, uint32_t* vals, uint32_t* lscratc
   count_launch();
   sort_big<<<num_sms * 4, kBigBlock, 0, stream>>>(keys, vals, lscratch, rscratch, begin, end,
                                                   lists + 3 * static_cast<size_t>(nseg), counts,
-                                                  tasks.f, tasks.n, tasks.d, counts + 4);
+                                                  tasks.f, tasks.n, tasks.d, counts + 4,
+                                                  counts + 5, counts + 7, tasks.cap,
+                                                  tasks.pair_reserve);
   count_launch();
   sort_tasks<<<num_sms * 3, kBlock, sizeof(CtaSmem), stream>>>(keys, vals, tasks.f, tasks.n, tasks.d,
                                                            counts + 4);
   count_launch();
-  sort_heaps<<<num_sms, kHeapBlock, kHeapSmem, stream>>>(keys, vals, lscratch, rscratch, tasks.f,
-                                                        tasks.n, counts + 4);
+  sort_heaps<<<(num_sms + 1) / 2 * 2, kHeapBlock, kHeapSmem, stream>>>(
+      keys, vals, lscratch, rscratch, tasks.f, tasks.n, counts + 5, counts + 6, counts + 7,
+      counts + 8, tasks.cap, tasks.pair_reserve);
   return cudaGetLastError();
 }
 

@@ -211,13 +211,15 @@ def test_std_sort_many_segments(gpu, oracle_mod):
 
 
 @pytest.mark.parametrize("n,scale", [(20_000, 1), (200_000, 1), (200_000, 1 << 41),
-                                     (300_000, 1)])
+                                     (300_000, 1), (400_000, 1), (400_000, 1 << 41)])
 def test_heap_fallback_ranges_match_libstdcxx(gpu, oracle_mod, n, scale):
     """Organ-pipe keys (every value twice) drive libstdc++'s introsort into
     heapsort on ranges of 4k-95k elements: n = 200,000 gives heap ranges of
-    47,105, 42,183, 21,505 and 12,089 elements, n = 300,000 one of 95,233.
-    The heap's order among equal keys must match; keys spanning more than 47
-    bits (scale 2**41) take the 12-byte heap instead of the rank-packed one.
+    47,105, 42,183, 21,505 and 12,089 elements (one block's shared memory),
+    n = 300,000 one of 95,233 and n = 400,000 ones of 95,233 and 84,615 (a
+    block pair's).  The heap's order among equal keys must match; keys spanning
+    more than 47 bits (scale 2**41) take the 12-byte heap in shared memory or
+    the one in device memory instead of the rank-packed ones.
     n = 20,000 spends its recursion budget inside a block-wide partition of a
     shared-memory task, leaving leaves of 12 and 16 elements at depth 0 that
     libstdc++ insertion-sorts rather than heap-sorts."""
