@@ -21,7 +21,13 @@ workload against the device-resident index, batched: all reads in one pass.
 * ``roofline``: the dominant stage's algorithmic bytes / its event time
   against the measured HBM copy bandwidth;
 * ``cpu_baseline``: the CPU oracle (a restatement of the reference's CPU
-  path) on the host's cores over a bounded sample of the same reads.
+  path) on the host's cores over a bounded sample of the same reads;
+* ``stage_rooflines``: every stage's algorithmic GB/s and fraction of the
+  HBM peak, with hit generation and chaining on their own;
+* ``configs``: the plain 1 Mb overlap configuration and the read-to-graph
+  configuration, each batched and one read per call (``--configs``);
+* ``serving``: continuous batching through cuflye_submit / cuflye_poll on a
+  100 Mb indexed genome at several Poisson arrival rates (p50 / p99).
 
 ``--impl reference`` times that CPU implementation alone, on the same
 workload, metric and unit.  Under torchrun every rank runs its own replica
@@ -297,6 +303,100 @@ def serving_run(args, device: int) -> dict:
     return out
 
 
+def stage_rooflines(names, stage_ms, stage_bytes, peak) -> dict:
+    """Achieved algorithmic GB/s and fraction of the measured HBM peak per
+    stage, and for hit generation and for chaining (groups + DP + backtrack)
+    on their own."""
+    def one(ms, by):
+        gbs = by / (ms / 1000.0) / 1e9 if ms > 0 else None
+        return {"achieved_gbs": gbs, "frac": (gbs / peak) if (gbs and peak) else None}
+    out = {n: one(float(stage_ms[i]), float(stage_bytes[i])) for i, n in enumerate(names)}
+    out["hit generation (target 0.5)"] = out[names[0]]
+    out["chaining (target 0.5)"] = one(float(stage_ms[2:5].sum()), float(stage_bytes[2:5].sum()))
+    return out
+
+
+def _pct(xs, q):
+    xs = sorted(xs)
+    return xs[min(len(xs) - 1, int(q * len(xs)))] if xs else None
+
+
+def _plain_pass(gpu, reads, call, sample):
+    """One read per call (and per launch sequence) over the first `sample`
+    reads: read-bases/s and p50 / p99 latency in ms."""
+    from cuflye_gb300.backend import Sequences
+    sub = reads.subset(np.arange(min(sample, reads.n)))
+    one = [Sequences(np.array([sub.ids[i]], dtype=np.int64),
+                     np.array([0, sub.offsets[i + 1] - sub.offsets[i]], dtype=np.int64),
+                     np.ascontiguousarray(sub.bases[sub.offsets[i]:sub.offsets[i + 1]]))
+           for i in range(sub.n)]
+    call(one[0])
+    lat = []
+    t = time.perf_counter()
+    for q in one:
+        t1 = time.perf_counter()
+        call(q)
+        lat.append(1000.0 * (time.perf_counter() - t1))
+    return {"read_bases_per_s": sub.total_bases / (time.perf_counter() - t), "reads": sub.n,
+            "p50_ms": _pct(lat, 0.5), "p99_ms": _pct(lat, 0.99)}
+
+
+def extra_configs(args, device: int) -> dict:
+    """The other single-GPU configurations of the metric, each batched (all
+    reads in one call through the C ABI, host buffers, wall time) and plain
+    (one read per call): config 1, plain overlap on a 1 Mb genome at 20x
+    (k = 15); config 3, read-to-graph chains of ONT 30x reads against a
+    400-edge graph of a 20 Mb genome (k = 15)."""
+    from cuflye_gb300 import synth
+    from cuflye_gb300.backend import CudaBackend, OverlapParams, R2GParams, Sequences
+    out = {}
+    if "1" in args.configs:
+        wl = synth.plain_overlap()
+        p = OverlapParams.make(**wl.params)
+        with CudaBackend(device=device, memory_budget_bytes=0) as be:
+            be.build_index(wl.reads, wl.k, wl.min_freq, wl.max_freq)
+            q = Sequences.of(wl.reads)
+            be.overlaps(q, p)
+            t = time.perf_counter()
+            for _ in range(3):
+                rows = be.overlaps(q, p)
+            wall = (time.perf_counter() - t) / 3
+            be.set_batch_queries(1)
+            plain = _plain_pass(be, wl.reads, lambda s: be.overlaps(s, p), args.config_plain_sample)
+            be.set_batch_queries(0)
+        out["1_plain_overlap"] = {
+            "workload": "1 Mb uniform genome; reads 20x lognormal(10 kb, 5 kb) in 1-50 kb, "
+                        "1/0.5/0.5 % sub/ins/del; k=15", "reads": wl.reads.n,
+            "read_bases": wl.reads.total_bases, "rows": len(rows),
+            "batched_read_bases_per_s": wl.reads.total_bases / wall, "plain": plain,
+            "batched_over_plain": wl.reads.total_bases / wall / plain["read_bases_per_s"]}
+    if "3" in args.configs:
+        wl = synth.read_to_graph()
+        g = wl.graph
+        p = OverlapParams.make(**wl.params)
+        r = R2GParams.make(**synth.R2G_PARAMS)
+        with CudaBackend(device=device, memory_budget_bytes=0) as be:
+            be.build_index(g.seqs, wl.k, wl.min_freq, wl.max_freq)
+            be.set_graph(g.edge_ids, g.seq_ids, g.left, g.right)
+            q = Sequences.of(wl.reads)
+            be.read_to_graph(q, p, r)
+            t = time.perf_counter()
+            rows = be.read_to_graph(q, p, r)
+            wall = time.perf_counter() - t
+            ms, _ = be.last_timing()
+            plain = _plain_pass(be, wl.reads, lambda s: be.read_to_graph(s, p, r),
+                                args.config_plain_sample)
+        out["3_read_to_graph"] = {
+            "workload": "20 Mb genome cut into 400 edges (log-uniform 5-500 kb, 10 % duplicated "
+                        "at 0.5 %); ONT 30x lognormal(20 kb, 12 kb) in 1-150 kb, 8 % error; k=15",
+            "reads": wl.reads.n, "read_bases": wl.reads.total_bases, "alignment_rows": len(rows),
+            "batched_read_bases_per_s": wl.reads.total_bases / wall,
+            "device_read_bases_per_s": wl.reads.total_bases / (sum(ms) / 1000.0),
+            "plain": plain,
+            "batched_over_plain": wl.reads.total_bases / wall / plain["read_bases_per_s"]}
+    return out
+
+
 def run_ours(args, world, rank, local) -> None:
     from cuflye_gb300 import abi
     from cuflye_gb300.backend import CudaBackend, OverlapParams, Sequences, load_library
@@ -409,6 +509,7 @@ def run_ours(args, world, rank, local) -> None:
         "stages_ms_per_step": {n: round(float(stage_tot[i]) / args.steps, 3)
                                for i, n in enumerate(names + ["output + D2H", "H2D"])},
         "sort_paths_per_step": sort_paths,
+        "stage_rooflines": stage_rooflines(names, stage_tot, bytes_tot, peak),
         "roofline": {"bound": "hbm", "stage": names[dom], "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": (achieved / peak) if peak else None,
                      "traffic": traffic,
@@ -427,6 +528,8 @@ def run_ours(args, world, rank, local) -> None:
     if cpu:
         line["cpu_baseline"] = cpu
     gpu.close()
+    if args.configs and world == 1:
+        line["configs"] = extra_configs(args, local)
     if args.serve_rates and world == 1:
         line["serving"] = serving_run(args, local)
     print(json.dumps(line), flush=True)
@@ -448,6 +551,10 @@ def main() -> int:
                     default=[1000.0, 10000.0, 50000.0],
                     help="offered request rates (reads/s) of the serving run; empty skips it")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
+    ap.add_argument("--configs", default="1,3",
+                    help="other configurations to measure (1: plain 1 Mb, 3: read-to-graph); "
+                         "empty to skip")
+    ap.add_argument("--config-plain-sample", type=int, default=200)
     ap.add_argument("--serve-workers", type=int, default=2)
     ap.add_argument("--serve-batch-bases", type=int, default=32_000_000,
                     help="most read bases one served batch takes")
