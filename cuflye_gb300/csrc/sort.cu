@@ -14,6 +14,9 @@
 // Every partition is a single pass: L stoppers get ranks from the left, R
 // stoppers left ranks too (the k-th R stopper from the right is the
 // (TR - k)-th from the left), so a partition reads its keys once.
+// A range sorted in shared memory first tries a radix sort: when its keys
+// turn out distinct, that is libstdc++'s result too (the sorted order of
+// distinct keys is unique), and only ranges with equal keys are emulated.
 #include <cooperative_groups.h>
 
 #include <algorithm>
@@ -435,6 +438,125 @@ __device__ void cta_sort(CtaSmem& sm, uint32_t n, int depth0) {
   __syncthreads();
 }
 
+// A range whose keys are all distinct has one sorted order, whatever
+// libstdc++'s introsort would do with it.  So a range in shared memory first
+// takes an LSD radix sort of its positions (16-bit, ping-ponging between the
+// two rank maps) by 7-bit digits of key - min, stable per warp-owned slice,
+// and a check of neighbours in that order.  It returns the sorted positions
+// when no two keys are equal, else null; the keys and values stay as loaded
+// either way.  The digit counters overlay the emulation's task-stack fields,
+// unused until then.
+constexpr int kRadixBits = 7;
+constexpr int kRadixBins = 1 << kRadixBits;
+
+struct CtaRadix {
+  uint32_t wc[kWarps][kRadixBins];
+  uint32_t dbase[kRadixBins];
+  uint32_t ws[kWarps];
+  uint32_t lo[kWarps], hi[kWarps], lo2[kWarps], hi2[kWarps];
+};
+
+__device__ const uint16_t* cta_radix_distinct(CtaSmem& sm, uint32_t n) {
+  static_assert(sizeof(CtaRadix) <= sizeof(sm.tf) + sizeof(sm.tl) + sizeof(sm.td) +
+                                        sizeof(sm.leaves),
+                "radix counters fit the task-stack fields");
+  CtaRadix& rx = *reinterpret_cast<CtaRadix*>(sm.tf);
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const uint32_t lt = (1u << lane) - 1u;
+  // smallest and largest key (64-bit, by warp shuffles)
+  uint64_t mn = ~0ull, mx = 0;
+  for (uint32_t i = t; i < n; i += kBlock) {
+    mn = min(mn, sm.K[i]);
+    mx = max(mx, sm.K[i]);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    mn = min(mn, static_cast<uint64_t>(__shfl_xor_sync(0xffffffffu, mn, o)));
+    mx = max(mx, static_cast<uint64_t>(__shfl_xor_sync(0xffffffffu, mx, o)));
+  }
+  if (lane == 0) {
+    rx.lo[warp] = static_cast<uint32_t>(mn);
+    rx.hi[warp] = static_cast<uint32_t>(mn >> 32);
+    rx.lo2[warp] = static_cast<uint32_t>(mx);
+    rx.hi2[warp] = static_cast<uint32_t>(mx >> 32);
+  }
+  __syncthreads();
+  uint64_t kmin = ~0ull, kmax = 0;
+#pragma unroll
+  for (int w = 0; w < kWarps; ++w) {
+    kmin = min(kmin, (static_cast<uint64_t>(rx.hi[w]) << 32) | rx.lo[w]);
+    kmax = max(kmax, (static_cast<uint64_t>(rx.hi2[w]) << 32) | rx.lo2[w]);
+  }
+  const uint64_t span = kmax - kmin;
+  const int kb = span ? 64 - __clzll(span) : 0;
+  if (kb == 0 && n > 1) return nullptr;  // all keys equal: emulate
+  uint16_t* src = sm.Lr;
+  uint16_t* dst = sm.Rr;
+  for (uint32_t i = t; i < n; i += kBlock) src[i] = static_cast<uint16_t>(i);
+  const uint32_t per_warp = (((n + 31) / 32 + kWarps - 1) / kWarps) * 32;
+  const uint32_t w0 = min(n, warp * per_warp);
+  const uint32_t w1 = min(n, w0 + per_warp);
+  for (int shift = 0; shift < kb; shift += kRadixBits) {
+    for (int i = t; i < kWarps * kRadixBins; i += kBlock) (&rx.wc[0][0])[i] = 0;
+    __syncthreads();
+    for (uint32_t r0 = w0; r0 < w1; r0 += 32) {
+      const uint32_t j = r0 + lane;
+      const bool valid = j < w1;
+      const uint32_t d =
+          valid ? static_cast<uint32_t>((sm.K[src[j]] - kmin) >> shift) & (kRadixBins - 1)
+                : kRadixBins;
+      const uint32_t peers = __match_any_sync(0xffffffffu, d);
+      if (valid && lane == __ffs(peers) - 1) rx.wc[warp][d] += __popc(peers);
+      __syncwarp();
+    }
+    __syncthreads();
+    // bases: digits in order, warps in order within a digit
+    uint32_t tot = 0;
+    if (t < kRadixBins) {
+      for (int w = 0; w < kWarps; ++w) {
+        const uint32_t c = rx.wc[w][t];
+        rx.wc[w][t] = tot;
+        tot += c;
+      }
+    }
+    uint32_t inc = tot;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += u;
+    }
+    if (lane == 31 && t < kRadixBins) rx.ws[warp] = inc;
+    __syncthreads();
+    if (t < kRadixBins) {
+      uint32_t before = 0;
+      for (int w = 0; w < warp; ++w) before += rx.ws[w];
+      rx.dbase[t] = before + inc - tot;
+    }
+    __syncthreads();
+    for (uint32_t r0 = w0; r0 < w1; r0 += 32) {
+      const uint32_t j = r0 + lane;
+      const bool valid = j < w1;
+      const uint16_t x = valid ? src[j] : 0;
+      const uint32_t d = valid ? static_cast<uint32_t>((sm.K[x] - kmin) >> shift) &
+                                     (kRadixBins - 1)
+                               : kRadixBins;
+      const uint32_t peers = __match_any_sync(0xffffffffu, d);
+      const uint32_t base = valid ? rx.dbase[d] + rx.wc[warp][d] : 0u;
+      __syncwarp();
+      if (valid && lane == __ffs(peers) - 1) rx.wc[warp][d] += __popc(peers);
+      __syncwarp();
+      if (valid) dst[base + __popc(peers & lt)] = x;
+    }
+    __syncthreads();
+    uint16_t* tmp = src;
+    src = dst;
+    dst = tmp;
+  }
+  bool tie = false;
+  for (uint32_t i = t + 1; i < n; i += kBlock) tie |= sm.K[src[i]] == sm.K[src[i - 1]];
+  return __syncthreads_or(tie) ? nullptr : src;
+}
+
 __device__ void cta_load_sort_store(uint64_t* K, uint32_t* V, uint64_t begin, uint32_t n,
                                     int depth, CtaSmem& sm) {
   for (uint32_t i = threadIdx.x; i < n; i += kBlock) {
@@ -442,6 +564,16 @@ __device__ void cta_load_sort_store(uint64_t* K, uint32_t* V, uint64_t begin, ui
     sm.V[i] = V[begin + i];
   }
   __syncthreads();
+  const uint16_t* perm = cta_radix_distinct(sm, n);
+  if (perm) {
+    for (uint32_t i = threadIdx.x; i < n; i += kBlock) {
+      K[begin + i] = sm.K[perm[i]];
+      V[begin + i] = sm.V[perm[i]];
+    }
+    __syncthreads();
+    return;
+  }
+  // equal keys: libstdc++'s order, from the range as loaded
   cta_sort(sm, n, depth);
   for (uint32_t i = threadIdx.x; i < n; i += kBlock) {
     K[begin + i] = sm.K[i];
