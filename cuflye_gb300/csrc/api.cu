@@ -681,9 +681,14 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp,
   int32_t* score = buf<int32_t>(c, "c_score", H);
   int32_t* bt = buf<int32_t>(c, "c_bt", H);
   GroupTop* top = buf<GroupTop>(c, "c_top", G);
+  // the surviving groups in length buckets, longest first, for the
+  // warp-per-group stages (warps take them from a counter)
+  uint32_t* blist = buf<uint32_t>(c, "g_lenlist", G);
+  CUFLYE_CHECK(groups_length_order(groups, dp_list, gcounts + 1, G32,
+                                   buf<uint32_t>(c, "g_lenscr", 10), blist, st));
   CUFLYE_CHECK(cudaEventRecord(c->ev[6], st));
   int32_t* pmc = buf<int32_t>(c, "c_pmc", chain_dp_pmc_words(H, G));
-  CUFLYE_CHECK(chain_dp(ps.keys, ps.vals, score, bt, groups, dp_list, gcounts, cp, top, pmc, work,
+  CUFLYE_CHECK(chain_dp(ps.keys, ps.vals, score, bt, groups, blist, gcounts, cp, top, pmc, work,
                         c->num_sms, st));
   CUFLYE_CHECK(cudaEventRecord(c->ev[7], st));
   // 5. the backtrack picks its chain starts by score itself; groups where
@@ -707,7 +712,7 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp,
   uint32_t* redo_count = buf<uint32_t>(c, "o_redocount", 1);
   CUFLYE_CHECK(cudaMemsetAsync(redo_count, 0, 4, st));
   const int64_t* slot_signed = c->idx.slot_signed;
-  CUFLYE_CHECK(chain_backtrack(ps.keys, ps.vals, score, bt, order, groups, dp_list, gcounts + 1, top,
+  CUFLYE_CHECK(chain_backtrack(ps.keys, ps.vals, score, bt, order, groups, blist, gcounts + 1, top,
                                redo, redo_count, ps.qinfo, ps.f_off, ps.fpos, slot_signed, c->logt,
                                cp, pool, pool_cap, pool_count, group_rows, c->status, G32, gmaps,
                                gmap_words, work, st));

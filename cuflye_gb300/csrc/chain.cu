@@ -999,6 +999,59 @@ cudaError_t groups_ext_presorted(const uint32_t* vals, GroupInfo* groups, const 
   return cudaGetLastError();
 }
 
+namespace {
+// Length buckets for the warp-per-group stages: groups of over 16,384,
+// 4,096, 1,024 and 256 hits, then the rest, longest bucket first, so the
+// longest groups start in the first wave and the short ones fill the tail.
+constexpr int kLenBuckets = 5;
+__device__ __forceinline__ int len_bucket(uint32_t n) {
+  return n > 16384 ? 0 : n > 4096 ? 1 : n > 1024 ? 2 : n > 256 ? 3 : 4;
+}
+
+__global__ void bucket_count_kernel(const GroupInfo* __restrict__ groups,
+                                    const uint32_t* __restrict__ list,
+                                    const uint32_t* __restrict__ list_count,
+                                    uint32_t* __restrict__ bcount) {
+  __shared__ uint32_t h[kLenBuckets];
+  if (threadIdx.x < kLenBuckets) h[threadIdx.x] = 0;
+  __syncthreads();
+  const uint32_t cnt = *list_count;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x)
+    atomicAdd(&h[len_bucket(groups[list[i]].n)], 1u);
+  __syncthreads();
+  if (threadIdx.x < kLenBuckets && h[threadIdx.x]) atomicAdd(&bcount[threadIdx.x], h[threadIdx.x]);
+}
+
+__global__ void bucket_scatter_kernel(const GroupInfo* __restrict__ groups,
+                                      const uint32_t* __restrict__ list,
+                                      const uint32_t* __restrict__ list_count,
+                                      const uint32_t* __restrict__ bcount,
+                                      uint32_t* __restrict__ bfill, uint32_t* __restrict__ out) {
+  const uint32_t cnt = *list_count;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
+    const uint32_t g = list[i];
+    const int b = len_bucket(groups[g].n);
+    uint32_t base = 0;
+    for (int c = 0; c < b; ++c) base += bcount[c];
+    out[base + atomicAdd(&bfill[b], 1u)] = g;
+  }
+}
+}  // namespace
+
+cudaError_t groups_length_order(const GroupInfo* groups, const uint32_t* list,
+                                const uint32_t* list_count, uint32_t max_groups,
+                                uint32_t* scratch, uint32_t* out, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(scratch, 0, 2 * kLenBuckets * sizeof(uint32_t), s);
+  if (e != cudaSuccess || max_groups == 0) return e;
+  const unsigned g = static_cast<unsigned>(std::min<uint64_t>((max_groups + 255) / 256, 2048));
+  count_launch();
+  bucket_count_kernel<<<g, 256, 0, s>>>(groups, list, list_count, scratch);
+  count_launch();
+  bucket_scatter_kernel<<<g, 256, 0, s>>>(groups, list, list_count, scratch,
+                                          scratch + kLenBuckets, out);
+  return cudaGetLastError();
+}
+
 cudaError_t chain_dp(const uint64_t* keys, const uint32_t* vals, int32_t* score, int32_t* bt,
                      const GroupInfo* groups, const uint32_t* dp_list, const uint32_t* counts,
                      const ChainParams& p, GroupTop* top, int32_t* pmc, uint32_t* work,

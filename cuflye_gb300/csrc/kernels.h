@@ -237,6 +237,11 @@ struct GroupTop {
 // work: one word of device scratch (the group counter of the launch); top
 // (indexed by group) receives each group's GroupTop; pmc: chain_dp_pmc_words
 // words of scratch (running score maxima per 32 elements).
+// The list reordered by length bucket, longest first (order within a bucket
+// unspecified).  scratch: 10 words.
+cudaError_t groups_length_order(const GroupInfo* groups, const uint32_t* list,
+                                const uint32_t* list_count, uint32_t max_groups,
+                                uint32_t* scratch, uint32_t* out, cudaStream_t s);
 cudaError_t chain_dp(const uint64_t* keys, const uint32_t* vals, int32_t* score, int32_t* bt,
                      const GroupInfo* groups, const uint32_t* dp_list, const uint32_t* counts,
                      const ChainParams& p, GroupTop* top, int32_t* pmc, uint32_t* work,
