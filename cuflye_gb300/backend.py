@@ -136,6 +136,8 @@ def load_library(path: Path | None = None) -> ctypes.CDLL:
     L.cuflye_last_timing.argtypes = [_vp, ctypes.POINTER(ctypes.c_double), _u64p, ctypes.c_size_t]
     L.cuflye_last_sort_stats.restype = S
     L.cuflye_last_sort_stats.argtypes = [_vp, _u64p, ctypes.c_size_t]
+    L.cuflye_last_passes.restype = S
+    L.cuflye_last_passes.argtypes = [_vp, _u64p]
     L.cuflye_server_open.restype = S
     L.cuflye_server_open.argtypes = [_vp, ctypes.c_int, ctypes.POINTER(OverlapParams),
                                      ctypes.c_uint64, ctypes.POINTER(_vp)]
@@ -256,6 +258,12 @@ class CudaBackend:
         v = (ctypes.c_uint64 * 7)()
         self._check(self._L.cuflye_last_sort_stats(self._h, v, 7))
         return dict(zip(self.SORT_STATS, list(v)))
+
+    def last_passes(self) -> int:
+        """Passes (runs of queries through the device) of the last call."""
+        v = ctypes.c_uint64()
+        self._check(self._L.cuflye_last_passes(self._h, ctypes.byref(v)))
+        return int(v.value)
 
     # -- index
     def build_index(self, targets, k: int, min_freq: int, max_freq: int) -> dict:

@@ -82,6 +82,7 @@ struct cuflye_ctx {
   double stage_ms[7]{};
   uint64_t stage_bytes[7]{};
   uint64_t sort_stats[7]{};  // see cuflye_last_sort_stats
+  uint64_t passes = 0;       // see cuflye_last_passes
 };
 
 namespace {
@@ -761,6 +762,7 @@ float elapsed(cudaEvent_t a, cudaEvent_t b) {
 }
 
 void reset_timing(cuflye_ctx* c) {
+  c->passes = 0;
   for (int i = 0; i < kStages; ++i) {
     c->stage_ms[i] = 0;
     c->stage_bytes[i] = 0;
@@ -819,6 +821,7 @@ void for_each_pass(cuflye_ctx* c, const Queries& Q, bool kmers, uint64_t bytes_p
       step = std::max<size_t>(ps.nq / 2, 1);
       continue;
     }
+    ++c->passes;
     q0 = q1;
   }
 }
@@ -1272,6 +1275,12 @@ cuflye_status cuflye_last_timing(const cuflye_ctx* c, double* stage_ms, uint64_t
 cuflye_status cuflye_last_sort_stats(const cuflye_ctx* c, uint64_t* counts, size_t n) {
   if (!c || (!counts && n)) return CUFLYE_ERR_INVALID;
   for (size_t i = 0; i < n && i < static_cast<size_t>(kSortStats); ++i) counts[i] = c->sort_stats[i];
+  return CUFLYE_OK;
+}
+
+cuflye_status cuflye_last_passes(const cuflye_ctx* c, uint64_t* passes) {
+  if (!c || !passes) return CUFLYE_ERR_INVALID;
+  *passes = c->passes;
   return CUFLYE_OK;
 }
 

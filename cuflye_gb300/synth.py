@@ -230,6 +230,29 @@ def read_to_graph(seed: int = 3, genome_len: int = 20_000_000, n_edges: int = 40
                     max_freq=64, params=params, graph=graph, seed=seed)
 
 
+def scale_ont(seed: int = 6, genome_len: int = 500_000_000, coverage: float = 30.0,
+              max_reads: int | None = None) -> Workload:
+    """The scale configuration's shapes: a genome with 10 % interspersed repeats
+    (families of 1-20 kb, copies at 0.5-5 % divergence); ONT-like reads,
+    lognormal(25 kb, 15 kb) in 1-150 kb, 6 % error (2 / 2 / 2 % sub / ins /
+    del); k = 17.  genome_len and coverage scale it down for tests."""
+    rng = np.random.default_rng(seed)
+    genome = random_genome(rng, genome_len)
+    placed = 0
+    while placed < 0.10 * genome_len:
+        fam = random_genome(rng, int(rng.integers(1_000, 20_001)))
+        for _ in range(int(rng.integers(2, 10))):
+            pos = int(rng.integers(0, max(1, genome_len - len(fam))))
+            copy = mutate(rng, fam, float(rng.uniform(0.005, 0.05)))[:genome_len - pos]
+            genome[pos:pos + len(copy)] = copy
+            placed += len(copy)
+    reads = sample_reads(rng, genome, coverage,
+                         lambda n: lognormal_lengths(rng, n, 25_000, 15_000, 1_000, 150_000),
+                         0.02, 0.02, 0.02, max_reads)
+    return Workload("scale-ont30x-k17", 17, reads, min_freq=2, max_freq=int(5 * coverage),
+                    params=dict(OVERLAP_PARAMS, kmer_size=17), seed=seed)
+
+
 R2G_PARAMS = dict(max_jump=1500, max_read_overlap=50, min_overlap=1000, max_separation=500,
                   long_edge=900, big_aln=500, max_chain_divergence=0.25)
 

@@ -319,6 +319,12 @@ cuflye_status cuflye_last_timing(const cuflye_ctx* ctx, double* stage_ms, uint64
  * scores could change their result. */
 cuflye_status cuflye_last_sort_stats(const cuflye_ctx* ctx, uint64_t* counts, size_t n);
 
+/* Passes of the last candidates / overlaps / read-to-graph call: runs of
+ * queries that fitted the memory budget (or cuflye_set_batch_queries) and
+ * went through the device one after another (no counterpart in the
+ * reference). */
+cuflye_status cuflye_last_passes(const cuflye_ctx* ctx, uint64_t* passes);
+
 /* Kernel launches issued by the library in this process so far. */
 cuflye_status cuflye_kernel_launches(uint64_t* total);
 

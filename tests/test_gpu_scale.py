@@ -1,0 +1,62 @@
+"""The scale configuration's path, scaled down: ONT-like reads with 6 % error
+over a repeat-bearing genome, streamed through the device in passes.  Rows
+are a property of the reads alone, so they must not depend on how a call is
+cut into passes, whether by a query count or by the memory budget; a sample
+of the longest reads is checked against the oracle bit for bit."""
+
+import numpy as np
+import pytest
+
+from test_gpu_parity import oracle_index, overlap_tuples_gpu, overlap_tuples_oracle
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def scale_case():
+    from cuflye_gb300 import synth
+    return synth.scale_ont(seed=6, genome_len=3_000_000, coverage=8.0)
+
+
+def test_passes_do_not_change_rows(built_lib, scale_case):
+    from cuflye_gb300.backend import CudaBackend, OverlapParams
+    wl = scale_case
+    p = OverlapParams.make(**wl.params)
+    with CudaBackend(device=0, memory_budget_bytes=0) as be:
+        be.build_index(wl.reads, wl.k, wl.min_freq, wl.max_freq)
+        build_peak = be.memory_stats()[1]
+        whole = be.overlaps(wl.reads, p)
+        assert be.last_passes() == 1
+        hits = be.last_timing()[1][1] // 24
+        be.set_batch_queries(97)
+        by_count = be.overlaps(wl.reads, p)
+        assert be.last_passes() == -(-wl.reads.n // 97)
+        be.set_batch_queries(0)
+    assert len(whole) > 0 and hits > 0
+    assert by_count.tobytes() == whole.tobytes()
+    # a budget that holds the index build and about a sixth of the hits' buffers
+    budget = int(build_peak + 64 * hits / 6 + (64 << 20))
+    with CudaBackend(device=0, memory_budget_bytes=budget) as be:
+        be.build_index(wl.reads, wl.k, wl.min_freq, wl.max_freq)
+        by_budget = be.overlaps(wl.reads, p)
+        assert be.last_passes() >= 3
+        peak = be.memory_stats()[1]
+    assert peak <= budget
+    assert by_budget.tobytes() == whole.tobytes()
+
+
+def test_long_ont_reads_match_oracle(gpu, oracle_mod, scale_case):
+    from cuflye_gb300.backend import OverlapParams
+    wl = scale_case
+    oracle_mod.set_stable(False)
+    idx, _ = oracle_index(oracle_mod, wl.reads, wl.k, wl.min_freq, wl.max_freq)
+    gpu.build_index(wl.reads, wl.k, wl.min_freq, wl.max_freq)
+    lens = np.diff(wl.reads.offsets)
+    q = wl.reads.subset(np.sort(np.argsort(lens)[-12:]))
+    b = oracle_mod.SeqBatch(q.ids, q.offsets, q.bases.tobytes())
+    for variant in ({}, {"only_max_ext": 0}):
+        params = dict(wl.params, **variant)
+        got = gpu.overlaps(q, OverlapParams.make(**params))
+        exp = oracle_mod.overlaps(idx, b, oracle_mod.default_params(**params))
+        assert len(got) > 0
+        assert overlap_tuples_gpu(got) == overlap_tuples_oracle(exp), variant
