@@ -602,9 +602,15 @@ ChainParams to_chain_params(const cuflye_overlap_params* p) {
 // Task-list buffers for the segmented sort, named by `prefix`.
 SortTasks sort_tasks(cuflye_ctx* c, const std::string& prefix, uint64_t nelems, uint32_t nseg) {
   const uint64_t w = segsort_task_words(nelems, nseg);
-  return SortTasks{buf<uint64_t>(c, prefix + "_tf", w), buf<uint32_t>(c, prefix + "_tn", w),
-                   buf<int>(c, prefix + "_td", w), static_cast<uint32_t>(w),
-                   segsort_pair_reserve(nelems)};
+  const size_t rb = segsort_round_bytes(nelems);
+  return SortTasks{buf<uint64_t>(c, prefix + "_tf", w),
+                   buf<uint32_t>(c, prefix + "_tn", w),
+                   buf<int>(c, prefix + "_td", w),
+                   static_cast<uint32_t>(w),
+                   segsort_pair_reserve(nelems),
+                   nelems,
+                   {buf<uint8_t>(c, prefix + "_r0", rb), buf<uint8_t>(c, prefix + "_r1", rb)},
+                   buf<uint32_t>(c, prefix + "_rc", 2 * (kSortRounds + 1))};
 }
 
 // Sort + chaining of the pass's hits; returns the number of overlap rows left

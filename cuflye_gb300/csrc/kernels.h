@@ -28,14 +28,20 @@ size_t segsort_smem_bytes();
 // Longest heap range one block sorts in its own shared memory; longer ones
 // take a block pair.
 constexpr uint32_t kHeapPackCap = 57344;
+// Rounds of the global phase (partitions of ranges beyond shared memory).
+constexpr int kSortRounds = 64;
 struct SortTasks {
   uint64_t* f;
   uint32_t* n;
   int* d;
   uint32_t cap;           // entries of f, n and d (segsort_task_words)
   uint32_t pair_reserve;  // top entries kept for heap ranges beyond kHeapPackCap
+  uint64_t nelems;        // elements of the call at most (no global phase up to 4,096)
+  void* round[2];         // two round lists of segsort_round_bytes(nelems) each
+  uint32_t* round_counts;  // 2 * (kSortRounds + 1) words
 };
 uint32_t segsort_pair_reserve(uint64_t nelems);
+size_t segsort_round_bytes(uint64_t nelems);
 size_t segsort_task_words(uint64_t nelems, uint32_t nseg);
 // lists: 4 * nseg words; counts: 16 words.  l/r scratch: one word per element.
 // nseg_dev (optional) holds the live segment count on the device (<= nseg).

@@ -46,7 +46,11 @@ constexpr size_t kOffSegs = align256(kOffCounts + 4 * 16);
 constexpr size_t kOffTf = align256(kOffSegs + 8 * (kMaxSegs + 1));
 constexpr size_t kOffTn = align256(kOffTf + 8 * kTaskCap);
 constexpr size_t kOffTd = align256(kOffTn + 4 * kTaskCap);
-constexpr size_t kScratchBytes = align256(kOffTd + 4 * kTaskCap);
+constexpr size_t kRoundBytes = (kMaxElems / 4096 + 1) * 16;  // segsort_round_bytes(kMaxElems)
+constexpr size_t kOffR0 = align256(kOffTd + 4 * kTaskCap);
+constexpr size_t kOffR1 = align256(kOffR0 + kRoundBytes);
+constexpr size_t kOffRc = align256(kOffR1 + kRoundBytes);
+constexpr size_t kScratchBytes = align256(kOffRc + 4 * 2 * (kSortRounds + 1));
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
@@ -118,7 +122,10 @@ extern "C" cuflye_status cuflye_std_sort_segments_noalloc(uint64_t* keys, uint32
   }
   SortTasks tasks{reinterpret_cast<uint64_t*>(base + kOffTf),
                   reinterpret_cast<uint32_t*>(base + kOffTn), reinterpret_cast<int*>(base + kOffTd),
-                  static_cast<uint32_t>(kTaskCap), segsort_pair_reserve(n_elements)};
+                  static_cast<uint32_t>(kTaskCap), segsort_pair_reserve(n_elements),
+                  n_elements, {base + kOffR0, base + kOffR1},
+                  reinterpret_cast<uint32_t*>(base + kOffRc)};
+  if (segsort_round_bytes(n_elements) > kRoundBytes) return CUFLYE_ERR_INVALID;
   // segmented_std_sort clears its counters (the task count included) itself
   const cudaError_t e = segmented_std_sort(
       keys, values, reinterpret_cast<uint32_t*>(base + kOffL),

@@ -9,8 +9,9 @@
 //                             partitions while tasks exceed kWarpMax, then all
 //                             16 warps partition different tasks concurrently
 //                             (level by level), then one thread per leaf task;
-//   * larger:                 one CTA partitions in global memory until its
-//                             tasks fit kCap, then finishes each in shared memory.
+//   * larger:                 partitions in global memory, in rounds over all
+//                             such ranges (one CTA per range), until the ranges
+//                             fit kCap; each is then finished in shared memory.
 // Every partition is a single pass: L stoppers get ranks from the left, R
 // stoppers left ranks too (the k-th R stopper from the right is the
 // (TR - k)-th from the left), so a partition reads its keys once.
@@ -671,97 +672,93 @@ __global__ void __launch_bounds__(kBlock, 3) sort_cta(uint64_t* K, uint32_t* V,
 
 // ---------------------------------------------------------------- large segments
 //
-// Global phase: one CTA of kBigBlock threads per segment partitions in global
-// memory (round_partition) until every task fits kCap, and appends the final
-// tasks to a list that sort_tasks finishes in shared memory.
+// Global phase, in rounds: each launch partitions every range of its round's
+// list (ranges longer than kCap with recursion budget left) in global memory
+// (round_partition), one CTA per range, CTAs taking ranges from a counter.
+// Children longer than kCap with budget left go to the next round's list,
+// shorter ones to the task list that sort_tasks finishes in shared memory,
+// and children whose budget ran out to the heap lists.  A range's partition
+// depends on its own elements only, so the rounds give libstdc++'s result in
+// a breadth-first order, and every CTA has work while ranges remain.
 
 constexpr int kBigBlock = 256;
 
-struct BigSmem {
-  RoundScratch<kBigBlock, 8> rs;
-  uint32_t gf[96], gl[96];
-  int gd[96];
-  int gn;
+struct RoundItem {
+  uint64_t f;
+  uint32_t n;
+  int d;
 };
 
-__global__ void __launch_bounds__(kBigBlock, 4) sort_big(uint64_t* K, uint32_t* V, uint32_t* Lg,
-                                                      uint32_t* Rg,
-                                                      const uint64_t* __restrict__ begin,
-                                                      const uint64_t* __restrict__ end,
-                                                      const uint32_t* __restrict__ list,
-                                                      const uint32_t* __restrict__ counts,
-                                                      uint64_t* task_f, uint32_t* task_n,
-                                                      int* task_d, uint32_t* task_count,
-                                                      uint32_t* heap_count, uint32_t* pair_count,
-                                                      uint32_t task_cap, uint32_t pair_reserve) {
-  __shared__ BigSmem sm;
-  const uint32_t cnt = counts[3];
-  for (uint32_t i = blockIdx.x; i < cnt; i += gridDim.x) {
-    const uint32_t s = list[i];
-    const uint64_t b = begin[s];
-    const uint32_t n = static_cast<uint32_t>(end[s] - b);
-    uint64_t* Ks = K + b;
-    uint32_t* Vs = V + b;
-    uint32_t* Ls = Lg + b;  // rank maps share the segment's index range
-    uint32_t* Rs = Rg + b;
-    if (threadIdx.x == 0) {
-      sm.gf[0] = 0;
-      sm.gl[0] = n;
-      sm.gd[0] = isort::depth_limit(n);
-      sm.gn = 1;
+// Where a child range of a global-phase partition goes.
+__device__ __forceinline__ void place_range(uint64_t f, uint32_t n, int d, RoundItem* out,
+                                            uint32_t* out_count, uint64_t* task_f,
+                                            uint32_t* task_n, int* task_d, uint32_t* task_count,
+                                            uint32_t* heap_count, uint32_t* pair_count,
+                                            uint32_t task_cap, uint32_t pair_reserve) {
+  if (n <= kCap) {
+    if (n > 1) {
+      const uint32_t slot = atomicAdd(task_count, 1u);
+      task_f[slot] = f;
+      task_n[slot] = n;
+      task_d[slot] = d;
     }
-    __syncthreads();
-    for (;;) {
-      const int nt = sm.gn;
-      if (nt == 0) break;
-      const uint32_t f = sm.gf[nt - 1], l = sm.gl[nt - 1];
-      const int d = sm.gd[nt - 1];
-      __syncthreads();
-      if (l - f <= kCap) {
-        if (threadIdx.x == 0) {
-          sm.gn = nt - 1;
-          if (l - f > 1) {
-            const uint32_t slot = atomicAdd(task_count, 1u);
-            task_f[slot] = b + f;
-            task_n[slot] = l - f;
-            task_d[slot] = d;
-          }
-        }
-        __syncthreads();
-        continue;
-      }
-      if (d == 0) {
-        // depth exhausted: libstdc++ heap-sorts the range; sort_heaps does it
-        // (a task longer than kCap, listed from the top of the task arrays:
-        // ranges beyond one block's shared memory first, then the others)
-        if (threadIdx.x == 0) {
-          sm.gn = nt - 1;
-          const uint32_t slot = l - f > kHeapPackCap
-                                    ? task_cap - 1u - atomicAdd(pair_count, 1u)
-                                    : task_cap - 1u - pair_reserve - atomicAdd(heap_count, 1u);
-          task_f[slot] = b + f;
-          task_n[slot] = l - f;
-          task_d[slot] = 0;
-        }
-        __syncthreads();
-        continue;
-      }
-      const uint32_t cut = round_partition<kBigBlock, uint32_t>(Ks, Vs, Ls, Rs, f, l, sm.rs);
-      if (threadIdx.x == 0) {
-        sm.gf[nt - 1] = cut;
-        sm.gl[nt - 1] = l;
-        sm.gd[nt - 1] = d - 1;
-        sm.gf[nt] = f;
-        sm.gl[nt] = cut;
-        sm.gd[nt] = d - 1;
-        sm.gn = nt + 1;
-      }
-      __syncthreads();
-    }
+  } else if (d == 0) {
+    // depth exhausted: libstdc++ heap-sorts the range; sort_heaps does it
+    // (listed from the top of the task arrays: ranges beyond one block's
+    // shared memory first, then the others)
+    const uint32_t slot = n > kHeapPackCap
+                              ? task_cap - 1u - atomicAdd(pair_count, 1u)
+                              : task_cap - 1u - pair_reserve - atomicAdd(heap_count, 1u);
+    task_f[slot] = f;
+    task_n[slot] = n;
+    task_d[slot] = 0;
+  } else {
+    out[atomicAdd(out_count, 1u)] = RoundItem{f, n, d};
   }
 }
 
-// Finishes the <= kCap tasks left by sort_big, one CTA per task.
+// The round-0 list: the segments longer than kCap with libstdc++'s budget.
+__global__ void round_seed(const uint64_t* __restrict__ begin, const uint64_t* __restrict__ end,
+                           const uint32_t* __restrict__ list, const uint32_t* __restrict__ counts,
+                           RoundItem* __restrict__ out) {
+  const uint32_t cnt = counts[3];
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
+    const uint32_t s = list[i];
+    const uint32_t n = static_cast<uint32_t>(end[s] - begin[s]);
+    out[i] = RoundItem{begin[s], n, isort::depth_limit(n)};
+  }
+}
+
+__global__ void __launch_bounds__(kBigBlock, 4)
+    sort_round(uint64_t* K, uint32_t* V, uint32_t* Lg, uint32_t* Rg,
+               const RoundItem* __restrict__ in, const uint32_t* __restrict__ in_count,
+               uint32_t* work, RoundItem* out, uint32_t* out_count, uint64_t* task_f,
+               uint32_t* task_n, int* task_d, uint32_t* task_count, uint32_t* heap_count,
+               uint32_t* pair_count, uint32_t task_cap, uint32_t pair_reserve) {
+  __shared__ RoundScratch<kBigBlock, 8> rs;
+  __shared__ uint32_t item;
+  const uint32_t cnt = *in_count;
+  for (;;) {
+    if (threadIdx.x == 0) item = atomicAdd(work, 1u);
+    __syncthreads();
+    const uint32_t i = item;
+    __syncthreads();
+    if (i >= cnt) break;
+    const RoundItem r = in[i];
+    // rank maps share the range's index range
+    const uint32_t cut =
+        round_partition<kBigBlock, uint32_t>(K + r.f, V + r.f, Lg + r.f, Rg + r.f, 0, r.n, rs);
+    if (threadIdx.x == 0) {
+      place_range(r.f, cut, r.d - 1, out, out_count, task_f, task_n, task_d, task_count,
+                  heap_count, pair_count, task_cap, pair_reserve);
+      place_range(r.f + cut, r.n - cut, r.d - 1, out, out_count, task_f, task_n, task_d,
+                  task_count, heap_count, pair_count, task_cap, pair_reserve);
+    }
+    __syncthreads();
+  }
+}
+
+// Finishes the <= kCap tasks left by the global phase, one CTA per task.
 __global__ void __launch_bounds__(kBlock, 3) sort_tasks(uint64_t* K, uint32_t* V,
                                                      const uint64_t* __restrict__ task_f,
                                                      const uint32_t* __restrict__ task_n,
@@ -1247,6 +1244,8 @@ uint32_t segsort_pair_reserve(uint64_t nelems) {
   return static_cast<uint32_t>(nelems / kHeapPackCap + 1);
 }
 
+size_t segsort_round_bytes(uint64_t nelems) { return (nelems / kCap + 1) * sizeof(RoundItem); }
+
 size_t segsort_task_words(uint64_t nelems, uint32_t nseg) {
   // final tasks of the global phase are disjoint and come from partitions of
   // tasks larger than kCap (at most depth_limit levels of them); heap tasks
@@ -1285,12 +1284,34 @@ cudaError_t segmented_std_sort(uint64_t* keys, uint32_t* vals, uint32_t* lscratc
   sort_cta<<<num_sms * 3, kBlock, sizeof(CtaSmem), stream>>>(keys, vals, begin, end,
                                                          lists + 2 * static_cast<size_t>(nseg),
                                                          counts);
-  count_launch();
-  sort_big<<<num_sms * 4, kBigBlock, 0, stream>>>(keys, vals, lscratch, rscratch, begin, end,
-                                                  lists + 3 * static_cast<size_t>(nseg), counts,
-                                                  tasks.f, tasks.n, tasks.d, counts + 4,
-                                                  counts + 5, counts + 7, tasks.cap,
-                                                  tasks.pair_reserve);
+  if (tasks.nelems > kCap) {
+    // global phase in rounds; the host looks at the next round's list after
+    // rounds 0, 1, 3, 7, ... and stops when it is empty (every range's budget
+    // runs out by round 62)
+    RoundItem* rl[2] = {static_cast<RoundItem*>(tasks.round[0]),
+                        static_cast<RoundItem*>(tasks.round[1])};
+    uint32_t* rcount = tasks.round_counts;                  // list size of round r
+    uint32_t* rwork = tasks.round_counts + kSortRounds + 1;  // claims of round r
+    cudaMemsetAsync(tasks.round_counts, 0, 2 * (kSortRounds + 1) * sizeof(uint32_t), stream);
+    count_launch();
+    round_seed<<<std::min((nseg + 255) / 256, 1024u), 256, 0, stream>>>(
+        begin, end, lists + 3 * static_cast<size_t>(nseg), counts, rl[0]);
+    for (int r = 0; r < kSortRounds; ++r) {
+      count_launch();
+      sort_round<<<num_sms * 4, kBigBlock, 0, stream>>>(
+          keys, vals, lscratch, rscratch, rl[r & 1], r == 0 ? counts + 3 : rcount + r, rwork + r,
+          rl[(r + 1) & 1], rcount + r + 1, tasks.f, tasks.n, tasks.d, counts + 4, counts + 5,
+          counts + 7, tasks.cap, tasks.pair_reserve);
+      if (((r + 1) & r) == 0) {
+        uint32_t next = 0;
+        cudaError_t e = cudaMemcpyAsync(&next, rcount + r + 1, sizeof(next),
+                                        cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        if (e != cudaSuccess) return e;
+        if (next == 0) break;
+      }
+    }
+  }
   count_launch();
   sort_tasks<<<num_sms * 3, kBlock, sizeof(CtaSmem), stream>>>(keys, vals, tasks.f, tasks.n, tasks.d,
                                                            counts + 4);
