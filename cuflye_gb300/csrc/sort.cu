@@ -681,7 +681,8 @@ __global__ void __launch_bounds__(kBlock, 3) sort_cta(uint64_t* K, uint32_t* V,
 // depends on its own elements only, so the rounds give libstdc++'s result in
 // a breadth-first order, and every CTA has work while ranges remain.
 
-constexpr int kBigBlock = 256;
+constexpr int kBigBlock = 512;
+constexpr int kBigPerSm = 2;
 
 struct RoundItem {
   uint64_t f;
@@ -729,7 +730,7 @@ __global__ void round_seed(const uint64_t* __restrict__ begin, const uint64_t* _
   }
 }
 
-__global__ void __launch_bounds__(kBigBlock, 4)
+__global__ void __launch_bounds__(kBigBlock, kBigPerSm)
     sort_round(uint64_t* K, uint32_t* V, uint32_t* Lg, uint32_t* Rg,
                const RoundItem* __restrict__ in, const uint32_t* __restrict__ in_count,
                uint32_t* work, RoundItem* out, uint32_t* out_count, uint64_t* task_f,
@@ -1298,7 +1299,7 @@ cudaError_t segmented_std_sort(uint64_t* keys, uint32_t* vals, uint32_t* lscratc
         begin, end, lists + 3 * static_cast<size_t>(nseg), counts, rl[0]);
     for (int r = 0; r < kSortRounds; ++r) {
       count_launch();
-      sort_round<<<num_sms * 4, kBigBlock, 0, stream>>>(
+      sort_round<<<num_sms * kBigPerSm, kBigBlock, 0, stream>>>(
           keys, vals, lscratch, rscratch, rl[r & 1], r == 0 ? counts + 3 : rcount + r, rwork + r,
           rl[(r + 1) & 1], rcount + r + 1, tasks.f, tasks.n, tasks.d, counts + 4, counts + 5,
           counts + 7, tasks.cap, tasks.pair_reserve);
