@@ -78,20 +78,26 @@ __global__ void __launch_bounds__(kGroupBlock) group_tiles_kernel(
     atomicOr(&qbits[j >> 5], 1u << (j & 31));
   }
   __syncthreads();
-  uint64_t g = WRITE ? tile_off[blockIdx.x] : 0;
-  uint32_t total = 0;
+  // every round's ext ids (and their predecessors') in flight before any use
+  uint32_t ex[kGroupRounds], pe[kGroupRounds];
+#pragma unroll
   for (int r = 0; r < kGroupRounds; ++r) {
     const uint32_t j = static_cast<uint32_t>(r) * kGroupBlock + threadIdx.x;
     const uint64_t i = t0 + j;
-    bool start = false;
-    uint32_t e = 0;
-    if (j < tn) {
-      e = static_cast<uint32_t>(keys[i] >> 32);
-      start = i == 0 || ((qbits[j >> 5] >> (j & 31)) & 1u) ||
-              e != static_cast<uint32_t>(keys[i - 1] >> 32);
-    }
+    ex[r] = j < tn ? static_cast<uint32_t>(keys[i] >> 32) : 0u;
+    pe[r] = j < tn && i > 0 ? static_cast<uint32_t>(keys[i - 1] >> 32) : 0u;
+  }
+  uint64_t g = WRITE ? tile_off[blockIdx.x] : 0;
+  uint32_t total = 0;
+#pragma unroll
+  for (int r = 0; r < kGroupRounds; ++r) {
+    const uint32_t j = static_cast<uint32_t>(r) * kGroupBlock + threadIdx.x;
+    const uint64_t i = t0 + j;
+    const uint32_t e = ex[r];
+    const bool start =
+        j < tn && (i == 0 || ((qbits[j >> 5] >> (j & 31)) & 1u) || e != pe[r]);
     if (!WRITE) {
-      total += __syncthreads_count(start);
+      total += start;
       continue;
     }
     const unsigned m = __ballot_sync(0xffffffffu, start);
@@ -113,7 +119,17 @@ __global__ void __launch_bounds__(kGroupBlock) group_tiles_kernel(
     g += round_total;
     __syncthreads();
   }
-  if (!WRITE && threadIdx.x == 0) tile_counts[blockIdx.x] = total;
+  if (!WRITE) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) total += __shfl_xor_sync(0xffffffffu, total, o);
+    if (lane == 0) wsum[warp] = total;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      uint32_t t = 0;
+      for (int w = 0; w < kGroupBlock / 32; ++w) t += wsum[w];
+      tile_counts[blockIdx.x] = t;
+    }
+  }
 }
 
 __global__ void prefilter_kernel(const uint64_t* __restrict__ keys,

@@ -107,8 +107,18 @@ __global__ void __launch_bounds__(256) match_hist_kernel(Src src,
     h[threadIdx.x] = 0;
     __syncthreads();
     const MatchTile tl = tiles[t];
-    for (uint32_t j = threadIdx.x; j < tl.n; j += blockDim.x)
-      atomicAdd(&h[(src.hi(tl.begin + j) >> shift) & 0xffu], 1u);
+    // eight keys in flight per thread before their counts
+    for (uint32_t j0 = 0; j0 < tl.n; j0 += 8 * 256) {
+      uint32_t d[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const uint32_t j = j0 + u * 256 + threadIdx.x;
+        d[u] = j < tl.n ? (src.hi(tl.begin + j) >> shift) & 0xffu : 256u;
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (d[u] < 256u) atomicAdd(&h[d[u]], 1u);
+    }
     __syncthreads();
     counts[static_cast<uint64_t>(t) * 256 + threadIdx.x] = h[threadIdx.x];
     __syncthreads();
