@@ -148,14 +148,26 @@ __global__ void prefilter_kernel(const uint64_t* __restrict__ keys,
   // unique query positions (changes of curPos, starting from prevPos = 0)
   uint32_t uniq = 0;
   int32_t mn = INT_MAX, mx = INT_MIN;
-  for (uint32_t j = lane; j < n; j += 32) {
-    const uint64_t i = gi.start + j;
-    const int32_t c = static_cast<int32_t>(keys[i] & 0xffffffffu);
-    const int32_t prev = j == 0 ? 0 : static_cast<int32_t>(keys[i - 1] & 0xffffffffu);
-    uniq += c != prev;
-    const int32_t e = static_cast<int32_t>(vals[i]);
-    mn = min(mn, e);
-    mx = max(mx, e);
+  // four rounds of loads in flight per lane
+  for (uint32_t j0 = lane; j0 < n; j0 += 4 * 32) {
+    int32_t c[4], pc[4], e[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t j = j0 + 32 * u;
+      const uint64_t i = gi.start + j;
+      const bool ok = j < n;
+      c[u] = ok ? static_cast<int32_t>(keys[i] & 0xffffffffu) : 0;
+      pc[u] = ok && j > 0 ? static_cast<int32_t>(keys[i - 1] & 0xffffffffu) : 0;
+      e[u] = ok ? static_cast<int32_t>(vals[i]) : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      if (j0 + 32 * u < n) {
+        uniq += c[u] != pc[u];
+        mn = min(mn, e[u]);
+        mx = max(mx, e[u]);
+      }
+    }
   }
   for (int d = 16; d > 0; d >>= 1) {
     uniq += __shfl_down_sync(0xffffffffu, uniq, d);
@@ -223,8 +235,17 @@ __global__ void ext_presorted_kernel(const uint32_t* __restrict__ vals,
     const uint32_t gid = ext_list[li];
     const GroupInfo g = groups[gid];
     bool up = true;
-    for (uint32_t j = lane + 1; j < g.n && up; j += 32)
-      up = vals[g.start + j] > vals[g.start + j - 1];
+    for (uint32_t j0 = lane + 1; j0 < g.n && up; j0 += 4 * 32) {
+      uint32_t a[4], b[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const uint32_t j = j0 + 32 * u;
+        a[u] = j < g.n ? vals[g.start + j] : 1u;
+        b[u] = j < g.n ? vals[g.start + j - 1] : 0u;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) up &= a[u] > b[u];
+    }
     up = __all_sync(0xffffffffu, up);
     if (lane == 0) {
       if (up)
