@@ -78,14 +78,17 @@ __global__ void __launch_bounds__(kGroupBlock) group_tiles_kernel(
     atomicOr(&qbits[j >> 5], 1u << (j & 31));
   }
   __syncthreads();
-  // every round's ext ids (and their predecessors') in flight before any use
+  // counting: every round's ext ids (and their predecessors') in flight
+  // before any use; writing: one round at a time (fewer registers)
   uint32_t ex[kGroupRounds], pe[kGroupRounds];
+  if (!WRITE) {
 #pragma unroll
-  for (int r = 0; r < kGroupRounds; ++r) {
-    const uint32_t j = static_cast<uint32_t>(r) * kGroupBlock + threadIdx.x;
-    const uint64_t i = t0 + j;
-    ex[r] = j < tn ? static_cast<uint32_t>(keys[i] >> 32) : 0u;
-    pe[r] = j < tn && i > 0 ? static_cast<uint32_t>(keys[i - 1] >> 32) : 0u;
+    for (int r = 0; r < kGroupRounds; ++r) {
+      const uint32_t j = static_cast<uint32_t>(r) * kGroupBlock + threadIdx.x;
+      const uint64_t i = t0 + j;
+      ex[r] = j < tn ? static_cast<uint32_t>(keys[i] >> 32) : 0u;
+      pe[r] = j < tn && i > 0 ? static_cast<uint32_t>(keys[i - 1] >> 32) : 0u;
+    }
   }
   uint64_t g = WRITE ? tile_off[blockIdx.x] : 0;
   uint32_t total = 0;
@@ -93,9 +96,16 @@ __global__ void __launch_bounds__(kGroupBlock) group_tiles_kernel(
   for (int r = 0; r < kGroupRounds; ++r) {
     const uint32_t j = static_cast<uint32_t>(r) * kGroupBlock + threadIdx.x;
     const uint64_t i = t0 + j;
-    const uint32_t e = ex[r];
+    uint32_t e, prev;
+    if (!WRITE) {
+      e = ex[r];
+      prev = pe[r];
+    } else {
+      e = j < tn ? static_cast<uint32_t>(keys[i] >> 32) : 0u;
+      prev = j < tn && i > 0 ? static_cast<uint32_t>(keys[i - 1] >> 32) : 0u;
+    }
     const bool start =
-        j < tn && (i == 0 || ((qbits[j >> 5] >> (j & 31)) & 1u) || e != pe[r]);
+        j < tn && (i == 0 || ((qbits[j >> 5] >> (j & 31)) & 1u) || e != prev);
     if (!WRITE) {
       total += start;
       continue;

@@ -155,13 +155,22 @@ __global__ void __launch_bounds__(256) match_offsets_kernel(const uint32_t* __re
     if (nt == 0) continue;
     const uint64_t t0 = tile_off[q];
     uint32_t tot = 0;
+#pragma unroll 8
     for (uint32_t t = 0; t < nt; ++t) tot += counts[(t0 + t) * 256 + d];
     uint32_t run = block256_exclusive(tot, ws);
-    for (uint32_t t = 0; t < nt; ++t) {
-      const uint64_t ix = (t0 + t) * 256 + d;
-      const uint32_t c = counts[ix];
-      counts[ix] = run;
-      run += c;
+    // eight tiles' counts in flight, then their offsets
+    for (uint32_t t8 = 0; t8 < nt; t8 += 8) {
+      uint32_t c[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        c[u] = t8 + u < nt ? counts[(t0 + t8 + u) * 256 + d] : 0u;
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        if (t8 + u < nt) {
+          counts[(t0 + t8 + u) * 256 + d] = run;
+          run += c[u];
+        }
+      }
     }
   }
 }
