@@ -170,7 +170,7 @@ struct QueryInfo {
 // (emu_begin, emu_end, *emu_count) for segmented_std_sort.
 constexpr uint32_t kMatchTile = 4096;  // hits per radix tile (never across queries)
 constexpr uint32_t kGroupCap = 16384;      // largest group re-sorted in shared memory
-constexpr uint32_t kBacktrackCap = 16384;  // largest group backtracked over shared-memory maps
+constexpr uint32_t kBacktrackCap = 8192;  // largest group backtracked over shared-memory maps
 
 struct MatchTile {
   uint64_t begin;
