@@ -350,7 +350,7 @@ __device__ __forceinline__ void load_match(const uint64_t* __restrict__ keys,
   e = static_cast<int32_t>(swapped ? lo : v);
 }
 
-__global__ void __launch_bounds__(kDpWarps * 32, 6) dp_kernel(
+__global__ void __launch_bounds__(kDpWarps * 32, 8) dp_kernel(
     const uint64_t* __restrict__ keys, const uint32_t* __restrict__ vals, int32_t* score,
     int32_t* bt, const GroupInfo* __restrict__ groups, const uint32_t* __restrict__ list,
     const uint32_t* __restrict__ counts, ChainParams p, GroupTop* __restrict__ top,
