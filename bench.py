@@ -421,8 +421,9 @@ def run_ours(args, world, rank, local) -> None:
     barrier(world)
     L.cuflye_kernel_launches(ctypes.byref(launches))
     l0 = launches.value
-    sampler = ClockSampler(local, REPO / "gpurun_out" / f"clocks_rank{rank}.csv") \
-        if (REPO / "gpurun_out").exists() else ClockSampler(local, Path("/tmp/cuflye_clocks.csv"))
+    log = Path(args.clock_log.format(rank=rank)) if args.clock_log else \
+        Path(f"/tmp/cuflye_clocks_rank{rank}.csv")
+    sampler = ClockSampler(local, log)
     dev_ms, wall_s, stage_tot, bytes_tot = [], [], np.zeros(7), np.zeros(7)
     nrows = 0
     for _ in range(args.steps):
@@ -551,6 +552,9 @@ def main() -> int:
                     default=[1000.0, 10000.0, 50000.0],
                     help="offered request rates (reads/s) of the serving run; empty skips it")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
+    ap.add_argument("--clock-log", default="",
+                    help="where the nvidia-smi clock samples of the timed region go "
+                         "({rank} is replaced); default /tmp")
     ap.add_argument("--configs", default="1,3",
                     help="other configurations to measure (1: plain 1 Mb, 3: read-to-graph); "
                          "empty to skip")
