@@ -83,6 +83,7 @@ struct cuflye_ctx {
   uint64_t stage_bytes[7]{};
   uint64_t sort_stats[7]{};  // see cuflye_last_sort_stats
   uint64_t passes = 0;       // see cuflye_last_passes
+  int servers = 0;           // open serving loops borrowing this index
 };
 
 namespace {
@@ -963,6 +964,8 @@ cuflye_status cuflye_index_build(cuflye_ctx* c, int k, size_t n, const int64_t* 
   CUFLYE_API_BEGIN(c)
   CUFLYE_CHECK(cudaSetDevice(c->device));
   if (!ids || !offsets || (!bases && n)) throw Error(CUFLYE_ERR_INVALID, "null input");
+  if (c->servers)
+    throw Error(CUFLYE_ERR_INVALID, "a serving loop borrows this context's index; close it first");
   build_index(c, k, n, ids, offsets, bases, min_freq, max_freq);
   CUFLYE_API_END(c)
 }
@@ -972,6 +975,8 @@ cuflye_status cuflye_index_from_entries(cuflye_ctx* c, int k, size_t n, const in
                                         size_t n_rep, const uint64_t* rep_keys) {
   CUFLYE_API_BEGIN(c)
   CUFLYE_CHECK(cudaSetDevice(c->device));
+  if (c->servers)
+    throw Error(CUFLYE_ERR_INVALID, "a serving loop borrows this context's index; close it first");
   build_index_entries(c, k, n, tids, positions, keys, n_rep, rep_keys);
   CUFLYE_API_END(c)
 }
@@ -1480,6 +1485,7 @@ cuflye_status cuflye_server_open(cuflye_ctx* owner, int workers,
     s->workers.push_back(c);
   }
   for (cuflye_ctx* c : s->workers) s->threads.emplace_back(serve_worker, s, c);
+  ++owner->servers;
   *out = s;
   CUFLYE_API_END(owner)
 }
@@ -1578,6 +1584,10 @@ void cuflye_server_close(cuflye_server* s) {
   s->cv_work.notify_all();
   for (std::thread& t : s->threads) t.join();
   for (cuflye_ctx* c : s->workers) cuflye_close(c);
+  {
+    std::lock_guard<std::mutex> g(s->owner->mu);
+    --s->owner->servers;
+  }
   delete s;
 }
 

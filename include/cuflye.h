@@ -265,8 +265,9 @@ cuflye_status cuflye_std_sort_segments_noalloc(uint64_t* keys, uint32_t* values,
  * the reference.
  *
  * cuflye_server_open borrows `owner`'s resident index (the owner must keep it
- * and stay open until cuflye_server_close) and starts `workers` (1-8) worker
- * contexts, each with its own stream and device arena; the owner's budget
+ * and stay open until cuflye_server_close; rebuilding the owner's index while
+ * a server is open fails with CUFLYE_ERR_INVALID) and starts `workers` (1-8)
+ * worker contexts, each with its own stream and device arena; the owner's budget
  * left over (or the free device memory less 8 GiB when unbounded) is split
  * between them.  A worker that falls idle takes every request that has
  * arrived, up to max_batch_bases query bases (0 = no limit), and runs them

@@ -73,5 +73,8 @@ def test_server_errors(gpu, golden_cases):
         assert rows is not None
         with pytest.raises(CuflyeError):
             srv.poll(t, 0)  # consumed
+        with pytest.raises(CuflyeError):  # the server borrows the index
+            gpu.build_index(reads, meta["k"], meta["min_freq"], meta["max_freq"])
+    gpu.build_index(reads, meta["k"], meta["min_freq"], meta["max_freq"])  # closed: fine
     with pytest.raises(CuflyeError):  # k of the params must match the index
         CudaServer(gpu, OverlapParams.make(**dict(meta["params"], kmer_size=meta["k"] + 2)))
