@@ -60,3 +60,36 @@ def test_long_ont_reads_match_oracle(gpu, oracle_mod, scale_case):
         exp = oracle_mod.overlaps(idx, b, oracle_mod.default_params(**params))
         assert len(got) > 0
         assert overlap_tuples_gpu(got) == overlap_tuples_oracle(exp), variant
+
+
+def test_read_to_graph_passes_do_not_change_rows(built_lib):
+    """Read-to-graph chains (ids numbered across the whole call) are the same
+    in one pass and in passes of 37 reads."""
+    from cuflye_gb300 import synth
+    from cuflye_gb300.backend import CudaBackend, OverlapParams, R2GParams
+    wl = synth.read_to_graph(seed=7, genome_len=2_000_000, n_edges=60, coverage=6.0)
+    g = wl.graph
+    p = OverlapParams.make(**wl.params)
+    r = R2GParams.make(**synth.R2G_PARAMS)
+    with CudaBackend(device=0, memory_budget_bytes=0) as be:
+        be.build_index(g.seqs, wl.k, wl.min_freq, wl.max_freq)
+        be.set_graph(g.edge_ids, g.seq_ids, g.left, g.right)
+        whole = be.read_to_graph(wl.reads, p, r)
+        be.set_batch_queries(37)
+        split = be.read_to_graph(wl.reads, p, r)
+        assert be.last_passes() == -(-wl.reads.n // 37)
+    assert len(whole) > 0
+    assert split.tobytes() == whole.tobytes()
+
+
+def test_candidates_passes_do_not_change_records(built_lib, scale_case):
+    from cuflye_gb300.backend import CudaBackend
+    wl = scale_case
+    q = wl.reads.subset(np.arange(200))
+    with CudaBackend(device=0, memory_budget_bytes=0) as be:
+        be.build_index(wl.reads, wl.k, wl.min_freq, wl.max_freq)
+        cand, filt = be.candidates(q)
+        be.set_batch_queries(29)
+        cand2, filt2 = be.candidates(q)
+    assert len(cand) > 0
+    assert cand2.tobytes() == cand.tobytes() and filt2.tobytes() == filt.tobytes()
