@@ -138,6 +138,10 @@ def load_library(path: Path | None = None) -> ctypes.CDLL:
     L.cuflye_last_sort_stats.argtypes = [_vp, _u64p, ctypes.c_size_t]
     L.cuflye_last_passes.restype = S
     L.cuflye_last_passes.argtypes = [_vp, _u64p]
+    L.cuflye_set_index_build_windows.restype = S
+    L.cuflye_set_index_build_windows.argtypes = [_vp, ctypes.c_uint64]
+    L.cuflye_last_index_ranges.restype = S
+    L.cuflye_last_index_ranges.argtypes = [_vp, _u64p]
     L.cuflye_server_open.restype = S
     L.cuflye_server_open.argtypes = [_vp, ctypes.c_int, ctypes.POINTER(OverlapParams),
                                      ctypes.c_uint64, ctypes.POINTER(_vp)]
@@ -263,6 +267,16 @@ class CudaBackend:
         """Passes (runs of queries through the device) of the last call."""
         v = ctypes.c_uint64()
         self._check(self._L.cuflye_last_passes(self._h, ctypes.byref(v)))
+        return int(v.value)
+
+    def set_index_build_windows(self, max_windows: int) -> None:
+        """Caps the windows of one key range of the index build (0: budget decides)."""
+        self._check(self._L.cuflye_set_index_build_windows(self._h, int(max_windows)))
+
+    def last_index_ranges(self) -> int:
+        """Key ranges the last index build ran in (1: all windows at once)."""
+        v = ctypes.c_uint64()
+        self._check(self._L.cuflye_last_index_ranges(self._h, ctypes.byref(v)))
         return int(v.value)
 
     # -- index

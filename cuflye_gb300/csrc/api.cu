@@ -83,6 +83,8 @@ struct cuflye_ctx {
   uint64_t stage_bytes[7]{};
   uint64_t sort_stats[7]{};  // see cuflye_last_sort_stats
   uint64_t passes = 0;       // see cuflye_last_passes
+  uint64_t build_window_cap = 0;  // see cuflye_set_index_build_windows
+  uint64_t build_ranges = 0;      // key ranges of the last index build
   int servers = 0;           // open serving loops borrowing this index
 };
 
@@ -210,7 +212,244 @@ int bits_for(uint64_t v) {
   return b;
 }
 
+// The memory budget, or the device's memory less an 8 GiB margin when unbounded.
+uint64_t effective_budget(cuflye_ctx* c) {
+  if (c->budget) return c->budget;
+  size_t free_b = 0, total_b = 0;
+  CUFLYE_CHECK(cudaMemGetInfo(&free_b, &total_b));
+  const uint64_t cap = static_cast<uint64_t>(free_b) + c->in_use;
+  const uint64_t margin = 8ull << 30;
+  return cap > margin ? cap - margin : cap / 2;
+}
+
 // ---------------------------------------------------------------- index build
+
+// The windows of the packed targets (device arrays).
+struct WindowSet {
+  const uint64_t* words;
+  const uint64_t* base_off;
+  const uint64_t* win_off;
+  const int32_t* slot_len;
+  uint32_t nslots;
+  uint64_t nwin;
+  int k;
+};
+
+struct BuiltIndex {
+  TableEntry* table = nullptr;
+  uint64_t cap = 0;
+  uint64_t* pos = nullptr;
+  uint64_t npos = 0, nsolid = 0, nrep = 0;
+};
+
+// Scratch of one key range's build.
+const char* const kBuildScratch[] = {"ib_keys",  "ib_vals",     "ib_keys2", "ib_vals2",
+                                     "ib_hist",  "ib_flags",    "ib_runid", "ib_runstart",
+                                     "ib_kept",  "ib_cls",      "ib_keptoff", "ib_scan",
+                                     "ib_prefix", "ib_count"};
+
+void release_build_scratch(cuflye_ctx* c) {
+  for (const char* t : kBuildScratch) release(c, t);
+}
+
+// Runs of nw windows sorted by (key, stored id, stored position).
+struct KeyRuns {
+  uint64_t* keys;
+  uint64_t* vals;
+  uint64_t* run_id;
+  uint64_t* run_start;
+  uint8_t* cls;
+  uint64_t* kept_off;
+  uint64_t nruns, npos, nsolid, nrep;
+};
+
+// Sorts the windows in ib_keys / ib_vals (the alternates ib_keys2 / ib_vals2
+// already sized), finds their runs and classifies them (solid, repetitive).
+KeyRuns sort_and_classify(cuflye_ctx* c, uint64_t nw, const std::vector<int>& digits,
+                          uint32_t min_freq, uint32_t max_freq) {
+  cudaStream_t st = c->stream;
+  uint64_t* keys = buf<uint64_t>(c, "ib_keys", nw);
+  uint64_t* vals = buf<uint64_t>(c, "ib_vals", nw);
+  uint64_t* keys2 = buf<uint64_t>(c, "ib_keys2", nw);
+  uint64_t* vals2 = buf<uint64_t>(c, "ib_vals2", nw);
+  uint32_t* hist = buf<uint32_t>(c, "ib_hist", radix_hist_words(nw));
+  int in_alt = 0;
+  if (nw)
+    CUFLYE_CHECK(radix_sort_pairs(keys, vals, keys2, vals2, nw, digits.data(),
+                                  static_cast<int>(digits.size()), hist, &in_alt, st));
+  if (in_alt) {
+    std::swap(keys, keys2);
+    std::swap(vals, vals2);
+  }
+  uint32_t* flags = buf<uint32_t>(c, "ib_flags", nw);
+  uint64_t* run_id = buf<uint64_t>(c, "ib_runid", nw + 1);
+  CUFLYE_CHECK(index_mark_runs(keys, nw, flags, st));
+  const uint64_t nruns = scan_u32(c, flags, run_id, nw, "ib_scan");
+  uint64_t* run_start = buf<uint64_t>(c, "ib_runstart", nruns + 1);
+  CUFLYE_CHECK(index_run_starts(flags, run_id, nw, nruns, run_start, st));
+  uint32_t* kept = buf<uint32_t>(c, "ib_kept", nruns);
+  uint8_t* cls = buf<uint8_t>(c, "ib_cls", nruns);
+  unsigned long long* tally = buf<unsigned long long>(c, "ib_count", 4);
+  CUFLYE_CHECK(index_classify_runs(run_start, nruns, min_freq, max_freq, kept, cls, tally, st));
+  uint64_t* kept_off = buf<uint64_t>(c, "ib_keptoff", nruns + 1);
+  const uint64_t npos = scan_u32(c, kept, kept_off, nruns, "ib_scan");
+  unsigned long long t[2];
+  CUFLYE_CHECK(cudaMemcpyAsync(t, tally, sizeof(t), cudaMemcpyDeviceToHost, st));
+  sync(c);
+  return KeyRuns{keys, vals, run_id, run_start, cls, kept_off, nruns, npos, t[0], t[1]};
+}
+
+uint64_t table_capacity(uint64_t entries) {
+  uint64_t cap = 16;
+  while (cap < 2 * entries) cap <<= 1;
+  return cap;
+}
+
+// All windows at once; the table is sized for every run (solid, repetitive
+// and absent) at load <= 1/2.
+BuiltIndex build_one_range(cuflye_ctx* c, const WindowSet& w, const std::vector<int>& digits,
+                           uint32_t min_freq, uint32_t max_freq) {
+  cudaStream_t st = c->stream;
+  // the four sort arrays first: a build that cannot hold them fails before any work
+  uint64_t* keys = buf<uint64_t>(c, "ib_keys", w.nwin);
+  uint64_t* vals = buf<uint64_t>(c, "ib_vals", w.nwin);
+  buf<uint64_t>(c, "ib_keys2", w.nwin);
+  buf<uint64_t>(c, "ib_vals2", w.nwin);
+  CUFLYE_CHECK(index_enumerate(w.words, w.base_off, w.win_off, w.slot_len, w.nslots, w.nwin,
+                               w.k, keys, vals, st));
+  const KeyRuns r = sort_and_classify(c, w.nwin, digits, min_freq, max_freq);
+  if (r.npos >= (1ull << 40)) throw Error(CUFLYE_ERR_UNSUPPORTED, "index larger than 2^40 entries");
+  BuiltIndex bi;
+  bi.pos = buf<uint64_t>(c, "ix_pos", r.npos);
+  CUFLYE_CHECK(index_copy_positions(r.vals, r.run_id, r.run_start, r.cls, r.kept_off, w.nwin,
+                                    bi.pos, st));
+  bi.cap = table_capacity(r.nruns);
+  bi.table = buf<TableEntry>(c, "ix_table", bi.cap);
+  CUFLYE_CHECK(cudaMemsetAsync(bi.table, 0xff, bi.cap * sizeof(TableEntry), st));
+  CUFLYE_CHECK(index_insert(r.keys, r.vals, r.run_start, r.cls, r.kept_off, r.nruns, true,
+                            bi.table, bi.cap - 1, c->status, st));
+  check_device_status(c);
+  bi.npos = r.npos;
+  bi.nsolid = r.nsolid;
+  bi.nrep = r.nrep;
+  return bi;
+}
+
+// Device bytes one window of a key range needs while the range is built: the
+// radix sort's two key/value pairs (32), run flag and id (12), the run
+// tables (21, at most one run per window) and the range's outputs (8 per
+// solid position, 16 per staged table entry), with margin.
+constexpr uint64_t kRangeBytesPerWindow = 96;
+constexpr int kPrefixBits = 14;
+
+// The index built one contiguous key range at a time, each range sized to
+// what the memory budget leaves (and to the caller's window cap).  Ranges
+// are cut from a histogram of key prefixes; a range's solid positions follow
+// the previous range's, so the position array equals the one-range build's.
+BuiltIndex build_key_ranges(cuflye_ctx* c, const WindowSet& w, const std::vector<int>& digits,
+                            uint32_t min_freq, uint32_t max_freq) {
+  cudaStream_t st = c->stream;
+  const int bits = std::min(2 * w.k, kPrefixBits);
+  const int shift = 2 * w.k - bits;
+  const int nbins = 1 << bits;
+  std::vector<unsigned long long> hist(nbins);
+  {
+    unsigned long long* d_hist = buf<unsigned long long>(c, "ib_prefix", nbins);
+    CUFLYE_CHECK(index_prefix_hist(w.words, w.base_off, w.win_off, w.slot_len, w.nslots, w.nwin,
+                                   w.k, shift, nbins, d_hist, c->num_sms, st));
+    CUFLYE_CHECK(cudaMemcpyAsync(hist.data(), d_hist, nbins * sizeof(unsigned long long),
+                                 cudaMemcpyDeviceToHost, st));
+    sync(c);
+    release(c, "ib_prefix");
+  }
+  struct RangeOut {
+    std::string pos_name, ek_name, em_name;
+    uint64_t pos_base, npos, nent;
+  };
+  std::vector<RangeOut> outs;
+  uint64_t pos_base = 0, nsolid = 0, nrep = 0;
+  int b = 0;
+  while (b < nbins) {
+    const uint64_t limit = effective_budget(c);
+    const uint64_t avail = limit > c->in_use ? limit - c->in_use : 0;
+    uint64_t cap = avail / kRangeBytesPerWindow;
+    if (c->build_window_cap) cap = std::min(cap, c->build_window_cap);
+    int e = b;
+    uint64_t nw = 0;
+    while (e < nbins && nw + hist[e] <= cap) nw += hist[e++];
+    if (e == b)
+      throw Error(CUFLYE_ERR_BUDGET,
+                  "k-mer index build: " + std::to_string(hist[b]) +
+                      " windows share one key prefix and need about " +
+                      std::to_string(hist[b] * kRangeBytesPerWindow) + " bytes; " +
+                      std::to_string(avail) + " bytes are left in the memory budget");
+    const uint64_t lo = static_cast<uint64_t>(b) << shift;
+    const uint64_t hi = static_cast<uint64_t>(e) << shift;
+    b = e;
+    if (nw == 0) continue;
+    uint64_t* keys = buf<uint64_t>(c, "ib_keys", nw);
+    uint64_t* vals = buf<uint64_t>(c, "ib_vals", nw);
+    buf<uint64_t>(c, "ib_keys2", nw);
+    buf<uint64_t>(c, "ib_vals2", nw);
+    unsigned long long* count = buf<unsigned long long>(c, "ib_count", 4);
+    CUFLYE_CHECK(index_enumerate_range(w.words, w.base_off, w.win_off, w.slot_len, w.nslots,
+                                       w.nwin, w.k, lo, hi, keys, vals, count, nw, st));
+    const unsigned long long got = read_scalar(c, count);
+    if (got != nw)
+      throw Error(CUFLYE_ERR_CUDA, "k-mer index build: key range [" + std::to_string(lo) + ", " +
+                                       std::to_string(hi) + ") enumerated " +
+                                       std::to_string(got) + " windows, the histogram " +
+                                       std::to_string(nw));
+    const KeyRuns r = sort_and_classify(c, nw, digits, min_freq, max_freq);
+    const uint64_t nent = r.nsolid + r.nrep;
+    RangeOut o{"ib_pos" + std::to_string(outs.size()), "ib_ek" + std::to_string(outs.size()),
+               "ib_em" + std::to_string(outs.size()), pos_base, r.npos, nent};
+    uint64_t* pos = buf<uint64_t>(c, o.pos_name, r.npos);
+    CUFLYE_CHECK(index_copy_positions(r.vals, r.run_id, r.run_start, r.cls, r.kept_off, nw, pos,
+                                      st));
+    uint64_t* ek = buf<uint64_t>(c, o.ek_name, nent);
+    uint64_t* em = buf<uint64_t>(c, o.em_name, nent);
+    CUFLYE_CHECK(index_stage_entries(r.keys, r.vals, r.run_start, r.cls, r.kept_off, r.nruns,
+                                     pos_base, ek, em, count, nent, st));
+    const unsigned long long staged = read_scalar(c, count);
+    if (staged != nent)
+      throw Error(CUFLYE_ERR_CUDA, "k-mer index build: staged " + std::to_string(staged) +
+                                       " table entries of " + std::to_string(nent));
+    release_build_scratch(c);
+    outs.push_back(o);
+    pos_base += r.npos;
+    nsolid += r.nsolid;
+    nrep += r.nrep;
+  }
+  if (pos_base >= (1ull << 40)) throw Error(CUFLYE_ERR_UNSUPPORTED, "index larger than 2^40 entries");
+  for (const char* t : {"ib_words", "ib_base", "ib_win"}) release(c, t);
+  BuiltIndex bi;
+  bi.cap = table_capacity(nsolid + nrep);
+  bi.table = buf<TableEntry>(c, "ix_table", bi.cap);
+  CUFLYE_CHECK(cudaMemsetAsync(bi.table, 0xff, bi.cap * sizeof(TableEntry), st));
+  for (const RangeOut& o : outs) {
+    CUFLYE_CHECK(index_insert_staged(buf<uint64_t>(c, o.ek_name, o.nent),
+                                     buf<uint64_t>(c, o.em_name, o.nent), o.nent, bi.table,
+                                     bi.cap - 1, c->status, st));
+    sync(c);
+    release(c, o.ek_name);
+    release(c, o.em_name);
+  }
+  check_device_status(c);
+  bi.pos = buf<uint64_t>(c, "ix_pos", pos_base);
+  for (const RangeOut& o : outs) {
+    if (o.npos)
+      CUFLYE_CHECK(cudaMemcpyAsync(bi.pos + o.pos_base, buf<uint64_t>(c, o.pos_name, o.npos),
+                                   o.npos * sizeof(uint64_t), cudaMemcpyDeviceToDevice, st));
+    sync(c);
+    release(c, o.pos_name);
+  }
+  bi.npos = pos_base;
+  bi.nsolid = nsolid;
+  bi.nrep = nrep;
+  c->build_ranges = outs.size();
+  return bi;
+}
 
 void build_index(cuflye_ctx* c, int k, size_t n, const int64_t* ids, const int64_t* offsets,
                  const char* bases, uint32_t min_freq, uint32_t max_freq) {
@@ -251,10 +490,25 @@ void build_index(cuflye_ctx* c, int k, size_t n, const int64_t* ids, const int64
   const uint64_t nbases = static_cast<uint64_t>(offsets[n] - offsets[0]);
   const uint64_t nwin = win_off[n];
   cudaStream_t st = c->stream;
-  uint8_t* d_ascii = buf<uint8_t>(c, "ib_ascii", nbases + 16);
-  CUFLYE_CHECK(cudaMemcpyAsync(d_ascii, bases + offsets[0], nbases, cudaMemcpyHostToDevice, st));
+  // the previous index's arrays go first (has_index is false from here on)
+  release(c, "ix_pos");
+  release(c, "ix_table");
+  // bases packed in chunks of 256 MiB (a multiple of 32 bases: chunks start on
+  // word boundaries; each chunk's trailing pad word is overwritten by the next)
   uint64_t* words = buf<uint64_t>(c, "ib_words", (nbases + 31) / 32 + 2);
-  CUFLYE_CHECK(pack_bases(d_ascii, nbases, words, st));
+  {
+    const uint64_t chunk = std::min<uint64_t>(nbases, 256ull << 20);
+    uint8_t* d_ascii = buf<uint8_t>(c, "ib_ascii", chunk + 16);
+    for (uint64_t b0 = 0; b0 < nbases; b0 += chunk) {
+      const uint64_t len = std::min(chunk, nbases - b0);
+      CUFLYE_CHECK(cudaMemcpyAsync(d_ascii, bases + offsets[0] + b0, len,
+                                   cudaMemcpyHostToDevice, st));
+      CUFLYE_CHECK(pack_bases(d_ascii, len, words + b0 / 32, st));
+    }
+    if (nbases == 0) CUFLYE_CHECK(cudaMemsetAsync(words, 0, 16, st));
+    sync(c);
+    release(c, "ib_ascii");
+  }
   uint64_t* d_base = buf<uint64_t>(c, "ib_base", n);
   uint64_t* d_win = buf<uint64_t>(c, "ib_win", n + 1);
   int32_t* d_len = buf<int32_t>(c, "ix_slot_len", n);
@@ -264,12 +518,7 @@ void build_index(cuflye_ctx* c, int k, size_t n, const int64_t* ids, const int64
   CUFLYE_CHECK(cudaMemcpyAsync(d_len, slot_len.data(), n * 4, cudaMemcpyHostToDevice, st));
   CUFLYE_CHECK(cudaMemcpyAsync(d_signed, c->slot_signed_h.data(), n * 8, cudaMemcpyHostToDevice,
                                st));
-  uint64_t* keys = buf<uint64_t>(c, "ib_keys", nwin);
-  uint64_t* vals = buf<uint64_t>(c, "ib_vals", nwin);
-  uint64_t* keys2 = buf<uint64_t>(c, "ib_keys2", nwin);
-  uint64_t* vals2 = buf<uint64_t>(c, "ib_vals2", nwin);
-  CUFLYE_CHECK(index_enumerate(words, d_base, d_win, d_len, static_cast<uint32_t>(n), nwin, k,
-                               keys, vals, st));
+  const WindowSet ws{words, d_base, d_win, d_len, static_cast<uint32_t>(n), nwin, k};
   // LSD digits: position bytes, stored-id bytes, key bytes
   std::vector<int> digits;
   const int pbytes = (bits_for(static_cast<uint64_t>(maxlen)) + 7) / 8;
@@ -278,63 +527,35 @@ void build_index(cuflye_ctx* c, int k, size_t n, const int64_t* ids, const int64
   for (int d = 0; d < pbytes; ++d) digits.push_back(d);
   for (int d = 0; d < dbytes; ++d) digits.push_back(4 + d);
   for (int d = 0; d < kbytes; ++d) digits.push_back(8 + d);
-  uint32_t* hist = buf<uint32_t>(c, "ib_hist", radix_hist_words(nwin));
-  int in_alt = 0;
-  if (nwin)
-    CUFLYE_CHECK(radix_sort_pairs(keys, vals, keys2, vals2, nwin, digits.data(),
-                                  static_cast<int>(digits.size()), hist, &in_alt, st));
-  if (in_alt) {
-    std::swap(keys, keys2);
-    std::swap(vals, vals2);
+  BuiltIndex bi;
+  bool ranges = c->build_window_cap != 0 && nwin > c->build_window_cap;
+  if (!ranges) {
+    try {
+      bi = build_one_range(c, ws, digits, min_freq, max_freq);
+      c->build_ranges = 1;
+    } catch (const Error& e) {
+      if (e.code != CUFLYE_ERR_BUDGET) throw;
+      sync(c);
+      release_build_scratch(c);
+      release(c, "ix_pos");
+      release(c, "ix_table");
+      ranges = true;
+    }
   }
-  // runs
-  uint32_t* flags = buf<uint32_t>(c, "ib_flags", nwin);
-  uint64_t* run_id = buf<uint64_t>(c, "ib_runid", nwin + 1);
-  CUFLYE_CHECK(index_mark_runs(keys, nwin, flags, st));
-  const uint64_t nruns = scan_u32(c, flags, run_id, nwin, "ib_scan");
-  uint64_t* run_start = buf<uint64_t>(c, "ib_runstart", nruns + 1);
-  CUFLYE_CHECK(index_run_starts(flags, run_id, nwin, nruns, run_start, st));
-  uint32_t* kept = buf<uint32_t>(c, "ib_kept", nruns);
-  uint8_t* cls = buf<uint8_t>(c, "ib_cls", nruns);
-  CUFLYE_CHECK(index_classify_runs(run_start, nruns, min_freq, max_freq, kept, cls, st));
-  uint64_t* kept_off = buf<uint64_t>(c, "ib_keptoff", nruns + 1);
-  const uint64_t npos = scan_u32(c, kept, kept_off, nruns, "ib_scan");
-  if (npos >= (1ull << 40)) throw Error(CUFLYE_ERR_UNSUPPORTED, "index larger than 2^40 entries");
-  uint64_t* pos = buf<uint64_t>(c, "ix_pos", npos);
-  CUFLYE_CHECK(index_copy_positions(vals, run_id, run_start, cls, kept_off, nwin, pos, st));
-  // table sized for every run (solid + repetitive + absent) at load <= 1/2
-  uint64_t cap = 16;
-  while (cap < 2 * nruns) cap <<= 1;
-  TableEntry* table = buf<TableEntry>(c, "ix_table", cap);
-  CUFLYE_CHECK(cudaMemsetAsync(table, 0xff, cap * sizeof(TableEntry), st));
-  CUFLYE_CHECK(index_insert(keys, vals, run_start, cls, kept_off, nruns, true, table, cap - 1,
-                            c->status, st));
-  check_device_status(c);
-  // statistics
-  std::vector<uint8_t> h_cls(nruns);
-  if (nruns)
-    CUFLYE_CHECK(cudaMemcpyAsync(h_cls.data(), cls, nruns, cudaMemcpyDeviceToHost, st));
-  sync(c);
-  uint64_t nsolid = 0, nrep = 0;
-  for (uint8_t v : h_cls) {
-    nsolid += v == 1;
-    nrep += v == 2;
-  }
-  for (const char* t : {"ib_ascii", "ib_words", "ib_base", "ib_win", "ib_keys", "ib_vals",
-                        "ib_keys2", "ib_vals2", "ib_hist", "ib_flags", "ib_runid", "ib_runstart",
-                        "ib_kept", "ib_cls", "ib_keptoff", "ib_scan"})
-    release(c, t);
+  if (ranges) bi = build_key_ranges(c, ws, digits, min_freq, max_freq);
+  release_build_scratch(c);
+  for (const char* t : {"ib_words", "ib_base", "ib_win"}) release(c, t);
   c->idx.k = k;
   c->idx.transform = true;
-  c->idx.table = table;
-  c->idx.mask = cap - 1;
-  c->idx.pos = pos;
-  c->idx.npos = npos;
+  c->idx.table = bi.table;
+  c->idx.mask = bi.cap - 1;
+  c->idx.pos = bi.pos;
+  c->idx.npos = bi.npos;
   c->idx.slot_len = d_len;
   c->idx.slot_signed = d_signed;
   c->idx.nslots = static_cast<uint32_t>(n);
-  c->idx.nkeys = nsolid + nrep;
-  c->idx.nrep = nrep;
+  c->idx.nkeys = bi.nsolid + bi.nrep;
+  c->idx.nrep = bi.nrep;
   c->has_index = true;
 }
 
@@ -396,7 +617,8 @@ void build_index_entries(cuflye_ctx* c, int k, size_t n, const int64_t* tids, co
   CUFLYE_CHECK(index_run_starts(flags, run_id, nn, nruns, run_start, st));
   uint32_t* kept = buf<uint32_t>(c, "ib_kept", nruns);
   uint8_t* cls = buf<uint8_t>(c, "ib_cls", nruns);
-  CUFLYE_CHECK(index_classify_runs(run_start, nruns, 1, (1u << kCountBits) - 2, kept, cls, st));
+  CUFLYE_CHECK(index_classify_runs(run_start, nruns, 1, (1u << kCountBits) - 2, kept, cls,
+                                    nullptr, st));
   uint64_t* kept_off = buf<uint64_t>(c, "ib_keptoff", nruns + 1);
   const uint64_t npos = scan_u32(c, kept, kept_off, nruns, "ib_scan");
   uint64_t* pos = buf<uint64_t>(c, "ix_pos", npos);
@@ -459,15 +681,6 @@ const char* const kPerHitBuffers[] = {"h_keys",  "h_vals",   "h_kmers", "s_l",  
                                       "m_tiles", "m_counts", "c_pmc",   "o_maps",  "g_tcount",
                                       "g_toff"};
 
-// The memory budget, or the device's memory less a 4 GiB margin when unbounded.
-uint64_t effective_budget(cuflye_ctx* c) {
-  if (c->budget) return c->budget;
-  size_t free_b = 0, total_b = 0;
-  CUFLYE_CHECK(cudaMemGetInfo(&free_b, &total_b));
-  const uint64_t cap = static_cast<uint64_t>(free_b) + c->in_use;
-  const uint64_t margin = 8ull << 30;
-  return cap > margin ? cap - margin : cap / 2;
-}
 
 // Upload a run of queries starting at q0 and produce the hits of the longest
 // prefix of them that fits in device memory (ps.nq queries), in Flye's
@@ -1292,6 +1505,18 @@ cuflye_status cuflye_last_sort_stats(const cuflye_ctx* c, uint64_t* counts, size
 cuflye_status cuflye_last_passes(const cuflye_ctx* c, uint64_t* passes) {
   if (!c || !passes) return CUFLYE_ERR_INVALID;
   *passes = c->passes;
+  return CUFLYE_OK;
+}
+
+cuflye_status cuflye_set_index_build_windows(cuflye_ctx* c, uint64_t max_windows) {
+  if (!c) return CUFLYE_ERR_INVALID;
+  c->build_window_cap = max_windows;
+  return CUFLYE_OK;
+}
+
+cuflye_status cuflye_last_index_ranges(const cuflye_ctx* c, uint64_t* ranges) {
+  if (!c || !ranges) return CUFLYE_ERR_INVALID;
+  *ranges = c->build_ranges;
   return CUFLYE_OK;
 }
 

@@ -13,6 +13,11 @@
 // Construction: enumerate windows -> stable LSD radix sort of
 // (key | stored id | stored position) -> run detection -> solid positions
 // copied in run order -> open-addressing insert (linear probing, load <= 1/2).
+// When the windows do not fit the memory budget at once, the same steps run
+// per contiguous key range (ranges cut from a histogram of key prefixes):
+// each range appends its solid positions after the previous range's and
+// stages its (key, table word) entries; the table is filled from the staged
+// entries at the end.  The position array is then the same as one range's.
 // A standard form never equals ~0 (the all-T k-mer's standard form is the
 // all-A k-mer, 0), so ~0 marks an empty slot.
 #include <cstdint>
@@ -37,25 +42,88 @@ __device__ __forceinline__ uint32_t find_segment(const uint64_t* __restrict__ of
   return lo;
 }
 
-__global__ void enumerate_kernel(const uint64_t* __restrict__ words,
-                                 const uint64_t* __restrict__ base_off,
-                                 const uint64_t* __restrict__ win_off,
-                                 const int32_t* __restrict__ slot_len, uint32_t nslots,
-                                 uint64_t nwin, int k, uint64_t* __restrict__ keys,
+struct Windows {
+  const uint64_t* __restrict__ words;
+  const uint64_t* __restrict__ base_off;
+  const uint64_t* __restrict__ win_off;
+  const int32_t* __restrict__ slot_len;
+  uint32_t nslots;
+  uint64_t nwin;
+  int k;
+
+  // Window w's standard-form key and (stored id << 32) | stored position.
+  __device__ __forceinline__ void entry(uint64_t w, uint64_t& key, uint64_t& val) const {
+    const uint32_t t = find_segment(win_off, nslots, w);
+    const uint64_t p = w - win_off[t];
+    const uint64_t x = kmer_at(words, base_off[t] + p, k);
+    const uint64_t rc = revcomp(x, k);
+    if (rc < x) {
+      key = rc;
+      val = (static_cast<uint64_t>(2u * t + 1u) << 32) |
+            static_cast<uint32_t>(slot_len[t] - static_cast<int32_t>(p) - k);
+    } else {
+      key = x;
+      val = (static_cast<uint64_t>(2u * t) << 32) | static_cast<uint32_t>(p);
+    }
+  }
+};
+
+__global__ void enumerate_kernel(Windows win, uint64_t* __restrict__ keys,
                                  uint64_t* __restrict__ vals) {
   const uint64_t w = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (w >= nwin) return;
-  const uint32_t t = find_segment(win_off, nslots, w);
-  const uint64_t p = w - win_off[t];
-  const uint64_t x = kmer_at(words, base_off[t] + p, k);
-  const uint64_t rc = revcomp(x, k);
-  if (rc < x) {
-    keys[w] = rc;
-    vals[w] = (static_cast<uint64_t>(2u * t + 1u) << 32) |
-              static_cast<uint32_t>(slot_len[t] - static_cast<int32_t>(p) - k);
-  } else {
-    keys[w] = x;
-    vals[w] = (static_cast<uint64_t>(2u * t) << 32) | static_cast<uint32_t>(p);
+  if (w >= win.nwin) return;
+  win.entry(w, keys[w], vals[w]);
+}
+
+// Windows per key prefix (key >> shift), counted in shared memory per block.
+__global__ void __launch_bounds__(1024) prefix_hist_kernel(Windows win, int shift, int nbins,
+                                                           unsigned long long* __restrict__ hist) {
+  extern __shared__ uint32_t bins[];
+  for (int i = threadIdx.x; i < nbins; i += blockDim.x) bins[i] = 0;
+  __syncthreads();
+  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+  for (uint64_t w = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x; w < win.nwin;
+       w += stride) {
+    uint64_t key, val;
+    win.entry(w, key, val);
+    atomicAdd(&bins[key >> shift], 1u);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nbins; i += blockDim.x)
+    if (bins[i]) atomicAdd(&hist[i], static_cast<unsigned long long>(bins[i]));
+}
+
+// Appends (warp-aggregated) the windows whose key lies in [lo, hi).  The
+// order of the appended entries does not matter: the radix sort that
+// follows orders them by (key, stored id, stored position), which is
+// distinct per window.
+__device__ __forceinline__ uint64_t warp_append(bool take, unsigned long long* count) {
+  const uint32_t m = __ballot_sync(0xffffffffu, take);
+  const int lane = threadIdx.x & 31;
+  unsigned long long base = 0;
+  if (m) {
+    const int leader = __ffs(m) - 1;
+    if (lane == leader) base = atomicAdd(count, static_cast<unsigned long long>(__popc(m)));
+    base = __shfl_sync(0xffffffffu, base, leader);
+  }
+  return base + __popc(m & ((1u << lane) - 1u));
+}
+
+__global__ void enumerate_range_kernel(Windows win, uint64_t lo, uint64_t hi,
+                                       uint64_t* __restrict__ keys, uint64_t* __restrict__ vals,
+                                       unsigned long long* count, uint64_t cap) {
+  // every warp is full (block 256, grid rounded up): lanes past the end take nothing
+  const uint64_t w = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  uint64_t key = 0, val = 0;
+  bool take = false;
+  if (w < win.nwin) {
+    win.entry(w, key, val);
+    take = key >= lo && key < hi;
+  }
+  const uint64_t i = warp_append(take, count);
+  if (take && i < cap) {
+    keys[i] = key;
+    vals[i] = val;
   }
 }
 
@@ -74,19 +142,30 @@ __global__ void run_starts_kernel(const uint32_t* __restrict__ flags,
   if (i == 0) run_start[nruns] = n;
 }
 
+// tally (optional): [0] += solid runs, [1] += repetitive runs.
 __global__ void classify_runs_kernel(const uint64_t* __restrict__ run_start, uint64_t nruns,
                                      uint32_t min_freq, uint32_t max_freq,
-                                     uint32_t* __restrict__ kept, uint8_t* __restrict__ cls) {
+                                     uint32_t* __restrict__ kept, uint8_t* __restrict__ cls,
+                                     unsigned long long* tally) {
   const uint64_t r = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (r >= nruns) return;
-  const uint64_t freq = run_start[r + 1] - run_start[r];
   uint8_t c = 0;
-  if (freq > max_freq)
-    c = 2;
-  else if (freq >= min_freq)
-    c = 1;
-  cls[r] = c;
-  kept[r] = c == 1 ? static_cast<uint32_t>(freq) : 0u;
+  if (r < nruns) {
+    const uint64_t freq = run_start[r + 1] - run_start[r];
+    if (freq > max_freq)
+      c = 2;
+    else if (freq >= min_freq)
+      c = 1;
+    cls[r] = c;
+    kept[r] = c == 1 ? static_cast<uint32_t>(freq) : 0u;
+  }
+  if (tally) {  // uniform over the launch: every lane of the warp is here
+    const uint32_t solid = __popc(__ballot_sync(0xffffffffu, c == 1));
+    const uint32_t rep = __popc(__ballot_sync(0xffffffffu, c == 2));
+    if ((threadIdx.x & 31) == 0) {
+      if (solid) atomicAdd(&tally[0], static_cast<unsigned long long>(solid));
+      if (rep) atomicAdd(&tally[1], static_cast<unsigned long long>(rep));
+    }
+  }
 }
 
 __global__ void copy_positions_kernel(const uint64_t* __restrict__ vals,
@@ -126,10 +205,27 @@ __device__ bool table_insert(TableEntry* table, uint64_t mask, uint64_t key, uin
   return false;
 }
 
-// vals: the run's entries, (stored id << 32) | stored position.  With
-// sorted_ids the entries of a run are in (id, position) order and a repeated
-// id shows as two neighbours; otherwise (explicit entries in input order)
-// every run of two or more entries is marked.
+// Table word of run r (class 1 solid or 2 repetitive) whose positions start
+// at pos_off in the position array.  vals: the run's entries, (stored id <<
+// 32) | stored position.  With sorted_ids the entries of a run are in (id,
+// position) order and a repeated id shows as two neighbours; otherwise
+// (explicit entries in input order) every run of two or more entries is
+// marked.
+__device__ __forceinline__ uint64_t run_meta(const uint64_t* __restrict__ vals, uint64_t r0,
+                                             uint64_t freq, uint8_t cls, uint64_t pos_off,
+                                             bool sorted_ids) {
+  if (cls == 2) {
+    const uint64_t c = freq < ((1ULL << kCountBits) - 1) ? freq : ((1ULL << kCountBits) - 1);
+    return kRepetitiveBit | (c << 40);
+  }
+  uint64_t meta = (pos_off & kOffsetMask) | (freq << 40);
+  bool dup = !sorted_ids && freq > 1;
+  for (uint64_t e = 1; sorted_ids && e < freq && !dup; ++e)
+    dup = (vals[r0 + e] >> 32) == (vals[r0 + e - 1] >> 32);
+  if (dup) meta |= kDupIdsBit;
+  return meta;
+}
+
 __global__ void insert_kernel(const uint64_t* __restrict__ keys,
                               const uint64_t* __restrict__ vals,
                               const uint64_t* __restrict__ run_start,
@@ -140,20 +236,42 @@ __global__ void insert_kernel(const uint64_t* __restrict__ keys,
   const uint64_t r = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (r >= nruns || cls[r] == 0) return;
   const uint64_t r0 = run_start[r];
-  const uint64_t key = keys[r0];
-  const uint64_t freq = run_start[r + 1] - r0;
-  uint64_t meta;
-  if (cls[r] == 2) {
-    const uint64_t c = freq < ((1ULL << kCountBits) - 1) ? freq : ((1ULL << kCountBits) - 1);
-    meta = kRepetitiveBit | (c << 40);
-  } else {
-    meta = (kept_off[r] & kOffsetMask) | (freq << 40);
-    bool dup = !sorted_ids && freq > 1;
-    for (uint64_t e = 1; sorted_ids && e < freq && !dup; ++e)
-      dup = (vals[r0 + e] >> 32) == (vals[r0 + e - 1] >> 32);
-    if (dup) meta |= kDupIdsBit;
+  const uint64_t meta =
+      run_meta(vals, r0, run_start[r + 1] - r0, cls[r], kept_off[r], sorted_ids);
+  if (!table_insert(table, mask, keys[r0], meta, false)) raise_status(st, kDevTableFull, 0, r);
+}
+
+// A key range's solid and repetitive runs as (key, table word) entries, the
+// positions of the range starting at pos_base of the final position array.
+__global__ void stage_entries_kernel(const uint64_t* __restrict__ keys,
+                                     const uint64_t* __restrict__ vals,
+                                     const uint64_t* __restrict__ run_start,
+                                     const uint8_t* __restrict__ cls,
+                                     const uint64_t* __restrict__ kept_off, uint64_t nruns,
+                                     uint64_t pos_base, uint64_t* __restrict__ ekeys,
+                                     uint64_t* __restrict__ emeta, unsigned long long* count,
+                                     uint64_t cap) {
+  const uint64_t r = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  const bool live = r < nruns && cls[r] != 0;
+  uint64_t key = 0, meta = 0;
+  if (live) {
+    const uint64_t r0 = run_start[r];
+    key = keys[r0];
+    meta = run_meta(vals, r0, run_start[r + 1] - r0, cls[r], pos_base + kept_off[r], true);
   }
-  if (!table_insert(table, mask, key, meta, false)) raise_status(st, kDevTableFull, 0, r);
+  const uint64_t i = warp_append(live, count);
+  if (live && i < cap) {
+    ekeys[i] = key;
+    emeta[i] = meta;
+  }
+}
+
+__global__ void insert_staged_kernel(const uint64_t* __restrict__ ekeys,
+                                     const uint64_t* __restrict__ emeta, uint64_t n,
+                                     TableEntry* table, uint64_t mask, DeviceStatus* st) {
+  const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (!table_insert(table, mask, ekeys[i], emeta[i], false)) raise_status(st, kDevTableFull, 2, i);
 }
 
 __global__ void insert_rep_kernel(const uint64_t* __restrict__ rep, uint64_t n, TableEntry* table,
@@ -174,8 +292,38 @@ cudaError_t index_enumerate(const uint64_t* words, const uint64_t* base_off,
                             cudaStream_t s) {
   if (nwin == 0) return cudaSuccess;
   count_launch();
-  enumerate_kernel<<<grid(nwin, 256), 256, 0, s>>>(words, base_off, win_off, slot_len, nslots,
-                                                   nwin, k, keys, vals);
+  enumerate_kernel<<<grid(nwin, 256), 256, 0, s>>>(
+      Windows{words, base_off, win_off, slot_len, nslots, nwin, k}, keys, vals);
+  return cudaGetLastError();
+}
+
+cudaError_t index_prefix_hist(const uint64_t* words, const uint64_t* base_off,
+                              const uint64_t* win_off, const int32_t* slot_len, uint32_t nslots,
+                              uint64_t nwin, int k, int shift, int nbins,
+                              unsigned long long* hist, int num_sms, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(hist, 0, sizeof(unsigned long long) * nbins, s);
+  if (e != cudaSuccess || nwin == 0) return e;
+  const size_t smem = sizeof(uint32_t) * static_cast<size_t>(nbins);
+  e = cudaFuncSetAttribute(prefix_hist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           static_cast<int>(smem));
+  if (e != cudaSuccess) return e;
+  count_launch();
+  prefix_hist_kernel<<<static_cast<unsigned>(num_sms), 1024, smem, s>>>(
+      Windows{words, base_off, win_off, slot_len, nslots, nwin, k}, shift, nbins, hist);
+  return cudaGetLastError();
+}
+
+cudaError_t index_enumerate_range(const uint64_t* words, const uint64_t* base_off,
+                                  const uint64_t* win_off, const int32_t* slot_len,
+                                  uint32_t nslots, uint64_t nwin, int k, uint64_t lo,
+                                  uint64_t hi, uint64_t* keys, uint64_t* vals,
+                                  unsigned long long* count, uint64_t cap, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(count, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess || nwin == 0) return e;
+  count_launch();
+  enumerate_range_kernel<<<grid(nwin, 256), 256, 0, s>>>(
+      Windows{words, base_off, win_off, slot_len, nslots, nwin, k}, lo, hi, keys, vals, count,
+      cap);
   return cudaGetLastError();
 }
 
@@ -196,11 +344,15 @@ cudaError_t index_run_starts(const uint32_t* flags, const uint64_t* run_id, uint
 
 cudaError_t index_classify_runs(const uint64_t* run_start, uint64_t nruns, uint32_t min_freq,
                                 uint32_t max_freq, uint32_t* kept, uint8_t* cls,
-                                cudaStream_t s) {
+                                unsigned long long* tally, cudaStream_t s) {
+  if (tally) {
+    const cudaError_t e = cudaMemsetAsync(tally, 0, 2 * sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+  }
   if (nruns == 0) return cudaSuccess;
   count_launch();
   classify_runs_kernel<<<grid(nruns, 256), 256, 0, s>>>(run_start, nruns, min_freq, max_freq,
-                                                        kept, cls);
+                                                        kept, cls, tally);
   return cudaGetLastError();
 }
 
@@ -223,6 +375,29 @@ cudaError_t index_insert(const uint64_t* keys, const uint64_t* vals, const uint6
   count_launch();
   insert_kernel<<<grid(nruns, 256), 256, 0, s>>>(keys, vals, run_start, cls, kept_off, nruns,
                                                  sorted_ids, table, mask, st);
+  return cudaGetLastError();
+}
+
+cudaError_t index_stage_entries(const uint64_t* keys, const uint64_t* vals,
+                                const uint64_t* run_start, const uint8_t* cls,
+                                const uint64_t* kept_off, uint64_t nruns, uint64_t pos_base,
+                                uint64_t* ekeys, uint64_t* emeta, unsigned long long* count,
+                                uint64_t cap, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(count, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess || nruns == 0) return e;
+  count_launch();
+  stage_entries_kernel<<<grid(nruns, 256), 256, 0, s>>>(keys, vals, run_start, cls, kept_off,
+                                                        nruns, pos_base, ekeys, emeta, count,
+                                                        cap);
+  return cudaGetLastError();
+}
+
+cudaError_t index_insert_staged(const uint64_t* ekeys, const uint64_t* emeta, uint64_t n,
+                                TableEntry* table, uint64_t mask, DeviceStatus* st,
+                                cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  count_launch();
+  insert_staged_kernel<<<grid(n, 256), 256, 0, s>>>(ekeys, emeta, n, table, mask, st);
   return cudaGetLastError();
 }
 

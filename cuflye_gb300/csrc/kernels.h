@@ -84,10 +84,23 @@ cudaError_t index_mark_runs(const uint64_t* keys, uint64_t n, uint32_t* flags, c
 // Given run ids (exclusive scan of flags), write run starts (nruns + 1 entries).
 cudaError_t index_run_starts(const uint32_t* flags, const uint64_t* run_id, uint64_t n,
                              uint64_t nruns, uint64_t* run_start, cudaStream_t s);
-// Per run: kept count (solid ? freq : 0) and class (0 none, 1 solid, 2 repetitive).
+// Windows per key prefix: hist[key >> shift] over nbins (<= 16384) bins.
+cudaError_t index_prefix_hist(const uint64_t* words, const uint64_t* base_off,
+                              const uint64_t* win_off, const int32_t* slot_len, uint32_t nslots,
+                              uint64_t nwin, int k, int shift, int nbins,
+                              unsigned long long* hist, int num_sms, cudaStream_t s);
+// The windows whose key lies in [lo, hi), appended in no particular order;
+// *count receives how many (at most cap are written).
+cudaError_t index_enumerate_range(const uint64_t* words, const uint64_t* base_off,
+                                  const uint64_t* win_off, const int32_t* slot_len,
+                                  uint32_t nslots, uint64_t nwin, int k, uint64_t lo,
+                                  uint64_t hi, uint64_t* keys, uint64_t* vals,
+                                  unsigned long long* count, uint64_t cap, cudaStream_t s);
+// Per run: kept count (solid ? freq : 0) and class (0 none, 1 solid, 2
+// repetitive); tally (optional, 2 words) counts solid and repetitive runs.
 cudaError_t index_classify_runs(const uint64_t* run_start, uint64_t nruns, uint32_t min_freq,
                                 uint32_t max_freq, uint32_t* kept, uint8_t* cls,
-                                cudaStream_t s);
+                                unsigned long long* tally, cudaStream_t s);
 cudaError_t index_copy_positions(const uint64_t* vals, const uint64_t* run_id,
                                  const uint64_t* run_start, const uint8_t* cls,
                                  const uint64_t* kept_off, uint64_t n, uint64_t* pos,
@@ -99,6 +112,16 @@ cudaError_t index_insert(const uint64_t* keys, const uint64_t* vals, const uint6
                          const uint8_t* cls, const uint64_t* kept_off, uint64_t nruns,
                          bool sorted_ids, TableEntry* table, uint64_t mask, DeviceStatus* st,
                          cudaStream_t s);
+// The solid and repetitive runs of one key range as (key, table word)
+// entries, with positions offset by pos_base (sorted ids).
+cudaError_t index_stage_entries(const uint64_t* keys, const uint64_t* vals,
+                                const uint64_t* run_start, const uint8_t* cls,
+                                const uint64_t* kept_off, uint64_t nruns, uint64_t pos_base,
+                                uint64_t* ekeys, uint64_t* emeta, unsigned long long* count,
+                                uint64_t cap, cudaStream_t s);
+cudaError_t index_insert_staged(const uint64_t* ekeys, const uint64_t* emeta, uint64_t n,
+                                TableEntry* table, uint64_t mask, DeviceStatus* st,
+                                cudaStream_t s);
 cudaError_t index_insert_repetitive(const uint64_t* rep_keys, uint64_t n, TableEntry* table,
                                     uint64_t mask, DeviceStatus* st, cudaStream_t s);
 

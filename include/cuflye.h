@@ -102,6 +102,17 @@ cuflye_status cuflye_index_from_entries(cuflye_ctx* ctx, int k, size_t n,
 cuflye_status cuflye_index_stats(const cuflye_ctx* ctx, uint64_t* keys, uint64_t* positions,
                                  uint64_t* repetitive);
 
+/* Index construction in key ranges (no counterpart in the reference, whose
+ * VertexIndex is built in host memory).  cuflye_index_build sorts all
+ * windows at once when they fit the memory budget; otherwise it builds one
+ * contiguous range of standard-form keys at a time, each range sized to what
+ * the budget leaves, and fills the table from every range's entries at the
+ * end.  The index is the same either way.  max_windows > 0 also caps the
+ * windows of one range (0, the default: the budget alone decides).
+ * cuflye_last_index_ranges gives the ranges of the last cuflye_index_build. */
+cuflye_status cuflye_set_index_build_windows(cuflye_ctx* ctx, uint64_t max_windows);
+cuflye_status cuflye_last_index_ranges(const cuflye_ctx* ctx, uint64_t* ranges);
+
 /* --------------------------------------------------------------------------
  * Candidate records (candidate-record-v1, docs/abi/candidate-record-v1.md:31-51).
  * Replaces collectCandidateMatchesCpu
