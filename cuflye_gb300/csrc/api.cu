@@ -243,10 +243,10 @@ struct BuiltIndex {
 };
 
 // Scratch of one key range's build.
-const char* const kBuildScratch[] = {"ib_keys",  "ib_vals",     "ib_keys2", "ib_vals2",
-                                     "ib_hist",  "ib_flags",    "ib_runid", "ib_runstart",
-                                     "ib_kept",  "ib_cls",      "ib_keptoff", "ib_scan",
-                                     "ib_prefix", "ib_count"};
+const char* const kBuildScratch[] = {"ib_keys", "ib_vals",  "ib_keys2",    "ib_vals2",
+                                     "ib_hist", "ib_flags", "ib_runid",    "ib_runstart",
+                                     "ib_kept", "ib_cls",   "ib_keptoff",  "ib_scan",
+                                     "ib_count"};
 
 void release_build_scratch(cuflye_ctx* c) {
   for (const char* t : kBuildScratch) release(c, t);
@@ -260,7 +260,7 @@ struct KeyRuns {
   uint64_t* run_start;
   uint8_t* cls;
   uint64_t* kept_off;
-  uint64_t nruns, npos, nsolid, nrep;
+  uint64_t nw, nruns, npos, nsolid, nrep;
 };
 
 // Sorts the windows in ib_keys / ib_vals (the alternates ib_keys2 / ib_vals2
@@ -296,14 +296,11 @@ KeyRuns sort_and_classify(cuflye_ctx* c, uint64_t nw, const std::vector<int>& di
   unsigned long long t[2];
   CUFLYE_CHECK(cudaMemcpyAsync(t, tally, sizeof(t), cudaMemcpyDeviceToHost, st));
   sync(c);
-  return KeyRuns{keys, vals, run_id, run_start, cls, kept_off, nruns, npos, t[0], t[1]};
+  return KeyRuns{keys, vals, run_id, run_start, cls, kept_off, nw, nruns, npos, t[0], t[1]};
 }
 
-uint64_t table_capacity(uint64_t entries) {
-  uint64_t cap = 16;
-  while (cap < 2 * entries) cap <<= 1;
-  return cap;
-}
+// Table slots for `entries` keys: twice as many (load 1/2), at least 16.
+uint64_t table_capacity(uint64_t entries) { return std::max<uint64_t>(16, 2 * entries); }
 
 // All windows at once; the table is sized for every run (solid, repetitive
 // and absent) at load <= 1/2.
@@ -326,8 +323,8 @@ BuiltIndex build_one_range(cuflye_ctx* c, const WindowSet& w, const std::vector<
   bi.cap = table_capacity(r.nruns);
   bi.table = buf<TableEntry>(c, "ix_table", bi.cap);
   CUFLYE_CHECK(cudaMemsetAsync(bi.table, 0xff, bi.cap * sizeof(TableEntry), st));
-  CUFLYE_CHECK(index_insert(r.keys, r.vals, r.run_start, r.cls, r.kept_off, r.nruns, true,
-                            bi.table, bi.cap - 1, c->status, st));
+  CUFLYE_CHECK(index_insert(r.keys, r.vals, r.run_start, r.cls, r.kept_off, r.nruns, 0, true,
+                            bi.table, bi.cap, c->status, st));
   check_device_status(c);
   bi.npos = r.npos;
   bi.nsolid = r.nsolid;
@@ -335,39 +332,23 @@ BuiltIndex build_one_range(cuflye_ctx* c, const WindowSet& w, const std::vector<
   return bi;
 }
 
-// Device bytes one window of a key range needs while the range is built: the
-// radix sort's two key/value pairs (32), run flag and id (12), the run
-// tables (21, at most one run per window) and the range's outputs (8 per
-// solid position, 16 per staged table entry), with margin.
-constexpr uint64_t kRangeBytesPerWindow = 96;
+// Device bytes one window of a key range needs while the range is built:
+// the radix sort's two key/value pairs (32), run flag and id (12) and the
+// run tables (21, at most one run per window), with margin.
+constexpr uint64_t kRangeBytesPerWindow = 72;
 constexpr int kPrefixBits = 14;
 
-// The index built one contiguous key range at a time, each range sized to
-// what the memory budget leaves (and to the caller's window cap).  Ranges
-// are cut from a histogram of key prefixes; a range's solid positions follow
-// the previous range's, so the position array equals the one-range build's.
-BuiltIndex build_key_ranges(cuflye_ctx* c, const WindowSet& w, const std::vector<int>& digits,
-                            uint32_t min_freq, uint32_t max_freq) {
+// Cuts [0, nbins) into contiguous ranges of prefix bins, each holding as many
+// windows as what the memory budget leaves allows (and at most the caller's
+// window cap), and runs body(first bin, sorted runs) on each after enumerating,
+// sorting and classifying its windows.  Returns the number of ranges.
+template <typename Body>
+uint64_t for_each_key_range(cuflye_ctx* c, const WindowSet& w, const std::vector<int>& digits,
+                            uint32_t min_freq, uint32_t max_freq,
+                            const std::vector<unsigned long long>& hist, int shift, Body body) {
   cudaStream_t st = c->stream;
-  const int bits = std::min(2 * w.k, kPrefixBits);
-  const int shift = 2 * w.k - bits;
-  const int nbins = 1 << bits;
-  std::vector<unsigned long long> hist(nbins);
-  {
-    unsigned long long* d_hist = buf<unsigned long long>(c, "ib_prefix", nbins);
-    CUFLYE_CHECK(index_prefix_hist(w.words, w.base_off, w.win_off, w.slot_len, w.nslots, w.nwin,
-                                   w.k, shift, nbins, d_hist, c->num_sms, st));
-    CUFLYE_CHECK(cudaMemcpyAsync(hist.data(), d_hist, nbins * sizeof(unsigned long long),
-                                 cudaMemcpyDeviceToHost, st));
-    sync(c);
-    release(c, "ib_prefix");
-  }
-  struct RangeOut {
-    std::string pos_name, ek_name, em_name;
-    uint64_t pos_base, npos, nent;
-  };
-  std::vector<RangeOut> outs;
-  uint64_t pos_base = 0, nsolid = 0, nrep = 0;
+  const int nbins = static_cast<int>(hist.size());
+  uint64_t ranges = 0;
   int b = 0;
   while (b < nbins) {
     const uint64_t limit = effective_budget(c);
@@ -383,6 +364,7 @@ BuiltIndex build_key_ranges(cuflye_ctx* c, const WindowSet& w, const std::vector
                       " windows share one key prefix and need about " +
                       std::to_string(hist[b] * kRangeBytesPerWindow) + " bytes; " +
                       std::to_string(avail) + " bytes are left in the memory budget");
+    const int first = b;
     const uint64_t lo = static_cast<uint64_t>(b) << shift;
     const uint64_t hi = static_cast<uint64_t>(e) << shift;
     b = e;
@@ -400,54 +382,87 @@ BuiltIndex build_key_ranges(cuflye_ctx* c, const WindowSet& w, const std::vector
                                        std::to_string(hi) + ") enumerated " +
                                        std::to_string(got) + " windows, the histogram " +
                                        std::to_string(nw));
-    const KeyRuns r = sort_and_classify(c, nw, digits, min_freq, max_freq);
-    const uint64_t nent = r.nsolid + r.nrep;
-    RangeOut o{"ib_pos" + std::to_string(outs.size()), "ib_ek" + std::to_string(outs.size()),
-               "ib_em" + std::to_string(outs.size()), pos_base, r.npos, nent};
-    uint64_t* pos = buf<uint64_t>(c, o.pos_name, r.npos);
-    CUFLYE_CHECK(index_copy_positions(r.vals, r.run_id, r.run_start, r.cls, r.kept_off, nw, pos,
-                                      st));
-    uint64_t* ek = buf<uint64_t>(c, o.ek_name, nent);
-    uint64_t* em = buf<uint64_t>(c, o.em_name, nent);
-    CUFLYE_CHECK(index_stage_entries(r.keys, r.vals, r.run_start, r.cls, r.kept_off, r.nruns,
-                                     pos_base, ek, em, count, nent, st));
-    const unsigned long long staged = read_scalar(c, count);
-    if (staged != nent)
-      throw Error(CUFLYE_ERR_CUDA, "k-mer index build: staged " + std::to_string(staged) +
-                                       " table entries of " + std::to_string(nent));
+    body(first, sort_and_classify(c, nw, digits, min_freq, max_freq));
+    sync(c);
     release_build_scratch(c);
-    outs.push_back(o);
-    pos_base += r.npos;
-    nsolid += r.nsolid;
-    nrep += r.nrep;
+    ++ranges;
   }
-  if (pos_base >= (1ull << 40)) throw Error(CUFLYE_ERR_UNSUPPORTED, "index larger than 2^40 entries");
-  for (const char* t : {"ib_words", "ib_base", "ib_win"}) release(c, t);
+  return ranges;
+}
+
+// The index built one contiguous key range at a time, in two passes over the
+// ranges.  The first counts each key prefix's solid positions and table
+// entries; the position array and the table are then allocated at their
+// final sizes, and the second pass writes each range's positions at its
+// first prefix's offset and inserts its runs.  The device holds the final
+// index and one range's scratch at most, and the position array equals the
+// one-range build's.
+BuiltIndex build_key_ranges(cuflye_ctx* c, const WindowSet& w, const std::vector<int>& digits,
+                            uint32_t min_freq, uint32_t max_freq) {
+  cudaStream_t st = c->stream;
+  const int bits = std::min(2 * w.k, kPrefixBits);
+  const int shift = 2 * w.k - bits;
+  const int nbins = 1 << bits;
+  std::vector<unsigned long long> hist(nbins), npos_bin(nbins), nent_bin(nbins);
+  unsigned long long* d_bins = buf<unsigned long long>(c, "ib_bins", 3ull * nbins);
+  CUFLYE_CHECK(index_prefix_hist(w.words, w.base_off, w.win_off, w.slot_len, w.nslots, w.nwin,
+                                 w.k, shift, nbins, d_bins, c->num_sms, st));
+  CUFLYE_CHECK(cudaMemcpyAsync(hist.data(), d_bins, nbins * sizeof(unsigned long long),
+                               cudaMemcpyDeviceToHost, st));
+  CUFLYE_CHECK(cudaMemsetAsync(d_bins + nbins, 0, 2ull * nbins * sizeof(unsigned long long), st));
+  sync(c);
+  uint64_t nsolid = 0, nrep = 0;
+  for_each_key_range(c, w, digits, min_freq, max_freq, hist, shift,
+                     [&](int, const KeyRuns& r) {
+                       CUFLYE_CHECK(index_bin_totals(r.keys, r.run_start, r.cls, r.nruns, shift,
+                                                     d_bins + nbins, d_bins + 2 * nbins, st));
+                       nsolid += r.nsolid;
+                       nrep += r.nrep;
+                     });
+  CUFLYE_CHECK(cudaMemcpyAsync(npos_bin.data(), d_bins + nbins,
+                               nbins * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+  CUFLYE_CHECK(cudaMemcpyAsync(nent_bin.data(), d_bins + 2 * nbins,
+                               nbins * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+  sync(c);
+  release(c, "ib_bins");
+  std::vector<uint64_t> pos_start(nbins + 1, 0);
+  uint64_t nent = 0;
+  for (int i = 0; i < nbins; ++i) {
+    pos_start[i + 1] = pos_start[i] + npos_bin[i];
+    nent += nent_bin[i];
+  }
+  const uint64_t npos = pos_start[nbins];
+  if (nent != nsolid + nrep)
+    throw Error(CUFLYE_ERR_CUDA, "k-mer index build: " + std::to_string(nent) +
+                                     " table entries by prefix, " +
+                                     std::to_string(nsolid + nrep) + " by run class");
+  if (npos >= (1ull << 40)) throw Error(CUFLYE_ERR_UNSUPPORTED, "index larger than 2^40 entries");
   BuiltIndex bi;
-  bi.cap = table_capacity(nsolid + nrep);
+  bi.pos = buf<uint64_t>(c, "ix_pos", npos);
+  bi.cap = table_capacity(nent);
   bi.table = buf<TableEntry>(c, "ix_table", bi.cap);
   CUFLYE_CHECK(cudaMemsetAsync(bi.table, 0xff, bi.cap * sizeof(TableEntry), st));
-  for (const RangeOut& o : outs) {
-    CUFLYE_CHECK(index_insert_staged(buf<uint64_t>(c, o.ek_name, o.nent),
-                                     buf<uint64_t>(c, o.em_name, o.nent), o.nent, bi.table,
-                                     bi.cap - 1, c->status, st));
-    sync(c);
-    release(c, o.ek_name);
-    release(c, o.em_name);
-  }
+  uint64_t written = 0;
+  c->build_ranges = for_each_key_range(
+      c, w, digits, min_freq, max_freq, hist, shift, [&](int first, const KeyRuns& r) {
+        const uint64_t base = pos_start[first];
+        if (base + r.npos > npos)
+          throw Error(CUFLYE_ERR_CUDA, "k-mer index build: a key range's positions overrun "
+                                       "the counted total");
+        CUFLYE_CHECK(index_copy_positions(r.vals, r.run_id, r.run_start, r.cls, r.kept_off, r.nw,
+                                          bi.pos + base, st));
+        CUFLYE_CHECK(index_insert(r.keys, r.vals, r.run_start, r.cls, r.kept_off, r.nruns, base,
+                                  true, bi.table, bi.cap, c->status, st));
+        written += r.npos;
+      });
+  if (written != npos)
+    throw Error(CUFLYE_ERR_CUDA, "k-mer index build: the second pass wrote " +
+                                     std::to_string(written) + " positions of " +
+                                     std::to_string(npos));
   check_device_status(c);
-  bi.pos = buf<uint64_t>(c, "ix_pos", pos_base);
-  for (const RangeOut& o : outs) {
-    if (o.npos)
-      CUFLYE_CHECK(cudaMemcpyAsync(bi.pos + o.pos_base, buf<uint64_t>(c, o.pos_name, o.npos),
-                                   o.npos * sizeof(uint64_t), cudaMemcpyDeviceToDevice, st));
-    sync(c);
-    release(c, o.pos_name);
-  }
-  bi.npos = pos_base;
+  bi.npos = npos;
   bi.nsolid = nsolid;
   bi.nrep = nrep;
-  c->build_ranges = outs.size();
   return bi;
 }
 
@@ -544,11 +559,11 @@ void build_index(cuflye_ctx* c, int k, size_t n, const int64_t* ids, const int64
   }
   if (ranges) bi = build_key_ranges(c, ws, digits, min_freq, max_freq);
   release_build_scratch(c);
-  for (const char* t : {"ib_words", "ib_base", "ib_win"}) release(c, t);
+  for (const char* t : {"ib_words", "ib_base", "ib_win", "ib_bins"}) release(c, t);
   c->idx.k = k;
   c->idx.transform = true;
   c->idx.table = bi.table;
-  c->idx.mask = bi.cap - 1;
+  c->idx.cap = bi.cap;
   c->idx.pos = bi.pos;
   c->idx.npos = bi.npos;
   c->idx.slot_len = d_len;
@@ -623,16 +638,15 @@ void build_index_entries(cuflye_ctx* c, int k, size_t n, const int64_t* tids, co
   const uint64_t npos = scan_u32(c, kept, kept_off, nruns, "ib_scan");
   uint64_t* pos = buf<uint64_t>(c, "ix_pos", npos);
   CUFLYE_CHECK(index_copy_positions(vals, run_id, run_start, cls, kept_off, nn, pos, st));
-  uint64_t cap = 16;
-  while (cap < 2 * (nruns + nrep)) cap <<= 1;
+  const uint64_t cap = table_capacity(nruns + nrep);
   TableEntry* table = buf<TableEntry>(c, "ix_table", cap);
   CUFLYE_CHECK(cudaMemsetAsync(table, 0xff, cap * sizeof(TableEntry), st));
-  CUFLYE_CHECK(index_insert(keys, vals, run_start, cls, kept_off, nruns, false, table, cap - 1,
+  CUFLYE_CHECK(index_insert(keys, vals, run_start, cls, kept_off, nruns, 0, false, table, cap,
                             c->status, st));
   if (nrep) {
     uint64_t* d_rep = buf<uint64_t>(c, "ib_rep", nrep);
     CUFLYE_CHECK(cudaMemcpyAsync(d_rep, rep_h, nrep * 8, cudaMemcpyHostToDevice, st));
-    CUFLYE_CHECK(index_insert_repetitive(d_rep, nrep, table, cap - 1, c->status, st));
+    CUFLYE_CHECK(index_insert_repetitive(d_rep, nrep, table, cap, c->status, st));
   }
   check_device_status(c);
   for (const char* t : {"ib_keys", "ib_vals", "ib_keys2", "ib_vals2", "ib_hist", "ib_flags",
@@ -642,7 +656,7 @@ void build_index_entries(cuflye_ctx* c, int k, size_t n, const int64_t* tids, co
   c->idx.k = k;
   c->idx.transform = false;
   c->idx.table = table;
-  c->idx.mask = cap - 1;
+  c->idx.cap = cap;
   c->idx.pos = pos;
   c->idx.npos = npos;
   c->idx.slot_len = d_len;
@@ -685,6 +699,42 @@ const char* const kPerHitBuffers[] = {"h_keys",  "h_vals",   "h_kmers", "s_l",  
 // Upload a run of queries starting at q0 and produce the hits of the longest
 // prefix of them that fits in device memory (ps.nq queries), in Flye's
 // generation order.
+// Device bytes per query window of a pass's run: bases (1), packed words
+// (0.25), hit and filter counts (8), window metadata (8) and flags (1), the
+// two offset arrays (16), rounded up.
+constexpr uint64_t kRunBytesPerWindow = 36;
+// Buffers sized by the windows of a pass's run (reused by the next pass).
+const char* const kPerWindowBuffers[] = {"q_ascii", "q_words",  "w_cnt",     "w_filt", "w_meta",
+                                         "w_flags", "w_hitoff", "w_filtoff", "w_scan"};
+
+// The end of the run of queries from q0 (at most q1) whose windows' buffers
+// take at most a quarter of the memory the budget leaves; the rest is for
+// the run's hits.  At least one query.
+size_t run_end(cuflye_ctx* c, const Queries& Q, size_t q0, size_t q1) {
+  const uint64_t limit = effective_budget(c);
+  uint64_t reusable = 0;
+  auto held = [&](const char* name) {
+    auto it = c->bufs.find(name);
+    if (it != c->bufs.end()) reusable += it->second.cap;
+  };
+  for (const char* nm : kPerWindowBuffers) held(nm);
+  for (const char* nm : kPerHitBuffers) held(nm);
+  const uint64_t used = c->in_use > reusable ? c->in_use - reusable : 0;
+  const uint64_t avail = limit > used ? limit - used : 0;
+  const uint64_t cap = avail / 4 / kRunBytesPerWindow;
+  const int64_t k = c->idx.k;
+  uint64_t nw = 0;
+  size_t q = q0;
+  while (q < q1) {
+    const int64_t len = Q.offsets[q + 1] - Q.offsets[q];
+    const uint64_t w = len >= k ? static_cast<uint64_t>(len - k + 1) : 0;
+    if (q > q0 && nw + w > cap) break;
+    nw += w;
+    ++q;
+  }
+  return q;
+}
+
 bool run_hits(cuflye_ctx* c, const Queries& Q, size_t q0, size_t q1, bool want_kmers,
               uint64_t bytes_per_hit, PassState& ps) {
   const int k = c->idx.k;
@@ -760,7 +810,10 @@ bool run_hits(cuflye_ctx* c, const Queries& Q, size_t q0, size_t q1, bool want_k
     if (it != c->bufs.end()) reusable += it->second.cap;
   }
   const uint64_t used = c->in_use - reusable;
-  const uint64_t avail = limit > used ? limit - used : 0;
+  // an eighth stays free for the pass body's other buffers (row pool, rows,
+  // per-group tables)
+  const uint64_t free_b = limit > used ? limit - used : 0;
+  const uint64_t avail = free_b - free_b / 8;
   if (ps.nhits * bytes_per_hit > avail) {
     std::vector<uint64_t> qoff(nq + 1);
     CUFLYE_CHECK(cudaMemcpyAsync(qoff.data(), ps.q_off, (nq + 1) * 8ull, cudaMemcpyDeviceToHost,
@@ -1025,9 +1078,10 @@ template <typename Body>
 void for_each_pass(cuflye_ctx* c, const Queries& Q, bool kmers, uint64_t bytes_per_hit,
                    Body body) {
   size_t q0 = 0;
-  size_t step = std::max<size_t>(pass_size(c, Q.n), 1);
+  const size_t full = std::max<size_t>(pass_size(c, Q.n), 1);
+  size_t step = full;
   while (q0 < Q.n) {
-    size_t q1 = std::min(Q.n, q0 + step);
+    size_t q1 = run_end(c, Q, q0, std::min(Q.n, q0 + step));
     PassState ps;
     CUFLYE_CHECK(cudaEventRecord(c->ev[0], c->stream));
     run_hits(c, Q, q0, q1, kmers, bytes_per_hit, ps);
@@ -1043,6 +1097,7 @@ void for_each_pass(cuflye_ctx* c, const Queries& Q, bool kmers, uint64_t bytes_p
     }
     ++c->passes;
     q0 = q1;
+    step = std::min(full, step * 2);  // a halved step grows back after a pass that fits
   }
 }
 

@@ -76,9 +76,21 @@ constexpr uint8_t kWinRev = 1;       // the window k-mer is not in standard form
 constexpr uint8_t kWinFiltered = 2;  // repetitive: a filtered position
 constexpr uint8_t kWinTrivial = 4;   // the bucket held the window's own position
 
+// A key's first slot in a table of cap slots (any cap >= 1): the high half
+// of mix64(key) * cap, which maps the hash onto [0, cap) evenly.  Probing
+// continues at slot + 1, wrapping at cap.
+__device__ __forceinline__ uint64_t table_slot(uint64_t key, uint64_t cap) {
+  return __umul64hi(mix64(key), cap);
+}
+__device__ __forceinline__ uint64_t table_next(uint64_t slot, uint64_t cap) {
+  return slot + 1 == cap ? 0 : slot + 1;
+}
+
+// The table keeps its load at 1/2 or below, so a probe always meets an
+// empty slot.
 __device__ __forceinline__ uint64_t table_probe(const TableEntry* __restrict__ table,
-                                                uint64_t mask, uint64_t key, bool* found) {
-  uint64_t slot = mix64(key) & mask;
+                                                uint64_t cap, uint64_t key, bool* found) {
+  uint64_t slot = table_slot(key, cap);
   for (;;) {
     const ulonglong2 e = __ldg(reinterpret_cast<const ulonglong2*>(table + slot));
     if (e.x == key) {
@@ -89,7 +101,7 @@ __device__ __forceinline__ uint64_t table_probe(const TableEntry* __restrict__ t
       *found = false;
       return 0;
     }
-    slot = (slot + 1) & mask;
+    slot = table_next(slot, cap);
   }
 }
 

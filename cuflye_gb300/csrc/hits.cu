@@ -57,7 +57,7 @@ __global__ void count_kernel(DeviceIndex idx, QueryBatch q, uint32_t* __restrict
   const uint64_t p = w - q.win_off[qi];
   const WindowKmer km = window_kmer(q, qi, p, idx.k);
   bool found;
-  const uint64_t meta = table_probe(idx.table, idx.mask, km.key, &found);
+  const uint64_t meta = table_probe(idx.table, idx.cap, km.key, &found);
   uint32_t c = 0;
   uint8_t fl = km.rev ? kWinRev : 0;
   if (found && (meta & kRepetitiveBit)) {

@@ -12,12 +12,14 @@
 //
 // Construction: enumerate windows -> stable LSD radix sort of
 // (key | stored id | stored position) -> run detection -> solid positions
-// copied in run order -> open-addressing insert (linear probing, load <= 1/2).
+// copied in run order -> open-addressing insert (linear probing, load <= 1/2,
+// the table sized at twice its entries).
 // When the windows do not fit the memory budget at once, the same steps run
-// per contiguous key range (ranges cut from a histogram of key prefixes):
-// each range appends its solid positions after the previous range's and
-// stages its (key, table word) entries; the table is filled from the staged
-// entries at the end.  The position array is then the same as one range's.
+// per contiguous key range (ranges cut from a histogram of key prefixes), in
+// two passes: the first counts each prefix's solid positions and table
+// entries, the second writes every range's positions at its prefix's offset
+// in the final array and inserts its runs into the final table.  The
+// position array is then the same as one range's.
 // A standard form never equals ~0 (the all-T k-mer's standard form is the
 // all-A k-mer, 0), so ~0 marks an empty slot.
 #include <cstdint>
@@ -185,10 +187,10 @@ __global__ void copy_positions_kernel(const uint64_t* __restrict__ vals,
   pos[kept_off[r] + (i - run_start[r])] = vals[i];
 }
 
-__device__ bool table_insert(TableEntry* table, uint64_t mask, uint64_t key, uint64_t meta,
+__device__ bool table_insert(TableEntry* table, uint64_t cap, uint64_t key, uint64_t meta,
                              bool merge_rep) {
-  uint64_t slot = mix64(key) & mask;
-  for (uint64_t step = 0; step <= mask; ++step) {
+  uint64_t slot = table_slot(key, cap);
+  for (uint64_t step = 0; step < cap; ++step) {
     unsigned long long* kp = reinterpret_cast<unsigned long long*>(&table[slot].key);
     const unsigned long long prev = atomicCAS(kp, kEmptyKey, key);
     if (prev == kEmptyKey) {
@@ -200,7 +202,7 @@ __device__ bool table_insert(TableEntry* table, uint64_t mask, uint64_t key, uin
         atomicOr(reinterpret_cast<unsigned long long*>(&table[slot].meta), kRepetitiveBit);
       return true;
     }
-    slot = (slot + 1) & mask;
+    slot = table_next(slot, cap);
   }
   return false;
 }
@@ -231,54 +233,57 @@ __global__ void insert_kernel(const uint64_t* __restrict__ keys,
                               const uint64_t* __restrict__ run_start,
                               const uint8_t* __restrict__ cls,
                               const uint64_t* __restrict__ kept_off, uint64_t nruns,
-                              bool sorted_ids, TableEntry* table, uint64_t mask,
-                              DeviceStatus* st) {
+                              uint64_t pos_base, bool sorted_ids, TableEntry* table,
+                              uint64_t cap, DeviceStatus* st) {
   const uint64_t r = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (r >= nruns || cls[r] == 0) return;
   const uint64_t r0 = run_start[r];
   const uint64_t meta =
-      run_meta(vals, r0, run_start[r + 1] - r0, cls[r], kept_off[r], sorted_ids);
-  if (!table_insert(table, mask, keys[r0], meta, false)) raise_status(st, kDevTableFull, 0, r);
+      run_meta(vals, r0, run_start[r + 1] - r0, cls[r], pos_base + kept_off[r], sorted_ids);
+  if (!table_insert(table, cap, keys[r0], meta, false)) raise_status(st, kDevTableFull, 0, r);
 }
 
-// A key range's solid and repetitive runs as (key, table word) entries, the
-// positions of the range starting at pos_base of the final position array.
-__global__ void stage_entries_kernel(const uint64_t* __restrict__ keys,
-                                     const uint64_t* __restrict__ vals,
-                                     const uint64_t* __restrict__ run_start,
-                                     const uint8_t* __restrict__ cls,
-                                     const uint64_t* __restrict__ kept_off, uint64_t nruns,
-                                     uint64_t pos_base, uint64_t* __restrict__ ekeys,
-                                     uint64_t* __restrict__ emeta, unsigned long long* count,
-                                     uint64_t cap) {
+// Per key prefix (key >> shift): solid positions and table entries (solid
+// and repetitive runs).  Runs arrive in key order, so a warp's runs share
+// few prefixes: each distinct prefix of the warp takes one atomic per count.
+__global__ void bin_totals_kernel(const uint64_t* __restrict__ keys,
+                                  const uint64_t* __restrict__ run_start,
+                                  const uint8_t* __restrict__ cls, uint64_t nruns, int shift,
+                                  unsigned long long* __restrict__ npos_bin,
+                                  unsigned long long* __restrict__ nent_bin) {
+  // every warp is full (block 256, grid rounded up): lanes past the end count nothing
   const uint64_t r = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  const bool live = r < nruns && cls[r] != 0;
-  uint64_t key = 0, meta = 0;
-  if (live) {
+  const int lane = threadIdx.x & 31;
+  bool live = false;
+  uint64_t bin = 0;
+  uint32_t npos = 0;
+  if (r < nruns && cls[r] != 0) {
     const uint64_t r0 = run_start[r];
-    key = keys[r0];
-    meta = run_meta(vals, r0, run_start[r + 1] - r0, cls[r], pos_base + kept_off[r], true);
+    live = true;
+    bin = keys[r0] >> shift;
+    npos = cls[r] == 1 ? static_cast<uint32_t>(run_start[r + 1] - r0) : 0u;  // < 2^22
   }
-  const uint64_t i = warp_append(live, count);
-  if (live && i < cap) {
-    ekeys[i] = key;
-    emeta[i] = meta;
+  uint32_t left = __ballot_sync(0xffffffffu, live);
+  while (left) {  // at most 32 rounds: each removes the leader's prefix
+    const int leader = __ffs(left) - 1;
+    const uint64_t b = __shfl_sync(0xffffffffu, bin, leader);
+    const bool mine = live && bin == b;
+    const uint32_t same = __ballot_sync(0xffffffffu, mine);
+    const uint32_t sum = __reduce_add_sync(0xffffffffu, mine ? npos : 0u);
+    if (lane == leader) {
+      atomicAdd(&nent_bin[b], static_cast<unsigned long long>(__popc(same)));
+      if (sum) atomicAdd(&npos_bin[b], static_cast<unsigned long long>(sum));
+    }
+    left &= ~same;
+    if (mine) live = false;
   }
-}
-
-__global__ void insert_staged_kernel(const uint64_t* __restrict__ ekeys,
-                                     const uint64_t* __restrict__ emeta, uint64_t n,
-                                     TableEntry* table, uint64_t mask, DeviceStatus* st) {
-  const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  if (!table_insert(table, mask, ekeys[i], emeta[i], false)) raise_status(st, kDevTableFull, 2, i);
 }
 
 __global__ void insert_rep_kernel(const uint64_t* __restrict__ rep, uint64_t n, TableEntry* table,
-                                  uint64_t mask, DeviceStatus* st) {
+                                  uint64_t cap, DeviceStatus* st) {
   const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  if (!table_insert(table, mask, rep[i], kRepetitiveBit, true))
+  if (!table_insert(table, cap, rep[i], kRepetitiveBit, true))
     raise_status(st, kDevTableFull, 1, i);
 }
 
@@ -369,43 +374,30 @@ cudaError_t index_copy_positions(const uint64_t* vals, const uint64_t* run_id,
 
 cudaError_t index_insert(const uint64_t* keys, const uint64_t* vals, const uint64_t* run_start,
                          const uint8_t* cls, const uint64_t* kept_off, uint64_t nruns,
-                         bool sorted_ids, TableEntry* table, uint64_t mask, DeviceStatus* st,
-                         cudaStream_t s) {
+                         uint64_t pos_base, bool sorted_ids, TableEntry* table, uint64_t cap,
+                         DeviceStatus* st, cudaStream_t s) {
   if (nruns == 0) return cudaSuccess;
   count_launch();
   insert_kernel<<<grid(nruns, 256), 256, 0, s>>>(keys, vals, run_start, cls, kept_off, nruns,
-                                                 sorted_ids, table, mask, st);
+                                                 pos_base, sorted_ids, table, cap, st);
   return cudaGetLastError();
 }
 
-cudaError_t index_stage_entries(const uint64_t* keys, const uint64_t* vals,
-                                const uint64_t* run_start, const uint8_t* cls,
-                                const uint64_t* kept_off, uint64_t nruns, uint64_t pos_base,
-                                uint64_t* ekeys, uint64_t* emeta, unsigned long long* count,
-                                uint64_t cap, cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(count, 0, sizeof(unsigned long long), s);
-  if (e != cudaSuccess || nruns == 0) return e;
+cudaError_t index_bin_totals(const uint64_t* keys, const uint64_t* run_start, const uint8_t* cls,
+                             uint64_t nruns, int shift, unsigned long long* npos_bin,
+                             unsigned long long* nent_bin, cudaStream_t s) {
+  if (nruns == 0) return cudaSuccess;
   count_launch();
-  stage_entries_kernel<<<grid(nruns, 256), 256, 0, s>>>(keys, vals, run_start, cls, kept_off,
-                                                        nruns, pos_base, ekeys, emeta, count,
-                                                        cap);
-  return cudaGetLastError();
-}
-
-cudaError_t index_insert_staged(const uint64_t* ekeys, const uint64_t* emeta, uint64_t n,
-                                TableEntry* table, uint64_t mask, DeviceStatus* st,
-                                cudaStream_t s) {
-  if (n == 0) return cudaSuccess;
-  count_launch();
-  insert_staged_kernel<<<grid(n, 256), 256, 0, s>>>(ekeys, emeta, n, table, mask, st);
+  bin_totals_kernel<<<grid(nruns, 256), 256, 0, s>>>(keys, run_start, cls, nruns, shift,
+                                                     npos_bin, nent_bin);
   return cudaGetLastError();
 }
 
 cudaError_t index_insert_repetitive(const uint64_t* rep_keys, uint64_t n, TableEntry* table,
-                                    uint64_t mask, DeviceStatus* st, cudaStream_t s) {
+                                    uint64_t cap, DeviceStatus* st, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
   count_launch();
-  insert_rep_kernel<<<grid(n, 256), 256, 0, s>>>(rep_keys, n, table, mask, st);
+  insert_rep_kernel<<<grid(n, 256), 256, 0, s>>>(rep_keys, n, table, cap, st);
   return cudaGetLastError();
 }
 

@@ -64,7 +64,7 @@ struct DeviceIndex {
   int k = 0;
   bool transform = true;
   TableEntry* table = nullptr;
-  uint64_t mask = 0;
+  uint64_t cap = 0;              // table slots (load <= 1/2)
   uint64_t* pos = nullptr;       // (dense id << 32) | stored position, bucket order
   uint64_t npos = 0;
   int32_t* slot_len = nullptr;   // target length per dense slot
@@ -105,25 +105,21 @@ cudaError_t index_copy_positions(const uint64_t* vals, const uint64_t* run_id,
                                  const uint64_t* run_start, const uint8_t* cls,
                                  const uint64_t* kept_off, uint64_t n, uint64_t* pos,
                                  cudaStream_t s);
-// Table insert of every solid and repetitive run.  Solid buckets that list
+// Table insert of every solid and repetitive run, a solid run's positions
+// at pos_base + kept_off of the position array.  Solid buckets that list
 // one stored id twice get kDupIdsBit (sorted_ids: runs are in (id, position)
 // order; otherwise every run of two or more entries is marked).
 cudaError_t index_insert(const uint64_t* keys, const uint64_t* vals, const uint64_t* run_start,
                          const uint8_t* cls, const uint64_t* kept_off, uint64_t nruns,
-                         bool sorted_ids, TableEntry* table, uint64_t mask, DeviceStatus* st,
-                         cudaStream_t s);
-// The solid and repetitive runs of one key range as (key, table word)
-// entries, with positions offset by pos_base (sorted ids).
-cudaError_t index_stage_entries(const uint64_t* keys, const uint64_t* vals,
-                                const uint64_t* run_start, const uint8_t* cls,
-                                const uint64_t* kept_off, uint64_t nruns, uint64_t pos_base,
-                                uint64_t* ekeys, uint64_t* emeta, unsigned long long* count,
-                                uint64_t cap, cudaStream_t s);
-cudaError_t index_insert_staged(const uint64_t* ekeys, const uint64_t* emeta, uint64_t n,
-                                TableEntry* table, uint64_t mask, DeviceStatus* st,
-                                cudaStream_t s);
+                         uint64_t pos_base, bool sorted_ids, TableEntry* table, uint64_t cap,
+                         DeviceStatus* st, cudaStream_t s);
+// Per key prefix (key >> shift) of sorted runs: solid positions into
+// npos_bin, solid and repetitive runs into nent_bin (both accumulate).
+cudaError_t index_bin_totals(const uint64_t* keys, const uint64_t* run_start, const uint8_t* cls,
+                             uint64_t nruns, int shift, unsigned long long* npos_bin,
+                             unsigned long long* nent_bin, cudaStream_t s);
 cudaError_t index_insert_repetitive(const uint64_t* rep_keys, uint64_t n, TableEntry* table,
-                                    uint64_t mask, DeviceStatus* st, cudaStream_t s);
+                                    uint64_t cap, DeviceStatus* st, cudaStream_t s);
 
 // ---------------------------------------------------------------- hits
 struct QueryBatch {

@@ -22,9 +22,12 @@ def test_passes_do_not_change_rows(built_lib, scale_case):
     from cuflye_gb300.backend import CudaBackend, OverlapParams
     wl = scale_case
     p = OverlapParams.make(**wl.params)
+    nwin = int(np.maximum(np.diff(wl.reads.offsets) - wl.k + 1, 0).sum())
     with CudaBackend(device=0, memory_budget_bytes=0) as be:
+        # the index laid out as a budget-bound build lays it out (key ranges)
+        be.set_index_build_windows(nwin // 4 + 1)
         be.build_index(wl.reads, wl.k, wl.min_freq, wl.max_freq)
-        build_peak = be.memory_stats()[1]
+        index_bytes = be.memory_stats()[0]
         whole = be.overlaps(wl.reads, p)
         assert be.last_passes() == 1
         hits = be.last_timing()[1][1] // 24
@@ -34,10 +37,12 @@ def test_passes_do_not_change_rows(built_lib, scale_case):
         be.set_batch_queries(0)
     assert len(whole) > 0 and hits > 0
     assert by_count.tobytes() == whole.tobytes()
-    # a budget that holds the index build and about a sixth of the hits' buffers
-    budget = int(build_peak + 64 * hits / 6 + (64 << 20))
+    # a budget that holds the index and about a sixth of the hits' buffers:
+    # the index is built in key ranges and the overlaps run in passes
+    budget = int(index_bytes + 64 * hits / 6 + (64 << 20))
     with CudaBackend(device=0, memory_budget_bytes=budget) as be:
         be.build_index(wl.reads, wl.k, wl.min_freq, wl.max_freq)
+        assert be.last_index_ranges() >= 2
         by_budget = be.overlaps(wl.reads, p)
         assert be.last_passes() >= 3
         peak = be.memory_stats()[1]
