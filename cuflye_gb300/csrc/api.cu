@@ -302,8 +302,9 @@ KeyRuns sort_and_classify(cuflye_ctx* c, uint64_t nw, const std::vector<int>& di
 // Table slots for `entries` keys: twice as many (load 1/2), at least 16.
 uint64_t table_capacity(uint64_t entries) { return std::max<uint64_t>(16, 2 * entries); }
 
-// All windows at once; the table is sized for every run (solid, repetitive
-// and absent) at load <= 1/2.
+// All windows at once.  This build fits the memory with room to spare, so
+// its table takes the power of two at or above twice every run (solid,
+// repetitive and absent): a load well under 1/2 keeps lookups short.
 BuiltIndex build_one_range(cuflye_ctx* c, const WindowSet& w, const std::vector<int>& digits,
                            uint32_t min_freq, uint32_t max_freq) {
   cudaStream_t st = c->stream;
@@ -320,7 +321,8 @@ BuiltIndex build_one_range(cuflye_ctx* c, const WindowSet& w, const std::vector<
   bi.pos = buf<uint64_t>(c, "ix_pos", r.npos);
   CUFLYE_CHECK(index_copy_positions(r.vals, r.run_id, r.run_start, r.cls, r.kept_off, w.nwin,
                                     bi.pos, st));
-  bi.cap = table_capacity(r.nruns);
+  bi.cap = 16;
+  while (bi.cap < 2 * r.nruns) bi.cap <<= 1;
   bi.table = buf<TableEntry>(c, "ix_table", bi.cap);
   CUFLYE_CHECK(cudaMemsetAsync(bi.table, 0xff, bi.cap * sizeof(TableEntry), st));
   CUFLYE_CHECK(index_insert(r.keys, r.vals, r.run_start, r.cls, r.kept_off, r.nruns, 0, true,
@@ -810,10 +812,11 @@ bool run_hits(cuflye_ctx* c, const Queries& Q, size_t q0, size_t q1, bool want_k
     if (it != c->bufs.end()) reusable += it->second.cap;
   }
   const uint64_t used = c->in_use - reusable;
-  // an eighth stays free for the pass body's other buffers (row pool, rows,
-  // per-group tables)
+  // under a caller's budget an eighth stays free for the pass body's other
+  // buffers (row pool, rows, per-group tables); without one, the device's
+  // own margin covers them
   const uint64_t free_b = limit > used ? limit - used : 0;
-  const uint64_t avail = free_b - free_b / 8;
+  const uint64_t avail = c->budget ? free_b - free_b / 8 : free_b;
   if (ps.nhits * bytes_per_hit > avail) {
     std::vector<uint64_t> qoff(nq + 1);
     CUFLYE_CHECK(cudaMemcpyAsync(qoff.data(), ps.q_off, (nq + 1) * 8ull, cudaMemcpyDeviceToHost,
