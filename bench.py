@@ -461,6 +461,13 @@ def run_ours(args, world, rank, local) -> None:
     t0 = time.perf_counter()
     stats = gpu.build_index(reads, wl.k, wl.min_freq, wl.max_freq)
     index_s = time.perf_counter() - t0
+    tune = None
+    if args.autotune > 0:
+        # the autotuner picks the launch shape on a sample before the timed steps
+        t0 = time.perf_counter()
+        tune = gpu.autotune(reads.subset(np.arange(min(args.autotune, reads.n))), params)
+        tune.update(sample_reads=min(args.autotune, reads.n),
+                    seconds=round(time.perf_counter() - t0, 3))
     # pinned host inputs / outputs for the end-to-end leg
     seqs = Sequences(pinned_like(np.ascontiguousarray(reads.ids, dtype=np.int64)),
                      pinned_like(np.ascontiguousarray(reads.offsets, dtype=np.int64)),
@@ -579,6 +586,7 @@ def run_ours(args, world, rank, local) -> None:
                               "mode": "plain path, one read per call through the C ABI"}
     if cpu:
         line["cpu_baseline"] = cpu
+    line["launch_shape"] = {"shape": gpu.launch_shape(), "autotune": tune}
     gpu.close()
     if args.configs and world == 1:
         line["configs"] = extra_configs(args, local)
@@ -615,6 +623,9 @@ def main() -> int:
     ap.add_argument("--serve-workers", type=int, default=2)
     ap.add_argument("--serve-batch-bases", type=int, default=32_000_000,
                     help="most read bases one served batch takes")
+    ap.add_argument("--autotune", type=int, default=1500,
+                    help="reads in the autotuner's sample, run before the timed steps "
+                         "(0: the default launch shape)")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":

@@ -77,6 +77,17 @@ class R2GParams(ctypes.Structure):
 
 
 _LIB = None
+class LaunchShape(ctypes.Structure):
+    """cuflye_launch_shape: blocks per SM of the chaining DP (1-8), the
+    backtrack (1-4), the KmerMatch radix scatter (1-2) and the rounds of the
+    libstdc++-order sort (1-2); 0 keeps a kernel's default."""
+    _fields_ = [("dp_blocks_per_sm", ctypes.c_int32), ("backtrack_blocks_per_sm", ctypes.c_int32),
+                ("scatter_blocks_per_sm", ctypes.c_int32), ("round_blocks_per_sm", ctypes.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {f: int(getattr(self, f)) for f, _ in self._fields_}
+
+
 _vp = ctypes.c_void_p
 _i64p = ctypes.POINTER(ctypes.c_int64)
 _i32p = ctypes.POINTER(ctypes.c_int32)
@@ -138,6 +149,14 @@ def load_library(path: Path | None = None) -> ctypes.CDLL:
     L.cuflye_last_sort_stats.argtypes = [_vp, _u64p, ctypes.c_size_t]
     L.cuflye_last_passes.restype = S
     L.cuflye_last_passes.argtypes = [_vp, _u64p]
+    L.cuflye_set_launch_shape.restype = S
+    L.cuflye_set_launch_shape.argtypes = [_vp, ctypes.POINTER(LaunchShape)]
+    L.cuflye_get_launch_shape.restype = S
+    L.cuflye_get_launch_shape.argtypes = [_vp, ctypes.POINTER(LaunchShape)]
+    L.cuflye_autotune.restype = S
+    L.cuflye_autotune.argtypes = [_vp, ctypes.c_size_t, _i64p, _i64p, ctypes.c_char_p,
+                                  ctypes.POINTER(OverlapParams), ctypes.POINTER(LaunchShape),
+                                  ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
     L.cuflye_set_index_build_windows.restype = S
     L.cuflye_set_index_build_windows.argtypes = [_vp, ctypes.c_uint64]
     L.cuflye_last_index_ranges.restype = S
@@ -268,6 +287,30 @@ class CudaBackend:
         v = ctypes.c_uint64()
         self._check(self._L.cuflye_last_passes(self._h, ctypes.byref(v)))
         return int(v.value)
+
+    def set_launch_shape(self, **blocks_per_sm) -> None:
+        """Sets blocks per SM by field name of LaunchShape (others keep their value)."""
+        cur = self.launch_shape()
+        cur.update(blocks_per_sm)
+        self._check(self._L.cuflye_set_launch_shape(self._h, ctypes.byref(LaunchShape(**cur))))
+
+    def launch_shape(self) -> dict:
+        v = LaunchShape()
+        self._check(self._L.cuflye_get_launch_shape(self._h, ctypes.byref(v)))
+        return v.as_dict()
+
+    def autotune(self, queries, params: "OverlapParams") -> dict:
+        """Picks the launch shape with the least device time on `queries` (a
+        sample of the workload) and keeps it for later calls."""
+        q = Sequences.of(queries)
+        shape = LaunchShape()
+        a, b = ctypes.c_double(), ctypes.c_double()
+        self._check(self._L.cuflye_autotune(self._h, q.n, _ptr(q.ids, _i64p),
+                                            _ptr(q.offsets, _i64p),
+                                            q.bases.ctypes.data_as(ctypes.c_char_p),
+                                            ctypes.byref(params), ctypes.byref(shape),
+                                            ctypes.byref(a), ctypes.byref(b)))
+        return {"shape": shape.as_dict(), "ms_start": a.value, "ms_chosen": b.value}
 
     def set_index_build_windows(self, max_windows: int) -> None:
         """Caps the windows of one key range of the index build (0: budget decides)."""

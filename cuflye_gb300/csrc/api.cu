@@ -84,6 +84,7 @@ struct cuflye_ctx {
   uint64_t sort_stats[7]{};  // see cuflye_last_sort_stats
   uint64_t passes = 0;       // see cuflye_last_passes
   uint64_t build_window_cap = 0;  // see cuflye_set_index_build_windows
+  cuflye_launch_shape shape{0, 0, 0, 0};  // see cuflye_set_launch_shape (0: defaults)
   uint64_t build_ranges = 0;      // key ranges of the last index build
   int servers = 0;           // open serving loops borrowing this index
 };
@@ -880,7 +881,8 @@ SortTasks sort_tasks(cuflye_ctx* c, const std::string& prefix, uint64_t nelems, 
                    segsort_pair_reserve(nelems),
                    nelems,
                    {buf<uint8_t>(c, prefix + "_r0", rb), buf<uint8_t>(c, prefix + "_r1", rb)},
-                   buf<uint32_t>(c, prefix + "_rc", 2 * (kSortRounds + 1))};
+                   buf<uint32_t>(c, prefix + "_rc", 2 * (kSortRounds + 1)),
+                   c->shape.round_blocks_per_sm};
 }
 
 // Sort + chaining of the pass's hits; returns the number of overlap rows left
@@ -918,7 +920,7 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp,
   CUFLYE_CHECK(match_tiles(ps.q_off, ntiles, tile_off, nq, tiles, st));
   CUFLYE_CHECK(match_radix(ps.keys, ps.vals, alt_keys, alt_vals, tiles,
                            static_cast<uint32_t>(NT), ps.q_off, ntiles, tile_off, nq, id_bits,
-                           mcounts, c->num_sms, st));
+                           mcounts, c->num_sms, c->shape.scatter_blocks_per_sm, st));
   CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, qb, qe, nq, ecount, lists,
                                   scounts, c->num_sms, st, sort_tasks(c, "s", H, nq)));
   CUFLYE_CHECK(cudaEventRecord(c->ev[2], st));
@@ -966,7 +968,7 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp,
   CUFLYE_CHECK(cudaEventRecord(c->ev[6], st));
   int32_t* pmc = buf<int32_t>(c, "c_pmc", chain_dp_pmc_words(H, G));
   CUFLYE_CHECK(chain_dp(ps.keys, ps.vals, score, bt, groups, blist, gcounts, cp, top, pmc, work,
-                        c->num_sms, st));
+                        c->num_sms, c->shape.dp_blocks_per_sm, st));
   CUFLYE_CHECK(cudaEventRecord(c->ev[7], st));
   // 5. the backtrack picks its chain starts by score itself; groups where
   // Flye's order among equal scores could matter get that order (libstdc++
@@ -992,7 +994,7 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp,
   CUFLYE_CHECK(chain_backtrack(ps.keys, ps.vals, score, bt, order, groups, blist, gcounts + 1, top,
                                redo, redo_count, ps.qinfo, ps.f_off, ps.fpos, slot_signed, c->logt,
                                cp, pool, pool_cap, pool_count, group_rows, c->status, G32, gmaps,
-                               gmap_words, work, st));
+                               gmap_words, work, c->shape.backtrack_blocks_per_sm, st));
   CUFLYE_CHECK(sort_stats_add(sstats, 4, 6, gcounts + 1, 0, redo_count, st));
   // groups whose result could depend on the order among equal scores: again
   // with the libstdc++ order
@@ -1002,7 +1004,7 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp,
   CUFLYE_CHECK(chain_backtrack(ps.keys, ps.vals, score, bt, order, groups, redo, redo_count, nullptr,
                                nullptr, nullptr, ps.qinfo, ps.f_off, ps.fpos, slot_signed, c->logt,
                                cp, pool, pool_cap, pool_count, group_rows, c->status, G32, gmaps,
-                               gmap_words, work, st));
+                               gmap_words, work, c->shape.backtrack_blocks_per_sm, st));
   check_device_status(c);
   // 7. max_overlaps + compaction in group order
   uint64_t* qg = buf<uint64_t>(c, "o_qg", nq + 1);
@@ -1266,6 +1268,93 @@ cuflye_status cuflye_set_batch_queries(cuflye_ctx* c, size_t q) {
   if (!c) return CUFLYE_ERR_INVALID;
   c->queries_per_pass = q;
   return CUFLYE_OK;
+}
+
+cuflye_status cuflye_set_launch_shape(cuflye_ctx* c, const cuflye_launch_shape* s) {
+  if (!c || !s) return CUFLYE_ERR_INVALID;
+  if (s->dp_blocks_per_sm < 0 || s->dp_blocks_per_sm > 8 || s->backtrack_blocks_per_sm < 0 ||
+      s->backtrack_blocks_per_sm > 4 || s->scatter_blocks_per_sm < 0 ||
+      s->scatter_blocks_per_sm > 2 || s->round_blocks_per_sm < 0 || s->round_blocks_per_sm > 2) {
+    std::lock_guard<std::mutex> g(c->mu);
+    c->err = "launch shape out of range (DP 0-8, backtrack 0-4, scatter 0-2, rounds 0-2)";
+    return CUFLYE_ERR_INVALID;
+  }
+  c->shape = *s;
+  return CUFLYE_OK;
+}
+
+cuflye_status cuflye_get_launch_shape(const cuflye_ctx* c, cuflye_launch_shape* s) {
+  if (!c || !s) return CUFLYE_ERR_INVALID;
+  *s = c->shape;
+  return CUFLYE_OK;
+}
+
+namespace {
+// Device time (stages 0-4) of one overlap call on Q; the rows stay on the
+// device.
+double overlaps_device_ms(cuflye_ctx* c, const Queries& Q, const ChainParams& cp) {
+  reset_timing(c);
+  for_each_pass(c, Q, false, kChainBytesPerHit, [&](size_t, size_t, PassState& ps) {
+    run_chain(c, ps, cp);
+    CUFLYE_CHECK(cudaEventRecord(c->ev[4], c->stream));
+    accumulate_timing(c, true);
+  });
+  double ms = 0;
+  for (int i = 0; i < 5; ++i) ms += c->stage_ms[i];
+  return ms;
+}
+}  // namespace
+
+cuflye_status cuflye_autotune(cuflye_ctx* c, size_t n, const int64_t* ids, const int64_t* offsets,
+                              const char* bases, const cuflye_overlap_params* params,
+                              cuflye_launch_shape* chosen, double* ms_start, double* ms_chosen) {
+  CUFLYE_API_BEGIN(c)
+  CUFLYE_CHECK(cudaSetDevice(c->device));
+  require_index(c);
+  check_params(c, params);
+  if (!ids || !offsets || (!bases && n)) throw Error(CUFLYE_ERR_INVALID, "null input");
+  const ChainParams cp = to_chain_params(params);
+  const Queries Q{n, ids, offsets, bases};
+  const cuflye_launch_shape start_shape = c->shape;
+  try {
+    auto best_of_two = [&]() {
+      const double a = overlaps_device_ms(c, Q, cp);
+      return std::min(a, overlaps_device_ms(c, Q, cp));
+    };
+    overlaps_device_ms(c, Q, cp);  // buffers at their sizes
+    const double start = best_of_two();
+    double best = start;
+    struct Knob {
+      int32_t cuflye_launch_shape::*field;
+      int32_t dflt;
+      std::vector<int32_t> values;
+    };
+    const Knob knobs[] = {{&cuflye_launch_shape::dp_blocks_per_sm, 8, {2, 4, 6, 8}},
+                          {&cuflye_launch_shape::backtrack_blocks_per_sm, 4, {1, 2, 3, 4}},
+                          {&cuflye_launch_shape::scatter_blocks_per_sm, 2, {1, 2}},
+                          {&cuflye_launch_shape::round_blocks_per_sm, 2, {1, 2}}};
+    for (const Knob& k : knobs) {
+      const int32_t cur = c->shape.*k.field ? c->shape.*k.field : k.dflt;
+      int32_t pick = cur;
+      for (int32_t v : k.values) {
+        if (v == cur) continue;
+        c->shape.*k.field = v;
+        const double t = best_of_two();
+        if (t < best * 0.99) {
+          best = t;
+          pick = v;
+        }
+      }
+      c->shape.*k.field = pick;
+    }
+    if (chosen) *chosen = c->shape;
+    if (ms_start) *ms_start = start;
+    if (ms_chosen) *ms_chosen = best;
+  } catch (...) {
+    c->shape = start_shape;
+    throw;
+  }
+  CUFLYE_API_END(c)
 }
 
 cuflye_status cuflye_candidates(cuflye_ctx* c, size_t n, const int64_t* ids,

@@ -1102,16 +1102,19 @@ cudaError_t groups_length_order(const GroupInfo* groups, const uint32_t* list,
 cudaError_t chain_dp(const uint64_t* keys, const uint32_t* vals, int32_t* score, int32_t* bt,
                      const GroupInfo* groups, const uint32_t* dp_list, const uint32_t* counts,
                      const ChainParams& p, GroupTop* top, int32_t* pmc, uint32_t* work,
-                     int num_sms, cudaStream_t s) {
+                     int num_sms, int per_sm, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(work, 0, 4, s);
   if (e != cudaSuccess) return e;
-  int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dp_kernel, kDpWarps * 32, 0);
+  // one resident wave taking groups from a counter: any grid gives the same
+  // result; per_sm (0: the occupancy limit) only sets how many warps share it
+  int most = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&most, dp_kernel, kDpWarps * 32, 0);
   if (e != cudaSuccess) return e;
+  most = std::max(most, 1);
+  const int blocks = per_sm > 0 ? std::min(per_sm, most) : most;
   count_launch();
-  dp_kernel<<<num_sms * std::max(per_sm, 1), kDpWarps * 32, 0, s>>>(keys, vals, score, bt, groups,
-                                                                   dp_list, counts, p, top,
-                                                                   pmc, work);
+  dp_kernel<<<num_sms * blocks, kDpWarps * 32, 0, s>>>(keys, vals, score, bt, groups, dp_list,
+                                                       counts, p, top, pmc, work);
   return cudaGetLastError();
 }
 
@@ -1151,7 +1154,7 @@ cudaError_t chain_backtrack(const uint64_t* keys, const uint32_t* vals, const in
                             const ChainParams& p, OverlapRow* pool, uint64_t pool_cap,
                             uint32_t* pool_count, uint32_t* group_rows, DeviceStatus* st,
                             uint32_t max_groups, uint32_t* gmaps, uint64_t gmap_words,
-                            uint32_t* work, cudaStream_t s) {
+                            uint32_t* work, int per_sm, cudaStream_t s) {
   if (max_groups == 0) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(work, 0, 4, s);
   if (e != cudaSuccess) return e;
@@ -1162,8 +1165,10 @@ cudaError_t chain_backtrack(const uint64_t* keys, const uint32_t* vals, const in
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (sms <= 0) sms = 1;
+  // blocks take groups from a counter: per_sm (1-4, 0: 4) sets only the wave
+  const int blocks = per_sm > 0 ? std::min(per_sm, 4) : 4;
   count_launch();
-  backtrack_kernel<<<sms * 4, kBtWarps * 32, smem, s>>>(
+  backtrack_kernel<<<sms * blocks, kBtWarps * 32, smem, s>>>(
       keys, vals, score, bt, order, groups, list, list_count, top, redo_list, redo_count,
       qinfo, f_off, fpos, slot_signed, logt,
       p, pool, pool_cap, pool_count, group_rows, st, gmaps, gmap_words, work);

@@ -600,13 +600,16 @@ cudaError_t match_radix(uint64_t* keys, uint32_t* vals, uint64_t* alt_keys, uint
                         const MatchTile* tiles, uint32_t ntile,
                         const uint64_t* q_off, const uint32_t* ntiles, const uint64_t* tile_off,
                         uint32_t nq, int id_bits, uint32_t* counts, int num_sms,
-                        cudaStream_t s) {
+                        int scatter_per_sm, cudaStream_t s) {
   if (ntile == 0 || id_bits <= 0) return cudaSuccess;
   const PairsAoS aos{keys, vals};
   const PairsAoS alt{alt_keys, alt_vals};
   allow_smem(match_scatter_kernel<PairsAoS, PairsAoS>, sizeof(TileSmem));
   const unsigned tgrid = static_cast<unsigned>(std::min<uint64_t>(ntile, 2ull * num_sms * 8));
-  const unsigned sgrid = static_cast<unsigned>(std::min<uint64_t>(ntile, 2ull * num_sms));
+  // tiles are taken grid-stride: the scatter's grid (scatter_per_sm blocks
+  // per SM, 1-2, 0: 2) changes no result
+  const uint64_t per_sm = scatter_per_sm > 0 ? std::min(scatter_per_sm, 2) : 2;
+  const unsigned sgrid = static_cast<unsigned>(std::min<uint64_t>(ntile, per_sm * num_sms));
   const unsigned qgrid = static_cast<unsigned>(std::min<uint64_t>(nq, 4ull * num_sms));
   bool in_aos = true;
   for (int sh = 0; sh < id_bits; sh += 8) {

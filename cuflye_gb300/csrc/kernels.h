@@ -39,6 +39,7 @@ struct SortTasks {
   uint64_t nelems;        // elements of the call at most (no global phase up to 4,096)
   void* round[2];         // two round lists of segsort_round_bytes(nelems) each
   uint32_t* round_counts;  // 2 * (kSortRounds + 1) words
+  int round_per_sm = 0;    // blocks per SM of the global phase (1-2; 0: 2)
 };
 uint32_t segsort_pair_reserve(uint64_t nelems);
 size_t segsort_round_bytes(uint64_t nelems);
@@ -211,7 +212,8 @@ cudaError_t match_tiles(const uint64_t* q_off, const uint32_t* ntiles, const uin
 cudaError_t match_radix(uint64_t* keys, uint32_t* vals, uint64_t* alt_keys, uint32_t* alt_vals,
                         const MatchTile* tiles, uint32_t ntile,
                         const uint64_t* q_off, const uint32_t* ntiles, const uint64_t* tile_off,
-                        uint32_t nq, int id_bits, uint32_t* counts, int num_sms, cudaStream_t s);
+                        uint32_t nq, int id_bits, uint32_t* counts, int num_sms,
+                        int scatter_per_sm, cudaStream_t s);
 // stats[i_emul] += *emul; stats[i_plain] += total - *emul (total from
 // total_dev when given, else total_host; i_plain < 0 skips it).
 cudaError_t sort_stats_add(uint64_t* stats, int i_plain, int i_emul, const uint32_t* total_dev,
@@ -270,7 +272,7 @@ cudaError_t groups_length_order(const GroupInfo* groups, const uint32_t* list,
 cudaError_t chain_dp(const uint64_t* keys, const uint32_t* vals, int32_t* score, int32_t* bt,
                      const GroupInfo* groups, const uint32_t* dp_list, const uint32_t* counts,
                      const ChainParams& p, GroupTop* top, int32_t* pmc, uint32_t* work,
-                     int num_sms, cudaStream_t s);
+                     int num_sms, int per_sm, cudaStream_t s);
 inline uint64_t chain_dp_pmc_words(uint64_t nhits, uint64_t ngroups) {
   return (nhits >> 5) + ngroups + 2;
 }
@@ -297,7 +299,7 @@ cudaError_t chain_backtrack(const uint64_t* keys, const uint32_t* vals, const in
                             const ChainParams& p, OverlapRow* pool, uint64_t pool_cap,
                             uint32_t* pool_count, uint32_t* group_rows, DeviceStatus* st,
                             uint32_t max_groups, uint32_t* gmaps, uint64_t gmap_words,
-                            uint32_t* work, cudaStream_t s);
+                            uint32_t* work, int per_sm, cudaStream_t s);
 // max_overlaps cutoff and group-order compaction of the pooled rows.
 cudaError_t rows_limit(const uint32_t* group_rows, const uint64_t* q_group_off, uint32_t nq,
                        int32_t max_overlaps, uint32_t* kept_rows, cudaStream_t s);

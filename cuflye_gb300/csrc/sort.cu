@@ -1297,9 +1297,13 @@ cudaError_t segmented_std_sort(uint64_t* keys, uint32_t* vals, uint32_t* lscratc
     count_launch();
     round_seed<<<std::min((nseg + 255) / 256, 1024u), 256, 0, stream>>>(
         begin, end, lists + 3 * static_cast<size_t>(nseg), counts, rl[0]);
+    // blocks claim ranges from a counter: the grid (round_per_sm blocks per
+    // SM, 1-2) changes no result
+    const int round_blocks =
+        tasks.round_per_sm > 0 ? std::min(tasks.round_per_sm, kBigPerSm) : kBigPerSm;
     for (int r = 0; r < kSortRounds; ++r) {
       count_launch();
-      sort_round<<<num_sms * kBigPerSm, kBigBlock, 0, stream>>>(
+      sort_round<<<num_sms * round_blocks, kBigBlock, 0, stream>>>(
           keys, vals, lscratch, rscratch, rl[r & 1], r == 0 ? counts + 3 : rcount + r, rwork + r,
           rl[(r + 1) & 1], rcount + r + 1, tasks.f, tasks.n, tasks.d, counts + 4, counts + 5,
           counts + 7, tasks.cap, tasks.pair_reserve);

@@ -187,6 +187,35 @@ cuflye_status cuflye_overlaps(cuflye_ctx* ctx, size_t n, const int64_t* query_id
 cuflye_status cuflye_set_batch_queries(cuflye_ctx* ctx, size_t queries_per_pass);
 
 /* --------------------------------------------------------------------------
+ * Launch shapes and the autotuner (no counterpart in the reference).
+ * Blocks per SM of the four kernels that take their work from a counter or
+ * grid-stride, so that their grid changes no result: the chaining DP (1-8),
+ * the backtrack (1-4), the KmerMatch radix scatter (1-2) and the rounds of
+ * the libstdc++-order sort (1-2).  0 keeps a kernel's default (8, 4, 2, 2).
+ * ------------------------------------------------------------------------ */
+typedef struct cuflye_launch_shape {
+  int32_t dp_blocks_per_sm;
+  int32_t backtrack_blocks_per_sm;
+  int32_t scatter_blocks_per_sm;
+  int32_t round_blocks_per_sm;
+} cuflye_launch_shape;
+
+cuflye_status cuflye_set_launch_shape(cuflye_ctx* ctx, const cuflye_launch_shape* shape);
+cuflye_status cuflye_get_launch_shape(const cuflye_ctx* ctx, cuflye_launch_shape* shape);
+
+/* Runs the overlap path on the given queries (a sample of the workload; the
+ * rows are discarded) under candidate shapes, one kernel at a time, and
+ * keeps for each kernel the blocks per SM with the least device time of
+ * stages 0-4 (the better of two calls; a change must gain 1 %).  The
+ * context's shape becomes the chosen one.  chosen (optional) receives it;
+ * ms_start / ms_chosen (optional) the device time of one call under the
+ * starting and the chosen shape. */
+cuflye_status cuflye_autotune(cuflye_ctx* ctx, size_t n, const int64_t* query_ids,
+                              const int64_t* offsets, const char* bases,
+                              const cuflye_overlap_params* params, cuflye_launch_shape* chosen,
+                              double* ms_start, double* ms_chosen);
+
+/* --------------------------------------------------------------------------
  * Read-to-graph chains (read-alignment-v1, docs/abi/read-alignment-v1.md:25-48).
  * Replaces the per-read body of ReadAligner::alignReads
  * (patches/flye/2.9.6/0039-cuflye-read-to-graph-input-boundary-oracle.patch:226-251,
