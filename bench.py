@@ -409,7 +409,7 @@ def scale_config(args, device: int) -> dict:
     memory budget scaled by the same factor, so the index is built in key
     ranges and the reads stream from pinned host buffers in passes.  One
     warm-up call, then one timed call through the C ABI."""
-    from cuflye_gb300 import synth
+    from cuflye_gb300 import abi, synth
     from cuflye_gb300.backend import CudaBackend, OverlapParams, Sequences
     scale = args.scale_genome / 500e6
     wl = synth.scale_ont(seed=6, genome_len=int(args.scale_genome), coverage=30.0)
@@ -423,9 +423,12 @@ def scale_config(args, device: int) -> dict:
         stats = be.build_index(wl.reads, wl.k, wl.min_freq, wl.max_freq)
         build_s = time.perf_counter() - t
         ranges = be.last_index_ranges()
-        be.overlaps(q, p)
+        # the warm-up call gives the row count: the timed call writes into a
+        # pinned buffer of that size (a short buffer would make it run twice)
+        warm = be.overlaps(q, p)
+        out = pinned_like(np.zeros(len(warm) + 1024, dtype=abi.OVERLAP_DTYPE))
         t = time.perf_counter()
-        rows = be.overlaps(q, p)
+        rows = be.overlaps(q, p, out=out)
         wall = time.perf_counter() - t
         ms, by = be.last_timing()
         passes = be.last_passes()

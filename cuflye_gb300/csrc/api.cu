@@ -712,8 +712,11 @@ const char* const kPerWindowBuffers[] = {"q_ascii", "q_words",  "w_cnt",     "w_
 
 // The end of the run of queries from q0 (at most q1) whose windows' buffers
 // take at most a quarter of the memory the budget leaves; the rest is for
-// the run's hits.  At least one query.
-size_t run_end(cuflye_ctx* c, const Queries& Q, size_t q0, size_t q1) {
+// the run's hits.  With the hits per window of the call's previous pass
+// (hpw > 0), the run also stops about where its hits stop fitting, so that
+// few of its queries are counted again by the next pass.  At least one query.
+size_t run_end(cuflye_ctx* c, const Queries& Q, size_t q0, size_t q1, uint64_t bytes_per_hit,
+               double hpw) {
   const uint64_t limit = effective_budget(c);
   uint64_t reusable = 0;
   auto held = [&](const char* name) {
@@ -724,7 +727,12 @@ size_t run_end(cuflye_ctx* c, const Queries& Q, size_t q0, size_t q1) {
   for (const char* nm : kPerHitBuffers) held(nm);
   const uint64_t used = c->in_use > reusable ? c->in_use - reusable : 0;
   const uint64_t avail = limit > used ? limit - used : 0;
-  const uint64_t cap = avail / 4 / kRunBytesPerWindow;
+  uint64_t cap = avail / 4 / kRunBytesPerWindow;
+  if (hpw > 0) {
+    const double fit =
+        1.1 * static_cast<double>(avail) / (static_cast<double>(bytes_per_hit) * hpw);
+    if (fit < static_cast<double>(cap)) cap = std::max<uint64_t>(1, static_cast<uint64_t>(fit));
+  }
   const int64_t k = c->idx.k;
   uint64_t nw = 0;
   size_t q = q0;
@@ -818,13 +826,24 @@ bool run_hits(cuflye_ctx* c, const Queries& Q, size_t q0, size_t q1, bool want_k
   // own margin covers them
   const uint64_t free_b = limit > used ? limit - used : 0;
   const uint64_t avail = c->budget ? free_b - free_b / 8 : free_b;
-  if (ps.nhits * bytes_per_hit > avail) {
+  const uint64_t fits = avail / bytes_per_hit;
+  uint64_t hit_limit = fits;
+  // Under a caller's budget a pass keeps to the per-hit buffers an earlier
+  // pass grew when they hold at least 90 % of what fits: growing them frees
+  // and reallocates them, and that synchronizes the device.
+  if (c->budget) {
+    auto it = c->bufs.find("h_keys");
+    const uint64_t held = it == c->bufs.end() ? 0 : it->second.cap / sizeof(uint64_t);
+    if (held < fits && held * 10 >= fits * 9) hit_limit = held;
+  }
+  if (ps.nhits > hit_limit) {
     std::vector<uint64_t> qoff(nq + 1);
     CUFLYE_CHECK(cudaMemcpyAsync(qoff.data(), ps.q_off, (nq + 1) * 8ull, cudaMemcpyDeviceToHost,
                                  st));
     sync(c);
     uint32_t m = 0;
-    while (m < nq && qoff[m + 1] * bytes_per_hit <= avail) ++m;
+    while (m < nq && qoff[m + 1] <= hit_limit) ++m;
+    if (m == 0 && qoff[1] <= fits) m = 1;  // a first query beyond the held buffers
     if (m == 0)
       throw Error(CUFLYE_ERR_BUDGET,
                   "device memory budget exceeded: query " + std::to_string(Q.ids[q0]) + " has " +
@@ -1085,8 +1104,9 @@ void for_each_pass(cuflye_ctx* c, const Queries& Q, bool kmers, uint64_t bytes_p
   size_t q0 = 0;
   const size_t full = std::max<size_t>(pass_size(c, Q.n), 1);
   size_t step = full;
+  double hpw = 0;  // hits per window of the previous pass
   while (q0 < Q.n) {
-    size_t q1 = run_end(c, Q, q0, std::min(Q.n, q0 + step));
+    size_t q1 = run_end(c, Q, q0, std::min(Q.n, q0 + step), bytes_per_hit, hpw);
     PassState ps;
     CUFLYE_CHECK(cudaEventRecord(c->ev[0], c->stream));
     run_hits(c, Q, q0, q1, kmers, bytes_per_hit, ps);
@@ -1103,6 +1123,7 @@ void for_each_pass(cuflye_ctx* c, const Queries& Q, bool kmers, uint64_t bytes_p
     ++c->passes;
     q0 = q1;
     step = std::min(full, step * 2);  // a halved step grows back after a pass that fits
+    if (ps.nwin) hpw = static_cast<double>(ps.nhits) / static_cast<double>(ps.nwin);
   }
 }
 
