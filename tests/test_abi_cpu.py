@@ -60,6 +60,51 @@ def test_record_layouts_match_header():
     assert abi.READ_ALIGNMENT_DTYPE.itemsize == 72
 
 
+_C_TYPES = {"int64_t": "<i8", "uint64_t": "<u8", "int32_t": "<i4", "float": "<f4"}
+
+
+def header_struct(name: str) -> list[tuple[str, str]]:
+    """(field, numpy type code) of `typedef struct name {...} name;` in cuflye.h."""
+    text = (REPO / "include" / "cuflye.h").read_text()
+    m = re.search(r"typedef struct %s \{(.*?)\} %s;" % (name, name), text, re.S)
+    assert m, name
+    body = re.sub(r"/\*.*?\*/", "", m.group(1), flags=re.S)
+    fields = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if not decl:
+            continue
+        ctype, names = decl.split(None, 1)
+        fields += [(n.strip(), _C_TYPES[ctype]) for n in names.split(",")]
+    return fields
+
+
+def _ctypes_fields(cls) -> list[tuple[str, str]]:
+    import ctypes
+    code = {ctypes.c_int32: "<i4", ctypes.c_float: "<f4", ctypes.c_int64: "<i8",
+            ctypes.c_uint64: "<u8"}
+    return [(n, code[t]) for n, t in cls._fields_]
+
+
+def test_host_mirrors_match_header_structs():
+    """Every struct the C ABI passes by pointer has the same fields, order and
+    types in the Python mirror (ctypes parameters, numpy records)."""
+    import ctypes
+    from cuflye_gb300 import abi
+    from cuflye_gb300.backend import LaunchShape, OverlapParams, R2GParams
+    for cls, name in ((OverlapParams, "cuflye_overlap_params"),
+                      (R2GParams, "cuflye_r2g_params"),
+                      (LaunchShape, "cuflye_launch_shape")):
+        fields = header_struct(name)
+        assert _ctypes_fields(cls) == fields, name
+        assert ctypes.sizeof(cls) == 4 * len(fields), name
+    for dt, name in ((abi.CANDIDATE_DTYPE, "cuflye_candidate"),
+                     (abi.FILTERED_DTYPE, "cuflye_filtered_pos"),
+                     (abi.OVERLAP_DTYPE, "cuflye_overlap_range"),
+                     (abi.READ_ALIGNMENT_DTYPE, "cuflye_read_alignment")):
+        assert [(n, dt.fields[n][0].str) for n in dt.names] == header_struct(name), name
+
+
 def test_float_text_follows_setprecision9():
     """C++ setprecision(9) of a float: 0.01f prints 0.00999999978
     (the reference's own TSV, tests/fixtures/read-alignment-replay-fixture-v0)."""
