@@ -372,9 +372,14 @@ class CudaBackend:
     # -- OverlapDetector::getSeqOverlaps
     def overlaps(self, queries, params: OverlapParams, capacity: int | None = None,
                  out: np.ndarray | None = None) -> np.ndarray:
-        """Rows of every query; ``out`` may supply a (pinned) output buffer."""
+        """Rows of every query; ``out`` may supply a (pinned) output buffer.
+
+        A call whose rows exceed the buffer returns CUFLYE_ERR_CAPACITY after
+        all its work and runs again with the exact size, so the default buffer
+        is generous: 256 rows per query (untouched pages cost no memory), at
+        most 2^27 rows."""
         q = Sequences.of(queries)
-        cap = capacity if capacity is not None else max(1024, 64 * q.n)
+        cap = capacity if capacity is not None else max(1024, min(256 * q.n, 1 << 27))
         if out is not None:
             cap = len(out)
         while True:
