@@ -149,6 +149,30 @@ def make_workload(args):
                                  coverage=args.coverage)
 
 
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the machine type)."""
+    import platform
+    import re
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        m = re.search(r"^Model name:\s*(.+)$", out, re.M)
+        if m:
+            return m.group(1).strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        txt = Path("/proc/cpuinfo").read_text()
+        m = re.search(r"^model name\s*:\s*(.+)$", txt, re.M)
+        if m:
+            return m.group(1).strip()
+        part = re.search(r"^CPU part\s*:\s*(\S+)", txt, re.M)
+        if part:
+            return f"{platform.machine()} CPU part {part.group(1)}"
+    except OSError:
+        pass
+    return platform.machine()
+
+
 def oracle_baseline(wl, sample_queries: int, repeats: int = 1) -> tuple[dict, list[float]]:
     """CPU oracle over the first `sample_queries` reads on all host cores."""
     from oracle import oracle as O
@@ -167,8 +191,8 @@ def oracle_baseline(wl, sample_queries: int, repeats: int = 1) -> tuple[dict, li
         t = time.perf_counter()
         O.overlaps(idx, qb, params, threads=threads)
         times.append(time.perf_counter() - t)
-    info = {"cores": threads, "sample_queries": int(sub.n), "sample_bases": int(sub.total_bases),
-            "index_build_s": round(build_s, 2)}
+    info = {"cores": threads, "cpu_model": cpu_model(), "sample_queries": int(sub.n),
+            "sample_bases": int(sub.total_bases), "index_build_s": round(build_s, 2)}
     return info, times
 
 
@@ -187,8 +211,8 @@ def run_reference(args, world, rank) -> None:
             "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "reads": wl.reads.n,
                        "read_bases": wl.reads.total_bases, "sample": sample},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": info["cores"], "kind": "port",
-                             "sample": sample},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": info["cores"],
+                             "cpu_model": info["cpu_model"], "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -549,7 +573,7 @@ def run_ours(args, world, rank, local) -> None:
     if rank == 0 and world == 1 and args.cpu_sample > 0:
         info, times = oracle_baseline(wl, args.cpu_sample)
         cpu = {"value": info["sample_bases"] / times[0], "unit": UNIT, "cores": info["cores"],
-               "kind": "port",
+               "cpu_model": info["cpu_model"], "kind": "port",
                "sample": f"first {info['sample_queries']} reads ({info['sample_bases']} bases) "
                          f"against the full index, CPU oracle on {info['cores']} threads"}
     if rank != 0:
