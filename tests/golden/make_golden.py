@@ -1,9 +1,9 @@
 #!/usr/bin/env python3
 """Generate the committed golden vectors that pin the CPU oracle.
 
-Run in a container that has the reference checkout (default
-``/root/reference``); the GPU machine never runs this script, it only reads
-the fixtures it writes.  For each seeded synthetic case it:
+Run where the reference checkout is present (default ``/root/reference``);
+the tests never run this script, they only read the fixtures it writes.
+For each seeded synthetic case it:
 
 1. builds the oracle's k-mer index and collects every query's candidate
    records in generation order;
