@@ -21,11 +21,17 @@ workload against the device-resident index, batched: all reads in one pass.
 * ``roofline``: the dominant stage's algorithmic bytes / its event time
   against the measured HBM copy bandwidth;
 * ``cpu_baseline``: the CPU oracle (a restatement of the reference's CPU
-  path) on the host's cores over a bounded sample of the same reads;
+  path) on the host's cores over a bounded sample of the same reads, with
+  the host's CPU model;
+* ``launch_shape``: blocks per SM of the counter-driven kernels, as the
+  autotuner chose them on the first ``--autotune`` reads before the timed
+  steps;
 * ``stage_rooflines``: every stage's algorithmic GB/s and fraction of the
   HBM peak, with hit generation and chaining on their own;
 * ``configs``: the plain 1 Mb overlap configuration and the read-to-graph
-  configuration, each batched and one read per call (``--configs``);
+  configuration, each batched and one read per call, and on request the
+  scale configuration at ``--scale-genome`` with the memory budget scaled
+  to match (``--configs 1,3,5``);
 * ``serving``: continuous batching through cuflye_submit / cuflye_poll on a
   100 Mb indexed genome at several Poisson arrival rates (p50 / p99).
 
