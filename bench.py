@@ -442,7 +442,9 @@ def scale_config(args, device: int) -> dict:
     from cuflye_gb300 import abi, synth
     from cuflye_gb300.backend import CudaBackend, OverlapParams, Sequences
     scale = args.scale_genome / 500e6
-    wl = synth.scale_ont(seed=6, genome_len=int(args.scale_genome), coverage=30.0)
+    # sparse error draws: the same error rates, fast enough for 15 Gbp of reads
+    wl = synth.scale_ont(seed=6, genome_len=int(args.scale_genome), coverage=30.0,
+                         sparse_errors=True)
     budget = int(180e9 * scale)
     p = OverlapParams.make(**wl.params)
     q = Sequences(pinned_like(np.ascontiguousarray(wl.reads.ids, dtype=np.int64)),

@@ -22,8 +22,12 @@ for _a, _b in zip(b"ACGTacgtN", b"TGCAtgcaN"):
     COMP[_a] = _b
 
 
+_COMP_TABLE = bytes(COMP)
+
+
 def revcomp(seq: np.ndarray) -> np.ndarray:
-    return COMP[seq[::-1]]
+    """Reverse complement of ASCII bases (a writable copy)."""
+    return np.frombuffer(bytearray(seq[::-1].tobytes()).translate(_COMP_TABLE), dtype=np.uint8)
 
 
 def random_genome(rng: np.random.Generator, length: int) -> np.ndarray:
@@ -52,6 +56,37 @@ def mutate(rng: np.random.Generator, seq: np.ndarray, sub: float, ins: float = 0
     ins_pos = ends[insert] - 1
     res[ins_pos] = BASES[rng.integers(0, 4, size=len(ins_pos), dtype=np.uint8)]
     return res
+
+
+def mutate_sparse(rng: np.random.Generator, seq: np.ndarray, sub: float, ins: float = 0.0,
+                  dele: float = 0.0) -> np.ndarray:
+    """The error model of `mutate` (each position substituted with
+    probability sub, deleted with probability dele, or followed by an inserted
+    base with probability ins), drawn as sparse events: the number of each
+    kind is binomial and their positions distinct and uniform.  Only the
+    touched positions cost random draws, so long reads generate many times
+    faster; the random stream differs from `mutate`'s."""
+    n = len(seq)
+    out = seq.copy()
+    if n == 0:
+        return out
+    ks = int(rng.binomial(n, sub)) if sub > 0 else 0
+    if ks:
+        pos = rng.choice(n, size=ks, replace=False)
+        shift = rng.integers(1, 4, size=ks, dtype=np.uint8)
+        code = np.searchsorted(BASES, out[pos])
+        out[pos] = BASES[(code + shift) % 4]
+    kd = int(rng.binomial(n, dele)) if dele > 0 else 0
+    ki = int(rng.binomial(n - kd, ins / (1.0 - dele))) if ins > 0 else 0
+    if kd + ki == 0:
+        return out
+    ev = rng.choice(n, size=kd + ki, replace=False)
+    dpos, ipos = np.sort(ev[:kd]), np.sort(ev[kd:])
+    kept = np.delete(out, dpos)
+    # an inserted base follows its anchor p, which sits at p - (deletions
+    # before p) once the deletions are gone
+    at = ipos - np.searchsorted(dpos, ipos) + 1
+    return np.insert(kept, at, BASES[rng.integers(0, 4, size=ki, dtype=np.uint8)])
 
 
 def lognormal_lengths(rng, n, mean, sd, lo, hi):
@@ -98,7 +133,7 @@ class ReadSet:
 
 
 def sample_reads(rng, genome: np.ndarray, coverage: float, lengths_fn, sub, ins, dele,
-                 max_reads: int | None = None) -> ReadSet:
+                 max_reads: int | None = None, sparse: bool = False) -> ReadSet:
     glen = len(genome)
     target = coverage * glen
     lens: list[np.ndarray] = []
@@ -116,11 +151,12 @@ def sample_reads(rng, genome: np.ndarray, coverage: float, lengths_fn, sub, ins,
     starts = rng.integers(0, glen - L + 1)
     strand = rng.random(n) < 0.5
     seqs = []
+    err = mutate_sparse if sparse else mutate
     for i in range(n):
         s = genome[starts[i]:starts[i] + L[i]]
         if strand[i]:
             s = revcomp(s)
-        seqs.append(mutate(rng, s, sub, ins, dele))
+        seqs.append(err(rng, s, sub, ins, dele))
     offs = np.zeros(n + 1, dtype=np.int64)
     offs[1:] = np.cumsum([len(s) for s in seqs])
     return ReadSet(np.arange(1, n + 1, dtype=np.int64), offs, np.concatenate(seqs))
@@ -231,11 +267,13 @@ def read_to_graph(seed: int = 3, genome_len: int = 20_000_000, n_edges: int = 40
 
 
 def scale_ont(seed: int = 6, genome_len: int = 500_000_000, coverage: float = 30.0,
-              max_reads: int | None = None) -> Workload:
+              max_reads: int | None = None, sparse_errors: bool = False) -> Workload:
     """The scale configuration's shapes: a genome with 10 % interspersed repeats
     (families of 1-20 kb, copies at 0.5-5 % divergence); ONT-like reads,
     lognormal(25 kb, 15 kb) in 1-150 kb, 6 % error (2 / 2 / 2 % sub / ins /
-    del); k = 17.  genome_len and coverage scale it down for tests."""
+    del); k = 17.  genome_len and coverage scale it down for tests.
+    sparse_errors draws the read errors with `mutate_sparse` (same rates,
+    another random stream), for the full-size configuration."""
     rng = np.random.default_rng(seed)
     genome = random_genome(rng, genome_len)
     placed = 0
@@ -248,7 +286,7 @@ def scale_ont(seed: int = 6, genome_len: int = 500_000_000, coverage: float = 30
             placed += len(copy)
     reads = sample_reads(rng, genome, coverage,
                          lambda n: lognormal_lengths(rng, n, 25_000, 15_000, 1_000, 150_000),
-                         0.02, 0.02, 0.02, max_reads)
+                         0.02, 0.02, 0.02, max_reads, sparse=sparse_errors)
     return Workload("scale-ont30x-k17", 17, reads, min_freq=2, max_freq=int(5 * coverage),
                     params=dict(OVERLAP_PARAMS, kmer_size=17), seed=seed)
 

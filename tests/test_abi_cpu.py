@@ -136,6 +136,36 @@ def test_logf_table_matches_c_library(built_lib, oracle_mod):
         assert oracle_mod.logf(float(x)) == float(y)
 
 
+def _is_subsequence(small: bytes, big: bytes) -> bool:
+    it = iter(big)
+    return all(c in it for c in small)
+
+
+def test_sparse_errors_follow_the_error_model():
+    """mutate_sparse (used for the full-size scale configuration) gives each
+    error kind at its rate, within five standard deviations."""
+    from cuflye_gb300 import synth
+    rng = np.random.default_rng(11)
+    n = 400_000
+    seq = synth.random_genome(rng, n)
+    sub = synth.mutate_sparse(np.random.default_rng(1), seq, 0.02)
+    assert len(sub) == n
+    rate = float(np.mean(sub != seq))
+    assert abs(rate - 0.02) < 5 * np.sqrt(0.02 * 0.98 / n)
+    dele = synth.mutate_sparse(np.random.default_rng(2), seq, 0.0, 0.0, 0.02)
+    assert abs((n - len(dele)) - 0.02 * n) < 5 * np.sqrt(0.02 * n)
+    short = seq[:20_000]
+    assert _is_subsequence(synth.mutate_sparse(np.random.default_rng(3), short, 0.0, 0.0, 0.05)
+                           .tobytes(), short.tobytes())
+    ins = synth.mutate_sparse(np.random.default_rng(4), short, 0.0, 0.05, 0.0)
+    assert abs((len(ins) - len(short)) - 0.05 * len(short)) < 5 * np.sqrt(0.05 * len(short))
+    assert _is_subsequence(short.tobytes(), ins.tobytes())
+    both = synth.mutate_sparse(np.random.default_rng(5), seq, 0.02, 0.02, 0.02)
+    assert abs(len(both) - n) < 5 * np.sqrt(0.04 * n)
+    again = synth.mutate_sparse(np.random.default_rng(5), seq, 0.02, 0.02, 0.02)
+    assert np.array_equal(both, again)
+
+
 def test_synthetic_generator_is_seeded():
     from cuflye_gb300 import synth
     a = synth.small_overlap_case(3, 20_000, 3.0, 3_000)
