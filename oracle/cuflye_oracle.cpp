@@ -30,7 +30,11 @@
 // calls std::sort itself at the same places, so equal keys land in the order
 // libstdc++ gives them.  A "stable" mode swaps in std::stable_sort so the
 // oracle can also be pinned against the reference's overlap replay, which
-// uses Python's stable sort.
+// uses Python's stable sort.  Each place can be switched on its own
+// (orc_set_sort_mode), so the oracle can also reproduce the reference's C++
+// CPU prototype, which re-sorts ext-sorted groups with std::sort but takes
+// scores in stable order (cuda/cuflye_cuda_overlap_chain_replay.cu:905-911,
+// 1587-1599, 1631-1635).
 //
 // Semantics the reference does not pin (Flye's VertexIndex is absent) and
 // that this oracle defines, shared verbatim by the CUDA library:
@@ -55,11 +59,20 @@
 
 namespace {
 
-int g_stable = 0;  // 0: libstdc++ std::sort (Flye); 1: std::stable_sort
+// The five places Flye sorts, as bits of the stable-sort mask.
+enum SortSite : unsigned {
+  kSiteKmerMatch = 1,  // KmerMatch sort by (ext id, cur pos)
+  kSiteExt = 2,        // ext-sorted group by ext pos
+  kSiteScore = 4,      // backtrack starts by score
+  kSitePrimary = 8,    // overlaps by score before primary selection
+  kSiteChainIn = 16,   // read-to-graph alignments by cur begin
+  kSiteAll = 31,
+};
+unsigned g_stable = 0;  // sites sorted with std::stable_sort; the rest std::sort (Flye)
 
 template <class It, class Cmp>
-void flyeSort(It first, It last, Cmp cmp) {
-  if (g_stable)
+void flyeSort(SortSite site, It first, It last, Cmp cmp) {
+  if (g_stable & site)
     std::stable_sort(first, last, cmp);
   else
     std::sort(first, last, cmp);
@@ -316,7 +329,7 @@ void collectCandidates(const Index& idx, int64_t queryId, const char* seq,
 }
 
 void sortMatches(std::vector<KmerMatch>& m) {
-  flyeSort(m.begin(), m.end(), [](const KmerMatch& a, const KmerMatch& b) {
+  flyeSort(kSiteKmerMatch, m.begin(), m.end(), [](const KmerMatch& a, const KmerMatch& b) {
     return a.extId != b.extId ? a.extId < b.extId : a.curPos < b.curPos;
   });
 }
@@ -399,7 +412,7 @@ void chainGroup(const KmerMatch* m, size_t n, int64_t queryId, int32_t curLen,
   std::vector<KmerMatch> w(m, m + n);
   const bool extSorted = extLen > curLen;
   if (extSorted)
-    flyeSort(w.begin(), w.end(),
+    flyeSort(kSiteExt, w.begin(), w.end(),
              [](const KmerMatch& a, const KmerMatch& b) { return a.extPos < b.extPos; });
 
   std::vector<int32_t> score(n, 0), bt(n, -1);
@@ -431,7 +444,7 @@ void chainGroup(const KmerMatch* m, size_t n, int64_t queryId, int32_t curLen,
 
   std::vector<int32_t> order(n);
   for (size_t i = 0; i < n; ++i) order[i] = static_cast<int32_t>(i);
-  flyeSort(order.begin(), order.end(),
+  flyeSort(kSiteScore, order.begin(), order.end(),
            [&](int32_t a, int32_t b) { return score[a] > score[b]; });
 
   std::vector<Overlap> ext;
@@ -464,7 +477,7 @@ void chainGroup(const KmerMatch* m, size_t n, int64_t queryId, int32_t curLen,
     if (!ok) continue;
     ext.push_back(o);
   }
-  flyeSort(ext.begin(), ext.end(),
+  flyeSort(kSitePrimary, ext.begin(), ext.end(),
            [](const Overlap& a, const Overlap& b) { return a.score > b.score; });
   std::vector<Overlap> primary;
   if (p.onlyMaxExt) {
@@ -646,7 +659,11 @@ struct orc_result {
   std::vector<uint64_t> queryMatchCounts;
 };
 
-void orc_set_stable(int stable) { g_stable = stable; }
+void orc_set_stable(int stable) { g_stable = stable ? kSiteAll : 0u; }
+
+// mask: SortSite bits sorted stably (KmerMatch 1, ext 2, score 4, primary 8,
+// read-to-graph input 16); the others use std::sort.
+void orc_set_sort_mode(unsigned mask) { g_stable = mask & kSiteAll; }
 
 void* orc_index_build(int k, int n, const int64_t* ids, const int64_t* offs,
                       const char* bases, uint32_t minFreq, uint32_t maxFreq) {
@@ -804,7 +821,7 @@ static void r2gRange(const Index* idx, const Graph* g, int q0, int q1, const int
       }
       alns.push_back(a);
     }
-    flyeSort(alns.begin(), alns.end(),
+    flyeSort(kSiteChainIn, alns.begin(), alns.end(),
              [](const EdgeAln& x, const EdgeAln& y) { return x.ovl.curBegin < y.ovl.curBegin; });
     std::vector<Chain> chains = chainReadAlignments(alns, *rp);
     std::vector<const Chain*> good;

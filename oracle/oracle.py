@@ -110,6 +110,7 @@ def lib() -> ctypes.CDLL:
         L.orc_logf.restype = ctypes.c_float
         L.orc_logf.argtypes = [ctypes.c_float]
         L.orc_set_stable.argtypes = [ctypes.c_int]
+        L.orc_set_sort_mode.argtypes = [ctypes.c_uint]
         for name in ("orc_n_matches", "orc_n_filtered", "orc_n_overlaps", "orc_n_rows"):
             getattr(L, name).restype = ctypes.c_size_t
             getattr(L, name).argtypes = [vp]
@@ -307,6 +308,15 @@ def std_sort_u64(keys: np.ndarray, payload: np.ndarray) -> tuple[np.ndarray, np.
 
 def set_stable(stable: bool) -> None:
     lib().orc_set_stable(int(stable))
+
+
+# Sort places for set_sort_mode (bits of the stable-sort mask).
+SORT_KMERMATCH, SORT_EXT, SORT_SCORE, SORT_PRIMARY, SORT_CHAIN_INPUT = 1, 2, 4, 8, 16
+
+
+def set_sort_mode(stable_mask: int) -> None:
+    """Stable sorts at the places in `stable_mask`, std::sort at the others."""
+    lib().orc_set_sort_mode(int(stable_mask))
 
 
 def logf(x: float) -> float:
