@@ -146,3 +146,100 @@ def test_reference_cpu_chaining_on_tandem_ties(oracle_mod, ref_overlap_bin, tmp_
     for name, want in expected.items():
         got = (tmp_path / "out" / name / "overlaps.tsv").read_text().splitlines()
         assert got == want, name
+
+
+# ---------------------------------------------------------------- read-to-graph chains
+
+
+@pytest.fixture(scope="module")
+def ref_r2g_bin():
+    from oracle import ref_build
+    ref_build.build()
+    path = ref_build.binary("read_alignment_chain_replay")
+    if path is None:
+        pytest.skip("the reference's CPU backends are not built here (no reference checkout)")
+    return path
+
+
+def _edge_alignments(rng, n_path: int) -> list[dict]:
+    """One read's edge alignments in read_begin order: a walk over graph
+    nodes (each edge's right node usually the next one's left node), with
+    gaps, small overlaps, broken links and alignments that start or end far
+    inside their edge, plus unrelated alignments on other nodes."""
+    rows = []
+    pos = int(rng.integers(0, 2_000))
+    node = int(rng.integers(0, 30))
+    for _ in range(n_path):
+        elen = int(rng.integers(600, 8_000))
+        eb = int(rng.integers(0, 150)) if rng.random() < 0.8 else int(rng.integers(0, 2_500))
+        ee = min(elen, eb + int(rng.integers(200, 6_000)))
+        if rng.random() < 0.8:
+            ee = max(ee, elen - int(rng.integers(0, 200)))
+        nxt = int(rng.integers(0, 30))
+        span = ee - eb + int(rng.integers(-40, 40))
+        rows.append([pos, pos + max(span, 50), eb, ee, elen, node, nxt])
+        node = nxt if rng.random() < 0.85 else int(rng.integers(0, 30))
+        pos = pos + max(span, 50) + int(rng.integers(-70, 300))
+    for _ in range(n_path // 3):
+        elen = int(rng.integers(600, 8_000))
+        eb = int(rng.integers(0, elen - 300))
+        ee = int(rng.integers(eb + 200, elen + 1))
+        rb = int(rng.integers(0, max(pos, 1)))
+        rows.append([rb, rb + ee - eb, eb, ee, elen, int(rng.integers(0, 30)),
+                     int(rng.integers(0, 30))])
+    rows.sort(key=lambda r: r[0])  # stable: equal read_begin keep this order
+    for i, r in enumerate(rows):
+        span = r[3] - r[2]
+        r.append(int(span * rng.uniform(0.3, 1.0)))           # score
+        r.append(float(np.float32(rng.uniform(0.0, 0.3))))    # seq divergence
+        r.append(1_000 + i)                                   # edge id (unique)
+    return rows
+
+
+def test_reference_cpu_read_alignment_chains_match_oracle(oracle_mod, ref_r2g_bin, tmp_path):
+    """Synthetic read-alignment replay fixtures
+    (docs/abi/read-alignment-replay-fixture-v0.md) chained by the read-
+    alignment replay's CPU backend in its pre-divergence mode
+    (cuflye_cuda_read_alignment_chain_replay.cu:872-984, every candidate
+    chain, no divergence filter) give the oracle's chains, segment for
+    segment."""
+    from cuflye_gb300 import synth
+    O = oracle_mod
+    p = synth.R2G_PARAMS
+    r2g = O.default_r2g(max_jump=p["max_jump"], max_read_overlap=p["max_read_overlap"],
+                        min_overlap=p["min_overlap"], max_separation=p["max_separation"])
+    rng = np.random.default_rng(31)
+    chains_seen = 0
+    for f in range(40):
+        rows = _edge_alignments(rng, int(rng.integers(4, 40)))
+        read_len = max(r[1] for r in rows) + int(rng.integers(0, 500))
+        d = tmp_path / f"read_{f}"
+        d.mkdir()
+        (d / "edge-overlaps.tsv").write_text("".join(
+            f"{i}\t{7}\t{r[0]}\t{r[1]}\t{read_len}\t{r[9]}\t{r[5]}\t{r[6]}\t{r[9] + 5000}\t"
+            f"{r[2]}\t{r[3]}\t{r[4]}\t{r[7]}\t{fmt9(r[8])}\n" for i, r in enumerate(rows)))
+        (d / "manifest.json").write_text(json.dumps({
+            "schema": "cuflye-read-alignment-replay-fixture-v0", "query_id": 7,
+            "alignment_input_records": len(rows), "candidate_chains": 0, "oracle_chains": 0,
+            "maximum_jump": p["max_jump"], "max_read_overlap": p["max_read_overlap"],
+            "minimum_overlap": p["min_overlap"], "max_separation": p["max_separation"],
+            "read_align_ovlp_divergence": p["max_chain_divergence"],
+            "reads_base_alignment": False}))
+        subprocess.run([str(ref_r2g_bin), "--fixture-dir", str(d), "--output-tsv",
+                        str(d / "out.tsv"), "--json-output", str(d / "out.json"), "--backend",
+                        "cpu", "--emit-pre-divergence-chains"],
+                       check=True, capture_output=True, text=True, timeout=120)
+        by_edge = {r[9]: i for i, r in enumerate(rows)}
+        got: list[list[int]] = []
+        for line in (d / "out.tsv").read_text().splitlines():
+            c = line.split("\t")
+            chain, seg = int(c[0]), int(c[1])
+            while len(got) <= chain:
+                got.append([])
+            assert seg == len(got[chain])
+            got[chain].append(by_edge[int(c[6])])
+        arr = np.array([[r[0], r[1], r[2], r[3], r[4], r[7]] for r in rows])
+        want = O.chain_read_alignments(arr, [r[5] for r in rows], [r[6] for r in rows], r2g)
+        assert got == want, f"read_{f}"
+        chains_seen += len(want)
+    assert chains_seen >= 40
