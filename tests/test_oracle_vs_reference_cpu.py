@@ -46,9 +46,10 @@ def _manifest_params(k: int, p: dict) -> dict:
     }
 
 
-def _write_fixtures(O, wl, root, limit):
+def _write_fixtures(O, wl, root, limit, **overrides):
     """One fixture directory per query with candidates (at most `limit`
-    queries); returns {fixture name: expected overlap-range-v1 lines}."""
+    queries), chaining parameters overridden by `overrides`; returns
+    {fixture name: expected overlap-range-v1 lines}."""
     reads = wl.reads
     batch = O.SeqBatch(reads.ids, reads.offsets, reads.bases.tobytes())
     idx = O.Index.build(wl.k, batch, wl.min_freq, wl.max_freq)
@@ -57,7 +58,7 @@ def _write_fixtures(O, wl, root, limit):
     srt = O.candidates(idx, batch, sorted_like_flye=True)
     lens = {int(reads.ids[i]): int(reads.offsets[i + 1] - reads.offsets[i])
             for i in range(reads.n)}
-    params = dict(wl.params, only_max_ext=1, max_overlaps=0)
+    params = dict(wl.params, **overrides, only_max_ext=1, max_overlaps=0)
     oparams = O.default_params(**params)
     mparams = _manifest_params(wl.k, params)
     expected = {}
@@ -146,6 +147,30 @@ def test_reference_cpu_chaining_on_tandem_ties(oracle_mod, ref_overlap_bin, tmp_
     for name, want in expected.items():
         got = (tmp_path / "out" / name / "overlaps.tsv").read_text().splitlines()
         assert got == want, name
+
+
+def test_reference_cpu_chaining_other_parameters(oracle_mod, ref_overlap_bin, tmp_path):
+    """No overhang check, local overlaps forced, a shorter jump, gap and
+    minimum overlap and a higher survival rate: the overlapTest and group
+    prefilter branches the default parameters do not reach."""
+    from cuflye_gb300 import synth
+    wl = synth.small_overlap_case(25, 40_000, 10.0, 4_000, 15, 0.02, 0.01, 0.01, True)
+    fx = tmp_path / "fixtures"
+    fx.mkdir()
+    expected = _write_fixtures(oracle_mod, wl, fx, limit=60, check_overhang=0, force_local=1,
+                               max_jump=1000, max_gap=300, min_overlap=800,
+                               min_kmer_survival_rate=0.02, max_divergence=0.5)
+    (tmp_path / "list.txt").write_text("".join(f"{fx / n}\n" for n in expected))
+    subprocess.run([str(ref_overlap_bin), "--batch-fixtures-file", str(tmp_path / "list.txt"),
+                    "--batch-output-dir", str(tmp_path / "out"), "--batch-json-output",
+                    str(tmp_path / "out.json"), "--backend", "cpu"],
+                   check=True, capture_output=True, text=True, timeout=300)
+    rows = 0
+    for name, want in expected.items():
+        got = (tmp_path / "out" / name / "overlaps.tsv").read_text().splitlines()
+        assert got == want, name
+        rows += len(got)
+    assert rows > 0
 
 
 # ---------------------------------------------------------------- read-to-graph chains
