@@ -179,46 +179,80 @@ def cpu_model() -> str:
     return platform.machine()
 
 
-def oracle_baseline(wl, sample_queries: int, repeats: int = 1) -> tuple[dict, list[float]]:
-    """CPU oracle over the first `sample_queries` reads on all host cores."""
+def oracle_index(wl):
+    """The CPU oracle's index of the workload's reads, and its build time."""
     from oracle import oracle as O
     O.build()
+    O.set_stable(False)  # libstdc++ std::sort order at every sort point, as Flye
     reads = wl.reads
     b = O.SeqBatch(reads.ids, reads.offsets, reads.bases.tobytes())
     t0 = time.time()
     idx = O.Index.build(wl.k, b, wl.min_freq, wl.max_freq)
-    build_s = time.time() - t0
-    sub = reads.subset(np.arange(min(sample_queries, reads.n)))
+    return idx, time.time() - t0
+
+
+def oracle_run(wl, idx, picks) -> tuple[dict, float]:
+    """The CPU oracle over the reads `picks` on all host cores: its rows and
+    its wall time."""
+    from oracle import oracle as O
+    sub = wl.reads.subset(picks)
     qb = O.SeqBatch(sub.ids, sub.offsets, sub.bases.tobytes())
-    params = O.default_params(**wl.params)
-    threads = os.cpu_count() or 1
-    times = []
-    for _ in range(repeats):
-        t = time.perf_counter()
-        O.overlaps(idx, qb, params, threads=threads)
-        times.append(time.perf_counter() - t)
-    info = {"cores": threads, "cpu_model": cpu_model(), "sample_queries": int(sub.n),
-            "sample_bases": int(sub.total_bases), "index_build_s": round(build_s, 2)}
-    return info, times
+    t = time.perf_counter()
+    res = O.overlaps(idx, qb, O.default_params(**wl.params), threads=os.cpu_count() or 1)
+    return res, time.perf_counter() - t
+
+
+def bench_config(wl) -> dict:
+    """The workload's description, identical in both arms' lines."""
+    return {"workload": WORKLOAD, "reads": wl.reads.n, "read_bases": wl.reads.total_bases,
+            "k": wl.k, "l2": "inputs larger than L2 (about 12 B x 7e9 hits per step, "
+                              "index 1.5 GB)"}
+
+
+def rows_tuples(rows) -> list:
+    """ABI overlap rows (GPU) as comparable tuples, divergence as float bits."""
+    return [(int(r["cur_id"]), int(r["cur_begin"]), int(r["cur_end"]), int(r["cur_len"]),
+             int(r["ext_id"]), int(r["ext_begin"]), int(r["ext_end"]), int(r["ext_len"]),
+             int(r["score"]), np.float32(r["seq_divergence"]).view(np.uint32).item())
+            for r in rows]
+
+
+def oracle_tuples(res) -> list:
+    return [tuple(int(v) for v in row) + (np.float32(dv).view(np.uint32).item(),)
+            for row, dv in zip(res["cols"], res["divergence"])]
 
 
 def run_reference(args, world, rank) -> None:
+    """The reference's CPU path (the oracle, a restatement of it) on every
+    host core.  Step i takes the next --reference-sample reads of the
+    workload (wrapping around), so the timed steps together cover
+    steps x sample reads."""
     if rank != 0:
         return
     wl = make_workload(args)
-    info, times = oracle_baseline(wl, args.reference_sample, repeats=args.warmup + args.steps)
-    timed = times[args.warmup:]
-    v = info["sample_bases"] * len(timed) / sum(timed)
-    sample = (f"first {info['sample_queries']} reads ({info['sample_bases']} bases) of the "
-              f"workload against the full index, {info['cores']} threads")
+    idx, build_s = oracle_index(wl)
+    n, m = wl.reads.n, max(1, min(args.reference_sample, wl.reads.n))
+    times, bases = [], []
+    for step in range(args.warmup + args.steps):
+        picks = (np.arange(m) + step * m) % n
+        _, t = oracle_run(wl, idx, picks)
+        times.append(t)
+        bases.append(int(np.diff(wl.reads.offsets)[picks].sum()))
+    timed, tb = times[args.warmup:], bases[args.warmup:]
+    v = sum(tb) / sum(timed)
+    cores = os.cpu_count() or 1
+    covered = min(n, args.steps * m)
+    sample = (f"each step the next {m} reads of the workload (wrapping), {covered} distinct "
+              f"reads and {sum(tb)} bases over the {args.steps} timed steps, against the full "
+              f"index; CPU oracle on {cores} threads")
     line = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1000 * sum(timed) / len(timed), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "reads": wl.reads.n,
-                       "read_bases": wl.reads.total_bases, "sample": sample},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": info["cores"],
-                             "cpu_model": info["cpu_model"], "kind": "port", "sample": sample},
+            "config": bench_config(wl),
+            "index_build_s": round(build_s, 2),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "cpu_model": cpu_model(),
+                             "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -578,12 +612,29 @@ def run_ours(args, world, rank, local) -> None:
                  "batched_over_plain": (bases / (sum(wall_s) / len(wall_s))) /
                                        (sub.total_bases / plain_s)}
     cpu = None
+    parity = None
     if rank == 0 and world == 1 and args.cpu_sample > 0:
-        info, times = oracle_baseline(wl, args.cpu_sample)
-        cpu = {"value": info["sample_bases"] / times[0], "unit": UNIT, "cores": info["cores"],
-               "cpu_model": info["cpu_model"], "kind": "port",
-               "sample": f"first {info['sample_queries']} reads ({info['sample_bases']} bases) "
-                         f"against the full index, CPU oracle on {info['cores']} threads"}
+        # the CPU oracle on a sample spread over the workload, timed, and its
+        # rows compared with the GPU's rows for the same reads
+        m = min(args.cpu_sample, reads.n)
+        picks = np.linspace(0, reads.n - 1, m).astype(np.int64)
+        idx, _ = oracle_index(wl)
+        res, secs = oracle_run(wl, idx, picks)
+        sub = reads.subset(picks)
+        got = rows_tuples(gpu.overlaps(sub, params))
+        exp = oracle_tuples(res)
+        sb = int(sub.total_bases)
+        cores = os.cpu_count() or 1
+        cpu = {"value": sb / secs, "unit": UNIT, "cores": cores, "cpu_model": cpu_model(),
+               "kind": "port",
+               "sample": f"{m} reads spread evenly over the workload ({sb} bases) against the "
+                         f"full index, CPU oracle on {cores} threads"}
+        first_diff = next((i for i, (a, b) in enumerate(zip(got, exp)) if a != b),
+                          None if len(got) == len(exp) else min(len(got), len(exp)))
+        parity = {"reads": m, "rows": len(exp), "gpu_rows": len(got), "equal": got == exp,
+                  "first_difference": first_diff,
+                  "compared": "every overlap row of the sample, all fields, divergence as "
+                              "float bits, GPU (C ABI) vs CPU oracle (libstdc++ sort order)"}
     if rank != 0:
         return
     mean_ms = 1000.0 * dev_total / args.steps
@@ -591,10 +642,10 @@ def run_ours(args, world, rank, local) -> None:
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": mean_ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "reads": reads.n, "read_bases": int(bases),
-                   "index_positions": stats["positions"], "index_keys": stats["keys"],
-                   "index_build_s": round(index_s, 3), "rows_per_step": nrows,
-                   "l2": "inputs larger than L2 (about 12 B x 7e9 hits per step, index 1.5 GB)"},
+        "config": bench_config(wl),
+        "index": {"positions": stats["positions"], "keys": stats["keys"],
+                  "build_s": round(index_s, 3)},
+        "rows_per_step": nrows,
         "e2e": {"value": e2e, "unit": UNIT,
                 "h2d_bytes_per_step": int(seqs.bases.nbytes + seqs.offsets.nbytes +
                                           seqs.ids.nbytes),
@@ -621,6 +672,7 @@ def run_ours(args, world, rank, local) -> None:
                               "mode": "plain path, one read per call through the C ABI"}
     if cpu:
         line["cpu_baseline"] = cpu
+        line["parity"] = parity
     line["launch_shape"] = {"shape": gpu.launch_shape(), "autotune": tune}
     gpu.close()
     if args.configs and world == 1:
@@ -639,9 +691,11 @@ def main() -> int:
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--genome-len", type=int, default=5_000_000)
     ap.add_argument("--coverage", type=float, default=40.0)
-    ap.add_argument("--plain-sample", type=int, default=200)
-    ap.add_argument("--cpu-sample", type=int, default=384)
-    ap.add_argument("--reference-sample", type=int, default=256)
+    ap.add_argument("--plain-sample", type=int, default=2000)
+    ap.add_argument("--cpu-sample", type=int, default=2000,
+                    help="reads of the CPU baseline, also compared row for row with the GPU")
+    ap.add_argument("--reference-sample", type=int, default=400,
+                    help="reads per step of --impl reference (each step takes the next ones)")
     ap.add_argument("--serve-rates", type=lambda v: [float(x) for x in v.split(",") if x],
                     default=[1000.0, 10000.0, 50000.0],
                     help="offered request rates (reads/s) of the serving run; empty skips it")
@@ -654,7 +708,7 @@ def main() -> int:
                          "5: scale, at --scale-genome); empty to skip")
     ap.add_argument("--scale-genome", type=int, default=50_000_000,
                     help="genome length of config 5 (the configuration's is 500 Mb)")
-    ap.add_argument("--config-plain-sample", type=int, default=200)
+    ap.add_argument("--config-plain-sample", type=int, default=2000)
     ap.add_argument("--serve-workers", type=int, default=2)
     ap.add_argument("--serve-batch-bases", type=int, default=32_000_000,
                     help="most read bases one served batch takes")

@@ -192,7 +192,7 @@ def stub_message(device: str | None = None, budget: str | None = None) -> str:
     device = device if device is not None else (os.environ.get("CUFLYE_CUDA_DEVICE") or "0")
     budget = budget if budget is not None else (
         os.environ.get("CUFLYE_CUDA_MEMORY_BUDGET_BYTES") or "unbounded")
-    return ("cuFlye CUDA candidate backend selected; adapter=gb300; "
+    return ("cuFlye CUDA candidate backend selected; adapter=cuflye_gb300; "
             f"CUFLYE_CUDA_DEVICE={device}; CUFLYE_CUDA_MEMORY_BUDGET_BYTES={budget}; ")
 
 
@@ -232,7 +232,9 @@ class CudaBackend:
         else:
             st = L.cuflye_open(int(device or 0), int(memory_budget_bytes or 0), ctypes.byref(h))
         if st != 0:
-            raise CuflyeError(st, stub_message() + "cuflye_open failed (see stderr)")
+            # the library keeps the failed open's message for this thread
+            msg = L.cuflye_last_error(None)
+            raise CuflyeError(st, msg.decode() if msg else stub_message() + "cuflye_open failed")
         self._h = h
         self._L = L
         self.k = None
@@ -380,6 +382,7 @@ class CudaBackend:
         most 2^27 rows."""
         q = Sequences.of(queries)
         cap = capacity if capacity is not None else max(1024, min(256 * q.n, 1 << 27))
+        caller_buffer = out is not None
         if out is not None:
             cap = len(out)
         while True:
@@ -392,9 +395,12 @@ class CudaBackend:
                                          ctypes.byref(n))
             if st == ERR_CAPACITY:
                 cap = n.value
+                caller_buffer = False
                 continue
             self._check(st)
-            return out[:n.value]
+            # a view of the caller's buffer; a copy of an internal one, so the
+            # generous default allocation is not kept alive by the result
+            return out[:n.value] if caller_buffer else out[:n.value].copy()
 
     # -- ReadAligner::alignReads per-read body
     def set_graph(self, edge_ids, seq_ids, left, right) -> None:

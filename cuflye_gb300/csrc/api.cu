@@ -15,6 +15,8 @@
 #include <dlfcn.h>
 
 #include <algorithm>
+#include <cerrno>
+#include <climits>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -1155,6 +1157,30 @@ struct GraphDev {
 
 // ================================================================ C ABI
 
+namespace {
+
+// The reference stub's fail-fast text names the adapter, the device and the
+// budget (patches/flye/2.9.6/0003-cuflye-cuda-backend-stub.patch:37-46); an
+// unsupported shape or an exhausted budget keeps those fields in front of
+// the reason, so Flye's runtime_error reads the same way.
+std::string stub_fields(int device, uint64_t budget) {
+  return "cuFlye CUDA candidate backend selected; adapter=cuflye_gb300; CUFLYE_CUDA_DEVICE=" +
+         std::to_string(device) + "; CUFLYE_CUDA_MEMORY_BUDGET_BYTES=" +
+         (budget ? std::to_string(budget) : std::string("unbounded")) + "; ";
+}
+
+std::string fail_text(const cuflye_ctx* c, const Error& e) {
+  if (e.code == CUFLYE_ERR_UNSUPPORTED || e.code == CUFLYE_ERR_BUDGET)
+    return stub_fields(c->device, c->budget) + e.what();
+  return e.what();
+}
+
+// Why the calling thread's last cuflye_open / cuflye_open_from_env failed
+// (there is no context to hold it); cuflye_last_error(NULL) returns it.
+thread_local std::string t_open_error;
+
+}  // namespace
+
 #define CUFLYE_API_BEGIN(ctx)                   \
   if (!(ctx)) return CUFLYE_ERR_INVALID;        \
   std::lock_guard<std::mutex> lock_((ctx)->mu); \
@@ -1162,7 +1188,7 @@ struct GraphDev {
 #define CUFLYE_API_END(ctx)           \
   }                                   \
   catch (const Error& e) {            \
-    (ctx)->err = e.what();            \
+    (ctx)->err = fail_text(ctx, e);   \
     return e.code;                    \
   }                                   \
   catch (const std::exception& e) {   \
@@ -1183,7 +1209,10 @@ int cuflye_candidate_backend(char* msg, size_t msg_cap) {
 }
 
 cuflye_status cuflye_open(int device, uint64_t memory_budget_bytes, cuflye_ctx** out) {
-  if (!out) return CUFLYE_ERR_INVALID;
+  if (!out) {
+    t_open_error = "cuflye_open: null output pointer";
+    return CUFLYE_ERR_INVALID;
+  }
   *out = nullptr;
   cuflye_ctx* c = new cuflye_ctx();
   try {
@@ -1203,10 +1232,11 @@ cuflye_status cuflye_open(int device, uint64_t memory_budget_bytes, cuflye_ctx**
     CUFLYE_CHECK(cudaMemset(c->status, 0, sizeof(DeviceStatus)));
     load_logf_table(c);
   } catch (const Error& e) {
-    std::fprintf(stderr, "cuflye_open: %s\n", e.what());
+    t_open_error = stub_fields(device, memory_budget_bytes) + e.what();
     cuflye_close(c);
     return e.code;
   }
+  t_open_error.clear();
   *out = c;
   return CUFLYE_OK;
 }
@@ -1216,16 +1246,28 @@ cuflye_status cuflye_open_from_env(cuflye_ctx** out) {
   const char* bud = std::getenv("CUFLYE_CUDA_MEMORY_BUDGET_BYTES");
   int d = 0;
   uint64_t b = 0;
+  auto bad = [&](const char* what) {
+    t_open_error = std::string("cuFlye CUDA candidate backend selected; adapter=cuflye_gb300; "
+                               "CUFLYE_CUDA_DEVICE=") +
+                   (dev && dev[0] ? dev : "0") + "; CUFLYE_CUDA_MEMORY_BUDGET_BYTES=" +
+                   (bud && bud[0] ? bud : "unbounded") + "; " + what;
+    if (out) *out = nullptr;
+    return CUFLYE_ERR_INVALID;
+  };
   if (dev && dev[0]) {
     char* end = nullptr;
+    errno = 0;
     long v = std::strtol(dev, &end, 10);
-    if (!end || *end) return CUFLYE_ERR_INVALID;
+    if (!end || *end || errno || v < 0 || v > INT_MAX)
+      return bad("CUFLYE_CUDA_DEVICE is not a device ordinal");
     d = static_cast<int>(v);
   }
   if (bud && bud[0] && std::strcmp(bud, "unbounded") != 0) {
     char* end = nullptr;
+    errno = 0;
     unsigned long long v = std::strtoull(bud, &end, 10);
-    if (!end || *end) return CUFLYE_ERR_INVALID;
+    if (!end || *end || errno || bud[0] == '-')
+      return bad("CUFLYE_CUDA_MEMORY_BUDGET_BYTES is neither a byte count nor \"unbounded\"");
     b = v;
   }
   return cuflye_open(d, b, out);
@@ -1243,7 +1285,9 @@ void cuflye_close(cuflye_ctx* c) {
   delete c;
 }
 
-const char* cuflye_last_error(const cuflye_ctx* c) { return c ? c->err.c_str() : "null context"; }
+const char* cuflye_last_error(const cuflye_ctx* c) {
+  return c ? c->err.c_str() : t_open_error.c_str();
+}
 
 cuflye_status cuflye_memory_stats(const cuflye_ctx* c, uint64_t* in_use, uint64_t* peak) {
   if (!c) return CUFLYE_ERR_INVALID;

@@ -15,7 +15,12 @@
 //
 // Host code cannot use g_noalloc_scratch's name as a device address; the
 // first call on each device, with that device current, asks the runtime for
-// the array's device address (cudaGetSymbolAddress) and caches it.  Calls
+// the array's device address (cudaGetSymbolAddress) and caches it.  The
+// cache assumes the device's primary context lives as long as the process:
+// after a cudaDeviceReset the cached address is stale and the call must not
+// be used again in that process.  A call over more than 4,096 elements
+// reads its round counts back between sort rounds and so waits on `stream`
+// before it returns; smaller calls return once the work is queued.  Calls
 // share the array and it keeps the previous call's contents: the counters
 // that must start at zero are cleared by every call, and calls whose work
 // overlaps on the GPU (different streams, or different host threads on one
@@ -103,6 +108,8 @@ extern "C" cuflye_status cuflye_std_sort_segments_noalloc(uint64_t* keys, uint32
   if (seg_offsets[n_segments] > n_elements) return CUFLYE_ERR_INVALID;
   if (segsort_task_words(n_elements, static_cast<uint32_t>(n_segments)) > kTaskCap)
     return CUFLYE_ERR_UNSUPPORTED;
+  if (segsort_round_bytes(n_elements) > kRoundBytes) return CUFLYE_ERR_UNSUPPORTED;
+  // every size check is above this line: a refused request queues nothing
   unsigned char* base = nullptr;
   const cuflye_status st = scratch_address(&base);
   if (st != CUFLYE_OK) return st;
@@ -125,7 +132,6 @@ extern "C" cuflye_status cuflye_std_sort_segments_noalloc(uint64_t* keys, uint32
                   static_cast<uint32_t>(kTaskCap), segsort_pair_reserve(n_elements),
                   n_elements, {base + kOffR0, base + kOffR1},
                   reinterpret_cast<uint32_t*>(base + kOffRc)};
-  if (segsort_round_bytes(n_elements) > kRoundBytes) return CUFLYE_ERR_INVALID;
   // segmented_std_sort clears its counters (the task count included) itself
   const cudaError_t e = segmented_std_sort(
       keys, values, reinterpret_cast<uint32_t*>(base + kOffL),

@@ -1259,17 +1259,22 @@ cudaError_t segmented_std_sort(uint64_t* keys, uint32_t* vals, uint32_t* lscratc
                                uint32_t nseg, const uint32_t* nseg_dev, uint32_t* lists,
                                uint32_t* counts, int num_sms, cudaStream_t stream,
                                SortTasks tasks) {
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(sort_cta, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         static_cast<int>(sizeof(CtaSmem)));
-    cudaFuncSetAttribute(sort_tasks, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         static_cast<int>(sizeof(CtaSmem)));
-    cudaFuncSetAttribute(sort_warp, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         static_cast<int>(sizeof(WarpSlice) * kWarpSegWarps));
-    cudaFuncSetAttribute(sort_heaps, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         static_cast<int>(kHeapSmem));
-    attr = true;
+  // The shared-memory limits are attributes of the current device: set them
+  // on every call (cheap), so a later call on another device, or from
+  // another host thread, finds them set too.
+  {
+    cudaError_t e = cudaFuncSetAttribute(sort_cta, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(sizeof(CtaSmem)));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(sort_tasks, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               static_cast<int>(sizeof(CtaSmem)));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(sort_warp, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               static_cast<int>(sizeof(WarpSlice) * kWarpSegWarps));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(sort_heaps, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               static_cast<int>(kHeapSmem));
+    if (e != cudaSuccess) return e;
   }
   if (nseg == 0) return cudaSuccess;
   cudaMemsetAsync(counts, 0, 9 * sizeof(uint32_t), stream);

@@ -101,6 +101,8 @@ class ReadSet:
     ids: np.ndarray  # int64 signed ids
     offsets: np.ndarray  # int64, n+1
     bases: np.ndarray  # uint8 ASCII, concatenated
+    # genome start of each read when it was sampled from a genome (else None)
+    origin: np.ndarray | None = None
 
     @property
     def n(self) -> int:
@@ -120,7 +122,8 @@ class ReadSet:
         offs = np.zeros(len(idx) + 1, dtype=np.int64)
         offs[1:] = np.cumsum(lens)
         return ReadSet(self.ids[idx].copy(), offs,
-                       np.concatenate(parts) if parts else np.zeros(0, np.uint8))
+                       np.concatenate(parts) if parts else np.zeros(0, np.uint8),
+                       None if self.origin is None else self.origin[idx].copy())
 
     @classmethod
     def from_strings(cls, ids, seqs) -> "ReadSet":
@@ -159,7 +162,8 @@ def sample_reads(rng, genome: np.ndarray, coverage: float, lengths_fn, sub, ins,
         seqs.append(err(rng, s, sub, ins, dele))
     offs = np.zeros(n + 1, dtype=np.int64)
     offs[1:] = np.cumsum([len(s) for s in seqs])
-    return ReadSet(np.arange(1, n + 1, dtype=np.int64), offs, np.concatenate(seqs))
+    return ReadSet(np.arange(1, n + 1, dtype=np.int64), offs, np.concatenate(seqs),
+                   np.asarray(starts, dtype=np.int64))
 
 
 @dataclass

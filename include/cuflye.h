@@ -67,6 +67,14 @@ cuflye_status cuflye_open(int device, uint64_t memory_budget_bytes, cuflye_ctx**
 cuflye_status cuflye_open_from_env(cuflye_ctx** out);
 
 void cuflye_close(cuflye_ctx* ctx);
+
+/* The last failure's one-line message.  With ctx == NULL: why the calling
+ * thread's last cuflye_open / cuflye_open_from_env failed (empty after a
+ * success).  Unsupported shapes, budget failures and failed opens carry the
+ * reference stub's fields first ("cuFlye CUDA candidate backend selected;
+ * adapter=cuflye_gb300; CUFLYE_CUDA_DEVICE=<d>;
+ * CUFLYE_CUDA_MEMORY_BUDGET_BYTES=<b>; <reason>"), as
+ * patches/flye/2.9.6/0003-cuflye-cuda-backend-stub.patch:37-46 throws them. */
 const char* cuflye_last_error(const cuflye_ctx* ctx);
 
 /* Device memory the context holds now and at its peak, in bytes. */
@@ -278,18 +286,23 @@ cuflye_status cuflye_std_sort_segments(cuflye_ctx* ctx, uint64_t* keys, uint32_t
  *
  * keys / values: the caller's DEVICE arrays, sorted in place.
  * seg_offsets:   HOST array of n_segments + 1 offsets into them, all within
- *                [0, n_elements].
- * stream:        a cudaStream_t (NULL = default stream); the call returns
- *                once the work is queued.
+ *                [0, n_elements]; elements past seg_offsets[n_segments]
+ *                are left untouched.
+ * stream:        a cudaStream_t (NULL = default stream).  With n_elements
+ *                <= 4,096 the call returns once the work is queued.  With
+ *                more, the sort reads its round counts back to the host
+ *                between rounds of its large-segment phase, so the call
+ *                waits on `stream` and returns after the work is done.
  * Needs no context and makes no cudaMalloc / cudaFree or other allocating
  * call: its scratch is one fixed device array of about 13.6 MiB that every
  * GPU loading the library holds until exit.  Limits: n_elements <=
  * CUFLYE_NOALLOC_MAX_ELEMENTS, n_segments <= CUFLYE_NOALLOC_MAX_SEGMENTS
- * (larger requests return CUFLYE_ERR_UNSUPPORTED without doing anything).
- * The first call on each device looks up that array's device address (with
- * that device current); make that first call before any stream capture.
- * Calls share the array: calls whose work overlaps on the GPU race and must
- * not be issued.
+ * (larger requests return CUFLYE_ERR_UNSUPPORTED before anything is
+ * queued).  The first call on each device looks up that array's device
+ * address (with that device current) and caches it for the life of the
+ * process (not valid across a cudaDeviceReset); make that first call before
+ * any stream capture.  Calls share the array: calls whose work overlaps on
+ * the GPU race and must not be issued.
  * ------------------------------------------------------------------------ */
 #define CUFLYE_NOALLOC_MAX_ELEMENTS 1048576u
 #define CUFLYE_NOALLOC_MAX_SEGMENTS 65536u

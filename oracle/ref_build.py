@@ -16,19 +16,24 @@ the CPU path never launches), into ``oracle/_ref/``, which is not committed.
 Only the CPU tests run them, to check the oracle; the library never does.
 A machine without the reference checkout skips the build and those tests.
 
+The checkout is taken from ``--reference``, else from the
+``CUFLYE_REFERENCE`` environment variable, else from the one place this
+build environment mounts it (``DEFAULT_REFERENCE``).
+
 Usage: python oracle/ref_build.py [--reference DIR]
 """
 
 from __future__ import annotations
 
 import argparse
+import os
 import shutil
 import subprocess
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref"
-DEFAULT_REFERENCE = Path("/root/reference")
+DEFAULT_REFERENCE = Path(os.environ.get("CUFLYE_REFERENCE") or "/root/reference")
 
 # output name -> source file under the reference's cuda/ directory
 PROGRAMS = {

@@ -1,7 +1,8 @@
 #!/usr/bin/env python3
 """Generate the committed golden vectors that pin the CPU oracle.
 
-Run where the reference checkout is present (default ``/root/reference``);
+Run where the reference checkout is present (``--reference DIR`` or the
+``CUFLYE_REFERENCE`` environment variable);
 the tests never run this script, they only read the fixtures it writes.
 For each seeded synthetic case it:
 
@@ -17,7 +18,7 @@ For each seeded synthetic case it:
    ``tests/golden/synthetic/<case>/``;
 4. asserts the oracle reproduces both outputs.
 
-Usage: python tests/golden/make_golden.py [--reference /root/reference]
+Usage: python tests/golden/make_golden.py [--reference DIR]
 """
 
 from __future__ import annotations
@@ -25,6 +26,7 @@ from __future__ import annotations
 import argparse
 import hashlib
 import json
+import os
 import sys
 from pathlib import Path
 
@@ -59,7 +61,9 @@ def write_reads(path: Path, reads: synth.ReadSet) -> None:
 
 def main() -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("CUFLYE_REFERENCE"),
+                    required=not os.environ.get("CUFLYE_REFERENCE"),
+                    help="the reference checkout (default: $CUFLYE_REFERENCE)")
     args = ap.parse_args()
     sys.path.insert(0, str(Path(args.reference) / "tools"))
     import replay_overlap_chains as ROC  # type: ignore

@@ -2,10 +2,11 @@
 """Generate the committed fixture of libstdc++ std::sort tie orders as the
 reference restates them in Python (``cpp_sort_in_place`` in
 ``tools/replay_read_to_graph_source_pack.py``), for seeded key sets with
-heavy ties.  Run in a container that has the reference checkout (default
-``/root/reference``); the tests only read ``sort_ties.json``.
+heavy ties.  Run where the reference checkout is present (``--reference
+DIR`` or the ``CUFLYE_REFERENCE`` environment variable); the tests only read
+``sort_ties.json``.
 
-Usage: python tests/golden/make_sort_ties.py [--reference /root/reference]
+Usage: python tests/golden/make_sort_ties.py [--reference DIR]
 """
 
 from __future__ import annotations
@@ -13,6 +14,7 @@ from __future__ import annotations
 import argparse
 import importlib.util
 import json
+import os
 import sys
 from pathlib import Path
 
@@ -24,7 +26,9 @@ SIZES = (3, 17, 40, 300, 2000)
 
 def main() -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("CUFLYE_REFERENCE"),
+                    required=not os.environ.get("CUFLYE_REFERENCE"),
+                    help="the reference checkout (default: $CUFLYE_REFERENCE)")
     args = ap.parse_args()
     tool = Path(args.reference) / "tools" / "replay_read_to_graph_source_pack.py"
     sys.path.insert(0, str(tool.parent))

@@ -172,3 +172,36 @@ def test_synthetic_generator_is_seeded():
     b = synth.small_overlap_case(3, 20_000, 3.0, 3_000)
     assert np.array_equal(a.reads.bases, b.reads.bases)
     assert np.array_equal(a.reads.offsets, b.reads.offsets)
+
+
+def _open_from_env_in_subprocess(device, budget):
+    env = dict(os.environ)
+    env["CUFLYE_CUDA_DEVICE"] = device
+    env["CUFLYE_CUDA_MEMORY_BUDGET_BYTES"] = budget
+    code = ("import sys, ctypes; sys.path.insert(0, %r)\n"
+            "from cuflye_gb300 import backend\n"
+            "L = backend.load_library()\n"
+            "h = ctypes.c_void_p()\n"
+            "st = L.cuflye_open_from_env(ctypes.byref(h))\n"
+            "print(st, h.value is None)\n"
+            "print(L.cuflye_last_error(None).decode())\n") % str(REPO)
+    return subprocess.run([sys.executable, "-c", code], env=env, capture_output=True,
+                          text=True, check=True).stdout.splitlines()
+
+
+@pytest.mark.parametrize("device,budget,reason", [
+    ("gpu0", "unbounded", "CUFLYE_CUDA_DEVICE is not a device ordinal"),
+    ("0", "40GB", "CUFLYE_CUDA_MEMORY_BUDGET_BYTES is neither"),
+    ("-1", "1000", "CUFLYE_CUDA_DEVICE is not a device ordinal"),
+])
+def test_open_from_env_failure_keeps_the_stub_fields(built_lib, device, budget, reason):
+    """An unparsable device or budget fails before any CUDA call, with a
+    message kept for the thread (cuflye_last_error(NULL)) that starts with
+    the reference stub's fields
+    (patches/flye/2.9.6/0003-cuflye-cuda-backend-stub.patch:37-46)."""
+    status, msg = _open_from_env_in_subprocess(device, budget)
+    assert status == "1 True"  # CUFLYE_ERR_INVALID, no context
+    assert msg.startswith("cuFlye CUDA candidate backend selected; adapter=cuflye_gb300; "
+                          f"CUFLYE_CUDA_DEVICE={device}; "
+                          f"CUFLYE_CUDA_MEMORY_BUDGET_BYTES={budget}; ")
+    assert reason in msg

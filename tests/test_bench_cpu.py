@@ -31,3 +31,7 @@ def test_reference_arm_prints_the_contract_line():
     e2e = line["e2e"]
     assert e2e["value"] == line["value"] and e2e["unit"] == line["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+    # both arms describe the workload with the same config object
+    import argparse
+    args = argparse.Namespace(seed=2, genome_len=200000, coverage=5.0)
+    assert line["config"] == json.loads(json.dumps(bench.bench_config(bench.make_workload(args))))

@@ -63,6 +63,51 @@ def test_noalloc_sort_matches_std_sort_entry_point_twice(built_lib):
             assert np.array_equal(got_v, exp_v)
 
 
+def _oracle_sort(oracle_mod, keys, vals, offs):
+    """libstdc++ std::sort by key of each segment (the oracle), elements past
+    the last offset untouched."""
+    k, v = keys.copy(), vals.copy()
+    for a, b in zip(offs[:-1].astype(np.int64), offs[1:].astype(np.int64)):
+        if b > a:
+            k[a:b], v[a:b] = oracle_mod.std_sort_u64(k[a:b], v[a:b])
+    return k, v
+
+
+def test_noalloc_sort_matches_libstdcxx_on_partial_ranges_and_mixed_sizes(built_lib,
+                                                                          oracle_mod):
+    """Against std::sort itself: empty segments, elements after the last
+    segment that must stay as they are, and a large call followed by a small
+    one and a large one again (the shared scratch keeps the previous call's
+    contents)."""
+    pytest.importorskip("torch")
+    fn = _lib()
+    rng = np.random.default_rng(7)
+    cases = []
+    # large: segments past 4,096 elements take the round-based phase
+    sizes = rng.integers(0, 40000, size=40)
+    sizes[::5] = 0
+    offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint64)
+    n = int(offs[-1]) + 5000  # 5,000 trailing elements outside every segment
+    cases.append((rng.integers(0, 300, size=n, dtype=np.uint64),
+                  rng.integers(0, 1 << 31, size=n, dtype=np.uint32), offs))
+    # small: every segment within one block
+    sizes = rng.integers(0, 60, size=500)
+    offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint64)
+    n = int(offs[-1]) + 17
+    cases.append((rng.integers(0, 8, size=n, dtype=np.uint64),
+                  rng.integers(0, 1 << 31, size=n, dtype=np.uint32), offs))
+    cases.append(cases[0])
+    for keys, vals, offs in cases:
+        assert len(keys) <= MAX_ELEMENTS
+        got_k, got_v = _noalloc_sort(fn, keys, vals, offs)
+        exp_k, exp_v = _oracle_sort(oracle_mod, keys, vals, offs)
+        assert np.array_equal(got_k, exp_k)
+        assert np.array_equal(got_v, exp_v)
+        tail = int(offs[-1])
+        assert np.array_equal(got_k[tail:], keys[tail:])
+        assert np.array_equal(got_v[tail:], vals[tail:])
+
+
 def test_noalloc_rejects_oversized_requests(built_lib):
     pytest.importorskip("torch")
     fn = _lib()
