@@ -149,6 +149,8 @@ def load_library(path: Path | None = None) -> ctypes.CDLL:
     L.cuflye_last_sort_stats.argtypes = [_vp, _u64p, ctypes.c_size_t]
     L.cuflye_last_passes.restype = S
     L.cuflye_last_passes.argtypes = [_vp, _u64p]
+    L.cuflye_set_sorted_emission.restype = S
+    L.cuflye_set_sorted_emission.argtypes = [_vp, ctypes.c_int]
     L.cuflye_set_launch_shape.restype = S
     L.cuflye_set_launch_shape.argtypes = [_vp, ctypes.POINTER(LaunchShape)]
     L.cuflye_get_launch_shape.restype = S
@@ -276,13 +278,17 @@ class CudaBackend:
         return list(ms), list(by)
 
     SORT_STATS = ("match_plain", "match_libstdcxx", "ext_plain", "ext_libstdcxx", "score_plain",
-                  "score_libstdcxx", "backtrack_redo")
+                  "score_libstdcxx", "backtrack_redo", "emission_fallbacks")
 
     def last_sort_stats(self) -> dict:
         """How the last overlaps / read-to-graph call's sort points ran (segments per path)."""
-        v = (ctypes.c_uint64 * 7)()
-        self._check(self._L.cuflye_last_sort_stats(self._h, v, 7))
+        v = (ctypes.c_uint64 * 8)()
+        self._check(self._L.cuflye_last_sort_stats(self._h, v, 8))
         return dict(zip(self.SORT_STATS, list(v)))
+
+    def set_sorted_emission(self, enable: bool) -> None:
+        """Hits straight into KmerMatch order (default) or emit + sort."""
+        self._check(self._L.cuflye_set_sorted_emission(self._h, int(bool(enable))))
 
     def last_passes(self) -> int:
         """Passes (runs of queries through the device) of the last call."""

@@ -23,7 +23,7 @@ LIB = OUT / "libcuflye_gb300.so"
 TABLE = OUT / "logf_exceptions.bin"
 
 SOURCES = ["api.cu", "sort.cu", "radix.cu", "util.cu", "index.cu", "hits.cu", "chain.cu", "r2g.cu",
-           "abi.cu", "noalloc.cu", "fastsort.cu"]
+           "abi.cu", "noalloc.cu", "fastsort.cu", "match_emit.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
          "-ffp-contract=off", "--expt-relaxed-constexpr"]

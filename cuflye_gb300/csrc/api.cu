@@ -83,12 +83,16 @@ struct cuflye_ctx {
   cudaEvent_t ev[8]{};
   double stage_ms[7]{};
   uint64_t stage_bytes[7]{};
-  uint64_t sort_stats[7]{};  // see cuflye_last_sort_stats
+  uint64_t sort_stats[8]{};  // see cuflye_last_sort_stats ([7]: emission fallbacks)
+  // hits of the last call by path, for the stages' algorithmic bytes
+  uint64_t hits_sorted_emission = 0, hits_flagged = 0, hits_prefiltered = 0, hits_emit_sort = 0;
   uint64_t passes = 0;       // see cuflye_last_passes
   uint64_t build_window_cap = 0;  // see cuflye_set_index_build_windows
   cuflye_launch_shape shape{0, 0, 0, 0};  // see cuflye_set_launch_shape (0: defaults)
   uint64_t build_ranges = 0;      // key ranges of the last index build
   int servers = 0;           // open serving loops borrowing this index
+  bool sorted_emission = true;  // see cuflye_set_sorted_emission
+  uint64_t emission_fallbacks = 0;  // passes of the last call that fell back to emit + sort
 };
 
 namespace {
@@ -160,6 +164,9 @@ void check_device_status(cuflye_ctx* c) {
                   "unsupported shape: divergence argument outside [1, 2^24)");
     case kDevTableFull:
       throw Error(CUFLYE_ERR_CUDA, "k-mer table insertion failed (table full)");
+    case kDevMatchDict:
+      throw Error(CUFLYE_ERR_CUDA, "sorted emission: a hit outside its query's dictionary "
+                                   "(detail " + std::to_string(st.detail) + ")");
     default:
       throw Error(CUFLYE_ERR_CUDA, "device status " + std::to_string(st.code));
   }
@@ -692,6 +699,15 @@ struct PassState {
   uint64_t* f_off = nullptr;  // nq + 1 filtered offsets
   QueryInfo* qinfo = nullptr;
   uint32_t* q_tie = nullptr;  // per query: its KmerMatch keys may repeat
+  // false: the hits are not yet written (the sorted emission writes them
+  // straight into KmerMatch order); the window tables below feed it
+  bool emitted = true;
+  QueryBatch qb;
+  const uint64_t* hit_off = nullptr;
+  const uint64_t* filt_off = nullptr;
+  const uint64_t* wmeta = nullptr;
+  const uint8_t* wflags = nullptr;
+  const uint32_t* wself = nullptr;
 };
 
 // Buffers sized by the hit count of a pass (reused by the next pass).
@@ -701,16 +717,23 @@ const char* const kPerHitBuffers[] = {"h_keys",  "h_vals",   "h_kmers", "s_l",  
                                       "g_toff"};
 
 
+// The pass's hits in Flye's generation order (and the filtered positions).
+void emit_generation_order(cuflye_ctx* c, PassState& ps) {
+  CUFLYE_CHECK(hits_emit(c->idx, ps.qb, ps.hit_off, ps.filt_off, ps.wmeta, ps.wflags, ps.keys,
+                         ps.vals, ps.kmers, ps.fpos, c->stream));
+  ps.emitted = true;
+}
+
 // Upload a run of queries starting at q0 and produce the hits of the longest
 // prefix of them that fits in device memory (ps.nq queries), in Flye's
 // generation order.
 // Device bytes per query window of a pass's run: bases (1), packed words
 // (0.25), hit and filter counts (8), window metadata (8) and flags (1), the
 // two offset arrays (16), rounded up.
-constexpr uint64_t kRunBytesPerWindow = 36;
+constexpr uint64_t kRunBytesPerWindow = 40;
 // Buffers sized by the windows of a pass's run (reused by the next pass).
 const char* const kPerWindowBuffers[] = {"q_ascii", "q_words",  "w_cnt",     "w_filt", "w_meta",
-                                         "w_flags", "w_hitoff", "w_filtoff", "w_scan"};
+                                         "w_flags", "w_hitoff", "w_filtoff", "w_scan", "w_self"};
 
 // The end of the run of queries from q0 (at most q1) whose windows' buffers
 // take at most a quarter of the memory the budget leaves; the rest is for
@@ -746,6 +769,12 @@ size_t run_end(cuflye_ctx* c, const Queries& Q, size_t q0, size_t q1, uint64_t b
     ++q;
   }
   return q;
+}
+
+// Whether a pass's hits go straight into KmerMatch order (match_emit.cu):
+// overlap and read-to-graph calls on a built index, unless switched off.
+bool sorted_emission(const cuflye_ctx* c, bool want_kmers) {
+  return !want_kmers && c->idx.transform && c->sorted_emission;
 }
 
 bool run_hits(cuflye_ctx* c, const Queries& Q, size_t q0, size_t q1, bool want_kmers,
@@ -805,7 +834,9 @@ bool run_hits(cuflye_ctx* c, const Queries& Q, size_t q0, size_t q1, bool want_k
   uint8_t* wflags = buf<uint8_t>(c, "w_flags", nwin);
   ps.q_tie = buf<uint32_t>(c, "q_tie", nq);
   CUFLYE_CHECK(cudaMemsetAsync(ps.q_tie, 0, std::max<uint64_t>(nq, 1) * 4ull, st));
-  CUFLYE_CHECK(hits_count(c->idx, qb, cnt, filt, wmeta, wflags, ps.q_tie, st));
+  const bool fused = sorted_emission(c, want_kmers);
+  uint32_t* wself = fused ? buf<uint32_t>(c, "w_self", nwin) : nullptr;
+  CUFLYE_CHECK(hits_count(c->idx, qb, cnt, filt, wmeta, wflags, ps.q_tie, wself, st));
   uint64_t* hit_off = buf<uint64_t>(c, "w_hitoff", nwin + 1);
   uint64_t* filt_off = buf<uint64_t>(c, "w_filtoff", nwin + 1);
   ps.nhits = scan_u32(c, cnt, hit_off, nwin, "w_scan");
@@ -866,8 +897,14 @@ bool run_hits(cuflye_ctx* c, const Queries& Q, size_t q0, size_t q1, bool want_k
   ps.vals = buf<uint32_t>(c, "h_vals", ps.nhits);
   ps.kmers = want_kmers ? buf<uint64_t>(c, "h_kmers", ps.nhits) : nullptr;
   ps.fpos = buf<int32_t>(c, "h_fpos", ps.nfilt);
-  CUFLYE_CHECK(hits_emit(c->idx, qb, hit_off, filt_off, wmeta, wflags, ps.keys, ps.vals, ps.kmers,
-                         ps.fpos, st));
+  ps.qb = qb;
+  ps.hit_off = hit_off;
+  ps.filt_off = filt_off;
+  ps.wmeta = wmeta;
+  ps.wflags = wflags;
+  ps.wself = wself;
+  ps.emitted = !fused;
+  if (!fused) emit_generation_order(c, ps);
   return true;
 }
 
@@ -920,46 +957,115 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp,
   uint32_t* ecount = buf<uint32_t>(c, "s_ecount", 1);
   uint64_t* sstats = buf<uint64_t>(c, "x_sortstats", kSortStats);
   CUFLYE_CHECK(cudaMemsetAsync(sstats, 0, kSortStats * 8, st));
-  // 1. KmerMatch sort per query by (ext id, cur pos) in libstdc++ order:
-  // queries whose keys are distinct by a radix sort on the ext id, the others
-  // by the emulated introsort
   uint64_t* qb = buf<uint64_t>(c, "s_qb", nq);
   uint64_t* qe = buf<uint64_t>(c, "s_qe", nq);
-  uint32_t* ntiles = buf<uint32_t>(c, "m_ntiles", nq);
-  uint64_t* tile_off = buf<uint64_t>(c, "m_tileoff", nq + 1);
-  // second buffer of the radix passes; later the exact score orders
+  // second buffer of the radix passes (or the sorted emission's dictionary);
+  // later the exact score orders
   uint64_t* alt_keys = buf<uint64_t>(c, "c_akeys", H + 1);
   uint32_t* alt_vals = buf<uint32_t>(c, "c_avals", H + 1);
-  int id_bits = 0;
-  while (id_bits < 32 && ((2ull * c->idx.nslots - 1) >> id_bits) != 0) ++id_bits;
-  CUFLYE_CHECK(cudaEventRecord(c->ev[1], st));
-  CUFLYE_CHECK(match_plan(ps.q_off, ps.q_tie, nq, ntiles, qb, qe, ecount, st));
-  CUFLYE_CHECK(sort_stats_add(sstats, 0, 1, nullptr, nq, ecount, st));
-  const uint64_t NT = scan_u32(c, ntiles, tile_off, nq, "m_scan");
-  MatchTile* tiles = buf<MatchTile>(c, "m_tiles", NT);
-  uint32_t* mcounts = buf<uint32_t>(c, "m_counts", 256 * NT);
-  CUFLYE_CHECK(match_tiles(ps.q_off, ntiles, tile_off, nq, tiles, st));
-  CUFLYE_CHECK(match_radix(ps.keys, ps.vals, alt_keys, alt_vals, tiles,
-                           static_cast<uint32_t>(NT), ps.q_off, ntiles, tile_off, nq, id_bits,
-                           mcounts, c->num_sms, c->shape.scatter_blocks_per_sm, st));
-  CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, qb, qe, nq, ecount, lists,
-                                  scounts, c->num_sms, st, sort_tasks(c, "s", H, nq)));
-  CUFLYE_CHECK(cudaEventRecord(c->ev[2], st));
-  // 2. groups: runs of one ext id within a query
-  const uint64_t gtiles = (H + kGroupTile - 1) / kGroupTile;
-  uint32_t* gtcount = buf<uint32_t>(c, "g_tcount", gtiles);
-  uint64_t* gtoff = buf<uint64_t>(c, "g_toff", gtiles + 1);
-  CUFLYE_CHECK(groups_count(ps.keys, ps.q_off, nq, H, gtcount, st));
-  const uint64_t G = scan_u32(c, gtcount, gtoff, gtiles, "g_scan");
-  if (G >= (1ull << 32)) throw Error(CUFLYE_ERR_UNSUPPORTED, "more than 2^32 target groups");
-  GroupInfo* groups = buf<GroupInfo>(c, "g_info", G);
-  CUFLYE_CHECK(groups_write(ps.keys, ps.q_off, nq, H, gtoff, groups, st));
-  uint32_t* ext_list = buf<uint32_t>(c, "g_extlist", G);
-  uint32_t* dp_list = buf<uint32_t>(c, "g_dplist", G);
-  uint32_t* gcounts = buf<uint32_t>(c, "g_counts", 4);
   const int* slot_len = c->idx.slot_len;
-  CUFLYE_CHECK(groups_prefilter_n(ps.keys, ps.vals, groups, G, H, ps.qinfo, slot_len, cp,
-                                  ext_list, dp_list, gcounts, st));
+  GroupInfo* groups = nullptr;
+  uint64_t G = 0;
+  uint32_t* ext_list = nullptr;
+  uint32_t* dp_list = nullptr;
+  uint32_t* gcounts = buf<uint32_t>(c, "g_counts", 4);
+  bool fused = !ps.emitted;
+  if (fused) {
+    // Sorted emission: each query's dictionary of ext ids, then its hits
+    // written in KmerMatch order with their groups; flagged queries'
+    // hits in generation order for the libstdc++-order sort.
+    MatchEmitArgs a;
+    a.idx = c->idx;
+    a.win_off = ps.qb.win_off;
+    a.q_off = ps.q_off;
+    a.hit_off = ps.hit_off;
+    a.wmeta = ps.wmeta;
+    a.wflags = ps.wflags;
+    a.wself = ps.wself;
+    a.filt_off = ps.filt_off;
+    a.fpos = ps.fpos;
+    a.status = c->status;
+    a.nq = nq;
+    uint32_t* q_ng = buf<uint32_t>(c, "m_qng", nq);
+    uint64_t* q_dbase = buf<uint64_t>(c, "m_qdbase", nq);
+    uint64_t* q_goff = buf<uint64_t>(c, "m_qgoff", nq + 1);
+    uint32_t* mwords = buf<uint32_t>(c, "m_words", 4);  // overflow, counter
+    unsigned long long* dcur = buf<unsigned long long>(c, "m_dcur", 3);  // cursor, tallies
+    CUFLYE_CHECK(cudaMemsetAsync(mwords, 0, 4 * sizeof(uint32_t), st));
+    CUFLYE_CHECK(cudaMemsetAsync(dcur, 0, 3 * sizeof(unsigned long long), st));
+    CUFLYE_CHECK(match_dict(a, alt_keys, dcur, q_ng, q_dbase, mwords, mwords + 1, c->num_sms, st));
+    G = scan_u32(c, q_ng, q_goff, nq, "m_scan");
+    if (read_scalar(c, mwords) != 0) {
+      // a query with more than kMatchDictCap ext ids: this pass takes the
+      // generation-order emission and the sort instead
+      ++c->emission_fallbacks;
+      emit_generation_order(c, ps);
+      fused = false;
+    } else {
+      if (G >= (1ull << 32)) throw Error(CUFLYE_ERR_UNSUPPORTED, "more than 2^32 target groups");
+      groups = buf<GroupInfo>(c, "g_info", G);
+      ext_list = buf<uint32_t>(c, "g_extlist", G);
+      dp_list = buf<uint32_t>(c, "g_dplist", G);
+      uint32_t* pf_list = buf<uint32_t>(c, "g_pflist", G);
+      CUFLYE_CHECK(cudaMemsetAsync(gcounts, 0, 4 * sizeof(uint32_t), st));
+      CUFLYE_CHECK(cudaMemsetAsync(ecount, 0, sizeof(uint32_t), st));
+      MatchEmitLists L{dp_list, pf_list, gcounts, qb, qe, ecount, dcur + 1};
+      CUFLYE_CHECK(match_emit(a, alt_keys, q_ng, q_dbase, q_goff, ps.q_tie, ps.qinfo, cp, ps.keys,
+                              ps.vals, groups, L, mwords + 1, c->num_sms, st));
+      CUFLYE_CHECK(cudaEventRecord(c->ev[1], st));
+      // 1. the flagged queries' KmerMatch sort in libstdc++ order
+      CUFLYE_CHECK(sort_stats_add(sstats, 0, 1, nullptr, nq, ecount, st));
+      CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, qb, qe, nq, ecount, lists,
+                                      scounts, c->num_sms, st, sort_tasks(c, "s", H, nq)));
+      CUFLYE_CHECK(cudaEventRecord(c->ev[2], st));
+      // 2. the prefilter of the groups the emission left open
+      CUFLYE_CHECK(groups_prefilter_list(ps.keys, ps.vals, groups, pf_list, ps.qinfo, slot_len, cp,
+                                         ext_list, dp_list, gcounts, static_cast<uint32_t>(G),
+                                         st));
+      unsigned long long tally[2];
+      CUFLYE_CHECK(cudaMemcpyAsync(tally, dcur + 1, sizeof(tally), cudaMemcpyDeviceToHost, st));
+      sync(c);
+      c->hits_flagged += tally[0];
+      c->hits_prefiltered += tally[1];
+      c->hits_sorted_emission += H;
+    }
+  }
+  if (!fused) {
+    // 1. KmerMatch sort per query by (ext id, cur pos) in libstdc++ order:
+    // queries whose keys are distinct by a radix sort on the ext id, the
+    // others by the emulated introsort
+    uint32_t* ntiles = buf<uint32_t>(c, "m_ntiles", nq);
+    uint64_t* tile_off = buf<uint64_t>(c, "m_tileoff", nq + 1);
+    int id_bits = 0;
+    while (id_bits < 32 && ((2ull * c->idx.nslots - 1) >> id_bits) != 0) ++id_bits;
+    CUFLYE_CHECK(cudaEventRecord(c->ev[1], st));
+    CUFLYE_CHECK(match_plan(ps.q_off, ps.q_tie, nq, ntiles, qb, qe, ecount, st));
+    CUFLYE_CHECK(sort_stats_add(sstats, 0, 1, nullptr, nq, ecount, st));
+    const uint64_t NT = scan_u32(c, ntiles, tile_off, nq, "m_scan");
+    MatchTile* tiles = buf<MatchTile>(c, "m_tiles", NT);
+    uint32_t* mcounts = buf<uint32_t>(c, "m_counts", 256 * NT);
+    CUFLYE_CHECK(match_tiles(ps.q_off, ntiles, tile_off, nq, tiles, st));
+    CUFLYE_CHECK(match_radix(ps.keys, ps.vals, alt_keys, alt_vals, tiles,
+                             static_cast<uint32_t>(NT), ps.q_off, ntiles, tile_off, nq, id_bits,
+                             mcounts, c->num_sms, c->shape.scatter_blocks_per_sm, st));
+    CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, qb, qe, nq, ecount, lists,
+                                    scounts, c->num_sms, st, sort_tasks(c, "s", H, nq)));
+    CUFLYE_CHECK(cudaEventRecord(c->ev[2], st));
+    // 2. groups: runs of one ext id within a query
+    const uint64_t gtiles = (H + kGroupTile - 1) / kGroupTile;
+    uint32_t* gtcount = buf<uint32_t>(c, "g_tcount", gtiles);
+    uint64_t* gtoff = buf<uint64_t>(c, "g_toff", gtiles + 1);
+    CUFLYE_CHECK(groups_count(ps.keys, ps.q_off, nq, H, gtcount, st));
+    G = scan_u32(c, gtcount, gtoff, gtiles, "g_scan");
+    if (G >= (1ull << 32)) throw Error(CUFLYE_ERR_UNSUPPORTED, "more than 2^32 target groups");
+    groups = buf<GroupInfo>(c, "g_info", G);
+    CUFLYE_CHECK(groups_write(ps.keys, ps.q_off, nq, H, gtoff, groups, st));
+    ext_list = buf<uint32_t>(c, "g_extlist", G);
+    dp_list = buf<uint32_t>(c, "g_dplist", G);
+    CUFLYE_CHECK(groups_prefilter_n(ps.keys, ps.vals, groups, G, H, ps.qinfo, slot_len, cp,
+                                    ext_list, dp_list, gcounts, st));
+    c->hits_emit_sort += H;
+  }
   uint64_t* sb = buf<uint64_t>(c, "g_sb", G);
   uint64_t* se = buf<uint64_t>(c, "g_se", G);
   uint32_t* glists = buf<uint32_t>(c, "g_lists", 4 * std::max<uint64_t>(G, 1));
@@ -1062,6 +1168,9 @@ float elapsed(cudaEvent_t a, cudaEvent_t b) {
 
 void reset_timing(cuflye_ctx* c) {
   c->passes = 0;
+  c->emission_fallbacks = 0;
+  c->sort_stats[7] = 0;
+  c->hits_sorted_emission = c->hits_flagged = c->hits_prefiltered = c->hits_emit_sort = 0;
   for (int i = 0; i < kStages; ++i) {
     c->stage_ms[i] = 0;
     c->stage_bytes[i] = 0;
@@ -1078,6 +1187,7 @@ void accumulate_timing(cuflye_ctx* c, bool chained) {
     CUFLYE_CHECK(cudaMemcpy(st, buf<uint64_t>(c, "x_sortstats", kSortStats), sizeof(st),
                             cudaMemcpyDeviceToHost));
     for (int i = 0; i < kSortStats; ++i) c->sort_stats[i] += st[i];
+    c->sort_stats[7] = c->emission_fallbacks;
   }
   c->stage_ms[6] += elapsed(c->ev[0], c->ev[5]);
   c->stage_ms[0] += elapsed(c->ev[5], c->ev[1]);
@@ -1088,6 +1198,22 @@ void accumulate_timing(cuflye_ctx* c, bool chained) {
     c->stage_ms[4] += elapsed(c->ev[7], c->ev[3]);
     c->stage_ms[5] += elapsed(c->ev[3], c->ev[4]);
   }
+}
+
+// Compulsory traffic per stage: the bases and one probe sector per window,
+// bucket entries read (8 B) and hit records written (12 B); a read and a
+// write of every 12-byte record the KmerMatch sort moves (all hits on the
+// emit + sort path, the flagged queries' hits on the sorted emission); the
+// group stage reads the records of the groups it prefilters (12 B each, and
+// on the emit + sort path another 8 B for the group bounds and ext
+// positions); the DP reads (cur, ext) and writes (score, backtrack); the
+// backtrack reads its table once.
+void set_stage_bytes(cuflye_ctx* c, uint64_t bases, uint64_t windows, uint64_t hits) {
+  c->stage_bytes[0] = bases / 4 + windows * 32 + hits * 20;
+  c->stage_bytes[1] = (c->hits_emit_sort + c->hits_flagged) * 24;
+  c->stage_bytes[2] = c->hits_emit_sort * 20 + c->hits_prefiltered * 12;
+  c->stage_bytes[3] = hits * 16;
+  c->stage_bytes[4] = hits * 4;
 }
 
 size_t pass_size(cuflye_ctx* c, size_t n) {
@@ -1335,6 +1461,13 @@ cuflye_status cuflye_set_batch_queries(cuflye_ctx* c, size_t q) {
   return CUFLYE_OK;
 }
 
+cuflye_status cuflye_set_sorted_emission(cuflye_ctx* c, int enable) {
+  if (!c || (enable != 0 && enable != 1)) return CUFLYE_ERR_INVALID;
+  std::lock_guard<std::mutex> lock(c->mu);
+  c->sorted_emission = enable != 0;
+  return CUFLYE_OK;
+}
+
 cuflye_status cuflye_set_launch_shape(cuflye_ctx* c, const cuflye_launch_shape* s) {
   if (!c || !s) return CUFLYE_ERR_INVALID;
   if (s->dp_blocks_per_sm < 0 || s->dp_blocks_per_sm > 8 || s->backtrack_blocks_per_sm < 0 ||
@@ -1498,18 +1631,7 @@ cuflye_status cuflye_overlaps(cuflye_ctx* c, size_t n, const int64_t* ids, const
     total += R;
     accumulate_timing(c, true);
   });
-  // algorithmic bytes per stage: packed bases + one 32-byte sector per window
-  // Compulsory traffic per stage: the bases and one probe sector per window,
-  // bucket entries read (8 B) and hit records written (12 B); a read and a
-  // write of every 12-byte record for the KmerMatch sort; the group stage
-  // reads the sorted records (12 B) and the ext positions of ext-sorted
-  // groups (counted as 8 B on average); the DP reads (cur, ext) and writes
-  // (score, backtrack); the backtrack reads its table once.
-  c->stage_bytes[0] = bases_total / 4 + windows_total * 32 + hits_total * 20;
-  c->stage_bytes[1] = hits_total * 24;
-  c->stage_bytes[2] = hits_total * 20;
-  c->stage_bytes[3] = hits_total * 16;
-  c->stage_bytes[4] = hits_total * 4;
+  set_stage_bytes(c, bases_total, windows_total, hits_total);
   if (n_out) *n_out = total;
   if (overflow)
     throw Error(CUFLYE_ERR_CAPACITY,
@@ -1710,7 +1832,7 @@ cuflye_status cuflye_last_timing(const cuflye_ctx* c, double* stage_ms, uint64_t
 
 cuflye_status cuflye_last_sort_stats(const cuflye_ctx* c, uint64_t* counts, size_t n) {
   if (!c || (!counts && n)) return CUFLYE_ERR_INVALID;
-  for (size_t i = 0; i < n && i < static_cast<size_t>(kSortStats); ++i) counts[i] = c->sort_stats[i];
+  for (size_t i = 0; i < n && i < 8; ++i) counts[i] = c->sort_stats[i];
   return CUFLYE_OK;
 }
 

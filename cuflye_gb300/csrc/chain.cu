@@ -142,20 +142,15 @@ __global__ void __launch_bounds__(kGroupBlock) group_tiles_kernel(
   }
 }
 
-__global__ void prefilter_kernel(const uint64_t* __restrict__ keys,
-                                 const uint32_t* __restrict__ vals, GroupInfo* __restrict__ groups,
-                                 uint64_t ngroups, uint64_t nhits,
-                                 const QueryInfo* __restrict__ qinfo,
-                                 const int32_t* __restrict__ slot_len, ChainParams p,
-                                 uint32_t* __restrict__ ext_list, uint32_t* __restrict__ dp_list,
-                                 uint32_t* __restrict__ counts) {
+// The prefilter of one group by one warp: unique query positions (changes
+// of curPos, starting from prevPos = 0), the ext-pos extremes, then
+// prefilter_keeps.  Writes n, ext_len, ext_sorted and survive into gi.
+__device__ __forceinline__ bool prefilter_group(const uint64_t* __restrict__ keys,
+                                                const uint32_t* __restrict__ vals, GroupInfo& gi,
+                                                uint32_t n, const QueryInfo* __restrict__ qinfo,
+                                                const int32_t* __restrict__ slot_len,
+                                                const ChainParams& p) {
   const int lane = threadIdx.x & 31;
-  const uint64_t g = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-  if (g >= ngroups) return;
-  GroupInfo gi = groups[g];
-  const uint64_t end = g + 1 < ngroups ? groups[g + 1].start : nhits;
-  const uint32_t n = static_cast<uint32_t>(end - gi.start);
-  // unique query positions (changes of curPos, starting from prevPos = 0)
   uint32_t uniq = 0;
   int32_t mn = INT_MAX, mx = INT_MIN;
   // four rounds of loads in flight per lane
@@ -184,26 +179,65 @@ __global__ void prefilter_kernel(const uint64_t* __restrict__ keys,
     mn = min(mn, __shfl_down_sync(0xffffffffu, mn, d));
     mx = max(mx, __shfl_down_sync(0xffffffffu, mx, d));
   }
-  if (lane != 0) return;
+  if (lane != 0) return false;
   const int32_t cur_len = qinfo[gi.query].len;
   const int32_t ext_len = slot_len[gi.ext_di >> 1];
   const int32_t min_cur = static_cast<int32_t>(keys[gi.start] & 0xffffffffu);
-  const int32_t max_cur = static_cast<int32_t>(keys[end - 1] & 0xffffffffu);
+  const int32_t max_cur = static_cast<int32_t>(keys[gi.start + n - 1] & 0xffffffffu);
   gi.n = n;
   gi.ext_len = ext_len;
   gi.ext_sorted = ext_len > cur_len;
-  bool ok = !(static_cast<float>(uniq) <
-              fmul(p.min_kmer_survival_rate, static_cast<float>(p.min_overlap)));
-  if (ok && (max_cur - min_cur < p.min_overlap || mx - mn < p.min_overlap)) ok = false;
-  if (ok && p.check_overhang && !p.force_local) {
-    if (min(min_cur, mn) > p.max_overhang) ok = false;
-    if (min(cur_len - max_cur, ext_len - mx) > p.max_overhang) ok = false;
-  }
+  const bool ok = prefilter_keeps(uniq, min_cur, max_cur, mn, mx, cur_len, ext_len, p);
   gi.survive = ok;
+  return ok;
+}
+
+__global__ void prefilter_kernel(const uint64_t* __restrict__ keys,
+                                 const uint32_t* __restrict__ vals, GroupInfo* __restrict__ groups,
+                                 uint64_t ngroups, uint64_t nhits,
+                                 const QueryInfo* __restrict__ qinfo,
+                                 const int32_t* __restrict__ slot_len, ChainParams p,
+                                 uint32_t* __restrict__ ext_list, uint32_t* __restrict__ dp_list,
+                                 uint32_t* __restrict__ counts) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t g = (static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  if (g >= ngroups) return;
+  GroupInfo gi = groups[g];
+  const uint64_t end = g + 1 < ngroups ? groups[g + 1].start : nhits;
+  const bool ok = prefilter_group(keys, vals, gi, static_cast<uint32_t>(end - gi.start), qinfo,
+                                  slot_len, p);
+  if (lane != 0) return;
   groups[g] = gi;
   if (ok) {
     dp_list[atomicAdd(&counts[1], 1u)] = static_cast<uint32_t>(g);
     if (gi.ext_sorted) ext_list[atomicAdd(&counts[0], 1u)] = static_cast<uint32_t>(g);
+  }
+}
+
+// The same over a list of groups whose GroupInfo already holds start and n.
+__global__ void prefilter_list_kernel(const uint64_t* __restrict__ keys,
+                                      const uint32_t* __restrict__ vals,
+                                      GroupInfo* __restrict__ groups,
+                                      const uint32_t* __restrict__ list,
+                                      const QueryInfo* __restrict__ qinfo,
+                                      const int32_t* __restrict__ slot_len, ChainParams p,
+                                      uint32_t* __restrict__ ext_list,
+                                      uint32_t* __restrict__ dp_list,
+                                      uint32_t* __restrict__ counts) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t cnt = counts[2];
+  const uint32_t nwarps = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t li = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; li < cnt; li += nwarps) {
+    const uint32_t g = list[li];
+    GroupInfo gi = groups[g];
+    const bool ok = prefilter_group(keys, vals, gi, gi.n, qinfo, slot_len, p);
+    if (lane == 0) {
+      groups[g] = gi;
+      if (ok) {
+        dp_list[atomicAdd(&counts[1], 1u)] = g;
+        if (gi.ext_sorted) ext_list[atomicAdd(&counts[0], 1u)] = g;
+      }
+    }
   }
 }
 
@@ -1024,6 +1058,20 @@ cudaError_t groups_prefilter_n(const uint64_t* keys, const uint32_t* vals, Group
   prefilter_kernel<<<grid(ngroups * 32, 256), 256, 0, s>>>(keys, vals, groups, ngroups, nhits,
                                                            qinfo, slot_len, p, ext_list, dp_list,
                                                            counts);
+  return cudaGetLastError();
+}
+
+cudaError_t groups_prefilter_list(const uint64_t* keys, const uint32_t* vals, GroupInfo* groups,
+                                  const uint32_t* list, const QueryInfo* qinfo,
+                                  const int32_t* slot_len, const ChainParams& p,
+                                  uint32_t* ext_list, uint32_t* dp_list, uint32_t* counts,
+                                  uint32_t max_groups, cudaStream_t s) {
+  if (max_groups == 0) return cudaSuccess;
+  count_launch();
+  prefilter_list_kernel<<<static_cast<unsigned>(std::min<uint64_t>(grid(max_groups * 32ull, 256),
+                                                                    4096)),
+                          256, 0, s>>>(keys, vals, groups, list, qinfo, slot_len, p,
+                                       ext_list, dp_list, counts);
   return cudaGetLastError();
 }
 

@@ -212,6 +212,7 @@ enum : int32_t {
   kDevLogDomain = 2,
   kDevChainOverflow = 3,
   kDevTableFull = 4,
+  kDevMatchDict = 5,  // a hit's ext id missing from its query's dictionary
 };
 
 #ifdef __CUDACC__

@@ -50,7 +50,8 @@ __device__ __forceinline__ WindowKmer window_kmer(const QueryBatch& q, uint32_t 
 
 __global__ void count_kernel(DeviceIndex idx, QueryBatch q, uint32_t* __restrict__ cnt,
                              uint32_t* __restrict__ filt, uint64_t* __restrict__ wmeta,
-                             uint8_t* __restrict__ wflags, uint32_t* __restrict__ q_tie) {
+                             uint8_t* __restrict__ wflags, uint32_t* __restrict__ q_tie,
+                             uint32_t* __restrict__ wself) {
   const uint64_t w = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (w >= q.nwin) return;
   const uint32_t qi = query_of(q.win_off, q.nq, w);
@@ -91,6 +92,7 @@ __global__ void count_kernel(DeviceIndex idx, QueryBatch q, uint32_t* __restrict
             hi = mid;
         }
         self_hits = (lo < c && __ldg(idx.pos + off + lo) == want) ? 1u : 0u;
+        if (self_hits && wself) wself[w] = lo;
       } else {
         // explicit entries keep input order and may repeat
         for (uint32_t e = 0; e < c; ++e) self_hits += __ldg(idx.pos + off + e) == want;
@@ -189,11 +191,11 @@ __global__ void gather_kernel(const uint64_t* __restrict__ win_off,
 
 cudaError_t hits_count(const DeviceIndex& idx, const QueryBatch& q, uint32_t* cnt,
                        uint32_t* filt, uint64_t* wmeta, uint8_t* wflags, uint32_t* q_tie,
-                       cudaStream_t s) {
+                       uint32_t* wself, cudaStream_t s) {
   if (q.nwin == 0) return cudaSuccess;
   count_launch();
-  count_kernel<<<static_cast<unsigned>((q.nwin + 255) / 256), 256, 0, s>>>(idx, q, cnt, filt,
-                                                                          wmeta, wflags, q_tie);
+  count_kernel<<<static_cast<unsigned>((q.nwin + 255) / 256), 256, 0, s>>>(
+      idx, q, cnt, filt, wmeta, wflags, q_tie, wself);
   return cudaGetLastError();
 }
 

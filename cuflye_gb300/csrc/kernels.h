@@ -133,10 +133,12 @@ struct QueryBatch {
 };
 
 // q_tie[i] (zeroed by the caller) becomes nonzero when query i looks up a
-// bucket with kDupIdsBit, i.e. when its KmerMatch keys may repeat.
+// bucket with kDupIdsBit, i.e. when its KmerMatch keys may repeat.  wself
+// (optional) receives, for windows flagged kWinTrivial, the bucket index of
+// the query's own position (built indexes only: one such entry at most).
 cudaError_t hits_count(const DeviceIndex& idx, const QueryBatch& q, uint32_t* cnt,
                        uint32_t* filt, uint64_t* wmeta, uint8_t* wflags, uint32_t* q_tie,
-                       cudaStream_t s);
+                       uint32_t* wself, cudaStream_t s);
 // keys[j] = (ext dense id << 32) | cur pos, vals[j] = ext pos, kmers
 // (optional), in generation order; filtered positions into fpos.
 cudaError_t hits_emit(const DeviceIndex& idx, const QueryBatch& q, const uint64_t* hit_off,
@@ -251,6 +253,82 @@ cudaError_t groups_prepare_ext_sort(uint64_t* keys, uint32_t* vals, const GroupI
 cudaError_t groups_ext_presorted(const uint32_t* vals, GroupInfo* groups, const uint32_t* ext_list,
                                  const uint32_t* counts, uint32_t* out, uint32_t* out_count,
                                  cudaStream_t s);
+// The group prefilter of tools/replay_overlap_chains.py:245-270: survival
+// (unique query positions against min_kmer_survival_rate * min_overlap), the
+// cur and ext spans against min_overlap, and the overhangs when
+// check_overhang && !force_local.  mn / mx: the group's least and greatest
+// ext pos; min_cur / max_cur its first and last cur pos.
+__device__ __forceinline__ bool prefilter_keeps(uint32_t uniq, int32_t min_cur, int32_t max_cur,
+                                                int32_t mn, int32_t mx, int32_t cur_len,
+                                                int32_t ext_len, const ChainParams& p) {
+  bool ok = !(static_cast<float>(uniq) <
+              __fmul_rn(p.min_kmer_survival_rate, static_cast<float>(p.min_overlap)));
+  if (ok && (max_cur - min_cur < p.min_overlap || mx - mn < p.min_overlap)) ok = false;
+  if (ok && p.check_overhang && !p.force_local) {
+    if (min(min_cur, mn) > p.max_overhang) ok = false;
+    if (min(cur_len - max_cur, ext_len - mx) > p.max_overhang) ok = false;
+  }
+  return ok;
+}
+
+// ---------------------------------------------------------------- sorted emission
+// Hits written straight into KmerMatch order (match_emit.cu).  A query whose
+// distinct ext ids exceed kMatchDictCap makes the pass take the emit + sort
+// path instead.
+constexpr uint32_t kMatchDictCap = 2048;
+
+struct MatchEmitArgs {
+  DeviceIndex idx;
+  const uint64_t* win_off = nullptr;   // nq + 1: each query's first window in the pass
+  const uint64_t* q_off = nullptr;     // nq + 1: each query's first hit in the pass
+  const uint64_t* hit_off = nullptr;   // per window: its first hit (generation order)
+  const uint64_t* wmeta = nullptr;     // per window: table meta of its k-mer
+  const uint8_t* wflags = nullptr;     // per window: kWin* flags
+  const uint32_t* wself = nullptr;     // per kWinTrivial window: bucket index of the self hit
+  const uint64_t* filt_off = nullptr;  // per window: its filtered-position slot
+  int32_t* fpos = nullptr;             // filtered positions (written by match_emit)
+  DeviceStatus* status = nullptr;
+  uint32_t nq = 0;
+};
+
+struct MatchEmitLists {
+  uint32_t* dp_list;    // surviving groups decided by match_emit
+  uint32_t* pf_list;    // groups left to the prefilter kernel
+  uint32_t* counts;     // [1]: dp_list entries, [2]: pf_list entries (zeroed by the caller)
+  uint64_t* emu_begin;  // flagged queries' hit ranges for the libstdc++-order sort
+  uint64_t* emu_end;
+  uint32_t* emu_count;  // zeroed by the caller
+  unsigned long long* tally;  // [0]: flagged queries' hits, [1]: hits of pf_list groups
+};
+
+size_t match_dict_smem_bytes();
+size_t match_emit_smem_bytes();
+// Per query: its distinct ext ids (sorted) with their hit counts, as words
+// (ext id << 32) | count at dict[q_dbase[q] ..] (dict needs one word per hit
+// at most; *dict_cursor zeroed by the caller), and their number q_ng[q].  A
+// query with more than kMatchDictCap ext ids gets q_ng = 0 and counts in
+// *overflow (zeroed by the caller).  counter: one word of scratch.
+cudaError_t match_dict(const MatchEmitArgs& a, uint64_t* dict, unsigned long long* dict_cursor,
+                       uint32_t* q_ng, uint64_t* q_dbase, uint32_t* overflow, uint32_t* counter,
+                       int num_sms, cudaStream_t s);
+// The hits of every query in KmerMatch order (flagged queries: generation
+// order, listed in emu_*), the filtered positions, one GroupInfo per
+// (query, ext id) at q_goff[q] + rank, and the prefilter of every group whose
+// ext positions rise strictly in cur-pos order (the others go to pf_list).
+cudaError_t match_emit(const MatchEmitArgs& a, const uint64_t* dict, const uint32_t* q_ng,
+                       const uint64_t* q_dbase, const uint64_t* q_goff, const uint32_t* q_tie,
+                       const QueryInfo* qinfo, const ChainParams& p, uint64_t* keys,
+                       uint32_t* vals, GroupInfo* groups, const MatchEmitLists& lists,
+                       uint32_t* counter, int num_sms, cudaStream_t s);
+// The prefilter of the groups list[0 .. counts[2]) (GroupInfo.n already set):
+// survivors go to dp_list (counts[1]) and, when ext-sorted, to ext_list
+// (counts[0]).  Does not clear the counts.
+cudaError_t groups_prefilter_list(const uint64_t* keys, const uint32_t* vals, GroupInfo* groups,
+                                  const uint32_t* list, const QueryInfo* qinfo,
+                                  const int32_t* slot_len, const ChainParams& p,
+                                  uint32_t* ext_list, uint32_t* dp_list, uint32_t* counts,
+                                  uint32_t max_groups, cudaStream_t s);
+
 // Highest score of a group, its first element and how many elements have it.
 struct GroupTop {
   int32_t score;

@@ -194,6 +194,16 @@ cuflye_status cuflye_overlaps(cuflye_ctx* ctx, size_t n, const int64_t* query_id
  * 1 gives the plain one-read-per-launch path. */
 cuflye_status cuflye_set_batch_queries(cuflye_ctx* ctx, size_t queries_per_pass);
 
+/* Sorted emission (no counterpart in the reference; on by default): overlap
+ * and read-to-graph calls on a built index write each query's candidate hits
+ * straight into the order of Flye's KmerMatch sort, one block per query, and
+ * decide most target groups' prefilter on the way, instead of writing them
+ * in generation order and sorting.  The rows are the same either way; 0
+ * selects the emit + sort path (for comparison), 1 restores the default.  A
+ * pass holding a query that hits more than 2,048 distinct targets takes the
+ * emit + sort path by itself (counted in cuflye_last_sort_stats, entry 7). */
+cuflye_status cuflye_set_sorted_emission(cuflye_ctx* ctx, int enable);
+
 /* --------------------------------------------------------------------------
  * Launch shapes and the autotuner (no counterpart in the reference).
  * Blocks per SM of the four kernels that take their work from a counter or
@@ -370,7 +380,9 @@ cuflye_status cuflye_last_timing(const cuflye_ctx* ctx, double* stage_ms, uint64
  * libstdc++-order; [4]: groups whose backtrack picked its starts by score
  * itself; [5]: 0 (no score order is sorted ahead of the backtrack); [6]:
  * groups whose backtrack ran again in the libstdc++ order because equal
- * scores could change their result. */
+ * scores could change their result; [7]: passes that left the sorted
+ * emission for the emit + sort path (a query with more distinct targets than
+ * its dictionary holds). */
 cuflye_status cuflye_last_sort_stats(const cuflye_ctx* ctx, uint64_t* counts, size_t n);
 
 /* Passes of the last candidates / overlaps / read-to-graph call: runs of

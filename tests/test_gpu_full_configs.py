@@ -123,9 +123,13 @@ def test_config3_read_to_graph_with_repeat_edges(gpu, oracle_mod):
                                    oracle_mod.default_params(**wl.params),
                                    oracle_mod.default_r2g(**synth.R2G_PARAMS))
     assert rows_gpu(got) == rows_oracle(exp)
-    # the duplicated edges (ids above 400) do carry alignments
-    assert any(abs(int(r["edge_id"])) > 400 for r in got)
     assert len(got) > 300
+    # the chaining input of the reads over duplicated edges holds overlaps with
+    # both copies (edge-sequence ids above 400 are the copies)
+    dup_reads = wl.reads.subset(np.array(over_dup))
+    ovl = gpu.overlaps(dup_reads, OverlapParams.make(**wl.params))
+    assert any(abs(int(r["ext_id"])) > 400 for r in ovl)
+    assert any(abs(int(r["ext_id"])) <= 400 for r in ovl)
 
 
 def test_config4_serving_requests_alone_and_in_flight(gpu, oracle_mod):
