@@ -1009,7 +1009,7 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp,
       uint32_t* pf_list = buf<uint32_t>(c, "g_pflist", G);
       CUFLYE_CHECK(cudaMemsetAsync(gcounts, 0, 4 * sizeof(uint32_t), st));
       CUFLYE_CHECK(cudaMemsetAsync(ecount, 0, sizeof(uint32_t), st));
-      MatchEmitLists L{dp_list, pf_list, gcounts, qb, qe, ecount, dcur + 1};
+      MatchEmitLists L{dp_list, ext_list, pf_list, gcounts, qb, qe, ecount, dcur + 1};
       CUFLYE_CHECK(match_emit(a, alt_keys, q_ng, q_dbase, q_goff, ps.q_tie, ps.qinfo, cp, ps.keys,
                               ps.vals, groups, L, mwords + 1, c->num_sms, st));
       CUFLYE_CHECK(cudaEventRecord(c->ev[1], st));

@@ -293,8 +293,9 @@ struct MatchEmitArgs {
 
 struct MatchEmitLists {
   uint32_t* dp_list;    // surviving groups decided by match_emit
-  uint32_t* pf_list;    // groups left to the prefilter kernel
-  uint32_t* counts;     // [1]: dp_list entries, [2]: pf_list entries (zeroed by the caller)
+  uint32_t* ext_list;   // those of them that are ext-sorted
+  uint32_t* pf_list;    // groups left to the prefilter kernel (flagged queries')
+  uint32_t* counts;     // [0] ext_list, [1] dp_list, [2] pf_list entries (zeroed by the caller)
   uint64_t* emu_begin;  // flagged queries' hit ranges for the libstdc++-order sort
   uint64_t* emu_end;
   uint32_t* emu_count;  // zeroed by the caller
@@ -313,8 +314,8 @@ cudaError_t match_dict(const MatchEmitArgs& a, uint64_t* dict, unsigned long lon
                        int num_sms, cudaStream_t s);
 // The hits of every query in KmerMatch order (flagged queries: generation
 // order, listed in emu_*), the filtered positions, one GroupInfo per
-// (query, ext id) at q_goff[q] + rank, and the prefilter of every group whose
-// ext positions rise strictly in cur-pos order (the others go to pf_list).
+// (query, ext id) at q_goff[q] + rank, and the prefilter of every group of
+// an unflagged query (a flagged query's groups go to pf_list).
 cudaError_t match_emit(const MatchEmitArgs& a, const uint64_t* dict, const uint32_t* q_ng,
                        const uint64_t* q_dbase, const uint64_t* q_goff, const uint32_t* q_tie,
                        const QueryInfo* qinfo, const ChainParams& p, uint64_t* keys,

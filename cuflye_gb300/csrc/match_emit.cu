@@ -17,23 +17,28 @@
 //                      with their counts are the query's groups (the
 //                      dictionary);
 //   match_emit_kernel  one block per query reads the entries again in batches
-//                      of up to 64 windows.  A hit's place in its group is the
-//                      group's running count plus the number of earlier windows
-//                      of the batch that hit the same ext id (a 64-bit mask per
-//                      group), so the batch is staged in shared memory in
-//                      group order and leaves in coalesced runs.  Each group's
-//                      first and last ext pos and whether its ext positions
-//                      rise strictly in cur-pos order are tracked on the way, so
-//                      the group's prefilter (survival, spans, overhangs) is
-//                      decided here for every group whose ext positions rise;
-//                      the others are listed for the prefilter kernel.
+//                      of up to 128 windows.  A window hits an ext id at most
+//                      once, so a hit's place in its group is the group's
+//                      running count plus the number of earlier windows of
+//                      the batch that hit the same ext id (a 128-bit mask per
+//                      group, set in a first phase, read in a second).  The
+//                      hits are stored there directly: a group's hits of one
+//                      batch fill consecutive slots, which the L2 cache merges
+//                      into whole sectors.  Each group's least and greatest
+//                      ext pos are kept on the way (shared-memory atomics), so
+//                      every group's prefilter (survival, spans, overhangs) is
+//                      decided here.
 //
 // A flagged query's hits are written in generation order instead (its equal
-// keys need the libstdc++-order sort), and all its groups are listed for the
+// keys need the libstdc++-order sort), and its groups are listed for the
 // prefilter after that sort.  Both kernels visit a window's entries in the
-// same order as hits_count / hits_emit: the bucket's stored entries, flipped
-// to the other strand when the window's k-mer is not in standard form, less
-// the query's own position (its index in the bucket is wself).
+// order hits_count / hits_emit do: the bucket's stored entries, flipped to
+// the other strand when the window's k-mer is not in standard form, less the
+// query's own position (its index in the bucket is wself).
+//
+// Work split: each thread takes kSePer consecutive entries of the batch (one
+// search for its first window, then a forward walk), and issues all of its
+// loads before using any.
 #include <algorithm>
 #include <climits>
 #include <cstdint>
@@ -46,17 +51,18 @@ namespace {
 
 constexpr int kSeBlock = 512;
 constexpr int kSeWarps = kSeBlock / 32;
-constexpr uint32_t kSeBatch = 2048;  // bucket entries per batch
-constexpr int kSeWin = 64;           // windows per batch (one 64-bit mask bit each)
-constexpr uint32_t kSePerThread = kSeBatch / kSeBlock;
+constexpr int kSeWin = 128;           // windows per batch (bits of the group masks)
+constexpr int kSeMaskWords = kSeWin / 64;
+constexpr uint32_t kSePer = 8;        // consecutive entries per thread
+constexpr uint32_t kSeBatch = kSePer * kSeBlock;  // bucket entries per batch
 constexpr int kHashBits = 12;
 constexpr uint32_t kHashSlots = 1u << kHashBits;  // load 1/2 at kMatchDictCap ids
 constexpr uint32_t kNone = 0xffffffffu;
 
-static_assert(kSeBatch % kSeBlock == 0, "batch entries per thread");
 static_assert(kHashSlots == 2 * kMatchDictCap, "hash slots: twice the dictionary");
 static_assert(kMatchDictCap % kSeBlock == 0, "dictionary ranks per thread");
 static_assert(kMatchDictCap <= 65536, "ranks fit 16 bits");
+static_assert(kSeWin <= kSeBlock, "one thread per batch window");
 
 // Fibonacci hashing of a dense target id onto the table's slots.
 __device__ __forceinline__ uint32_t hash_slot(uint32_t id) {
@@ -66,24 +72,24 @@ __device__ __forceinline__ uint32_t hash_slot(uint32_t id) {
 // The windows of one batch, in shared memory.
 struct BatchWin {
   uint64_t ebase[kSeWin];    // index of the window's first bucket entry in idx.pos
+  uint64_t hoff[kSeWin];     // the window's first hit (generation order)
   uint32_t cum[kSeWin + 1];  // batch-local index of each window's first visited entry
-  uint32_t first[kSeWin];    // first visited entry of the window (e0 for a split window)
+  uint32_t first[kSeWin];    // first visited bucket index of the window (e0 when split)
   uint32_t self[kSeWin];     // bucket index of the query's own position, or kNone
   uint32_t p[kSeWin];        // window position in the query (cur pos)
-  uint64_t hoff[kSeWin];     // hit offset of the window (generation order)
   uint8_t rev[kSeWin];       // the window's k-mer is not in standard form
+  uint32_t wsum[kSeWin / 32];
   uint32_t nw, total;
   uint64_t next_w;
   uint32_t next_e;
-  uint32_t wsum[2];
 };
 
 struct EmitQuery {
   uint64_t w0, w1;  // the query's windows [w0, w1) in the pass
-  uint64_t h0;      // the query's first hit in the pass
+  uint64_t h0, h1;  // its hits [h0, h1) in the pass
 };
 
-// Sets up the batch that starts at window w (entry e0 of it): as many
+// Sets up the batch that starts at window w (bucket entry e0 of it): as many
 // windows as fit kSeBatch entries and kSeWin windows, or kSeBatch entries of
 // one window that has more.  Writes the filtered positions of the batch's
 // windows when fpos is given.  Every thread of the block calls it.
@@ -93,10 +99,9 @@ __device__ void batch_setup(BatchWin& b, const MatchEmitArgs& a, const EmitQuery
   uint32_t raw = 0;
   if (t < kSeWin) {
     const uint64_t wi = w + t;
-    uint64_t ebase = 0;
+    uint64_t ebase = 0, hoff = 0;
     uint32_t self = kNone;
     uint8_t rev = 0;
-    uint64_t hoff = 0;
     if (wi < eq.w1) {
       const uint8_t fl = a.wflags[wi];
       rev = (fl & kWinRev) ? 1 : 0;
@@ -111,12 +116,11 @@ __device__ void batch_setup(BatchWin& b, const MatchEmitArgs& a, const EmitQuery
     const uint32_t f = t == 0 ? e0 : 0u;
     raw -= f;
     b.ebase[t] = ebase;
+    b.hoff[t] = hoff;
     b.first[t] = f;
     b.self[t] = self;
     b.rev[t] = rev;
-    b.hoff[t] = hoff;
     b.p[t] = static_cast<uint32_t>(wi - eq.w0);
-    // inclusive scan of the raw counts over the 64 windows (two warps)
     uint32_t inc = raw;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -124,15 +128,18 @@ __device__ void batch_setup(BatchWin& b, const MatchEmitArgs& a, const EmitQuery
       if ((t & 31) >= o) inc += u;
     }
     if ((t & 31) == 31) b.wsum[t >> 5] = inc;
-    raw = inc;  // inclusive, warp-local for now
+    raw = inc;  // inclusive within the warp
   }
   __syncthreads();
   if (t < kSeWin) {
-    const uint32_t inc = raw + (t >= 32 ? b.wsum[0] : 0u);
-    b.cum[t + 1] = inc;
+    uint32_t before = 0;
+#pragma unroll
+    for (int k = 0; k < kSeWin / 32; ++k) before += k < (t >> 5) ? b.wsum[k] : 0u;
+    raw += before;
+    b.cum[t + 1] = raw;
     if (t == 0) b.cum[0] = 0;
-    raw = inc;
   }
+  // windows whose entries all fit the batch (the cumulative counts rise)
   const int m = __syncthreads_count(t < kSeWin && raw <= kSeBatch);
   if (t == 0) {
     if (m == 0) {  // the first window alone holds more than a batch
@@ -148,8 +155,8 @@ __device__ void batch_setup(BatchWin& b, const MatchEmitArgs& a, const EmitQuery
     }
   }
   __syncthreads();
-  // filtered positions of the windows this batch covers (each window once:
-  // a window that spans batches has entries, so it is not filtered)
+  // filtered positions of the windows this batch covers: a filtered window
+  // has no entries, so it lies in exactly one batch
   if (a.fpos && t < static_cast<int>(b.nw)) {
     const uint64_t wi = w + t;
     if (wi < eq.w1 && (a.wflags[wi] & kWinFiltered))
@@ -171,31 +178,51 @@ __device__ __forceinline__ int entry_window(const BatchWin& b, uint32_t j) {
   return lo;
 }
 
-// One visited entry: its target (dense internal id) and position after the
-// strand transform, its bucket index, and whether it is a hit (not the
-// query's own position).
-struct Entry {
-  uint32_t id;
-  uint32_t pos;
-  uint32_t e;
-  int wl;
-  bool hit;
+// The thread's kSePer consecutive entries of the batch: their windows and
+// bucket indexes, then all their loads.  Bit u of valid marks entry u as
+// present.
+struct Entries {
+  uint64_t sv[kSePer];
+  uint32_t e[kSePer];
+  uint8_t wl[kSePer];
+  uint32_t valid;
 };
 
-__device__ __forceinline__ Entry load_entry(const BatchWin& b, const MatchEmitArgs& a, uint32_t j) {
-  Entry x;
-  x.wl = entry_window(b, j);
-  x.e = b.first[x.wl] + (j - b.cum[x.wl]);
-  const uint64_t sv = __ldg(a.idx.pos + b.ebase[x.wl] + x.e);
-  x.id = static_cast<uint32_t>(sv >> 32);
-  x.pos = static_cast<uint32_t>(sv & 0xffffffffu);
-  if (b.rev[x.wl]) {
-    x.pos = static_cast<uint32_t>(__ldg(a.idx.slot_len + (x.id >> 1)) - static_cast<int32_t>(x.pos) -
-                                  a.idx.k);
-    x.id ^= 1u;
+__device__ __forceinline__ void load_entries(const BatchWin& b, const MatchEmitArgs& a,
+                                             Entries& x) {
+  const uint32_t j0 = threadIdx.x * kSePer;
+  x.valid = 0;
+  if (j0 >= b.total) return;
+  int wl = entry_window(b, j0);
+#pragma unroll
+  for (uint32_t u = 0; u < kSePer; ++u) {
+    const uint32_t j = j0 + u;
+    if (j < b.total) {
+      while (b.cum[wl + 1] <= j) ++wl;  // on to the next window with entries
+      x.wl[u] = static_cast<uint8_t>(wl);
+      x.e[u] = b.first[wl] + (j - b.cum[wl]);
+      x.valid |= 1u << u;
+    }
   }
-  x.hit = x.e != b.self[x.wl];
-  return x;
+#pragma unroll
+  for (uint32_t u = 0; u < kSePer; ++u)
+    if (x.valid & (1u << u)) x.sv[u] = __ldg(a.idx.pos + b.ebase[x.wl[u]] + x.e[u]);
+}
+
+// Entry u after the strand transform: (target dense id, position); false for
+// the query's own position.
+__device__ __forceinline__ bool entry_hit(const BatchWin& b, const MatchEmitArgs& a,
+                                          const Entries& x, uint32_t u, uint32_t& id,
+                                          uint32_t& pos) {
+  const int wl = x.wl[u];
+  id = static_cast<uint32_t>(x.sv[u] >> 32);
+  pos = static_cast<uint32_t>(x.sv[u] & 0xffffffffu);
+  if (b.rev[wl]) {
+    pos = static_cast<uint32_t>(__ldg(a.idx.slot_len + (id >> 1)) - static_cast<int32_t>(pos) -
+                                a.idx.k);
+    id ^= 1u;
+  }
+  return x.e[u] != b.self[wl];
 }
 
 // Next query of the block from the launch's counter.
@@ -237,27 +264,30 @@ __global__ void __launch_bounds__(kSeBlock) match_dict_kernel(MatchEmitArgs a, u
       sm.nkeys = 0;
       sm.nlist = 0;
     }
-    EmitQuery eq{a.win_off[q], a.win_off[q + 1], a.q_off[q]};
+    const EmitQuery eq{a.win_off[q], a.win_off[q + 1], a.q_off[q], a.q_off[q + 1]};
     __syncthreads();
     uint64_t w = eq.w0;
     uint32_t e0 = 0;
     bool over = false;
     while (w < eq.w1 && !over) {
       batch_setup(sm.b, a, eq, w, e0);
-      for (uint32_t j = t; j < sm.b.total; j += kSeBlock) {
-        const Entry x = load_entry(sm.b, a, j);
-        if (!x.hit) continue;
-        uint32_t s = hash_slot(x.id);
+      Entries x;
+      load_entries(sm.b, a, x);
+#pragma unroll
+      for (uint32_t u = 0; u < kSePer; ++u) {
+        uint32_t id, pos;
+        if (!(x.valid & (1u << u)) || !entry_hit(sm.b, a, x, u, id, pos)) continue;
+        uint32_t s = hash_slot(id);
         for (uint32_t probe = 0; probe < kHashSlots; ++probe) {
           uint32_t k = sm.key[s];
           if (k == kNone) {
-            k = atomicCAS(&sm.key[s], kNone, x.id);
+            k = atomicCAS(&sm.key[s], kNone, id);
             if (k == kNone) {
               atomicAdd(&sm.nkeys, 1u);
-              k = x.id;
+              k = id;
             }
           }
-          if (k == x.id) {
+          if (k == id) {
             atomicAdd(&sm.cnt[s], 1u);
             break;
           }
@@ -297,10 +327,10 @@ __global__ void __launch_bounds__(kSeBlock) match_dict_kernel(MatchEmitArgs a, u
           const uint32_t lo = 2 * i - (i & (stride - 1));
           const uint32_t hi = lo + stride;
           const bool up = (lo & size) == 0;
-          const uint64_t x = sm.list[lo], y = sm.list[hi];
-          if ((x > y) == up) {
-            sm.list[lo] = y;
-            sm.list[hi] = x;
+          const uint64_t x0 = sm.list[lo], x1 = sm.list[hi];
+          if ((x0 > x1) == up) {
+            sm.list[lo] = x1;
+            sm.list[hi] = x0;
           }
         }
         __syncthreads();
@@ -323,23 +353,17 @@ __global__ void __launch_bounds__(kSeBlock) match_dict_kernel(MatchEmitArgs a, u
 struct EmitSmem {
   uint32_t hkey[kHashSlots];
   uint16_t hrank[kHashSlots];
-  uint32_t cursor[kMatchDictCap];  // the group's next hit, relative to the query's first
-  uint64_t mask[kMatchDictCap];    // windows of the batch that hit the group
-  uint32_t sbase[kMatchDictCap];   // the group's first slot in the staged batch
-  uint32_t firstx[kMatchDictCap];  // ext pos of the group's first hit (kNone: none yet)
-  uint32_t lastx[kMatchDictCap];   // ext pos of its latest hit
-  uint8_t notinc[kMatchDictCap];   // ext positions do not rise strictly in cur-pos order
-  uint64_t skey[kSeBatch];         // the batch's hits in group order
-  uint32_t sval[kSeBatch];
-  uint16_t srank[kSeBatch];
+  uint32_t cursor[kMatchDictCap];  // the group's next hit, counted from the query's first
+  unsigned long long mask[kSeMaskWords][kMatchDictCap];  // batch windows that hit the group
+  int32_t mnx[kMatchDictCap];      // least ext pos of the group's hits
+  int32_t mxx[kMatchDictCap];      // greatest
   BatchWin b;
   uint32_t ws[kSeWarps];
-  uint32_t qslot, nkept;
+  uint32_t qslot;
 };
 
-// Exclusive scan of v over the block's threads (thread order); returns the
-// prefix and writes the total to *total.
-__device__ __forceinline__ uint32_t block_exclusive(uint32_t v, uint32_t* ws, uint32_t* total) {
+// Exclusive scan of v over the block's threads (thread order).
+__device__ __forceinline__ uint32_t block_exclusive(uint32_t v, uint32_t* ws) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t inc = v;
 #pragma unroll
@@ -349,15 +373,10 @@ __device__ __forceinline__ uint32_t block_exclusive(uint32_t v, uint32_t* ws, ui
   }
   if (lane == 31) ws[warp] = inc;
   __syncthreads();
-  uint32_t before = 0, all = 0;
+  uint32_t before = 0;
 #pragma unroll
-  for (int w = 0; w < kSeWarps; ++w) {
-    const uint32_t c = ws[w];
-    before += w < warp ? c : 0u;
-    all += c;
-  }
+  for (int w = 0; w < kSeWarps; ++w) before += w < warp ? ws[w] : 0u;
   __syncthreads();
-  *total = all;
   return before + inc - v;
 }
 
@@ -376,12 +395,21 @@ __device__ __forceinline__ uint32_t rank_of(const EmitSmem& sm, uint32_t id, Dev
   return kNone;
 }
 
+// Hits of group r in the batch's windows before wl.
+__device__ __forceinline__ uint32_t earlier_hits(const EmitSmem& sm, uint32_t r, int wl) {
+  const unsigned long long m0 = sm.mask[0][r];
+  if (wl < 64) return static_cast<uint32_t>(__popcll(m0 & ((1ULL << wl) - 1)));
+  const unsigned long long m1 = sm.mask[1][r];
+  return static_cast<uint32_t>(__popcll(m0) + __popcll(m1 & ((1ULL << (wl - 64)) - 1)));
+}
+
 __global__ void __launch_bounds__(kSeBlock, 2) match_emit_kernel(
     MatchEmitArgs a, const uint64_t* __restrict__ dict, const uint32_t* __restrict__ q_ng,
     const uint64_t* __restrict__ q_dbase, const uint64_t* __restrict__ q_goff,
     const uint32_t* __restrict__ q_tie, const QueryInfo* __restrict__ qinfo, ChainParams p,
     uint64_t* __restrict__ keys, uint32_t* __restrict__ vals, GroupInfo* __restrict__ groups,
     MatchEmitLists lists, uint32_t* counter) {
+  static_assert(kSeMaskWords == 2, "two mask words per group");
   extern __shared__ __align__(16) unsigned char emit_raw[];
   EmitSmem& sm = *reinterpret_cast<EmitSmem*>(emit_raw);
   const int t = threadIdx.x;
@@ -389,8 +417,7 @@ __global__ void __launch_bounds__(kSeBlock, 2) match_emit_kernel(
   for (;;) {
     const uint32_t q = next_query(counter, &sm.qslot);
     if (q >= a.nq) return;
-    const EmitQuery eq{a.win_off[q], a.win_off[q + 1], a.q_off[q]};
-    const uint64_t h1 = a.q_off[q + 1];
+    const EmitQuery eq{a.win_off[q], a.win_off[q + 1], a.q_off[q], a.q_off[q + 1]};
     const uint32_t ng = min(q_ng[q], kMatchDictCap);
     const uint64_t dbase = q_dbase[q];
     const bool flagged = q_tie[q] != 0;
@@ -419,17 +446,16 @@ __global__ void __launch_bounds__(kSeBlock, 2) match_emit_kernel(
       }
       sum += c[u];
     }
-    uint32_t all;
-    uint32_t run = block_exclusive(sum, sm.ws, &all);
+    uint32_t run = block_exclusive(sum, sm.ws);
 #pragma unroll
     for (uint32_t u = 0; u < kPer; ++u) {
       const uint32_t r = t * kPer + u;
       if (r < ng) {
         sm.cursor[r] = run;
-        sm.mask[r] = 0;
-        sm.firstx[r] = kNone;
-        sm.lastx[r] = kNone;
-        sm.notinc[r] = 0;
+        sm.mask[0][r] = 0;
+        sm.mask[1][r] = 0;
+        sm.mnx[r] = INT_MAX;
+        sm.mxx[r] = INT_MIN;
       }
       run += c[u];
     }
@@ -438,94 +464,67 @@ __global__ void __launch_bounds__(kSeBlock, 2) match_emit_kernel(
     uint32_t e0 = 0;
     while (w < eq.w1) {
       batch_setup(sm.b, a, eq, w, e0);
-      const uint32_t total = sm.b.total;
+      Entries x;
+      load_entries(sm.b, a, x);
       if (flagged) {
-        // generation order: the window's hit offset plus the entry's index
+        // generation order: the window's first hit plus the entry's index
         // among the window's hits
-        for (uint32_t j = t; j < total; j += kSeBlock) {
-          const Entry x = load_entry(sm.b, a, j);
-          if (!x.hit) continue;
-          const uint32_t self = sm.b.self[x.wl];
-          const uint64_t d = sm.b.hoff[x.wl] + x.e - (self != kNone && self < x.e ? 1u : 0u);
-          if (d < h1) {  // always: the window's hits lie in the query's range
-            keys[d] = (static_cast<uint64_t>(x.id) << 32) | sm.b.p[x.wl];
-            vals[d] = x.pos;
+#pragma unroll
+        for (uint32_t u = 0; u < kSePer; ++u) {
+          uint32_t id, pos;
+          if (!(x.valid & (1u << u)) || !entry_hit(sm.b, a, x, u, id, pos)) continue;
+          const int wl = x.wl[u];
+          const uint32_t self = sm.b.self[wl];
+          const uint64_t d = sm.b.hoff[wl] + x.e[u] - (self != kNone && self < x.e[u] ? 1u : 0u);
+          if (d < eq.h1) {  // always: the window's hits lie in the query's range
+            keys[d] = (static_cast<uint64_t>(id) << 32) | sm.b.p[wl];
+            vals[d] = pos;
           }
         }
       } else {
-        uint32_t rk[kSePerThread], ps[kSePerThread], id[kSePerThread];
-        int wl[kSePerThread];
+        // first phase: each hit's group rank (in e) and transformed entry
+        // (id << 32 | pos, in sv); the group masks and ext-pos extremes
 #pragma unroll
-        for (uint32_t u = 0; u < kSePerThread; ++u) {
-          const uint32_t j = t + u * kSeBlock;
-          rk[u] = kNone;
-          if (j < total) {
-            const Entry x = load_entry(sm.b, a, j);
-            if (x.hit) {
-              rk[u] = rank_of(sm, x.id, a.status);
-              ps[u] = x.pos;
-              id[u] = x.id;
-              wl[u] = x.wl;
-              if (rk[u] != kNone)
-                atomicOr(reinterpret_cast<unsigned long long*>(&sm.mask[rk[u]]), 1ULL << x.wl);
+        for (uint32_t u = 0; u < kSePer; ++u) {
+          uint32_t id, pos, r = kNone;
+          if ((x.valid & (1u << u)) && entry_hit(sm.b, a, x, u, id, pos)) {
+            r = rank_of(sm, id, a.status);
+            x.sv[u] = (static_cast<uint64_t>(id) << 32) | pos;
+            if (r != kNone) {
+              const int wl = x.wl[u];
+              atomicOr(&sm.mask[wl >> 6][r], 1ULL << (wl & 63));
+              atomicMin(&sm.mnx[r], static_cast<int32_t>(pos));
+              atomicMax(&sm.mxx[r], static_cast<int32_t>(pos));
             }
           }
+          x.e[u] = r;
         }
         __syncthreads();
-        // staging slots: groups in rank order, windows in order within a group
-        uint32_t cc[kPer], csum = 0;
+        // second phase: each hit at its group's place
 #pragma unroll
-        for (uint32_t u = 0; u < kPer; ++u) {
-          const uint32_t r = t * kPer + u;
-          cc[u] = r < ng ? static_cast<uint32_t>(__popcll(sm.mask[r])) : 0u;
-          csum += cc[u];
-        }
-        uint32_t kept;
-        uint32_t sb = block_exclusive(csum, sm.ws, &kept);
-#pragma unroll
-        for (uint32_t u = 0; u < kPer; ++u) {
-          const uint32_t r = t * kPer + u;
-          if (r < ng) sm.sbase[r] = sb;
-          sb += cc[u];
-        }
-        __syncthreads();
-#pragma unroll
-        for (uint32_t u = 0; u < kSePerThread; ++u) {
-          if (rk[u] != kNone) {
-            const uint32_t r = rk[u];
-            const uint32_t slot =
-                sm.sbase[r] + static_cast<uint32_t>(__popcll(sm.mask[r] & ((1ULL << wl[u]) - 1)));
-            sm.skey[slot] = (static_cast<uint64_t>(id[u]) << 32) | sm.b.p[wl[u]];
-            sm.sval[slot] = ps[u];
-            sm.srank[slot] = static_cast<uint16_t>(r);
-          }
-        }
-        __syncthreads();
-        // out in group runs; each hit's ext pos against its group predecessor
-        for (uint32_t j = t; j < kept; j += kSeBlock) {
-          const uint32_t r = sm.srank[j];
-          const uint32_t x = sm.sval[j];
-          const uint32_t local = j - sm.sbase[r];
-          const uint64_t d = eq.h0 + sm.cursor[r] + local;
-          if (d < h1) {  // always, with the dictionary's counts
-            keys[d] = sm.skey[j];
-            vals[d] = x;
+        for (uint32_t u = 0; u < kSePer; ++u) {
+          const uint32_t r = x.e[u];
+          if (r == kNone) continue;
+          const int wl = x.wl[u];
+          const uint64_t d = eq.h0 + sm.cursor[r] + earlier_hits(sm, r, wl);
+          if (d < eq.h1) {  // always, with the dictionary's counts
+            keys[d] = (x.sv[u] & 0xffffffff00000000ULL) | sm.b.p[wl];
+            vals[d] = static_cast<uint32_t>(x.sv[u]);
           } else {
             raise_status(a.status, kDevMatchDict, 1, static_cast<int64_t>(q));
           }
-          const uint32_t prev = local ? sm.sval[j - 1] : sm.lastx[r];
-          if ((local || sm.firstx[r] != kNone) && x <= prev) sm.notinc[r] = 1;
         }
         __syncthreads();
 #pragma unroll
         for (uint32_t u = 0; u < kPer; ++u) {
           const uint32_t r = t * kPer + u;
-          if (r < ng && cc[u]) {
-            const uint32_t sbr = sm.sbase[r];
-            if (sm.firstx[r] == kNone) sm.firstx[r] = sm.sval[sbr];
-            sm.lastx[r] = sm.sval[sbr + cc[u] - 1];
-            sm.cursor[r] += cc[u];
-            sm.mask[r] = 0;
+          if (r < ng) {
+            const unsigned long long m0 = sm.mask[0][r], m1 = sm.mask[1][r];
+            if (m0 | m1) {
+              sm.cursor[r] += static_cast<uint32_t>(__popcll(m0) + __popcll(m1));
+              sm.mask[0][r] = 0;
+              sm.mask[1][r] = 0;
+            }
           }
         }
       }
@@ -533,8 +532,8 @@ __global__ void __launch_bounds__(kSeBlock, 2) match_emit_kernel(
       e0 = sm.b.next_e;
       __syncthreads();
     }
-    // the query's groups: GroupInfo, and the prefilter where the group's ext
-    // positions rose strictly (first and last ext pos are its extremes)
+    // the query's groups: GroupInfo and the prefilter; flagged queries' groups
+    // wait for their libstdc++-order sort
     const int32_t cur_len = qinfo[q].len;
     const uint64_t g0 = q_goff[q];
     for (uint32_t r = t; r < ng; r += kSeBlock) {
@@ -549,32 +548,46 @@ __global__ void __launch_bounds__(kSeBlock, 2) match_emit_kernel(
       gi.ext_len = __ldg(a.idx.slot_len + (ext >> 1));
       gi.survive = 0;
       gi.ext_sorted = 0;
-      const uint64_t g = g0 + r;
-      if (!flagged && !sm.notinc[r]) {
+      const uint32_t g = static_cast<uint32_t>(g0 + r);
+      if (!flagged) {
+        // in KmerMatch order the group's cur positions rise, each once: its
+        // first and last hits hold the least and greatest
         const int32_t min_cur = static_cast<int32_t>(keys[gi.start] & 0xffffffffu);
         const int32_t max_cur = static_cast<int32_t>(keys[gi.start + n - 1] & 0xffffffffu);
         const uint32_t uniq = n - (min_cur == 0 ? 1u : 0u);
-        const bool ok = prefilter_keeps(uniq, min_cur, max_cur, static_cast<int32_t>(sm.firstx[r]),
-                                        static_cast<int32_t>(sm.lastx[r]), cur_len, gi.ext_len, p);
-        if (ok) {
+        gi.ext_sorted = gi.ext_len > cur_len ? 1 : 0;
+        if (prefilter_keeps(uniq, min_cur, max_cur, sm.mnx[r], sm.mxx[r], cur_len, gi.ext_len,
+                            p)) {
           gi.survive = 1;
-          gi.ext_sorted = gi.ext_len > cur_len ? 2 : 0;  // already in ext-pos order
-          lists.dp_list[atomicAdd(lists.counts + 1, 1u)] = static_cast<uint32_t>(g);
+          lists.dp_list[atomicAdd(lists.counts + 1, 1u)] = g;
+          if (gi.ext_sorted) lists.ext_list[atomicAdd(lists.counts + 0, 1u)] = g;
         }
       } else {
-        lists.pf_list[atomicAdd(lists.counts + 2, 1u)] = static_cast<uint32_t>(g);
+        lists.pf_list[atomicAdd(lists.counts + 2, 1u)] = g;
         atomicAdd(lists.tally + 1, static_cast<unsigned long long>(n));
       }
       groups[g] = gi;
     }
-    if (flagged && t == 0 && eq.h0 + 1 < a.q_off[q + 1]) {
+    if (flagged && t == 0 && eq.h0 + 1 < eq.h1) {
       const uint32_t s = atomicAdd(lists.emu_count, 1u);
       lists.emu_begin[s] = eq.h0;
-      lists.emu_end[s] = a.q_off[q + 1];
-      atomicAdd(lists.tally, static_cast<unsigned long long>(a.q_off[q + 1] - eq.h0));
+      lists.emu_end[s] = eq.h1;
+      atomicAdd(lists.tally, static_cast<unsigned long long>(eq.h1 - eq.h0));
     }
     __syncthreads();
   }
+}
+
+// Blocks of a kernel resident per SM, at least one.
+template <class K>
+int resident(K kernel, size_t smem) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kSeBlock, smem) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return 1;
+  }
+  return std::max(per_sm, 1);
 }
 
 }  // namespace
@@ -592,12 +605,8 @@ cudaError_t match_dict(const MatchEmitArgs& a, uint64_t* dict, unsigned long lon
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), s);
   if (e != cudaSuccess) return e;
-  int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, match_dict_kernel, kSeBlock,
-                                                    sizeof(DictSmem));
-  if (e != cudaSuccess) return e;
-  const unsigned grid = static_cast<unsigned>(
-      std::min<uint64_t>(static_cast<uint64_t>(std::max(per_sm, 1)) * num_sms, a.nq));
+  const unsigned grid = static_cast<unsigned>(std::min<uint64_t>(
+      static_cast<uint64_t>(resident(match_dict_kernel, sizeof(DictSmem))) * num_sms, a.nq));
   MatchEmitArgs da = a;
   da.fpos = nullptr;  // the filtered positions are match_emit's to write
   count_launch();
@@ -618,12 +627,8 @@ cudaError_t match_emit(const MatchEmitArgs& a, const uint64_t* dict, const uint3
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), s);
   if (e != cudaSuccess) return e;
-  int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, match_emit_kernel, kSeBlock,
-                                                    sizeof(EmitSmem));
-  if (e != cudaSuccess) return e;
-  const unsigned grid = static_cast<unsigned>(
-      std::min<uint64_t>(static_cast<uint64_t>(std::max(per_sm, 1)) * num_sms, a.nq));
+  const unsigned grid = static_cast<unsigned>(std::min<uint64_t>(
+      static_cast<uint64_t>(resident(match_emit_kernel, sizeof(EmitSmem))) * num_sms, a.nq));
   count_launch();
   match_emit_kernel<<<grid, kSeBlock, sizeof(EmitSmem), s>>>(a, dict, q_ng, q_dbase, q_goff, q_tie,
                                                              qinfo, p, keys, vals, groups, lists,
