@@ -69,15 +69,18 @@ __device__ __forceinline__ uint32_t hash_slot(uint32_t id) {
   return (id * 0x9E3779B1u) >> (32 - kHashBits);
 }
 
-// The windows of one batch, in shared memory.
+// The windows of one batch, in shared memory.  Entry j of the batch (its
+// visited entries numbered in window order) belongs to window wl_of[j]; its
+// bucket entry is idx.pos[jbase[wl] + j], its generation-order slot
+// hbase[wl] + j (less one past the self hit), and it is the query's own
+// position when j == self_j[wl].
 struct BatchWin {
-  uint64_t ebase[kSeWin];    // index of the window's first bucket entry in idx.pos
-  uint64_t hoff[kSeWin];     // the window's first hit (generation order)
+  uint64_t jbase[kSeWin];    // ebase + first - cum (modulo 2^64)
+  uint64_t hbase[kSeWin];    // hoff + first - cum (modulo 2^64)
+  int32_t self_j[kSeWin];    // batch-local index of the self entry (may be < 0), or INT_MAX
+  uint32_t prev[kSeWin];     // cur pos | rev << 31
   uint32_t cum[kSeWin + 1];  // batch-local index of each window's first visited entry
-  uint32_t first[kSeWin];    // first visited bucket index of the window (e0 when split)
-  uint32_t self[kSeWin];     // bucket index of the query's own position, or kNone
-  uint32_t p[kSeWin];        // window position in the query (cur pos)
-  uint8_t rev[kSeWin];       // the window's k-mer is not in standard form
+  uint8_t wl_of[kSeBatch];
   uint32_t wsum[kSeWin / 32];
   uint32_t nw, total;
   uint64_t next_w;
@@ -97,14 +100,12 @@ __device__ void batch_setup(BatchWin& b, const MatchEmitArgs& a, const EmitQuery
                             uint32_t e0) {
   const int t = threadIdx.x;
   uint32_t raw = 0;
+  uint64_t ebase = 0, hoff = 0;
+  uint32_t self = kNone, prev = 0;
   if (t < kSeWin) {
     const uint64_t wi = w + t;
-    uint64_t ebase = 0, hoff = 0;
-    uint32_t self = kNone;
-    uint8_t rev = 0;
     if (wi < eq.w1) {
       const uint8_t fl = a.wflags[wi];
-      rev = (fl & kWinRev) ? 1 : 0;
       if (!(fl & kWinFiltered)) {
         const uint64_t meta = a.wmeta[wi];
         raw = static_cast<uint32_t>((meta >> 40) & ((1ULL << kCountBits) - 1));
@@ -112,15 +113,9 @@ __device__ void batch_setup(BatchWin& b, const MatchEmitArgs& a, const EmitQuery
       }
       if (fl & kWinTrivial) self = a.wself[wi];
       hoff = a.hit_off[wi];
+      prev = static_cast<uint32_t>(wi - eq.w0) | ((fl & kWinRev) ? 0x80000000u : 0u);
     }
-    const uint32_t f = t == 0 ? e0 : 0u;
-    raw -= f;
-    b.ebase[t] = ebase;
-    b.hoff[t] = hoff;
-    b.first[t] = f;
-    b.self[t] = self;
-    b.rev[t] = rev;
-    b.p[t] = static_cast<uint32_t>(wi - eq.w0);
+    raw -= t == 0 ? e0 : 0u;
     uint32_t inc = raw;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -135,12 +130,22 @@ __device__ void batch_setup(BatchWin& b, const MatchEmitArgs& a, const EmitQuery
     uint32_t before = 0;
 #pragma unroll
     for (int k = 0; k < kSeWin / 32; ++k) before += k < (t >> 5) ? b.wsum[k] : 0u;
-    raw += before;
+    raw += before;  // inclusive over the batch's windows
     b.cum[t + 1] = raw;
     if (t == 0) b.cum[0] = 0;
   }
   // windows whose entries all fit the batch (the cumulative counts rise)
   const int m = __syncthreads_count(t < kSeWin && raw <= kSeBatch);
+  if (t < kSeWin) {
+    const uint32_t first = t == 0 ? e0 : 0u;
+    const uint32_t start = b.cum[t];
+    b.jbase[t] = ebase + first - start;
+    b.hbase[t] = hoff + first - start;
+    b.self_j[t] = self == kNone ? INT_MAX
+                                : static_cast<int32_t>(self) - static_cast<int32_t>(first) +
+                                      static_cast<int32_t>(start);
+    b.prev[t] = prev;
+  }
   if (t == 0) {
     if (m == 0) {  // the first window alone holds more than a batch
       b.nw = 1;
@@ -162,51 +167,57 @@ __device__ void batch_setup(BatchWin& b, const MatchEmitArgs& a, const EmitQuery
     if (wi < eq.w1 && (a.wflags[wi] & kWinFiltered))
       a.fpos[a.filt_off[wi]] = static_cast<int32_t>(wi - eq.w0);
   }
-}
-
-// Batch-local window of visited entry j: the last window whose first entry
-// is at or before j (windows without entries are skipped that way).
-__device__ __forceinline__ int entry_window(const BatchWin& b, uint32_t j) {
-  int lo = 0, hi = static_cast<int>(b.nw) - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (b.cum[mid] <= j)
-      lo = mid;
-    else
-      hi = mid - 1;
+  // entry -> window table: each thread its kSePer consecutive entries (one
+  // search, then a forward walk over windows without entries)
+  const uint32_t j0 = static_cast<uint32_t>(t) * kSePer;
+  if (j0 < b.total) {
+    int lo = 0, hi = static_cast<int>(b.nw) - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (b.cum[mid] <= j0)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+#pragma unroll
+    for (uint32_t u = 0; u < kSePer; ++u) {
+      const uint32_t j = j0 + u;
+      if (j < b.total) {
+        while (b.cum[lo + 1] <= j) ++lo;
+        b.wl_of[j] = static_cast<uint8_t>(lo);
+      }
+    }
   }
-  return lo;
+  __syncthreads();
 }
 
-// The thread's kSePer consecutive entries of the batch: their windows and
-// bucket indexes, then all their loads.  Bit u of valid marks entry u as
-// present.
+// The thread's entries of the batch, j = threadIdx.x + u * kSeBlock (a warp
+// takes 32 consecutive entries, mostly of one window), all loads issued
+// before any use.  Bit u of valid marks entry u as present.
 struct Entries {
   uint64_t sv[kSePer];
-  uint32_t e[kSePer];
   uint8_t wl[kSePer];
   uint32_t valid;
 };
 
 __device__ __forceinline__ void load_entries(const BatchWin& b, const MatchEmitArgs& a,
                                              Entries& x) {
-  const uint32_t j0 = threadIdx.x * kSePer;
   x.valid = 0;
-  if (j0 >= b.total) return;
-  int wl = entry_window(b, j0);
 #pragma unroll
   for (uint32_t u = 0; u < kSePer; ++u) {
-    const uint32_t j = j0 + u;
+    const uint32_t j = threadIdx.x + u * kSeBlock;
     if (j < b.total) {
-      while (b.cum[wl + 1] <= j) ++wl;  // on to the next window with entries
-      x.wl[u] = static_cast<uint8_t>(wl);
-      x.e[u] = b.first[wl] + (j - b.cum[wl]);
+      x.wl[u] = b.wl_of[j];
       x.valid |= 1u << u;
     }
   }
 #pragma unroll
-  for (uint32_t u = 0; u < kSePer; ++u)
-    if (x.valid & (1u << u)) x.sv[u] = __ldg(a.idx.pos + b.ebase[x.wl[u]] + x.e[u]);
+  for (uint32_t u = 0; u < kSePer; ++u) {
+    if (x.valid & (1u << u)) {
+      const uint32_t j = threadIdx.x + u * kSeBlock;
+      x.sv[u] = __ldg(a.idx.pos + (b.jbase[x.wl[u]] + j));
+    }
+  }
 }
 
 // Entry u after the strand transform: (target dense id, position); false for
@@ -215,14 +226,15 @@ __device__ __forceinline__ bool entry_hit(const BatchWin& b, const MatchEmitArgs
                                           const Entries& x, uint32_t u, uint32_t& id,
                                           uint32_t& pos) {
   const int wl = x.wl[u];
+  const int32_t j = static_cast<int32_t>(threadIdx.x + u * kSeBlock);
   id = static_cast<uint32_t>(x.sv[u] >> 32);
   pos = static_cast<uint32_t>(x.sv[u] & 0xffffffffu);
-  if (b.rev[wl]) {
+  if (b.prev[wl] & 0x80000000u) {
     pos = static_cast<uint32_t>(__ldg(a.idx.slot_len + (id >> 1)) - static_cast<int32_t>(pos) -
                                 a.idx.k);
     id ^= 1u;
   }
-  return x.e[u] != b.self[wl];
+  return j != b.self_j[wl];
 }
 
 // Next query of the block from the launch's counter.
@@ -474,16 +486,18 @@ __global__ void __launch_bounds__(kSeBlock, 2) match_emit_kernel(
           uint32_t id, pos;
           if (!(x.valid & (1u << u)) || !entry_hit(sm.b, a, x, u, id, pos)) continue;
           const int wl = x.wl[u];
-          const uint32_t self = sm.b.self[wl];
-          const uint64_t d = sm.b.hoff[wl] + x.e[u] - (self != kNone && self < x.e[u] ? 1u : 0u);
-          if (d < eq.h1) {  // always: the window's hits lie in the query's range
-            keys[d] = (static_cast<uint64_t>(id) << 32) | sm.b.p[wl];
+          const int32_t j = static_cast<int32_t>(t + u * kSeBlock);
+          const uint64_t d = sm.b.hbase[wl] + static_cast<uint64_t>(j) -
+                             (sm.b.self_j[wl] < j ? 1u : 0u);
+          if (d >= eq.h0 && d < eq.h1) {  // always: the window's hits lie in the query's range
+            keys[d] = (static_cast<uint64_t>(id) << 32) | (sm.b.prev[wl] & 0x7fffffffu);
             vals[d] = pos;
           }
         }
       } else {
-        // first phase: each hit's group rank (in e) and transformed entry
-        // (id << 32 | pos, in sv); the group masks and ext-pos extremes
+        // first phase: each hit's group rank and transformed entry (id << 32
+        // | pos, in sv); the group masks and ext-pos extremes
+        uint32_t rk[kSePer];
 #pragma unroll
         for (uint32_t u = 0; u < kSePer; ++u) {
           uint32_t id, pos, r = kNone;
@@ -492,23 +506,24 @@ __global__ void __launch_bounds__(kSeBlock, 2) match_emit_kernel(
             x.sv[u] = (static_cast<uint64_t>(id) << 32) | pos;
             if (r != kNone) {
               const int wl = x.wl[u];
-              atomicOr(&sm.mask[wl >> 6][r], 1ULL << (wl & 63));
+              atomicOr(reinterpret_cast<unsigned*>(&sm.mask[wl >> 6][r]) + ((wl >> 5) & 1),
+                       1u << (wl & 31));
               atomicMin(&sm.mnx[r], static_cast<int32_t>(pos));
               atomicMax(&sm.mxx[r], static_cast<int32_t>(pos));
             }
           }
-          x.e[u] = r;
+          rk[u] = r;
         }
         __syncthreads();
         // second phase: each hit at its group's place
 #pragma unroll
         for (uint32_t u = 0; u < kSePer; ++u) {
-          const uint32_t r = x.e[u];
+          const uint32_t r = rk[u];
           if (r == kNone) continue;
           const int wl = x.wl[u];
           const uint64_t d = eq.h0 + sm.cursor[r] + earlier_hits(sm, r, wl);
           if (d < eq.h1) {  // always, with the dictionary's counts
-            keys[d] = (x.sv[u] & 0xffffffff00000000ULL) | sm.b.p[wl];
+            keys[d] = (x.sv[u] & 0xffffffff00000000ULL) | (sm.b.prev[wl] & 0x7fffffffu);
             vals[d] = static_cast<uint32_t>(x.sv[u]);
           } else {
             raise_status(a.status, kDevMatchDict, 1, static_cast<int64_t>(q));
@@ -602,6 +617,10 @@ cudaError_t match_dict(const MatchEmitArgs& a, uint64_t* dict, unsigned long lon
   cudaError_t e = cudaFuncSetAttribute(match_dict_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(sizeof(DictSmem)));
+  // all of the SM's shared memory, so that four blocks fit
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(match_dict_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             100);
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), s);
   if (e != cudaSuccess) return e;
@@ -624,6 +643,9 @@ cudaError_t match_emit(const MatchEmitArgs& a, const uint64_t* dict, const uint3
   cudaError_t e = cudaFuncSetAttribute(match_emit_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(sizeof(EmitSmem)));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(match_emit_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             100);
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), s);
   if (e != cudaSuccess) return e;
