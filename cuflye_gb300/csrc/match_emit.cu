@@ -63,6 +63,7 @@ static_assert(kHashSlots == 2 * kMatchDictCap, "hash slots: twice the dictionary
 static_assert(kMatchDictCap % kSeBlock == 0, "dictionary ranks per thread");
 static_assert(kMatchDictCap <= 65536, "ranks fit 16 bits");
 static_assert(kSeWin <= kSeBlock, "one thread per batch window");
+static_assert(kHashSlots % kSeBlock == 0, "hash slots per thread");
 
 // Fibonacci hashing of a dense target id onto the table's slots.
 __device__ __forceinline__ uint32_t hash_slot(uint32_t id) {
@@ -249,15 +250,19 @@ __device__ __forceinline__ uint32_t next_query(uint32_t* counter, uint32_t* slot
 // ------------------------------------------------------------ dictionary
 
 struct DictSmem {
-  uint32_t key[kHashSlots];
+  // the hash table; once counted, its slots are compacted into list (which
+  // takes the place of key: kMatchDictCap words of 8 bytes)
+  union {
+    uint32_t key[kHashSlots];
+    uint64_t list[kMatchDictCap];
+  };
   uint32_t cnt[kHashSlots];
-  uint64_t list[kMatchDictCap];
   BatchWin b;
   unsigned long long dslot;  // the query's first word in dict
   uint32_t nkeys, nlist, qslot;
 };
 
-__global__ void __launch_bounds__(kSeBlock) match_dict_kernel(MatchEmitArgs a, uint64_t* dict,
+__global__ void __launch_bounds__(kSeBlock, 3) match_dict_kernel(MatchEmitArgs a, uint64_t* dict,
                                                                unsigned long long* dict_cursor,
                                                                uint32_t* q_ng, uint64_t* q_dbase,
                                                                uint32_t* overflow,
@@ -321,11 +326,17 @@ __global__ void __launch_bounds__(kSeBlock) match_dict_kernel(MatchEmitArgs a, u
       continue;
     }
     const uint32_t n = sm.nkeys;
-    for (uint32_t s = t; s < kHashSlots; s += kSeBlock) {
-      if (sm.key[s] != kNone) {
-        const uint32_t i = atomicAdd(&sm.nlist, 1u);
-        sm.list[i] = (static_cast<uint64_t>(sm.key[s]) << 32) | sm.cnt[s];
-      }
+    constexpr uint32_t kSlotsPer = kHashSlots / kSeBlock;
+    uint64_t kc[kSlotsPer];
+#pragma unroll
+    for (uint32_t u = 0; u < kSlotsPer; ++u) {
+      const uint32_t s = t + u * kSeBlock;
+      kc[u] = (static_cast<uint64_t>(sm.key[s]) << 32) | sm.cnt[s];
+    }
+    __syncthreads();  // list overwrites key from here on
+#pragma unroll
+    for (uint32_t u = 0; u < kSlotsPer; ++u) {
+      if ((kc[u] >> 32) != kNone) sm.list[atomicAdd(&sm.nlist, 1u)] = kc[u];
     }
     __syncthreads();
     // bitonic sort of the (ext id, count) words by ext id, padded to a power of two
