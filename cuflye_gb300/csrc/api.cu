@@ -989,14 +989,11 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp,
     uint32_t* q_ng = buf<uint32_t>(c, "m_qng", nq);
     uint64_t* q_dbase = buf<uint64_t>(c, "m_qdbase", nq);
     uint64_t* q_goff = buf<uint64_t>(c, "m_qgoff", nq + 1);
-    // overflow, heavy count, two counters per kernel pair
-    uint32_t* mwords = buf<uint32_t>(c, "m_words", 8);
-    uint32_t* heavy = buf<uint32_t>(c, "m_heavy", nq);
+    uint32_t* mwords = buf<uint32_t>(c, "m_words", 4);  // overflow, counter
     unsigned long long* dcur = buf<unsigned long long>(c, "m_dcur", 3);  // cursor, tallies
-    CUFLYE_CHECK(cudaMemsetAsync(mwords, 0, 8 * sizeof(uint32_t), st));
+    CUFLYE_CHECK(cudaMemsetAsync(mwords, 0, 4 * sizeof(uint32_t), st));
     CUFLYE_CHECK(cudaMemsetAsync(dcur, 0, 3 * sizeof(unsigned long long), st));
-    CUFLYE_CHECK(match_dict(a, alt_keys, dcur, q_ng, q_dbase, mwords, heavy, mwords + 1,
-                            mwords + 2, c->num_sms, st));
+    CUFLYE_CHECK(match_dict(a, alt_keys, dcur, q_ng, q_dbase, mwords, mwords + 1, c->num_sms, st));
     G = scan_u32(c, q_ng, q_goff, nq, "m_scan");
     if (read_scalar(c, mwords) != 0) {
       // a query with more than kMatchDictCap ext ids: this pass takes the
@@ -1014,7 +1011,7 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp,
       CUFLYE_CHECK(cudaMemsetAsync(ecount, 0, sizeof(uint32_t), st));
       MatchEmitLists L{dp_list, ext_list, pf_list, gcounts, qb, qe, ecount, dcur + 1};
       CUFLYE_CHECK(match_emit(a, alt_keys, q_ng, q_dbase, q_goff, ps.q_tie, ps.qinfo, cp, ps.keys,
-                              ps.vals, groups, L, heavy, mwords + 1, mwords + 4, c->num_sms, st));
+                              ps.vals, groups, L, mwords + 1, c->num_sms, st));
       CUFLYE_CHECK(cudaEventRecord(c->ev[1], st));
       // 1. the flagged queries' KmerMatch sort in libstdc++ order
       CUFLYE_CHECK(sort_stats_add(sstats, 0, 1, nullptr, nq, ecount, st));

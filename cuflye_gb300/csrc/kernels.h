@@ -307,25 +307,20 @@ size_t match_emit_smem_bytes();
 // Per query: its distinct ext ids (sorted) with their hit counts, as words
 // (ext id << 32) | count at dict[q_dbase[q] ..] (dict needs one word per hit
 // at most; *dict_cursor zeroed by the caller), and their number q_ng[q].  A
-// warp per query counts up to 512 ids; queries with more are listed in
-// heavy_list / *heavy_count and counted by a block each.  A query with more
-// than kMatchDictCap ext ids gets q_ng = 0 and counts in *overflow (zeroed by
-// the caller).  counters: two words of scratch.
+// query with more than kMatchDictCap ext ids gets q_ng = 0 and counts in
+// *overflow (zeroed by the caller).  counter: one word of scratch.
 cudaError_t match_dict(const MatchEmitArgs& a, uint64_t* dict, unsigned long long* dict_cursor,
-                       uint32_t* q_ng, uint64_t* q_dbase, uint32_t* overflow,
-                       uint32_t* heavy_list, uint32_t* heavy_count, uint32_t* counters,
+                       uint32_t* q_ng, uint64_t* q_dbase, uint32_t* overflow, uint32_t* counter,
                        int num_sms, cudaStream_t s);
 // The hits of every query in KmerMatch order (flagged queries: generation
 // order, listed in emu_*), the filtered positions, one GroupInfo per
 // (query, ext id) at q_goff[q] + rank, and the prefilter of every group of
-// an unflagged query (a flagged query's groups go to pf_list).  A warp per
-// query, a block per heavy query.  counters: two words of scratch.
+// an unflagged query (a flagged query's groups go to pf_list).
 cudaError_t match_emit(const MatchEmitArgs& a, const uint64_t* dict, const uint32_t* q_ng,
                        const uint64_t* q_dbase, const uint64_t* q_goff, const uint32_t* q_tie,
                        const QueryInfo* qinfo, const ChainParams& p, uint64_t* keys,
                        uint32_t* vals, GroupInfo* groups, const MatchEmitLists& lists,
-                       const uint32_t* heavy_list, const uint32_t* heavy_count,
-                       uint32_t* counters, int num_sms, cudaStream_t s);
+                       uint32_t* counter, int num_sms, cudaStream_t s);
 // The prefilter of the groups list[0 .. counts[2]) (GroupInfo.n already set):
 // survivors go to dp_list (counts[1]) and, when ext-sorted, to ext_list
 // (counts[0]).  Does not clear the counts.
