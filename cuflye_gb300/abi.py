@@ -35,6 +35,38 @@ READ_ALIGNMENT_DTYPE = np.dtype([("chain_id", "<i8"), ("segment_id", "<i8"), ("r
                                  ("edge_end", "<i4"), ("edge_len", "<i4"), ("score", "<i4"),
                                  ("seq_divergence", "<f4")], align=True)
 
+# cuflye_chain_record: a candidate chain's segment, the fields of one
+# compact-binary record (docs/abi/read-alignment-compact-binary-v0.md:37-58)
+CHAIN_RECORD_DTYPE = np.dtype([("query_id", "<i8"), ("chain_id", "<i4"), ("segment_id", "<i4"),
+                               ("overlap_index", "<i4"), ("reserved", "<i4"),
+                               ("candidate_id", "<i8"), ("read_id", "<i8"), ("edge_id", "<i8"),
+                               ("edge_seq_id", "<i8"), ("read_begin", "<i4"),
+                               ("read_end", "<i4"), ("read_len", "<i4"), ("edge_left", "<i4"),
+                               ("edge_right", "<i4"), ("edge_begin", "<i4"),
+                               ("edge_end", "<i4"), ("edge_len", "<i4"), ("score", "<i4"),
+                               ("seq_divergence", "<f4")], align=True)
+# cuflye_edge_overlap: a read-alignment replay fixture's input row
+# (edge-overlaps.tsv of docs/abi/read-alignment-replay-fixture-v0.md)
+EDGE_OVERLAP_DTYPE = np.dtype([("candidate_id", "<i8"), ("read_id", "<i8"),
+                               ("read_begin", "<i4"), ("read_end", "<i4"), ("read_len", "<i4"),
+                               ("edge_left", "<i4"), ("edge_right", "<i4"),
+                               ("edge_begin", "<i4"), ("edge_end", "<i4"), ("edge_len", "<i4"),
+                               ("edge_id", "<i8"), ("edge_seq_id", "<i8"), ("score", "<i4"),
+                               ("seq_divergence", "<f4")], align=True)
+# the compact binary payload's fixed-width little-endian record (92 bytes,
+# no padding), for reading a payload back
+COMPACT_RECORD_DTYPE = np.dtype([("query_id", "<i8"), ("chain_id", "<i4"), ("segment_id", "<i4"),
+                                 ("overlap_index", "<i4"), ("candidate_id", "<i8"),
+                                 ("read_id", "<i8"), ("read_begin", "<i4"), ("read_end", "<i4"),
+                                 ("read_len", "<i4"), ("edge_id", "<i8"), ("edge_left", "<i4"),
+                                 ("edge_right", "<i4"), ("edge_seq_id", "<i8"),
+                                 ("edge_begin", "<i4"), ("edge_end", "<i4"),
+                                 ("edge_len", "<i4"), ("score", "<i4"),
+                                 ("seq_divergence", "<f4")])
+
+assert CHAIN_RECORD_DTYPE.itemsize == 96
+assert EDGE_OVERLAP_DTYPE.itemsize == 72
+assert COMPACT_RECORD_DTYPE.itemsize == 92
 assert CANDIDATE_DTYPE.itemsize == 32
 assert FILTERED_DTYPE.itemsize == 16
 assert OVERLAP_DTYPE.itemsize == 48
@@ -88,3 +120,16 @@ def canonical_sha256(lines: list[str]) -> str:
     for line in sorted(lines, key=_canonical_key):
         h.update(line.encode("utf-8"))
     return h.hexdigest()
+
+
+def read_compact_binary(data: bytes) -> tuple[dict, np.ndarray]:
+    """The header fields and records of a compact binary payload."""
+    u32 = lambda o: int.from_bytes(data[o:o + 4], "little")
+    u64 = lambda o: int.from_bytes(data[o:o + 8], "little")
+    head = {"magic": data[:8], "header_bytes": u32(8), "record_bytes": u32(12),
+            "version": (u32(16), u32(20)), "fixtures": u64(24), "records": u64(32),
+            "total_inputs": u64(40), "min_inputs": u32(48), "max_inputs": u32(52),
+            "output_mode": u32(56), "reserved": u32(60)}
+    recs = np.frombuffer(data, dtype=COMPACT_RECORD_DTYPE, offset=64,
+                         count=(len(data) - 64) // 92)
+    return head, recs

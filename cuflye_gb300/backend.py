@@ -139,6 +139,20 @@ def load_library(path: Path | None = None) -> ctypes.CDLL:
     L.cuflye_read_to_graph.argtypes = [_vp, ctypes.c_size_t, _i64p, _i64p, ctypes.c_char_p,
                                        ctypes.POINTER(OverlapParams), ctypes.POINTER(R2GParams),
                                        _vp, ctypes.c_size_t, _szp]
+    L.cuflye_read_to_graph_chains.restype = S
+    L.cuflye_read_to_graph_chains.argtypes = [_vp, ctypes.c_size_t, _i64p, _i64p,
+                                              ctypes.c_char_p, ctypes.POINTER(OverlapParams),
+                                              ctypes.POINTER(R2GParams), _vp, ctypes.c_size_t,
+                                              _szp, _u64p]
+    L.cuflye_chain_read_alignments.restype = S
+    L.cuflye_chain_read_alignments.argtypes = [
+        _vp, ctypes.c_size_t, _u64p, _i64p, _vp, ctypes.POINTER(R2GParams),
+        ctypes.POINTER(ctypes.c_float), ctypes.c_size_t, _vp, ctypes.c_size_t, _szp,
+        ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_uint8), ctypes.c_size_t, _szp,
+        _vp, ctypes.c_size_t, _szp]
+    L.cuflye_compact_binary.restype = S
+    L.cuflye_compact_binary.argtypes = [_vp, ctypes.c_size_t, ctypes.c_size_t, _u64p, _vp,
+                                        ctypes.c_size_t, _szp]
     L.cuflye_std_sort_segments.restype = S
     L.cuflye_std_sort_segments.argtypes = [_vp, _u64p, _u32p, _u64p, ctypes.c_size_t]
     L.cuflye_kernel_launches.restype = S
@@ -435,6 +449,61 @@ class CudaBackend:
             self._check(st)
             return out[:n.value].copy()
 
+    def read_to_graph_chains(self, reads, params: OverlapParams, r2g: R2GParams,
+                             capacity: int | None = None) -> tuple[np.ndarray, np.ndarray]:
+        """Candidate chains (before the divergence filter) as chain records,
+        and each read's chain-input overlap count."""
+        q = Sequences.of(reads)
+        cap = capacity if capacity is not None else max(1024, 64 * q.n)
+        inputs = np.zeros(max(q.n, 1), dtype=np.uint64)
+        while True:
+            out = np.empty(cap, dtype=abi.CHAIN_RECORD_DTYPE)
+            n = ctypes.c_size_t()
+            st = self._L.cuflye_read_to_graph_chains(
+                self._h, q.n, _ptr(q.ids, _i64p), _ptr(q.offsets, _i64p),
+                q.bases.ctypes.data_as(ctypes.c_char_p), ctypes.byref(params), ctypes.byref(r2g),
+                out.ctypes.data, cap, ctypes.byref(n), _ptr(inputs, _u64p))
+            if st == ERR_CAPACITY:
+                cap = n.value
+                continue
+            self._check(st)
+            return out[:n.value].copy(), inputs[:q.n].copy()
+
+    def chain_read_alignments(self, fixtures: list[np.ndarray], query_ids, r2g: R2GParams,
+                              chain_divergences=None) -> dict:
+        """Read-alignment replay fixtures (arrays of EDGE_OVERLAP_DTYPE):
+        candidate chains as chain records, per chain its divergence and
+        whether it is kept, and the kept chains' rows with complements."""
+        offs = np.zeros(len(fixtures) + 1, dtype=np.uint64)
+        offs[1:] = np.cumsum([len(f) for f in fixtures])
+        ov = (np.concatenate(fixtures) if fixtures else
+              np.zeros(0, dtype=abi.EDGE_OVERLAP_DTYPE)).astype(abi.EDGE_OVERLAP_DTYPE)
+        ov = np.ascontiguousarray(ov)
+        qids = np.ascontiguousarray(query_ids, dtype=np.int64)
+        din = None if chain_divergences is None else np.ascontiguousarray(chain_divergences,
+                                                                           dtype=np.float32)
+        cap = max(64, 4 * len(ov))
+        while True:
+            out = np.empty(cap, dtype=abi.CHAIN_RECORD_DTYPE)
+            div = np.empty(cap, dtype=np.float32)
+            kept = np.empty(cap, dtype=np.uint8)
+            rows = np.empty(2 * cap, dtype=abi.READ_ALIGNMENT_DTYPE)
+            n, nc, nr = ctypes.c_size_t(), ctypes.c_size_t(), ctypes.c_size_t()
+            st = self._L.cuflye_chain_read_alignments(
+                self._h, len(fixtures), _ptr(offs, _u64p), _ptr(qids, _i64p), ov.ctypes.data,
+                ctypes.byref(r2g),
+                None if din is None else din.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                0 if din is None else len(din), out.ctypes.data, cap, ctypes.byref(n),
+                div.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                kept.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), cap, ctypes.byref(nc),
+                rows.ctypes.data, 2 * cap, ctypes.byref(nr))
+            if st == ERR_CAPACITY:
+                cap = max(cap * 2, n.value, nc.value, nr.value)
+                continue
+            self._check(st)
+            return {"records": out[:n.value].copy(), "divergence": div[:nc.value].copy(),
+                    "kept": kept[:nc.value].astype(bool), "rows": rows[:nr.value].copy()}
+
     # -- the device sort behind every Flye sort point
     def std_sort_segments(self, keys, values, seg_offsets) -> tuple[np.ndarray, np.ndarray]:
         k = np.array(keys, dtype=np.uint64)
@@ -522,3 +591,22 @@ def collect_candidate_matches_cuda(backend: CudaBackend, query_id: int, sequence
     q = Sequences(np.array([query_id], dtype=np.int64),
                   np.array([0, len(seq)], dtype=np.int64), seq.copy())
     return backend.candidates(q)
+
+
+def compact_binary(records: np.ndarray, inputs_per_fixture) -> bytes:
+    """The compact binary payload of chain records (host code of the
+    library, no device)."""
+    L = load_library()
+    rec = np.ascontiguousarray(records, dtype=abi.CHAIN_RECORD_DTYPE)
+    inp = np.ascontiguousarray(inputs_per_fixture, dtype=np.uint64)
+    n = ctypes.c_size_t()
+    st = L.cuflye_compact_binary(rec.ctypes.data, len(rec), len(inp), _ptr(inp, _u64p), None, 0,
+                                 ctypes.byref(n))
+    if st not in (0, ERR_CAPACITY):
+        raise CuflyeError(st, "compact binary payload")
+    out = np.zeros(n.value, dtype=np.uint8)
+    st = L.cuflye_compact_binary(rec.ctypes.data, len(rec), len(inp), _ptr(inp, _u64p),
+                                 out.ctypes.data, len(out), ctypes.byref(n))
+    if st != 0:
+        raise CuflyeError(st, "compact binary payload")
+    return out.tobytes()

@@ -2,6 +2,7 @@
 // (candidate-record-v1 / overlap-range-v1 fields), so results leave the GPU
 // in their final layout with one D2H copy.
 #include <cstdint>
+#include <cstring>
 
 #include "../../include/cuflye.h"
 #include "kernels.h"
@@ -108,6 +109,68 @@ cudaError_t filtered_to_abi(const int32_t* fpos, uint64_t n, const uint64_t* f_o
   count_launch();
   filtered_abi_kernel<<<grid(n, 256), 256, 0, s>>>(fpos, n, f_off, nq, qinfo, out);
   return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- compact payload
+// Fields are stored byte by byte, least significant first, so the payload is
+// the same on any host (docs/abi/read-alignment-compact-binary-v0.md: "not a
+// raw C++ struct dump").
+namespace {
+unsigned char* put_u32(unsigned char* p, uint32_t v) {
+  for (int i = 0; i < 4; ++i) *p++ = static_cast<unsigned char>((v >> (8 * i)) & 0xffu);
+  return p;
+}
+unsigned char* put_u64(unsigned char* p, uint64_t v) {
+  for (int i = 0; i < 8; ++i) *p++ = static_cast<unsigned char>((v >> (8 * i)) & 0xffu);
+  return p;
+}
+unsigned char* put_i32(unsigned char* p, int32_t v) { return put_u32(p, static_cast<uint32_t>(v)); }
+unsigned char* put_i64(unsigned char* p, int64_t v) { return put_u64(p, static_cast<uint64_t>(v)); }
+unsigned char* put_f32(unsigned char* p, float v) {
+  uint32_t bits;
+  std::memcpy(&bits, &v, sizeof(bits));
+  return put_u32(p, bits);
+}
+}  // namespace
+
+void compact_write_header(unsigned char* out, uint64_t fixtures, uint64_t records,
+                          uint64_t total_inputs, uint32_t min_inputs, uint32_t max_inputs) {
+  static const char kMagic[8] = {'C', 'U', 'F', 'R', 'A', 'L', 'B', '0'};
+  std::memcpy(out, kMagic, 8);
+  unsigned char* p = out + 8;
+  p = put_u32(p, CUFLYE_COMPACT_HEADER_BYTES);
+  p = put_u32(p, CUFLYE_COMPACT_RECORD_BYTES);
+  p = put_u32(p, 0);  // version major
+  p = put_u32(p, 0);  // version minor
+  p = put_u64(p, fixtures);
+  p = put_u64(p, records);
+  p = put_u64(p, total_inputs);
+  p = put_u32(p, min_inputs);
+  p = put_u32(p, max_inputs);
+  p = put_u32(p, 1);  // output mode: pre-divergence chains
+  put_u32(p, 0);      // reserved
+}
+
+void compact_write_record(unsigned char* out, const cuflye_chain_record& r) {
+  unsigned char* p = out;
+  p = put_i64(p, r.query_id);
+  p = put_i32(p, r.chain_id);
+  p = put_i32(p, r.segment_id);
+  p = put_i32(p, r.overlap_index);
+  p = put_i64(p, r.candidate_id);
+  p = put_i64(p, r.read_id);
+  p = put_i32(p, r.read_begin);
+  p = put_i32(p, r.read_end);
+  p = put_i32(p, r.read_len);
+  p = put_i64(p, r.edge_id);
+  p = put_i32(p, r.edge_left);
+  p = put_i32(p, r.edge_right);
+  p = put_i64(p, r.edge_seq_id);
+  p = put_i32(p, r.edge_begin);
+  p = put_i32(p, r.edge_end);
+  p = put_i32(p, r.edge_len);
+  p = put_i32(p, r.score);
+  put_f32(p, r.seq_divergence);
 }
 
 }  // namespace cuflye

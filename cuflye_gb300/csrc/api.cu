@@ -1147,6 +1147,8 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp,
   const uint32_t npool = read_scalar(c, pool_count);
   OverlapRow* rows = buf<OverlapRow>(c, "o_rows", R);
   CUFLYE_CHECK(rows_scatter(pool, npool, kept, kept_off, rows, st));
+  // each query's first row (rows are in query order)
+  CUFLYE_CHECK(gather_query_offsets(qg, kept_off, nq, buf<uint64_t>(c, "o_qrowoff", nq + 1), st));
   if (rows_per_query) {
     uint64_t* qrows = buf<uint64_t>(c, "o_qrows", nq);
     CUFLYE_CHECK(query_row_counts(qg, kept_off, nq, qrows, st));
@@ -1675,6 +1677,159 @@ cuflye_status cuflye_graph_set(cuflye_ctx* c, size_t ne, const int64_t* edge_ids
   CUFLYE_API_END(c)
 }
 
+}  // extern "C"
+
+namespace {
+
+// Device state of one pass's read-to-graph chain stage.
+struct R2GPass {
+  uint32_t nq = 0;
+  uint64_t A = 0;                // chain-input rows
+  OverlapRow* rows = nullptr;    // chain input, per read in curBegin order
+  R2GRowMeta* meta = nullptr;
+  uint64_t* a_off = nullptr;     // nq + 1
+  void* recs = nullptr;
+  int32_t* cand = nullptr;
+  uint32_t* n_cand = nullptr;
+  int64_t* read_ids = nullptr;   // nq
+};
+
+R2GParams to_r2g_params(const cuflye_r2g_params* r2g) {
+  return R2GParams{r2g->max_jump,       r2g->max_read_overlap, r2g->min_overlap,
+                   r2g->max_separation, r2g->long_edge,        r2g->big_aln,
+                   r2g->max_chain_divergence};
+}
+
+void check_r2g(cuflye_ctx* c, const cuflye_r2g_params* r2g) {
+  if (!c->has_graph) throw Error(CUFLYE_ERR_INVALID, "no graph: call cuflye_graph_set");
+  if (!r2g) throw Error(CUFLYE_ERR_INVALID, "r2g params must not be null");
+}
+
+// Buffers of the chain stage for A rows of nq reads.
+void r2g_alloc(cuflye_ctx* c, R2GPass& rp2, uint64_t A, uint32_t nq) {
+  rp2.nq = nq;
+  rp2.A = A;
+  rp2.meta = buf<R2GRowMeta>(c, "r_meta", A);
+  rp2.recs = buf<uint8_t>(c, "r_recs", A * r2g_rec_bytes());
+  rp2.cand = buf<int32_t>(c, "r_cand", A);
+  rp2.n_cand = buf<uint32_t>(c, "r_ncand", nq);
+  rp2.read_ids = buf<int64_t>(c, "r_ids", nq);
+}
+
+// quickSeqOverlaps rows of the pass -> the LONG_EDGE / BIG_ALN filter -> the
+// curBegin sort -> candidate chains.
+R2GPass r2g_candidates(cuflye_ctx* c, PassState& ps, const ChainParams& cp, const R2GParams& rp,
+                       const int64_t* ids) {
+  cudaStream_t st = c->stream;
+  const uint64_t R = run_chain(c, ps, cp);
+  const uint32_t nq = ps.nq;
+  const uint32_t ns = c->idx.nslots;
+  R2GGraph g{buf<int64_t>(c, "gr_edge", ns), buf<int32_t>(c, "gr_left", ns),
+             buf<int32_t>(c, "gr_right", ns), c->idx.slot_signed};
+  OverlapRow* rows = buf<OverlapRow>(c, "o_rows", R);
+  const uint64_t* row_off = buf<uint64_t>(c, "o_qrowoff", nq + 1);
+  uint32_t* keep = buf<uint32_t>(c, "r_keep", R);
+  uint64_t* kpos = buf<uint64_t>(c, "r_kpos", R + 1);
+  CUFLYE_CHECK(r2g_filter(rows, R, rp, keep, st));
+  const uint64_t A = scan_u32(c, keep, kpos, R, "r_scan");
+  OverlapRow* aln = buf<OverlapRow>(c, "r_aln", A);
+  uint64_t* src = buf<uint64_t>(c, "r_src", A);
+  CUFLYE_CHECK(r2g_compact(rows, R, keep, kpos, aln, src, st));
+  R2GPass out;
+  r2g_alloc(c, out, A, nq);
+  // each read's first kept row: the kept-row scan at the read's first row
+  out.a_off = buf<uint64_t>(c, "r_aoff", nq + 1);
+  CUFLYE_CHECK(gather_query_offsets(row_off, kpos, nq, out.a_off, st));
+  uint64_t* skeys = buf<uint64_t>(c, "r_skeys", A);
+  uint32_t* svals = buf<uint32_t>(c, "r_svals", A);
+  CUFLYE_CHECK(r2g_sort_keys(aln, out.a_off, nq, skeys, svals, st));
+  uint32_t* sl = buf<uint32_t>(c, "r_sl", A + 1);
+  uint32_t* sr = buf<uint32_t>(c, "r_sr", A + 1);
+  uint32_t* slists = buf<uint32_t>(c, "r_slists", 4ull * nq);
+  uint32_t* scounts = buf<uint32_t>(c, "r_scounts", 16);
+  CUFLYE_CHECK(segmented_std_sort(skeys, svals, sl, sr, out.a_off, out.a_off + 1, nq, nullptr,
+                                  slists, scounts, c->num_sms, st, sort_tasks(c, "r", A, nq)));
+  out.rows = buf<OverlapRow>(c, "r_sorted", A);
+  CUFLYE_CHECK(r2g_permute(aln, out.a_off, nq, svals, src, row_off, g, out.rows, out.meta, st));
+  CUFLYE_CHECK(cudaMemcpyAsync(out.read_ids, ids, nq * sizeof(int64_t), cudaMemcpyHostToDevice,
+                               st));
+  CUFLYE_CHECK(r2g_chain(out.rows, out.a_off, nq, out.meta, rp, out.recs,
+                         buf<int32_t>(c, "r_act", A), buf<int32_t>(c, "r_frz", A), out.cand,
+                         out.n_cand, st));
+  return out;
+}
+
+// Exclusive scan of n 32-bit counts on the device; the offsets are also
+// returned on the host (n + 1 entries, starting at base).
+std::vector<uint64_t> host_offsets(cuflye_ctx* c, const uint32_t* counts, uint32_t n,
+                                   uint64_t base = 0) {
+  std::vector<uint32_t> h(n);
+  if (n) CUFLYE_CHECK(cudaMemcpyAsync(h.data(), counts, n * 4ull, cudaMemcpyDeviceToHost,
+                                      c->stream));
+  sync(c);
+  std::vector<uint64_t> off(n + 1);
+  off[0] = base;
+  for (uint32_t i = 0; i < n; ++i) off[i + 1] = off[i] + h[i];
+  return off;
+}
+
+uint64_t* upload(cuflye_ctx* c, const char* name, const std::vector<uint64_t>& v) {
+  uint64_t* d = buf<uint64_t>(c, name, v.size());
+  CUFLYE_CHECK(cudaMemcpyAsync(d, v.data(), v.size() * 8ull, cudaMemcpyHostToDevice, c->stream));
+  return d;
+}
+
+// Divergence + accept of the pass's candidate chains, then the kept chains
+// and their complements as rows (chain ids from chain_base).  Returns the
+// rows; they stay in "r_out".
+uint64_t r2g_good_rows(cuflye_ctx* c, R2GPass& r, const R2GParams& rp, const float* div_in,
+                       const uint64_t* div_off, float* div_out, uint8_t* acc_out,
+                       uint64_t& chain_base) {
+  cudaStream_t st = c->stream;
+  const uint32_t nq = r.nq;
+  int32_t* good = buf<int32_t>(c, "r_good", r.A);
+  uint32_t* n_good = buf<uint32_t>(c, "r_ngood", nq);
+  uint32_t* n_rows = buf<uint32_t>(c, "r_nrows", nq);
+  CUFLYE_CHECK(r2g_divergence(r.rows, r.a_off, nq, r.recs, r.cand, r.n_cand, div_in, div_off, rp,
+                              div_out, acc_out, good, n_good, n_rows, nullptr, st));
+  uint64_t* row_off = buf<uint64_t>(c, "r_rowoff", nq + 1);
+  const uint64_t nrows = scan_u32(c, n_rows, row_off, nq, "r_scan");
+  // chain ids: two per good chain (the chain and its complement)
+  std::vector<uint64_t> coff = host_offsets(c, n_good, nq, 0);
+  for (auto& v : coff) v = chain_base + 2 * v;
+  uint64_t* d_coff = upload(c, "r_coff", coff);
+  cuflye_read_alignment* d_out = buf<cuflye_read_alignment>(c, "r_out", nrows);
+  int32_t* tmp = buf<int32_t>(c, "r_tmp", r.A);
+  CUFLYE_CHECK(r2g_emit(r.rows, r.a_off, nq, r.meta, r.read_ids, r.recs, good, n_good, d_coff,
+                        row_off, tmp, d_out, st));
+  chain_base = coff[nq];
+  return nrows;
+}
+
+// The pass's candidate chains as chain records (in "r_records"); returns their
+// number.  query_ids (device, nq) name the fixtures.
+uint64_t r2g_chain_records(cuflye_ctx* c, R2GPass& r, const R2GParams& rp,
+                           const int64_t* query_ids) {
+  cudaStream_t st = c->stream;
+  const uint32_t nq = r.nq;
+  uint32_t* n_good = buf<uint32_t>(c, "r_ngood", nq);
+  uint32_t* n_rows = buf<uint32_t>(c, "r_nrows", nq);
+  uint32_t* n_segs = buf<uint32_t>(c, "r_nsegs", nq);
+  CUFLYE_CHECK(r2g_divergence(r.rows, r.a_off, nq, r.recs, r.cand, r.n_cand, nullptr, nullptr, rp,
+                              nullptr, nullptr, buf<int32_t>(c, "r_good", r.A), n_good, n_rows,
+                              n_segs, st));
+  uint64_t* rec_off = buf<uint64_t>(c, "r_recoff", nq + 1);
+  const uint64_t nrec = scan_u32(c, n_segs, rec_off, nq, "r_scan");
+  cuflye_chain_record* d = buf<cuflye_chain_record>(c, "r_records", nrec);
+  CUFLYE_CHECK(r2g_records(r.rows, r.a_off, nq, r.meta, query_ids, r.read_ids, r.recs, r.cand,
+                           r.n_cand, rec_off, d, st));
+  return nrec;
+}
+
+}  // namespace
+
+extern "C" {
+
 cuflye_status cuflye_read_to_graph(cuflye_ctx* c, size_t n, const int64_t* ids,
                                    const int64_t* offsets, const char* bases,
                                    const cuflye_overlap_params* params,
@@ -1684,91 +1839,29 @@ cuflye_status cuflye_read_to_graph(cuflye_ctx* c, size_t n, const int64_t* ids,
   CUFLYE_CHECK(cudaSetDevice(c->device));
   require_index(c);
   check_params(c, params);
-  if (!c->has_graph) throw Error(CUFLYE_ERR_INVALID, "no graph: call cuflye_graph_set");
-  if (!r2g) throw Error(CUFLYE_ERR_INVALID, "r2g params must not be null");
+  check_r2g(c, r2g);
+  if (!ids || !offsets || (!bases && n)) throw Error(CUFLYE_ERR_INVALID, "null input");
   reset_timing(c);
   const ChainParams cp = to_chain_params(params);
-  R2GParams rp{r2g->max_jump,       r2g->max_read_overlap, r2g->min_overlap,
-               r2g->max_separation, r2g->long_edge,        r2g->big_aln,
-               r2g->max_chain_divergence};
-  const uint32_t ns = c->idx.nslots;
-  R2GGraph g{buf<int64_t>(c, "gr_edge", ns), buf<int32_t>(c, "gr_left", ns),
-             buf<int32_t>(c, "gr_right", ns), c->idx.slot_signed};
+  const R2GParams rp = to_r2g_params(r2g);
   Queries Q{n, ids, offsets, bases};
   size_t total = 0;
   uint64_t chain_base = 0;
   bool overflow = false;
-  for_each_pass(c, Q, false, kChainBytesPerHit, [&](size_t, size_t, PassState& ps) {
-    cudaStream_t st = c->stream;
-    const uint64_t R = run_chain(c, ps, cp);
-    const uint32_t nq = ps.nq;
-    OverlapRow* rows = buf<OverlapRow>(c, "o_rows", R);
-    uint32_t* keep = buf<uint32_t>(c, "r_keep", R);
-    uint64_t* kpos = buf<uint64_t>(c, "r_kpos", R + 1);
-    CUFLYE_CHECK(r2g_filter(rows, R, rp, keep, st));
-    const uint64_t A = scan_u32(c, keep, kpos, R, "r_scan");
-    OverlapRow* aln = buf<OverlapRow>(c, "r_aln", A);
-    CUFLYE_CHECK(r2g_compact(rows, R, keep, kpos, aln, st));
-    // per-read alignment offsets: rows are in read order
-    {
-      std::vector<OverlapRow> tmp(R);
-      if (R) CUFLYE_CHECK(cudaMemcpyAsync(tmp.data(), rows, R * sizeof(OverlapRow),
-                                          cudaMemcpyDeviceToHost, st));
-      std::vector<uint32_t> hkeep(R);
-      if (R) CUFLYE_CHECK(cudaMemcpyAsync(hkeep.data(), keep, R * 4ull, cudaMemcpyDeviceToHost, st));
-      sync(c);
-      std::vector<uint64_t> a_off(nq + 1, 0);
-      for (uint64_t i = 0; i < R; ++i)
-        if (hkeep[i]) a_off[tmp[i].query + 1] += 1;
-      for (uint32_t q = 0; q < nq; ++q) a_off[q + 1] += a_off[q];
-      uint64_t* d_aoff = buf<uint64_t>(c, "r_aoff", nq + 1);
-      CUFLYE_CHECK(cudaMemcpyAsync(d_aoff, a_off.data(), (nq + 1) * 8ull, cudaMemcpyHostToDevice,
-                                   st));
-    }
-    uint64_t* d_aoff = buf<uint64_t>(c, "r_aoff", nq + 1);
-    uint64_t* skeys = buf<uint64_t>(c, "r_skeys", A);
-    uint32_t* svals = buf<uint32_t>(c, "r_svals", A);
-    CUFLYE_CHECK(r2g_sort_keys(aln, d_aoff, nq, skeys, svals, st));
-    uint32_t* sl = buf<uint32_t>(c, "r_sl", A + 1);
-    uint32_t* sr = buf<uint32_t>(c, "r_sr", A + 1);
-    uint32_t* slists = buf<uint32_t>(c, "r_slists", 4ull * nq);
-    uint32_t* scounts = buf<uint32_t>(c, "r_scounts", 16);
-    CUFLYE_CHECK(segmented_std_sort(skeys, svals, sl, sr, d_aoff, d_aoff + 1, nq, nullptr, slists,
-                                    scounts, c->num_sms, st, sort_tasks(c, "r", A, nq)));
-    OverlapRow* sorted = buf<OverlapRow>(c, "r_sorted", A);
-    CUFLYE_CHECK(r2g_permute(aln, d_aoff, nq, svals, sorted, st));
-    void* recs = buf<uint8_t>(c, "r_recs", A * r2g_rec_bytes());
-    int32_t* act = buf<int32_t>(c, "r_act", A);
-    int32_t* frz = buf<int32_t>(c, "r_frz", A);
-    int32_t* good = buf<int32_t>(c, "r_good", A);
-    uint32_t* n_good = buf<uint32_t>(c, "r_ngood", nq);
-    uint32_t* n_rows = buf<uint32_t>(c, "r_nrows", nq);
-    CUFLYE_CHECK(r2g_chain(sorted, d_aoff, nq, g, rp, recs, act, frz, good, n_good, n_rows, st));
-    uint64_t* row_off = buf<uint64_t>(c, "r_rowoff", nq + 1);
-    const uint64_t nrows = scan_u32(c, n_rows, row_off, nq, "r_scan");
-    // chain ids: 2 * good chains per read
-    std::vector<uint32_t> hg(nq);
-    if (nq) CUFLYE_CHECK(cudaMemcpyAsync(hg.data(), n_good, nq * 4ull, cudaMemcpyDeviceToHost, st));
-    sync(c);
-    std::vector<uint64_t> coff(nq + 1);
-    coff[0] = chain_base;
-    for (uint32_t q = 0; q < nq; ++q) coff[q + 1] = coff[q] + 2ull * hg[q];
-    uint64_t* d_coff = buf<uint64_t>(c, "r_coff", nq + 1);
-    CUFLYE_CHECK(cudaMemcpyAsync(d_coff, coff.data(), (nq + 1) * 8ull, cudaMemcpyHostToDevice, st));
-    cuflye_read_alignment* d_out = buf<cuflye_read_alignment>(c, "r_out", nrows);
-    int32_t* tmp = buf<int32_t>(c, "r_tmp", A);
-    CUFLYE_CHECK(r2g_emit(sorted, d_aoff, nq, g, ps.qinfo, recs, good, n_good, d_coff, row_off,
-                          tmp, d_out, st));
+  for_each_pass(c, Q, false, kChainBytesPerHit, [&](size_t q0, size_t, PassState& ps) {
+    R2GPass r = r2g_candidates(c, ps, cp, rp, ids + q0);
+    const uint64_t nrows =
+        r2g_good_rows(c, r, rp, nullptr, nullptr, nullptr, nullptr, chain_base);
     if (!overflow && total + nrows <= out_cap) {
       if (nrows)
-        CUFLYE_CHECK(cudaMemcpyAsync(out + total, d_out, nrows * sizeof(cuflye_read_alignment),
-                                     cudaMemcpyDeviceToHost, st));
+        CUFLYE_CHECK(cudaMemcpyAsync(out + total, buf<cuflye_read_alignment>(c, "r_out", nrows),
+                                     nrows * sizeof(cuflye_read_alignment),
+                                     cudaMemcpyDeviceToHost, c->stream));
     } else {
       overflow = true;
     }
-    CUFLYE_CHECK(cudaEventRecord(c->ev[4], st));
+    CUFLYE_CHECK(cudaEventRecord(c->ev[4], c->stream));
     total += nrows;
-    chain_base = coff[nq];
     accumulate_timing(c, true);
   });
   if (n_out) *n_out = total;
@@ -1776,6 +1869,192 @@ cuflye_status cuflye_read_to_graph(cuflye_ctx* c, size_t n, const int64_t* ids,
     throw Error(CUFLYE_ERR_CAPACITY,
                 "output capacity too small: need " + std::to_string(total) + " alignment rows");
   CUFLYE_API_END(c)
+}
+
+cuflye_status cuflye_read_to_graph_chains(cuflye_ctx* c, size_t n, const int64_t* ids,
+                                          const int64_t* offsets, const char* bases,
+                                          const cuflye_overlap_params* params,
+                                          const cuflye_r2g_params* r2g,
+                                          cuflye_chain_record* out, size_t out_cap,
+                                          size_t* n_out, uint64_t* inputs_per_read) {
+  CUFLYE_API_BEGIN(c)
+  CUFLYE_CHECK(cudaSetDevice(c->device));
+  require_index(c);
+  check_params(c, params);
+  check_r2g(c, r2g);
+  if (!ids || !offsets || (!bases && n)) throw Error(CUFLYE_ERR_INVALID, "null input");
+  reset_timing(c);
+  const ChainParams cp = to_chain_params(params);
+  const R2GParams rp = to_r2g_params(r2g);
+  Queries Q{n, ids, offsets, bases};
+  size_t total = 0;
+  bool overflow = false;
+  for_each_pass(c, Q, false, kChainBytesPerHit, [&](size_t q0, size_t, PassState& ps) {
+    R2GPass r = r2g_candidates(c, ps, cp, rp, ids + q0);
+    const uint64_t nrec = r2g_chain_records(c, r, rp, r.read_ids);
+    if (!overflow && total + nrec <= out_cap) {
+      if (nrec)
+        CUFLYE_CHECK(cudaMemcpyAsync(out + total, buf<cuflye_chain_record>(c, "r_records", nrec),
+                                     nrec * sizeof(cuflye_chain_record), cudaMemcpyDeviceToHost,
+                                     c->stream));
+    } else {
+      overflow = true;
+    }
+    if (inputs_per_read) {
+      std::vector<uint64_t> a(r.nq + 1);
+      CUFLYE_CHECK(cudaMemcpyAsync(a.data(), r.a_off, (r.nq + 1) * 8ull, cudaMemcpyDeviceToHost,
+                                   c->stream));
+      sync(c);
+      for (uint32_t q = 0; q < r.nq; ++q) inputs_per_read[q0 + q] = a[q + 1] - a[q];
+    }
+    CUFLYE_CHECK(cudaEventRecord(c->ev[4], c->stream));
+    total += nrec;
+    accumulate_timing(c, true);
+  });
+  if (n_out) *n_out = total;
+  if (overflow)
+    throw Error(CUFLYE_ERR_CAPACITY,
+                "output capacity too small: need " + std::to_string(total) + " chain records");
+  CUFLYE_API_END(c)
+}
+
+cuflye_status cuflye_chain_read_alignments(
+    cuflye_ctx* c, size_t n_fixtures, const uint64_t* fixture_offsets, const int64_t* query_ids,
+    const cuflye_edge_overlap* overlaps, const cuflye_r2g_params* r2g, const float* chain_div_in,
+    size_t n_chain_div_in, cuflye_chain_record* out, size_t out_cap, size_t* n_out,
+    float* chain_div, uint8_t* chain_kept, size_t chain_cap, size_t* n_chains,
+    cuflye_read_alignment* kept_rows, size_t rows_cap, size_t* n_rows) {
+  CUFLYE_API_BEGIN(c)
+  CUFLYE_CHECK(cudaSetDevice(c->device));
+  if (!r2g) throw Error(CUFLYE_ERR_INVALID, "r2g params must not be null");
+  if (n_fixtures && (!fixture_offsets || !query_ids))
+    throw Error(CUFLYE_ERR_INVALID, "null input");
+  if (n_fixtures >= (1ull << 31)) throw Error(CUFLYE_ERR_UNSUPPORTED, "too many fixtures");
+  const uint64_t total_rows = n_fixtures ? fixture_offsets[n_fixtures] : 0;
+  if (total_rows && !overlaps) throw Error(CUFLYE_ERR_INVALID, "null overlaps");
+  for (size_t f = 0; f < n_fixtures; ++f) {
+    if (fixture_offsets[f + 1] < fixture_offsets[f])
+      throw Error(CUFLYE_ERR_INVALID, "fixture offsets must not decrease");
+    if (fixture_offsets[f + 1] - fixture_offsets[f] >= (1ull << 31))
+      throw Error(CUFLYE_ERR_UNSUPPORTED, "fixture longer than 2^31 overlaps");
+  }
+  if (fixture_offsets && n_fixtures && fixture_offsets[0] != 0)
+    throw Error(CUFLYE_ERR_INVALID, "fixture offsets must start at 0");
+  reset_timing(c);
+  const R2GParams rp = to_r2g_params(r2g);
+  cudaStream_t st = c->stream;
+  const uint32_t nq = static_cast<uint32_t>(n_fixtures);
+  R2GPass r;
+  r2g_alloc(c, r, total_rows, nq);
+  r.rows = buf<OverlapRow>(c, "r_sorted", total_rows);
+  cuflye_edge_overlap* d_in = buf<cuflye_edge_overlap>(c, "r_replay_in", total_rows);
+  if (total_rows)
+    CUFLYE_CHECK(cudaMemcpyAsync(d_in, overlaps, total_rows * sizeof(cuflye_edge_overlap),
+                                 cudaMemcpyHostToDevice, st));
+  r.a_off = upload(c, "r_aoff", std::vector<uint64_t>(fixture_offsets, fixture_offsets + nq + 1));
+  // a fixture's read id: its first overlap's (the query id when it has none)
+  std::vector<int64_t> rids(nq);
+  for (uint32_t f = 0; f < nq; ++f)
+    rids[f] = fixture_offsets[f + 1] > fixture_offsets[f] ? overlaps[fixture_offsets[f]].read_id
+                                                          : query_ids[f];
+  if (nq)
+    CUFLYE_CHECK(cudaMemcpyAsync(r.read_ids, rids.data(), nq * 8ull, cudaMemcpyHostToDevice, st));
+  int64_t* d_qids = buf<int64_t>(c, "r_qids", nq);
+  if (nq)
+    CUFLYE_CHECK(cudaMemcpyAsync(d_qids, query_ids, nq * 8ull, cudaMemcpyHostToDevice, st));
+  CUFLYE_CHECK(r2g_replay_rows(d_in, total_rows, r.rows, r.meta, st));
+  CUFLYE_CHECK(r2g_chain(r.rows, r.a_off, nq, r.meta, rp, r.recs,
+                         buf<int32_t>(c, "r_act", total_rows), buf<int32_t>(c, "r_frz", total_rows),
+                         r.cand, r.n_cand, st));
+  // candidate chains per fixture
+  const std::vector<uint64_t> coff = host_offsets(c, r.n_cand, nq);
+  const uint64_t nchains = coff[nq];
+  if (n_chains) *n_chains = nchains;
+  if (chain_div_in && n_chain_div_in != nchains)
+    throw Error(CUFLYE_ERR_INVALID, "chain divergences: " + std::to_string(n_chain_div_in) +
+                                        " given for " + std::to_string(nchains) +
+                                        " candidate chains");
+  uint64_t* d_coff = upload(c, "r_divoff", coff);
+  float* d_divin = nullptr;
+  if (chain_div_in) {
+    d_divin = buf<float>(c, "r_divin", nchains);
+    if (nchains)
+      CUFLYE_CHECK(cudaMemcpyAsync(d_divin, chain_div_in, nchains * 4ull, cudaMemcpyHostToDevice,
+                                   st));
+  }
+  float* d_div = buf<float>(c, "r_div", total_rows);
+  uint8_t* d_acc = buf<uint8_t>(c, "r_acc", total_rows);
+  uint64_t chain_base = 0;
+  const uint64_t nrows = r2g_good_rows(c, r, rp, d_divin, d_coff, d_div, d_acc, chain_base);
+  const uint64_t nrec = r2g_chain_records(c, r, rp, d_qids);
+  // the per-chain values, compacted from per-fixture slots into chain order
+  std::vector<float> hdiv(total_rows);
+  std::vector<uint8_t> hacc(total_rows);
+  if (total_rows) {
+    CUFLYE_CHECK(cudaMemcpyAsync(hdiv.data(), d_div, total_rows * 4ull, cudaMemcpyDeviceToHost,
+                                 st));
+    CUFLYE_CHECK(cudaMemcpyAsync(hacc.data(), d_acc, total_rows, cudaMemcpyDeviceToHost, st));
+  }
+  bool short_buf = false;
+  if (nrec <= out_cap) {
+    if (nrec && out)
+      CUFLYE_CHECK(cudaMemcpyAsync(out, buf<cuflye_chain_record>(c, "r_records", nrec),
+                                   nrec * sizeof(cuflye_chain_record), cudaMemcpyDeviceToHost,
+                                   st));
+  } else {
+    short_buf = true;
+  }
+  if (kept_rows && nrows <= rows_cap) {
+    if (nrows)
+      CUFLYE_CHECK(cudaMemcpyAsync(kept_rows, buf<cuflye_read_alignment>(c, "r_out", nrows),
+                                   nrows * sizeof(cuflye_read_alignment), cudaMemcpyDeviceToHost,
+                                   st));
+  } else if (kept_rows) {
+    short_buf = true;
+  }
+  sync(c);
+  if (nchains > chain_cap && (chain_div || chain_kept)) short_buf = true;
+  if (!short_buf) {
+    for (uint32_t f = 0; f < nq; ++f) {
+      for (uint64_t t = 0; t < coff[f + 1] - coff[f]; ++t) {
+        const uint64_t from = fixture_offsets[f] + t;
+        if (chain_div) chain_div[coff[f] + t] = hdiv[from];
+        if (chain_kept) chain_kept[coff[f] + t] = hacc[from];
+      }
+    }
+  }
+  if (n_out) *n_out = nrec;
+  if (n_rows) *n_rows = nrows;
+  if (short_buf)
+    throw Error(CUFLYE_ERR_CAPACITY, "output capacity too small: need " + std::to_string(nrec) +
+                                         " chain records, " + std::to_string(nchains) +
+                                         " chains, " + std::to_string(nrows) + " rows");
+  CUFLYE_API_END(c)
+}
+
+cuflye_status cuflye_compact_binary(const cuflye_chain_record* records, size_t n_records,
+                                    size_t fixtures, const uint64_t* inputs_per_fixture,
+                                    unsigned char* out, size_t out_cap, size_t* n_out) {
+  if ((!records && n_records) || (!inputs_per_fixture && fixtures) || !n_out)
+    return CUFLYE_ERR_INVALID;
+  const uint64_t bytes = CUFLYE_COMPACT_HEADER_BYTES +
+                         static_cast<uint64_t>(n_records) * CUFLYE_COMPACT_RECORD_BYTES;
+  *n_out = static_cast<size_t>(bytes);
+  if (!out || out_cap < bytes) return CUFLYE_ERR_CAPACITY;
+  uint64_t total = 0, mn = 0, mx = 0;
+  for (size_t f = 0; f < fixtures; ++f) {
+    const uint64_t v = inputs_per_fixture[f];
+    total += v;
+    mn = f == 0 ? v : std::min(mn, v);
+    mx = std::max(mx, v);
+  }
+  if (mx > 0xffffffffull) return CUFLYE_ERR_UNSUPPORTED;
+  compact_write_header(out, fixtures, n_records, total, static_cast<uint32_t>(mn),
+                       static_cast<uint32_t>(mx));
+  for (size_t i = 0; i < n_records; ++i)
+    compact_write_record(out + CUFLYE_COMPACT_HEADER_BYTES + i * CUFLYE_COMPACT_RECORD_BYTES,
+                         records[i]);
+  return CUFLYE_OK;
 }
 
 cuflye_status cuflye_std_sort_segments(cuflye_ctx* c, uint64_t* keys, uint32_t* values,

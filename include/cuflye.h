@@ -278,6 +278,98 @@ cuflye_status cuflye_read_to_graph(cuflye_ctx* ctx, size_t n, const int64_t* rea
                                    size_t out_cap, size_t* n_out);
 
 /* --------------------------------------------------------------------------
+ * Candidate chains before the divergence filter (Flye's readChains,
+ * patches/flye/2.9.6/0026-cuflye-read-alignment-replay-fixture-dump.patch:215-226)
+ * as the records of the compact binary payload
+ * (docs/abi/read-alignment-compact-binary-v0.md:37-58; the reference writes
+ * them in cuda/cuflye_cuda_read_alignment_chain_replay.cu:2575-2660).  Per
+ * read (fixture): chains in acceptance order, segments in chain order.
+ * overlap_index is the segment's position in the read's chain input (its
+ * edge overlaps after the LONG_EDGE / BIG_ALN filter and the curBegin sort);
+ * candidate_id is the replay fixture's candidate id, or for in-process reads
+ * the overlap's index among the read's quickSeqOverlaps rows before the
+ * filter.  query_id is the fixture's query id (in-process: the read id).
+ * ------------------------------------------------------------------------ */
+typedef struct cuflye_chain_record {
+  int64_t query_id;
+  int32_t chain_id;
+  int32_t segment_id;
+  int32_t overlap_index;
+  int32_t reserved;
+  int64_t candidate_id;
+  int64_t read_id;
+  int64_t edge_id;
+  int64_t edge_seq_id;
+  int32_t read_begin, read_end, read_len;
+  int32_t edge_left, edge_right;
+  int32_t edge_begin, edge_end, edge_len;
+  int32_t score;
+  float seq_divergence;
+} cuflye_chain_record;
+
+/* Read-to-graph up to the candidate chains: quickSeqOverlaps against the edge
+ * index, the LONG_EDGE / BIG_ALN filter, the curBegin sort and
+ * chainReadAlignments, for each read; the candidate chains as chain records.
+ * inputs_per_read (optional, n entries) receives each read's chain-input
+ * overlaps (the payload header's input record counts). */
+cuflye_status cuflye_read_to_graph_chains(cuflye_ctx* ctx, size_t n, const int64_t* read_ids,
+                                          const int64_t* offsets, const char* bases,
+                                          const cuflye_overlap_params* params,
+                                          const cuflye_r2g_params* r2g,
+                                          cuflye_chain_record* out, size_t out_cap,
+                                          size_t* n_out, uint64_t* inputs_per_read);
+
+/* Read-alignment replay fixtures (docs/abi/read-alignment-replay-fixture-v0.md):
+ * the GPU path of cuda/cuflye_cuda_read_alignment_chain_replay.cu:1044-1253.
+ * Fixture f is one read's chain input, overlaps[fixture_offsets[f] ..
+ * fixture_offsets[f + 1]) in edge-overlaps.tsv order, with query id
+ * query_ids[f].  The call chains every fixture on the device and returns its
+ * candidate chains as chain records, and per candidate chain (fixture by
+ * fixture, chains in acceptance order) its divergence and whether it is kept
+ * (divergence < r2g->max_chain_divergence, Flye's read_align_ovlp_divergence
+ * test).  With chain_div_in == NULL the divergence is this library's k-mer
+ * form (the curRange-weighted mean of the segments' divergences, summed in
+ * chain order in float); otherwise chain_div_in holds one value per candidate
+ * chain (chain-divergence.tsv, fixture by fixture) and n_chain_div_in must
+ * equal the number of candidate chains, else CUFLYE_ERR_INVALID with that
+ * number in *n_chains.  kept_rows (optional) receives the read-alignment
+ * rows of the kept chains and their complements (read-alignment-v1, chain
+ * ids numbered across fixtures), as cuflye_read_to_graph emits them. */
+typedef struct cuflye_edge_overlap {
+  int64_t candidate_id;
+  int64_t read_id;
+  int32_t read_begin, read_end, read_len;
+  int32_t edge_left, edge_right;
+  int32_t edge_begin, edge_end, edge_len;
+  int64_t edge_id;
+  int64_t edge_seq_id;
+  int32_t score;
+  float seq_divergence;
+} cuflye_edge_overlap;
+
+cuflye_status cuflye_chain_read_alignments(
+    cuflye_ctx* ctx, size_t n_fixtures, const uint64_t* fixture_offsets,
+    const int64_t* query_ids, const cuflye_edge_overlap* overlaps,
+    const cuflye_r2g_params* r2g, const float* chain_div_in, size_t n_chain_div_in,
+    cuflye_chain_record* out, size_t out_cap, size_t* n_out, float* chain_div,
+    uint8_t* chain_kept, size_t chain_cap, size_t* n_chains, cuflye_read_alignment* kept_rows,
+    size_t rows_cap, size_t* n_rows);
+
+/* The compact binary payload (docs/abi/read-alignment-compact-binary-v0.md):
+ * a 64-byte header (magic CUFRALB0, sizes, version 0.0, fixture count,
+ * record count, input record totals, output mode 1 = pre-divergence chains)
+ * and one 92-byte little-endian record per chain record, written into the
+ * caller's buffer (host code only, no device).  fixtures: the reads or
+ * fixtures the records come from; inputs_per_fixture: each one's chain-input
+ * overlaps (for the header's total, minimum and maximum).  out_cap too small:
+ * CUFLYE_ERR_CAPACITY with the payload size in *n_out. */
+#define CUFLYE_COMPACT_HEADER_BYTES 64u
+#define CUFLYE_COMPACT_RECORD_BYTES 92u
+cuflye_status cuflye_compact_binary(const cuflye_chain_record* records, size_t n_records,
+                                    size_t fixtures, const uint64_t* inputs_per_fixture,
+                                    unsigned char* out, size_t out_cap, size_t* n_out);
+
+/* --------------------------------------------------------------------------
  * The device sort every Flye sort point above runs on: sorts each segment
  * [seg_offsets[s], seg_offsets[s+1]) of (key, value) pairs in place, leaving
  * equal keys in exactly the order libstdc++'s std::sort(first, last,

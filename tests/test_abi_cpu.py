@@ -101,7 +101,9 @@ def test_host_mirrors_match_header_structs():
     for dt, name in ((abi.CANDIDATE_DTYPE, "cuflye_candidate"),
                      (abi.FILTERED_DTYPE, "cuflye_filtered_pos"),
                      (abi.OVERLAP_DTYPE, "cuflye_overlap_range"),
-                     (abi.READ_ALIGNMENT_DTYPE, "cuflye_read_alignment")):
+                     (abi.READ_ALIGNMENT_DTYPE, "cuflye_read_alignment"),
+                     (abi.CHAIN_RECORD_DTYPE, "cuflye_chain_record"),
+                     (abi.EDGE_OVERLAP_DTYPE, "cuflye_edge_overlap")):
         assert [(n, dt.fields[n][0].str) for n in dt.names] == header_struct(name), name
 
 
