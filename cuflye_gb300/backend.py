@@ -113,6 +113,8 @@ def load_library(path: Path | None = None) -> ctypes.CDLL:
     L.cuflye_open_from_env.restype = S
     L.cuflye_open_from_env.argtypes = [ctypes.POINTER(_vp)]
     L.cuflye_close.argtypes = [_vp]
+    L.cuflye_open_shared.restype = S
+    L.cuflye_open_shared.argtypes = [_vp, ctypes.c_uint64, ctypes.POINTER(_vp)]
     L.cuflye_last_error.restype = ctypes.c_char_p
     L.cuflye_last_error.argtypes = [_vp]
     L.cuflye_memory_stats.restype = S

@@ -82,7 +82,29 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         subprocess.run(cmd, check=True)
     if force or _stale(TABLE, [gen]):
         subprocess.run([str(gen), str(TABLE)], check=True, stdout=subprocess.DEVNULL)
+    build_abi_caller(force)
     return LIB
+
+
+CALLER_SRC = HERE.parent / "tests" / "c" / "abi_caller.cpp"
+CALLER = OUT / "abi_caller"
+
+
+def build_abi_caller(force: bool = False) -> Path | None:
+    """The compiled C++ caller of the C ABI (tests/c/abi_caller.cpp, through
+    the Flye-side adapter cuflye_gb300/flye/cuflye_flye.hpp), linked against
+    the library with an rpath to this directory.  None when the source is
+    not in the tree."""
+    if not CALLER_SRC.exists():
+        return None
+    adapter = HERE / "flye" / "cuflye_flye.hpp"
+    header = HERE.parent / "include" / "cuflye.h"
+    if force or _stale(CALLER, [CALLER_SRC, adapter, header, LIB]):
+        cxx = shutil.which("g++") or "g++"
+        subprocess.run([cxx, "-std=c++17", "-O2", "-pthread", "-I", str(HERE.parent / "include"),
+                        "-I", str(HERE / "flye"), str(CALLER_SRC), "-o", str(CALLER),
+                        "-L", str(OUT), "-lcuflye_gb300", "-Wl,-rpath,$ORIGIN"], check=True)
+    return CALLER
 
 
 if __name__ == "__main__":

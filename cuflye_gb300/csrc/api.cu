@@ -90,7 +90,8 @@ struct cuflye_ctx {
   uint64_t build_window_cap = 0;  // see cuflye_set_index_build_windows
   cuflye_launch_shape shape{0, 0, 0, 0};  // see cuflye_set_launch_shape (0: defaults)
   uint64_t build_ranges = 0;      // key ranges of the last index build
-  int servers = 0;           // open serving loops borrowing this index
+  int servers = 0;           // open serving loops and shared contexts borrowing this index
+  cuflye_ctx* lender = nullptr;  // the context whose index this one borrows (cuflye_open_shared)
   bool sorted_emission = true;  // see cuflye_set_sorted_emission
   uint64_t emission_fallbacks = 0;  // passes of the last call that fell back to emit + sort
 };
@@ -1401,8 +1402,45 @@ cuflye_status cuflye_open_from_env(cuflye_ctx** out) {
   return cuflye_open(d, b, out);
 }
 
+cuflye_status cuflye_open_shared(cuflye_ctx* owner, uint64_t memory_budget_bytes,
+                                 cuflye_ctx** out) {
+  if (!out) return CUFLYE_ERR_INVALID;
+  *out = nullptr;
+  if (!owner) return CUFLYE_ERR_INVALID;
+  int device = 0;
+  {
+    std::lock_guard<std::mutex> lock(owner->mu);
+    if (!owner->has_index) {
+      owner->err = "cuflye_open_shared: the owner has no index";
+      return CUFLYE_ERR_NO_INDEX;
+    }
+    if (owner->lender) {
+      owner->err = "cuflye_open_shared: the owner borrows its index itself";
+      return CUFLYE_ERR_INVALID;
+    }
+    device = owner->device;
+  }
+  cuflye_ctx* c = nullptr;
+  const cuflye_status st = cuflye_open(device, memory_budget_bytes, &c);
+  if (st != CUFLYE_OK) return st;
+  std::lock_guard<std::mutex> lock(owner->mu);
+  // the owner's resident index, read only (its device buffers stay the owner's)
+  c->idx = owner->idx;
+  c->slot_of = owner->slot_of;
+  c->slot_signed_h = owner->slot_signed_h;
+  c->has_index = true;
+  c->lender = owner;
+  ++owner->servers;
+  *out = c;
+  return CUFLYE_OK;
+}
+
 void cuflye_close(cuflye_ctx* c) {
   if (!c) return;
+  if (c->lender) {
+    std::lock_guard<std::mutex> lock(c->lender->mu);
+    --c->lender->servers;
+  }
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (auto& kv : c->bufs)
@@ -1431,7 +1469,10 @@ cuflye_status cuflye_index_build(cuflye_ctx* c, int k, size_t n, const int64_t* 
   CUFLYE_CHECK(cudaSetDevice(c->device));
   if (!ids || !offsets || (!bases && n)) throw Error(CUFLYE_ERR_INVALID, "null input");
   if (c->servers)
-    throw Error(CUFLYE_ERR_INVALID, "a serving loop borrows this context's index; close it first");
+    throw Error(CUFLYE_ERR_INVALID, "a serving loop or shared context borrows this context's "
+                                    "index; close it first");
+  if (c->lender)
+    throw Error(CUFLYE_ERR_INVALID, "this context shares another context's index");
   build_index(c, k, n, ids, offsets, bases, min_freq, max_freq);
   CUFLYE_API_END(c)
 }
@@ -1442,7 +1483,10 @@ cuflye_status cuflye_index_from_entries(cuflye_ctx* c, int k, size_t n, const in
   CUFLYE_API_BEGIN(c)
   CUFLYE_CHECK(cudaSetDevice(c->device));
   if (c->servers)
-    throw Error(CUFLYE_ERR_INVALID, "a serving loop borrows this context's index; close it first");
+    throw Error(CUFLYE_ERR_INVALID, "a serving loop or shared context borrows this context's "
+                                    "index; close it first");
+  if (c->lender)
+    throw Error(CUFLYE_ERR_INVALID, "this context shares another context's index");
   build_index_entries(c, k, n, tids, positions, keys, n_rep, rep_keys);
   CUFLYE_API_END(c)
 }

@@ -66,6 +66,17 @@ cuflye_status cuflye_open(int device, uint64_t memory_budget_bytes, cuflye_ctx**
  * environment. */
 cuflye_status cuflye_open_from_env(cuflye_ctx** out);
 
+/* A context of its own (stream, device arena, budget) that uses `owner`'s
+ * resident index, read only, so that host threads can each run queries on
+ * one index (no counterpart in the reference, whose adapter serialises every
+ * call behind one mutex: patches/flye/2.9.6/0004-cuflye-cuda-adapter-shell.patch:105-109,
+ * 390-392).  The owner must have an index, keep it (rebuilding it fails with
+ * CUFLYE_ERR_INVALID while shared contexts are open) and stay open until
+ * they are closed.  A shared context cannot build an index of its own; it
+ * starts without a graph (cuflye_graph_set gives it one). */
+cuflye_status cuflye_open_shared(cuflye_ctx* owner, uint64_t memory_budget_bytes,
+                                 cuflye_ctx** out);
+
 void cuflye_close(cuflye_ctx* ctx);
 
 /* The last failure's one-line message.  With ctx == NULL: why the calling

@@ -207,3 +207,17 @@ def test_open_from_env_failure_keeps_the_stub_fields(built_lib, device, budget, 
                           f"CUFLYE_CUDA_DEVICE={device}; "
                           f"CUFLYE_CUDA_MEMORY_BUDGET_BYTES={budget}; ")
     assert reason in msg
+
+
+def test_cpp_caller_fails_fast_with_the_stub_fields(built_lib):
+    """The compiled C++ caller (tests/c/abi_caller.cpp) opens the device
+    through the Flye-side adapter; an unparsable CUFLYE_CUDA_DEVICE throws
+    before any CUDA call, with the reference stub's fields."""
+    from cuflye_gb300 import build
+    path = build.build_abi_caller()
+    assert path is not None
+    env = dict(os.environ, CUFLYE_CUDA_DEVICE="cuda:zero")
+    r = subprocess.run([str(path), "open"], env=env, capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1
+    assert r.stdout.startswith("ERROR\tcuFlye CUDA candidate backend selected; "
+                               "adapter=cuflye_gb300; CUFLYE_CUDA_DEVICE=cuda:zero; ")
