@@ -302,9 +302,10 @@ class CudaBackend:
         self._check(self._L.cuflye_last_sort_stats(self._h, v, 8))
         return dict(zip(self.SORT_STATS, list(v)))
 
-    def set_sorted_emission(self, enable: bool) -> None:
-        """Hits straight into KmerMatch order (default) or emit + sort."""
-        self._check(self._L.cuflye_set_sorted_emission(self._h, int(bool(enable))))
+    def set_sorted_emission(self, mode) -> None:
+        """Hits straight into KmerMatch order: 1 / True where windows are
+        dense (the default), 2 for every pass, 0 / False never (emit + sort)."""
+        self._check(self._L.cuflye_set_sorted_emission(self._h, int(mode)))
 
     def last_passes(self) -> int:
         """Passes (runs of queries through the device) of the last call."""

@@ -86,13 +86,14 @@ struct cuflye_ctx {
   uint64_t sort_stats[8]{};  // see cuflye_last_sort_stats ([7]: emission fallbacks)
   // hits of the last call by path, for the stages' algorithmic bytes
   uint64_t hits_sorted_emission = 0, hits_flagged = 0, hits_prefiltered = 0, hits_emit_sort = 0;
+  unsigned long long emit_tally[2]{};  // a pass's flagged and prefiltered hits, read back
   uint64_t passes = 0;       // see cuflye_last_passes
   uint64_t build_window_cap = 0;  // see cuflye_set_index_build_windows
   cuflye_launch_shape shape{0, 0, 0, 0};  // see cuflye_set_launch_shape (0: defaults)
   uint64_t build_ranges = 0;      // key ranges of the last index build
   int servers = 0;           // open serving loops and shared contexts borrowing this index
   cuflye_ctx* lender = nullptr;  // the context whose index this one borrows (cuflye_open_shared)
-  bool sorted_emission = true;  // see cuflye_set_sorted_emission
+  int sorted_emission = 1;  // see cuflye_set_sorted_emission
   uint64_t emission_fallbacks = 0;  // passes of the last call that fell back to emit + sort
 };
 
@@ -171,6 +172,16 @@ void check_device_status(cuflye_ctx* c) {
     default:
       throw Error(CUFLYE_ERR_CUDA, "device status " + std::to_string(st.code));
   }
+}
+
+// Exclusive scan with out[n] = total, left on the device.
+void scan_u32_async(cuflye_ctx* c, const uint32_t* in, uint64_t* out, uint64_t n,
+                    const char* temp_name) {
+  uint64_t* temp = buf<uint64_t>(c, temp_name, scan_temp_words(n));
+  CUFLYE_CHECK(exclusive_scan_u32_to_u64(in, out, n, temp, c->stream));
+  const uint64_t ntiles = scan_temp_words(n) - 1;
+  CUFLYE_CHECK(cudaMemcpyAsync(out + n, temp + (n ? ntiles : 0), sizeof(uint64_t),
+                               cudaMemcpyDeviceToDevice, c->stream));
 }
 
 uint64_t scan_u32(cuflye_ctx* c, const uint32_t* in, uint64_t* out, uint64_t n,
@@ -772,10 +783,14 @@ size_t run_end(cuflye_ctx* c, const Queries& Q, size_t q0, size_t q1, uint64_t b
   return q;
 }
 
-// Whether a pass's hits go straight into KmerMatch order (match_emit.cu):
-// overlap and read-to-graph calls on a built index, unless switched off.
+// Hits per window below which a pass takes the emit + sort path.
+constexpr uint64_t kSortedEmissionMinHitsPerWindow = 6;
+
+// Whether a pass's hits may go straight into KmerMatch order (match_emit.cu):
+// overlap and read-to-graph calls on a built index, unless switched off; the
+// pass's hit density decides in the end.
 bool sorted_emission(const cuflye_ctx* c, bool want_kmers) {
-  return !want_kmers && c->idx.transform && c->sorted_emission;
+  return !want_kmers && c->idx.transform && c->sorted_emission != 0;
 }
 
 bool run_hits(cuflye_ctx* c, const Queries& Q, size_t q0, size_t q1, bool want_kmers,
@@ -904,8 +919,11 @@ bool run_hits(cuflye_ctx* c, const Queries& Q, size_t q0, size_t q1, bool want_k
   ps.wmeta = wmeta;
   ps.wflags = wflags;
   ps.wself = wself;
-  ps.emitted = !fused;
-  if (!fused) emit_generation_order(c, ps);
+  // The sorted emission pays off where windows hit many targets; a pass of
+  // sparse hits (reads against a genome or a graph) is cheaper to emit and sort.
+  ps.emitted = !(fused && (c->sorted_emission == 2 ||
+                           ps.nhits >= kSortedEmissionMinHitsPerWindow * ps.nwin));
+  if (ps.emitted) emit_generation_order(c, ps);
   return true;
 }
 
@@ -971,6 +989,7 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp,
   uint32_t* dp_list = nullptr;
   uint32_t* gcounts = buf<uint32_t>(c, "g_counts", 4);
   bool fused = !ps.emitted;
+  bool tally_pending = false;
   if (fused) {
     // Sorted emission: each query's dictionary of ext ids, then its hits
     // written in KmerMatch order with their groups; flagged queries'
@@ -995,8 +1014,14 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp,
     CUFLYE_CHECK(cudaMemsetAsync(mwords, 0, 4 * sizeof(uint32_t), st));
     CUFLYE_CHECK(cudaMemsetAsync(dcur, 0, 3 * sizeof(unsigned long long), st));
     CUFLYE_CHECK(match_dict(a, alt_keys, dcur, q_ng, q_dbase, mwords, mwords + 1, c->num_sms, st));
-    G = scan_u32(c, q_ng, q_goff, nq, "m_scan");
-    if (read_scalar(c, mwords) != 0) {
+    // the group count and the overflow count in one read back
+    scan_u32_async(c, q_ng, q_goff, nq, "m_scan");
+    uint64_t back[2] = {0, 0};
+    CUFLYE_CHECK(cudaMemcpyAsync(&back[0], q_goff + nq, 8, cudaMemcpyDeviceToHost, st));
+    CUFLYE_CHECK(cudaMemcpyAsync(&back[1], mwords, 4, cudaMemcpyDeviceToHost, st));
+    sync(c);
+    G = back[0];
+    if (back[1] != 0) {
       // a query with more than kMatchDictCap ext ids: this pass takes the
       // generation-order emission and the sort instead
       ++c->emission_fallbacks;
@@ -1023,11 +1048,10 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp,
       CUFLYE_CHECK(groups_prefilter_list(ps.keys, ps.vals, groups, pf_list, ps.qinfo, slot_len, cp,
                                          ext_list, dp_list, gcounts, static_cast<uint32_t>(G),
                                          st));
-      unsigned long long tally[2];
-      CUFLYE_CHECK(cudaMemcpyAsync(tally, dcur + 1, sizeof(tally), cudaMemcpyDeviceToHost, st));
-      sync(c);
-      c->hits_flagged += tally[0];
-      c->hits_prefiltered += tally[1];
+      // read back with the survivor count below (one stream sync)
+      CUFLYE_CHECK(cudaMemcpyAsync(c->emit_tally, dcur + 1, sizeof(c->emit_tally),
+                                   cudaMemcpyDeviceToHost, st));
+      tally_pending = true;
       c->hits_sorted_emission += H;
     }
   }
@@ -1109,6 +1133,10 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp,
   // 6. backtrack, proposals, primary selection; the row pool is sized by the
   // groups that survived the prefilter
   const uint32_t survivors = read_scalar(c, gcounts + 1);
+  if (tally_pending) {
+    c->hits_flagged += c->emit_tally[0];
+    c->hits_prefiltered += c->emit_tally[1];
+  }
   const uint64_t pool_cap = 8ull * survivors + 1024;
   OverlapRow* pool = buf<OverlapRow>(c, "o_pool", pool_cap);
   uint32_t* pool_count = buf<uint32_t>(c, "o_poolcount", 1);
@@ -1508,9 +1536,9 @@ cuflye_status cuflye_set_batch_queries(cuflye_ctx* c, size_t q) {
 }
 
 cuflye_status cuflye_set_sorted_emission(cuflye_ctx* c, int enable) {
-  if (!c || (enable != 0 && enable != 1)) return CUFLYE_ERR_INVALID;
+  if (!c || enable < 0 || enable > 2) return CUFLYE_ERR_INVALID;
   std::lock_guard<std::mutex> lock(c->mu);
-  c->sorted_emission = enable != 0;
+  c->sorted_emission = enable;
   return CUFLYE_OK;
 }
 

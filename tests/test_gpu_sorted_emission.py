@@ -19,14 +19,14 @@ pytestmark = pytest.mark.gpu
 def _both_paths(gpu, reads, params):
     from cuflye_gb300.backend import OverlapParams
     p = OverlapParams.make(**params)
-    gpu.set_sorted_emission(True)
+    gpu.set_sorted_emission(2)  # every pass, sparse ones included
     fused = overlap_tuples_gpu(gpu.overlaps(reads, p))
     stats = gpu.last_sort_stats()
-    gpu.set_sorted_emission(False)
+    gpu.set_sorted_emission(0)
     try:
         plain = overlap_tuples_gpu(gpu.overlaps(reads, p))
     finally:
-        gpu.set_sorted_emission(True)
+        gpu.set_sorted_emission(1)
     return fused, plain, stats
 
 
@@ -62,11 +62,13 @@ def test_sorted_emission_long_reads_and_passes(gpu, oracle_mod):
     fused, plain, _ = _both_paths(gpu, sw.queries, sw.params)
     assert fused == plain and len(fused) > 0
     gpu.set_batch_queries(7)
+    gpu.set_sorted_emission(2)
     try:
         cut = overlap_tuples_gpu(gpu.overlaps(sw.queries, OverlapParams.make(**sw.params)))
         assert gpu.last_passes() > 1
     finally:
         gpu.set_batch_queries(0)
+        gpu.set_sorted_emission(1)
     assert cut == fused
 
 
@@ -78,12 +80,16 @@ def test_sorted_emission_read_to_graph(gpu):
     gpu.build_index(g.seqs, wl.k, wl.min_freq, wl.max_freq)
     gpu.set_graph(g.edge_ids, g.seq_ids, g.left, g.right)
     p, r = OverlapParams.make(**wl.params), R2GParams.make(**synth.R2G_PARAMS)
-    fused = gpu.read_to_graph(wl.reads, p, r)
-    gpu.set_sorted_emission(False)
+    gpu.set_sorted_emission(2)
+    try:
+        fused = gpu.read_to_graph(wl.reads, p, r)
+    finally:
+        gpu.set_sorted_emission(1)
+    gpu.set_sorted_emission(0)
     try:
         plain = gpu.read_to_graph(wl.reads, p, r)
     finally:
-        gpu.set_sorted_emission(True)
+        gpu.set_sorted_emission(1)
     assert fused.tobytes() == plain.tobytes() and len(fused) > 0
 
 
