@@ -919,10 +919,13 @@ bool run_hits(cuflye_ctx* c, const Queries& Q, size_t q0, size_t q1, bool want_k
   ps.wmeta = wmeta;
   ps.wflags = wflags;
   ps.wself = wself;
-  // The sorted emission pays off where windows hit many targets; a pass of
-  // sparse hits (reads against a genome or a graph) is cheaper to emit and sort.
+  // The sorted emission pays off where windows hit many targets and the
+  // pass has queries for every SM (it runs a block per query); a pass of
+  // sparse hits (reads against a genome or a graph) or of a few queries (the
+  // one-read path) is cheaper to emit and sort.
   ps.emitted = !(fused && (c->sorted_emission == 2 ||
-                           ps.nhits >= kSortedEmissionMinHitsPerWindow * ps.nwin));
+                           (ps.nhits >= kSortedEmissionMinHitsPerWindow * ps.nwin &&
+                            ps.nq >= 2ull * static_cast<uint64_t>(c->num_sms))));
   if (ps.emitted) emit_generation_order(c, ps);
   return true;
 }

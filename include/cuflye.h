@@ -210,9 +210,10 @@ cuflye_status cuflye_set_batch_queries(cuflye_ctx* ctx, size_t queries_per_pass)
  * straight into the order of Flye's KmerMatch sort, one block per query, and
  * decide most target groups' prefilter on the way, instead of writing them
  * in generation order and sorting.  The rows are the same either way.  1
- * (the default) takes it for passes whose windows average at least 6 hits,
- * where it pays off; sparser passes (reads against a genome or a graph) emit
- * and sort.  2 takes it for every pass, 0 for none (for comparison).  A pass
+ * (the default) takes it for passes whose windows average at least 6 hits
+ * and that hold at least two queries per SM, where it pays off; sparser
+ * passes (reads against a genome or a graph) and small ones (the one-read
+ * path) emit and sort.  2 takes it for every pass, 0 for none (for comparison).  A pass
  * holding a query that hits more than 2,048 distinct targets takes the emit
  * + sort path by itself (counted in cuflye_last_sort_stats, entry 7). */
 cuflye_status cuflye_set_sorted_emission(cuflye_ctx* ctx, int enable);
