@@ -1,8 +1,9 @@
 """Multi-rank host logic of the bench on CPU (gloo, world size 2).
 
 The overlap path shards by reads with no data-path collective: every rank
-runs its own replica, and ranks meet only to agree on the timed region
-(barrier) and to combine their results (sum of bases, max of times)."""
+takes a length-balanced share of the reads against the index of all of
+them, and ranks meet only to agree on the timed region (barrier) and to
+combine their results (sum of bases, max of times)."""
 
 import os
 import socket
@@ -48,7 +49,7 @@ def test_two_gloo_ranks_combine_like_the_bench():
             p.join(120)
             assert p.exitcode == 0
         got = dict(results)
-    # weak scaling: all bases over the slowest rank's time, the same on every rank
+    # all bases over the slowest rank's time, the same on every rank
     for r in range(world):
         assert got[r] == (3000.0, 1.0, 3000.0)
 
@@ -60,3 +61,21 @@ def test_single_rank_needs_no_process_group(monkeypatch):
     assert bench.dist_setup() == (1, 0, 0)
     assert bench.reduce_max(1, 2.5) == 2.5
     assert bench.reduce_sum(1, 7.0) == 7.0
+
+
+@pytest.mark.parametrize("world", [1, 2, 3, 8])
+def test_read_shards_are_disjoint_complete_and_balanced(world):
+    import numpy as np
+    import bench
+    rng = np.random.default_rng(world)
+    lengths = np.clip(rng.lognormal(np.log(15_000), 0.2, size=1_000).astype(np.int64), 1_000,
+                      100_000)
+    shards = bench.shard_reads(lengths, world)
+    assert len(shards) == world
+    allidx = np.sort(np.concatenate(shards))
+    assert np.array_equal(allidx, np.arange(len(lengths)))  # each read exactly once
+    for s in shards:
+        assert np.all(np.diff(s) > 0)  # input order within a shard
+    loads = np.array([lengths[s].sum() for s in shards])
+    # greedy longest-first: no rank exceeds another by more than the longest read
+    assert loads.max() - loads.min() <= lengths.max()
