@@ -93,27 +93,50 @@ struct EmitQuery {
   uint64_t h0, h1;  // its hits [h0, h1) in the pass
 };
 
+// A window's fields as the batch setup reads them, all four loads issued at
+// once (wself holds a value only for trivial windows; it is read anyway and
+// used only then).
+struct WinLoad {
+  uint64_t meta = 0, hoff = 0;
+  uint32_t self = 0;
+  uint8_t fl = 0;
+  bool in = false;
+};
+
+__device__ __forceinline__ WinLoad load_window(const MatchEmitArgs& a, const EmitQuery& eq,
+                                               uint64_t wi) {
+  WinLoad x;
+  if (threadIdx.x < kSeWin && wi < eq.w1) {
+    x.in = true;
+    x.fl = a.wflags[wi];
+    x.meta = a.wmeta[wi];
+    x.self = a.wself[wi];
+    x.hoff = a.hit_off[wi];
+  }
+  return x;
+}
+
 // Sets up the batch that starts at window w (bucket entry e0 of it): as many
 // windows as fit kSeBatch entries and kSeWin windows, or kSeBatch entries of
-// one window that has more.  Writes the filtered positions of the batch's
-// windows when fpos is given.  Every thread of the block calls it.
+// one window that has more.  win: thread t's load of window w + t (issued
+// ahead, while the previous batch ran).  Writes the filtered positions of the
+// batch's windows when fpos is given.  Every thread of the block calls it.
 __device__ void batch_setup(BatchWin& b, const MatchEmitArgs& a, const EmitQuery& eq, uint64_t w,
-                            uint32_t e0) {
+                            uint32_t e0, const WinLoad& win) {
   const int t = threadIdx.x;
   uint32_t raw = 0;
   uint64_t ebase = 0, hoff = 0;
   uint32_t self = kNone, prev = 0;
   if (t < kSeWin) {
     const uint64_t wi = w + t;
-    if (wi < eq.w1) {
-      const uint8_t fl = a.wflags[wi];
+    if (win.in) {
+      const uint8_t fl = win.fl;
       if (!(fl & kWinFiltered)) {
-        const uint64_t meta = a.wmeta[wi];
-        raw = static_cast<uint32_t>((meta >> 40) & ((1ULL << kCountBits) - 1));
-        ebase = meta & kOffsetMask;
+        raw = static_cast<uint32_t>((win.meta >> 40) & ((1ULL << kCountBits) - 1));
+        ebase = win.meta & kOffsetMask;
       }
-      if (fl & kWinTrivial) self = a.wself[wi];
-      hoff = a.hit_off[wi];
+      if (fl & kWinTrivial) self = win.self;
+      hoff = win.hoff;
       prev = static_cast<uint32_t>(wi - eq.w0) | ((fl & kWinRev) ? 0x80000000u : 0u);
     }
     raw -= t == 0 ? e0 : 0u;
@@ -163,10 +186,9 @@ __device__ void batch_setup(BatchWin& b, const MatchEmitArgs& a, const EmitQuery
   __syncthreads();
   // filtered positions of the windows this batch covers: a filtered window
   // has no entries, so it lies in exactly one batch
-  if (a.fpos && t < static_cast<int>(b.nw)) {
+  if (a.fpos && t < static_cast<int>(b.nw) && win.in && (win.fl & kWinFiltered)) {
     const uint64_t wi = w + t;
-    if (wi < eq.w1 && (a.wflags[wi] & kWinFiltered))
-      a.fpos[a.filt_off[wi]] = static_cast<int32_t>(wi - eq.w0);
+    a.fpos[a.filt_off[wi]] = static_cast<int32_t>(wi - eq.w0);
   }
   // entry -> window table: each thread its kSePer consecutive entries (one
   // search, then a forward walk over windows without entries)
@@ -286,8 +308,11 @@ __global__ void __launch_bounds__(kSeBlock, 3) match_dict_kernel(MatchEmitArgs a
     uint64_t w = eq.w0;
     uint32_t e0 = 0;
     bool over = false;
+    WinLoad win = load_window(a, eq, w + t);
     while (w < eq.w1 && !over) {
-      batch_setup(sm.b, a, eq, w, e0);
+      batch_setup(sm.b, a, eq, w, e0, win);
+      // the next batch's windows load while this one runs
+      win = load_window(a, eq, sm.b.next_w + t);
       Entries x;
       load_entries(sm.b, a, x);
 #pragma unroll
@@ -485,8 +510,11 @@ __global__ void __launch_bounds__(kSeBlock, 2) match_emit_kernel(
     __syncthreads();
     uint64_t w = eq.w0;
     uint32_t e0 = 0;
+    WinLoad win = load_window(a, eq, w + t);
     while (w < eq.w1) {
-      batch_setup(sm.b, a, eq, w, e0);
+      batch_setup(sm.b, a, eq, w, e0, win);
+      // the next batch's windows load while this one runs
+      win = load_window(a, eq, sm.b.next_w + t);
       Entries x;
       load_entries(sm.b, a, x);
       if (flagged) {

@@ -277,7 +277,13 @@ def scale_ont(seed: int = 6, genome_len: int = 500_000_000, coverage: float = 30
     lognormal(25 kb, 15 kb) in 1-150 kb, 6 % error (2 / 2 / 2 % sub / ins /
     del); k = 17.  genome_len and coverage scale it down for tests.
     sparse_errors draws the read errors with `mutate_sparse` (same rates,
-    another random stream), for the full-size configuration."""
+    another random stream), for the full-size configuration.
+
+    Solid k-mers are those seen at least max(2, coverage / 10) times: at 30x
+    with 6 % error the 15 Gbp of reads fill much of the 4^17 k-mer space with
+    erroneous windows, and about 3e9 of those meet once more by chance, so a
+    cutoff of 2 would index them all (as Flye's coverage-derived cutoff
+    would not)."""
     rng = np.random.default_rng(seed)
     genome = random_genome(rng, genome_len)
     placed = 0
@@ -291,8 +297,9 @@ def scale_ont(seed: int = 6, genome_len: int = 500_000_000, coverage: float = 30
     reads = sample_reads(rng, genome, coverage,
                          lambda n: lognormal_lengths(rng, n, 25_000, 15_000, 1_000, 150_000),
                          0.02, 0.02, 0.02, max_reads, sparse=sparse_errors)
-    return Workload("scale-ont30x-k17", 17, reads, min_freq=2, max_freq=int(5 * coverage),
-                    params=dict(OVERLAP_PARAMS, kmer_size=17), seed=seed)
+    return Workload("scale-ont30x-k17", 17, reads, min_freq=max(2, int(round(coverage / 10))),
+                    max_freq=int(5 * coverage), params=dict(OVERLAP_PARAMS, kmer_size=17),
+                    seed=seed)
 
 
 R2G_PARAMS = dict(max_jump=1500, max_read_overlap=50, min_overlap=1000, max_separation=500,

@@ -54,7 +54,7 @@ def test_config3_read_to_graph_shapes():
 def test_config5_scale_shapes(sparse):
     from cuflye_gb300 import synth
     wl = synth.scale_ont(genome_len=2_000_000, coverage=30.0, sparse_errors=sparse)
-    assert wl.k == 17
+    assert wl.k == 17 and wl.min_freq == 3 and wl.max_freq == 150
     _check_reads(wl.reads, 2_000_000, 30.0, 25_000, 15_000, 1_000, 150_000)
 
 
