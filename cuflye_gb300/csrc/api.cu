@@ -94,6 +94,7 @@ struct cuflye_ctx {
   int servers = 0;           // open serving loops and shared contexts borrowing this index
   cuflye_ctx* lender = nullptr;  // the context whose index this one borrows (cuflye_open_shared)
   int sorted_emission = 1;  // see cuflye_set_sorted_emission
+  double other_per_hit = 0;  // a pass body's buffers beyond the per-hit ones, per hit
   uint64_t emission_fallbacks = 0;  // passes of the last call that fell back to emit + sort
 };
 
@@ -492,6 +493,7 @@ BuiltIndex build_key_ranges(cuflye_ctx* c, const WindowSet& w, const std::vector
 
 void build_index(cuflye_ctx* c, int k, size_t n, const int64_t* ids, const int64_t* offsets,
                  const char* bases, uint32_t min_freq, uint32_t max_freq) {
+  c->other_per_hit = 0;  // a new workload: learned again
   if (k < 1 || k > 31) throw Error(CUFLYE_ERR_UNSUPPORTED, "k must be in [1, 31]");
   if (n == 0) throw Error(CUFLYE_ERR_INVALID, "index needs at least one target");
   if (max_freq >= (1u << kCountBits) - 1)
@@ -875,7 +877,9 @@ bool run_hits(cuflye_ctx* c, const Queries& Q, size_t q0, size_t q1, bool want_k
   // own margin covers them
   const uint64_t free_b = limit > used ? limit - used : 0;
   const uint64_t avail = c->budget ? free_b - free_b / 8 : free_b;
-  const uint64_t fits = avail / bytes_per_hit;
+  // the pass body's other buffers, per hit, as earlier passes needed them
+  const uint64_t fits = static_cast<uint64_t>(
+      static_cast<double>(avail) / (static_cast<double>(bytes_per_hit) + c->other_per_hit));
   uint64_t hit_limit = fits;
   // Under a caller's budget a pass keeps to the per-hit buffers an earlier
   // pass grew when they hold at least 90 % of what fits: growing them frees
@@ -1255,6 +1259,35 @@ size_t pass_size(cuflye_ctx* c, size_t n) {
   return n;
 }
 
+// Buffers a pass body does not own: the index, the graph, the logf table, the
+// status word, and the per-hit and per-window buffers that passes reuse.
+bool kept_buffer(const std::string& name) {
+  static const char* const kPrefixes[] = {"ix_", "gr_", "logf_", "q_"};
+  for (const char* p : kPrefixes)
+    if (name.compare(0, std::strlen(p), p) == 0) return true;
+  if (name == "status") return true;
+  for (const char* nm : kPerHitBuffers)
+    if (name == nm) return true;
+  for (const char* nm : kPerWindowBuffers)
+    if (name == nm) return true;
+  return false;
+}
+
+uint64_t held_bytes(cuflye_ctx* c) {
+  uint64_t b = 0;
+  for (const auto& kv : c->bufs)
+    if (kept_buffer(kv.first)) b += kv.second.cap;
+  return b;
+}
+
+// Frees every buffer of the pass body (its tables, lists and rows).
+void release_pass_buffers(cuflye_ctx* c) {
+  std::vector<std::string> names;
+  for (const auto& kv : c->bufs)
+    if (!kept_buffer(kv.first)) names.push_back(kv.first);
+  for (const std::string& n : names) release(c, n);
+}
+
 // Runs passes over [0, n): `body(q0, q1, ps)` consumes each pass.  A body
 // whose later buffers (per-group tables, the row pool) do not fit the budget
 // runs again on the first half of the pass's queries; bodies make their
@@ -1278,9 +1311,15 @@ void for_each_pass(cuflye_ctx* c, const Queries& Q, bool kmers, uint64_t bytes_p
       body(q0, q1, ps);
     } catch (const Error& e) {
       if (e.code != CUFLYE_ERR_BUDGET || ps.nq <= 1) throw;
+      // the failed body's buffers go, so that half the queries find room
       sync(c);
+      release_pass_buffers(c);
       step = std::max<size_t>(ps.nq / 2, 1);
       continue;
+    }
+    if (c->budget && ps.nhits) {
+      const double other = static_cast<double>(c->in_use - held_bytes(c));
+      c->other_per_hit = std::max(c->other_per_hit, other / static_cast<double>(ps.nhits));
     }
     ++c->passes;
     q0 = q1;

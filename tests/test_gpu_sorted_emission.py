@@ -120,8 +120,12 @@ def test_query_beyond_the_dictionary_falls_back(gpu, oracle_mod):
     k, min_freq, max_freq = 15, 1, 100_000
     gpu.build_index(tg, k, min_freq, max_freq)
     params = dict(synth.OVERLAP_PARAMS, kmer_size=k, only_max_ext=0)
-    got = gpu.overlaps(q, OverlapParams.make(**params))
-    assert gpu.last_sort_stats()["emission_fallbacks"] >= 1
+    gpu.set_sorted_emission(2)  # two queries: below the default's queries per SM
+    try:
+        got = gpu.overlaps(q, OverlapParams.make(**params))
+        assert gpu.last_sort_stats()["emission_fallbacks"] >= 1
+    finally:
+        gpu.set_sorted_emission(1)
     idx, _ = oracle_index(oracle_mod, tg, k, min_freq, max_freq)
     b = oracle_mod.SeqBatch(q.ids, q.offsets, q.bases.tobytes())
     exp = oracle_mod.overlaps(idx, b, oracle_mod.default_params(**params))
