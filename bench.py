@@ -499,6 +499,7 @@ def scale_config(args, device: int) -> dict:
         wall = time.perf_counter() - t
         ms, by = be.last_timing()
         passes = be.last_passes()
+        pass_stats = be.last_pass_stats()
         dev_peak = be.memory_stats()[1]
     ms = np.array(ms)
     by = np.array(by, dtype=np.float64)
@@ -511,6 +512,7 @@ def scale_config(args, device: int) -> dict:
         "memory_budget_bytes": budget, "device_peak_bytes": int(dev_peak),
         "index_build_s": round(build_s, 3), "index_key_ranges": ranges,
         "index_positions": stats["positions"], "passes": passes,
+        "pass_retries": pass_stats["retries"], "host_alloc_ms": pass_stats["alloc_ms"],
         "batched_read_bases_per_s": bases / wall,
         "device_read_bases_per_s": bases / (float(ms[:5].sum()) / 1000.0),
         "stages_ms": {n: round(float(ms[i]), 3)

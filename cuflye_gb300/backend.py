@@ -163,6 +163,8 @@ def load_library(path: Path | None = None) -> ctypes.CDLL:
     L.cuflye_last_timing.argtypes = [_vp, ctypes.POINTER(ctypes.c_double), _u64p, ctypes.c_size_t]
     L.cuflye_last_sort_stats.restype = S
     L.cuflye_last_sort_stats.argtypes = [_vp, _u64p, ctypes.c_size_t]
+    L.cuflye_last_pass_stats.restype = S
+    L.cuflye_last_pass_stats.argtypes = [_vp, _u64p, _u64p, ctypes.POINTER(ctypes.c_double)]
     L.cuflye_last_passes.restype = S
     L.cuflye_last_passes.argtypes = [_vp, _u64p]
     L.cuflye_set_sorted_emission.restype = S
@@ -306,6 +308,13 @@ class CudaBackend:
         """Hits straight into KmerMatch order: 1 / True where windows are
         dense (the default), 2 for every pass, 0 / False never (emit + sort)."""
         self._check(self._L.cuflye_set_sorted_emission(self._h, int(mode)))
+
+    def last_pass_stats(self) -> dict:
+        """Passes of the last call, budget retries, and host ms in allocation."""
+        a, b, t = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_double()
+        self._check(self._L.cuflye_last_pass_stats(self._h, ctypes.byref(a), ctypes.byref(b),
+                                                   ctypes.byref(t)))
+        return {"passes": a.value, "retries": b.value, "alloc_ms": round(t.value, 1)}
 
     def last_passes(self) -> int:
         """Passes (runs of queries through the device) of the last call."""

@@ -95,6 +95,8 @@ struct cuflye_ctx {
   cuflye_ctx* lender = nullptr;  // the context whose index this one borrows (cuflye_open_shared)
   int sorted_emission = 1;  // see cuflye_set_sorted_emission
   double other_per_hit = 0;  // a pass body's buffers beyond the per-hit ones, per hit
+  uint64_t pass_retries = 0;   // passes of the last call run again on half their queries
+  double alloc_ms = 0;         // host time of the last call in cudaMalloc / cudaFree
   uint64_t emission_fallbacks = 0;  // passes of the last call that fell back to emit + sort
 };
 
@@ -117,6 +119,15 @@ T* buf(cuflye_ctx* c, const std::string& name, uint64_t count) {
                       " of CUFLYE_CUDA_MEMORY_BUDGET_BYTES=" + std::to_string(c->budget));
   }
   const size_t alloc = (c->budget && c->in_use - b.cap + want > c->budget) ? bytes : want;
+  const auto t0 = std::chrono::steady_clock::now();
+  struct AllocTimer {
+    cuflye_ctx* c;
+    std::chrono::steady_clock::time_point t0;
+    ~AllocTimer() {
+      c->alloc_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() -
+                                                               t0).count();
+    }
+  } timer{c, t0};
   if (b.p) CUFLYE_CHECK(cudaFree(b.p));
   c->in_use -= b.cap;
   b.p = nullptr;
@@ -136,7 +147,10 @@ T* buf(cuflye_ctx* c, const std::string& name, uint64_t count) {
 void release(cuflye_ctx* c, const std::string& name) {
   auto it = c->bufs.find(name);
   if (it == c->bufs.end()) return;
+  const auto t0 = std::chrono::steady_clock::now();
   if (it->second.p) cudaFree(it->second.p);
+  c->alloc_ms +=
+      std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   c->in_use -= it->second.cap;
   c->bufs.erase(it);
 }
@@ -1206,6 +1220,8 @@ float elapsed(cudaEvent_t a, cudaEvent_t b) {
 
 void reset_timing(cuflye_ctx* c) {
   c->passes = 0;
+  c->pass_retries = 0;
+  c->alloc_ms = 0;
   c->emission_fallbacks = 0;
   c->sort_stats[7] = 0;
   c->hits_sorted_emission = c->hits_flagged = c->hits_prefiltered = c->hits_emit_sort = 0;
@@ -1314,6 +1330,7 @@ void for_each_pass(cuflye_ctx* c, const Queries& Q, bool kmers, uint64_t bytes_p
       // the failed body's buffers go, so that half the queries find room
       sync(c);
       release_pass_buffers(c);
+      ++c->pass_retries;
       step = std::max<size_t>(ps.nq / 2, 1);
       continue;
     }
@@ -2232,6 +2249,15 @@ cuflye_status cuflye_last_sort_stats(const cuflye_ctx* c, uint64_t* counts, size
 cuflye_status cuflye_last_passes(const cuflye_ctx* c, uint64_t* passes) {
   if (!c || !passes) return CUFLYE_ERR_INVALID;
   *passes = c->passes;
+  return CUFLYE_OK;
+}
+
+cuflye_status cuflye_last_pass_stats(const cuflye_ctx* c, uint64_t* passes, uint64_t* retries,
+                                     double* alloc_ms) {
+  if (!c) return CUFLYE_ERR_INVALID;
+  if (passes) *passes = c->passes;
+  if (retries) *retries = c->pass_retries;
+  if (alloc_ms) *alloc_ms = c->alloc_ms;
   return CUFLYE_OK;
 }
 

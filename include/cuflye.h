@@ -497,6 +497,13 @@ cuflye_status cuflye_last_sort_stats(const cuflye_ctx* ctx, uint64_t* counts, si
  * reference). */
 cuflye_status cuflye_last_passes(const cuflye_ctx* ctx, uint64_t* passes);
 
+/* Host-side statistics of the last call (no counterpart in the reference):
+ * its passes, the passes that ran again on half their queries because their
+ * later buffers exceeded the memory budget, and the host milliseconds spent
+ * in device allocation and release. */
+cuflye_status cuflye_last_pass_stats(const cuflye_ctx* ctx, uint64_t* passes, uint64_t* retries,
+                                     double* alloc_ms);
+
 /* Kernel launches issued by the library in this process so far. */
 cuflye_status cuflye_kernel_launches(uint64_t* total);
 
