@@ -96,6 +96,7 @@ struct cuflye_ctx {
   int sorted_emission = 1;  // see cuflye_set_sorted_emission
   double other_per_hit = 0;  // a pass body's buffers beyond the per-hit ones, per hit
   uint64_t pass_retries = 0;   // passes of the last call run again on half their queries
+  uint64_t pass_hit_cap = 0;   // hits a pass may take after a retry in this call (0: no cap)
   double alloc_ms = 0;         // host time of the last call in cudaMalloc / cudaFree
   uint64_t emission_fallbacks = 0;  // passes of the last call that fell back to emit + sort
 };
@@ -110,7 +111,10 @@ T* buf(cuflye_ctx* c, const std::string& name, uint64_t count) {
   const size_t bytes = std::max<size_t>(static_cast<size_t>(count) * sizeof(T), 16);
   DevBuf& b = c->bufs[name];
   if (b.cap >= bytes) return static_cast<T*>(b.p);
-  const size_t want = std::max(bytes, b.cap + b.cap / 2);
+  // grow by half, or under a budget that has no room for that, by an eighth
+  // if there is room for that (fewer reallocations from pass to pass)
+  size_t want = std::max(bytes, b.cap + b.cap / 2);
+  if (c->budget && c->in_use - b.cap + want > c->budget) want = bytes + bytes / 8;
   if (c->budget && c->in_use - b.cap + want > c->budget) {
     if (c->in_use - b.cap + bytes > c->budget)
       throw Error(CUFLYE_ERR_BUDGET,
@@ -895,6 +899,7 @@ bool run_hits(cuflye_ctx* c, const Queries& Q, size_t q0, size_t q1, bool want_k
   const uint64_t fits = static_cast<uint64_t>(
       static_cast<double>(avail) / (static_cast<double>(bytes_per_hit) + c->other_per_hit));
   uint64_t hit_limit = fits;
+  if (c->pass_hit_cap) hit_limit = std::min(hit_limit, c->pass_hit_cap);
   // Under a caller's budget a pass keeps to the per-hit buffers an earlier
   // pass grew when they hold at least 90 % of what fits: growing them frees
   // and reallocates them, and that synchronizes the device.
@@ -1221,6 +1226,7 @@ float elapsed(cudaEvent_t a, cudaEvent_t b) {
 void reset_timing(cuflye_ctx* c) {
   c->passes = 0;
   c->pass_retries = 0;
+  c->pass_hit_cap = 0;
   c->alloc_ms = 0;
   c->emission_fallbacks = 0;
   c->sort_stats[7] = 0;
@@ -1331,6 +1337,8 @@ void for_each_pass(cuflye_ctx* c, const Queries& Q, bool kmers, uint64_t bytes_p
       sync(c);
       release_pass_buffers(c);
       ++c->pass_retries;
+      // later passes of the call stay at the size that is tried next
+      c->pass_hit_cap = std::max<uint64_t>(1, ps.nhits / 2);
       step = std::max<size_t>(ps.nq / 2, 1);
       continue;
     }

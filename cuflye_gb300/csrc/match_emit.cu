@@ -315,37 +315,10 @@ __global__ void __launch_bounds__(kSeBlock, 3) match_dict_kernel(MatchEmitArgs a
       win = load_window(a, eq, sm.b.next_w + t);
       Entries x;
       load_entries(sm.b, a, x);
-      // read-only probes of all entries first (ids already in the table are
-      // the common case), then the counts and the rare insertions
-      uint32_t ids[kSePer], slot[kSePer];
 #pragma unroll
       for (uint32_t u = 0; u < kSePer; ++u) {
-        uint32_t id = kNone, pos, sl = kNone;
-        if ((x.valid & (1u << u)) && entry_hit(sm.b, a, x, u, id, pos)) {
-          uint32_t s = hash_slot(id);
-          for (uint32_t probe = 0; probe < kHashSlots; ++probe) {
-            const uint32_t k = sm.key[s];
-            if (k == id) {
-              sl = s;
-              break;
-            }
-            if (k == kNone) break;
-            s = (s + 1) & (kHashSlots - 1);
-          }
-        } else {
-          id = kNone;
-        }
-        ids[u] = id;
-        slot[u] = sl;
-      }
-#pragma unroll
-      for (uint32_t u = 0; u < kSePer; ++u) {
-        const uint32_t id = ids[u];
-        if (id == kNone) continue;
-        if (slot[u] != kNone) {
-          atomicAdd(&sm.cnt[slot[u]], 1u);
-          continue;
-        }
+        uint32_t id, pos;
+        if (!(x.valid & (1u << u)) || !entry_hit(sm.b, a, x, u, id, pos)) continue;
         uint32_t s = hash_slot(id);
         for (uint32_t probe = 0; probe < kHashSlots; ++probe) {
           uint32_t k = sm.key[s];
@@ -426,7 +399,8 @@ __global__ void __launch_bounds__(kSeBlock, 3) match_dict_kernel(MatchEmitArgs a
 // ------------------------------------------------------------ emission
 
 struct EmitSmem {
-  unsigned long long hslot[kHashSlots];  // (ext id << 32) | rank; ~0: empty
+  uint32_t hkey[kHashSlots];
+  uint16_t hrank[kHashSlots];
   uint32_t cursor[kMatchDictCap];  // the group's next hit, counted from the query's first
   unsigned long long mask[kSeMaskWords][kMatchDictCap];  // batch windows that hit the group
   int32_t mnx[kMatchDictCap];      // least ext pos of the group's hits
@@ -460,9 +434,9 @@ __device__ __forceinline__ uint32_t block_exclusive(uint32_t v, uint32_t* ws) {
 __device__ __forceinline__ uint32_t rank_of(const EmitSmem& sm, uint32_t id, DeviceStatus* st) {
   uint32_t s = hash_slot(id);
   for (uint32_t probe = 0; probe < kHashSlots; ++probe) {
-    const unsigned long long v = sm.hslot[s];  // key and rank in one load
-    if (static_cast<uint32_t>(v >> 32) == id) return static_cast<uint32_t>(v);
-    if (v == ~0ULL) break;
+    const uint32_t k = sm.hkey[s];
+    if (k == id) return sm.hrank[s];
+    if (k == kNone) break;
     s = (s + 1) & (kHashSlots - 1);
   }
   raise_status(st, kDevMatchDict, 0, id);
@@ -496,7 +470,7 @@ __global__ void __launch_bounds__(kSeBlock, 2) match_emit_kernel(
     const uint64_t dbase = q_dbase[q];
     const bool flagged = q_tie[q] != 0;
     // dictionary -> hash of ext id to rank, and each group's first hit
-    for (uint32_t s = t; s < kHashSlots; s += kSeBlock) sm.hslot[s] = ~0ULL;
+    for (uint32_t s = t; s < kHashSlots; s += kSeBlock) sm.hkey[s] = kNone;
     __syncthreads();
     uint32_t c[kPer], sum = 0;
 #pragma unroll
@@ -510,9 +484,11 @@ __global__ void __launch_bounds__(kSeBlock, 2) match_emit_kernel(
         // ng <= kMatchDictCap distinct ids in 2 * kMatchDictCap slots: a free
         // slot is always found within the table
         uint32_t s = hash_slot(id);
-        const unsigned long long v = (static_cast<unsigned long long>(id) << 32) | r;
         for (uint32_t probe = 0; probe < kHashSlots; ++probe) {
-          if (atomicCAS(&sm.hslot[s], ~0ULL, v) == ~0ULL) break;
+          if (atomicCAS(&sm.hkey[s], kNone, id) == kNone) {
+            sm.hrank[s] = static_cast<uint16_t>(r);
+            break;
+          }
           s = (s + 1) & (kHashSlots - 1);
         }
       }
@@ -560,8 +536,6 @@ __global__ void __launch_bounds__(kSeBlock, 2) match_emit_kernel(
       } else {
         // first phase: each hit's group rank and transformed entry (id << 32
         // | pos, in sv); the group masks and ext-pos extremes
-        // (all lookups first, then the updates, so that the entries'
-        // shared-memory reads overlap)
         uint32_t rk[kSePer];
 #pragma unroll
         for (uint32_t u = 0; u < kSePer; ++u) {
@@ -569,35 +543,26 @@ __global__ void __launch_bounds__(kSeBlock, 2) match_emit_kernel(
           if ((x.valid & (1u << u)) && entry_hit(sm.b, a, x, u, id, pos)) {
             r = rank_of(sm, id, a.status);
             x.sv[u] = (static_cast<uint64_t>(id) << 32) | pos;
+            if (r != kNone) {
+              const int wl = x.wl[u];
+              atomicOr(reinterpret_cast<unsigned*>(&sm.mask[wl >> 6][r]) + ((wl >> 5) & 1),
+                       1u << (wl & 31));
+              atomicMin(&sm.mnx[r], static_cast<int32_t>(pos));
+              atomicMax(&sm.mxx[r], static_cast<int32_t>(pos));
+            }
           }
           rk[u] = r;
         }
+        __syncthreads();
+        // second phase: each hit at its group's place
 #pragma unroll
         for (uint32_t u = 0; u < kSePer; ++u) {
           const uint32_t r = rk[u];
           if (r == kNone) continue;
           const int wl = x.wl[u];
-          const int32_t pos = static_cast<int32_t>(static_cast<uint32_t>(x.sv[u]));
-          atomicOr(reinterpret_cast<unsigned*>(&sm.mask[wl >> 6][r]) + ((wl >> 5) & 1),
-                   1u << (wl & 31));
-          atomicMin(&sm.mnx[r], pos);
-          atomicMax(&sm.mxx[r], pos);
-        }
-        __syncthreads();
-        // second phase: each hit at its group's place
-        uint64_t dst[kSePer];
-#pragma unroll
-        for (uint32_t u = 0; u < kSePer; ++u) {
-          const uint32_t r = rk[u];
-          dst[u] = r == kNone ? ~0ULL
-                              : eq.h0 + sm.cursor[r] + earlier_hits(sm, r, x.wl[u]);
-        }
-#pragma unroll
-        for (uint32_t u = 0; u < kSePer; ++u) {
-          if (rk[u] == kNone) continue;
-          const uint64_t d = dst[u];
+          const uint64_t d = eq.h0 + sm.cursor[r] + earlier_hits(sm, r, wl);
           if (d < eq.h1) {  // always, with the dictionary's counts
-            keys[d] = (x.sv[u] & 0xffffffff00000000ULL) | (sm.b.prev[x.wl[u]] & 0x7fffffffu);
+            keys[d] = (x.sv[u] & 0xffffffff00000000ULL) | (sm.b.prev[wl] & 0x7fffffffu);
             vals[d] = static_cast<uint32_t>(x.sv[u]);
           } else {
             raise_status(a.status, kDevMatchDict, 1, static_cast<int64_t>(q));
