@@ -29,9 +29,10 @@ workload against the device-resident index, batched: all reads in one pass.
 * ``stage_rooflines``: every stage's algorithmic GB/s and fraction of the
   HBM peak, with hit generation and chaining on their own;
 * ``configs``: the plain 1 Mb overlap configuration and the read-to-graph
-  configuration, each batched and one read per call, and on request the
-  scale configuration at ``--scale-genome`` with the memory budget scaled
-  to match (``--configs 1,3,5``);
+  configuration, each batched and one read per call, and the scale
+  configuration (500 Mb genome, 15 Gbp of ONT reads, 180 GB budget; one
+  warm-up call and one timed call through the C ABI from pinned buffers;
+  ``--scale-genome`` shrinks it with its budget);
 * ``serving``: continuous batching through cuflye_submit / cuflye_poll on a
   100 Mb indexed genome at several Poisson arrival rates (p50 / p99).
 
@@ -723,11 +724,12 @@ def main() -> int:
     ap.add_argument("--clock-log", default="",
                     help="where the nvidia-smi clock samples of the timed region go "
                          "({rank} is replaced); default /tmp")
-    ap.add_argument("--configs", default="1,3",
+    ap.add_argument("--configs", default="1,3,5",
                     help="other configurations to measure (1: plain 1 Mb, 3: read-to-graph, "
                          "5: scale, at --scale-genome); empty to skip")
-    ap.add_argument("--scale-genome", type=int, default=50_000_000,
-                    help="genome length of config 5 (the configuration's is 500 Mb)")
+    ap.add_argument("--scale-genome", type=int, default=500_000_000,
+                    help="genome length of config 5 (the configuration's 500 Mb by default; "
+                         "smaller values scale its memory budget too)")
     ap.add_argument("--config-plain-sample", type=int, default=2000)
     ap.add_argument("--serve-workers", type=int, default=2)
     ap.add_argument("--serve-batch-bases", type=int, default=32_000_000,
