@@ -800,11 +800,12 @@ constexpr int kHeapWarps = kHeapBlock / 32;
 constexpr size_t kHeapSmem =
     std::max<size_t>(kHeapCap * (sizeof(uint64_t) + sizeof(uint32_t)), (kPackCap + 2) * 4);
 
-// key(a) < key(b) for entries rank << SH | low bits
+// key(a) < key(b) for entries rank << SH | low bits: a's rank is below b's
+// exactly when a < (b with its low bits cleared)
 template <int SH>
 __device__ __forceinline__ bool rank_less(uint32_t a, uint32_t b) {
-  constexpr uint32_t lo = (1u << SH) - 1u;
-  return (a | lo) < (b & ~lo);
+  constexpr uint32_t hi = ~((1u << SH) - 1u);
+  return a < (b & hi);
 }
 
 // Node x lives at word x + 1, so the children 2x + 1 and 2x + 2 of x share
@@ -812,14 +813,48 @@ __device__ __forceinline__ bool rank_less(uint32_t a, uint32_t b) {
 struct OwnHeap {
   uint32_t* E;
   __device__ __forceinline__ uint32_t* at(uint32_t i) const { return E + i; }
+  __device__ __forceinline__ uint32_t ld(uint32_t w) const { return E[w]; }
+  __device__ __forceinline__ uint2 ld2(uint32_t w) const {
+    return *reinterpret_cast<const uint2*>(E + w);
+  }
+  __device__ __forceinline__ uint4 ld4(uint32_t w) const {
+    return *reinterpret_cast<const uint4*>(E + w);
+  }
+  __device__ __forceinline__ void st(uint32_t w, uint32_t x) const { E[w] = x; }
 };
 // Words from kPackCap on live in the partner block (a multiple of 8, so no
-// aligned 8- or 16-byte word straddles the two).
+// aligned 8- or 16-byte word straddles the two).  The heap's own loads and
+// stores address both blocks in the cluster's shared window (lb: this
+// block's word 0, rb: the partner's, which holds word kPackCap).
 struct PairHeap {
   uint32_t* E;
   uint32_t* E1;
+  uint32_t lb, rb;
   __device__ __forceinline__ uint32_t* at(uint32_t i) const {
     return i < kPackCap ? E + i : E1 + (i - kPackCap);
+  }
+  __device__ __forceinline__ uint32_t addr(uint32_t w) const {
+    return w < kPackCap ? lb + 4u * w : rb + 4u * (w - kPackCap);
+  }
+  __device__ __forceinline__ uint32_t ld(uint32_t w) const {
+    uint32_t x;
+    asm volatile("ld.shared::cluster.u32 %0, [%1];" : "=r"(x) : "r"(addr(w)));
+    return x;
+  }
+  __device__ __forceinline__ uint2 ld2(uint32_t w) const {
+    uint2 x;
+    asm volatile("ld.shared::cluster.v2.u32 {%0, %1}, [%2];" : "=r"(x.x), "=r"(x.y) : "r"(addr(w)));
+    return x;
+  }
+  __device__ __forceinline__ uint4 ld4(uint32_t w) const {
+    uint4 x;
+    asm volatile("ld.shared::cluster.v4.u32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(x.x), "=r"(x.y), "=r"(x.z), "=r"(x.w)
+                 : "r"(addr(w)));
+    return x;
+  }
+  __device__ __forceinline__ void st(uint32_t w, uint32_t x) const {
+    asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(addr(w)), "r"(x) : "memory");
   }
 };
 
@@ -832,10 +867,10 @@ __device__ __forceinline__ void packed_adjust(H h, uint32_t hole, uint32_t len, 
   // three of libstdc++'s steps at once while every node two levels below the
   // hole has two children: the 2 + 4 + 8 candidate nodes load together
   while (4 * child + 6 < lim) {
-    const uint2 a = *reinterpret_cast<const uint2*>(h.at(2 * (child + 1)));
-    const uint4 b = *reinterpret_cast<const uint4*>(h.at(4 * (child + 1)));
-    const uint4 c0 = *reinterpret_cast<const uint4*>(h.at(8 * (child + 1)));
-    const uint4 c1 = *reinterpret_cast<const uint4*>(h.at(8 * (child + 1) + 4));
+    const uint2 a = h.ld2(2 * (child + 1));
+    const uint4 b = h.ld4(4 * (child + 1));
+    const uint4 c0 = h.ld4(8 * (child + 1));
+    const uint4 c1 = h.ld4(8 * (child + 1) + 4);
     const bool s1 = !rank_less<SH>(a.y, a.x);  // the right child unless right < left
     const uint32_t v1 = s1 ? a.y : a.x;
     const uint32_t l2 = s1 ? b.z : b.x, r2 = s1 ? b.w : b.y;
@@ -847,36 +882,36 @@ __device__ __forceinline__ void packed_adjust(H h, uint32_t hole, uint32_t len, 
     const uint32_t v3 = s3 ? r3 : l3;
     const uint32_t n1 = 2 * child + 1 + s1;
     const uint32_t n2 = 2 * n1 + 1 + s2;
-    *h.at(child + 1) = v1;
-    *h.at(n1 + 1) = v2;
-    *h.at(n2 + 1) = v3;
+    h.st(child + 1, v1);
+    h.st(n1 + 1, v2);
+    h.st(n2 + 1, v3);
     child = 2 * n2 + 1 + s3;
   }
   hole = child;
   while (child < lim) {
     child = 2 * (child + 1);
-    const uint2 pr = *reinterpret_cast<const uint2*>(h.at(child));  // nodes child - 1, child
+    const uint2 pr = h.ld2(child);  // nodes child - 1, child
     uint32_t c = pr.y;
     if (rank_less<SH>(pr.y, pr.x)) {
       --child;
       c = pr.x;
     }
-    *h.at(hole + 1) = c;
+    h.st(hole + 1, c);
     hole = child;
   }
   if ((len & 1u) == 0 && len >= 2 && child == (len - 2) / 2) {
     child = 2 * (child + 1);
-    *h.at(hole + 1) = *h.at(child);
+    h.st(hole + 1, h.ld(child));
     hole = child - 1;
   }
   while (hole > top) {
     const uint32_t parent = (hole - 1) / 2;
-    const uint32_t pv = *h.at(parent + 1);
+    const uint32_t pv = h.ld(parent + 1);
     if (!rank_less<SH>(pv, v)) break;
-    *h.at(hole + 1) = pv;
+    h.st(hole + 1, pv);
     hole = parent;
   }
-  *h.at(hole + 1) = v;
+  h.st(hole + 1, v);
 }
 
 // make_heap by levels (all threads), then sort_heap (thread 0).
@@ -887,13 +922,13 @@ __device__ void packed_heap_run(H h, uint32_t n) {
     const uint32_t lo = (1u << lv) - 1u;
     const uint32_t hi = min((2u << lv) - 2u, last_parent);
     for (uint32_t p = lo + threadIdx.x; p <= hi; p += kHeapBlock)
-      packed_adjust<SH>(h, p, n, *h.at(p + 1));
+      packed_adjust<SH>(h, p, n, h.ld(p + 1));
     __syncthreads();
   }
   if (threadIdx.x == 0) {
     for (uint32_t last = n - 1; last >= 1; --last) {
-      const uint32_t v = *h.at(last + 1);
-      *h.at(last + 1) = *h.at(1);
+      const uint32_t v = h.ld(last + 1);
+      h.st(last + 1, h.ld(1));
       packed_adjust<SH>(h, 0, last, v);
     }
   }
@@ -1204,7 +1239,11 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kHeapBlock, 1)
       uint64_t kmin = 0;
       int kb = 0;
       heap_key_span(K, f, n, hs, kmin, kb);
-      const PairHeap h{E, cluster.map_shared_rank(E, 1)};
+      const uint32_t sa = static_cast<uint32_t>(__cvta_generic_to_shared(E));
+      uint32_t lb, rb;
+      asm("mapa.shared::cluster.u32 %0, %1, 0;" : "=r"(lb) : "r"(sa));
+      asm("mapa.shared::cluster.u32 %0, %1, 1;" : "=r"(rb) : "r"(sa));
+      const PairHeap h{E, cluster.map_shared_rank(E, 1), lb, rb};
       const bool done = n <= kPairCap && kb <= 46 && pair_heap_sort(K, V, Lg, Rg, f, n, kmin, kb, h, hs);
       if (!done) {
         if (threadIdx.x == 0) isort::heap_sort(K + f, V + f, 0, n);
