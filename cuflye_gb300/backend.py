@@ -188,6 +188,9 @@ def load_library(path: Path | None = None) -> ctypes.CDLL:
     L.cuflye_submit.argtypes = [_vp, ctypes.c_size_t, _i64p, _i64p, ctypes.c_char_p, _u64p]
     L.cuflye_poll.restype = S
     L.cuflye_poll.argtypes = [_vp, ctypes.c_uint64, ctypes.c_int, _vp, ctypes.c_size_t, _szp]
+    L.cuflye_poll_any.restype = S
+    L.cuflye_poll_any.argtypes = [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_uint64), _vp,
+                                  ctypes.c_size_t, _szp]
     L.cuflye_server_stats.restype = S
     L.cuflye_server_stats.argtypes = [_vp, _u64p, _u64p, _u64p]
     L.cuflye_server_last_error.restype = ctypes.c_char_p
@@ -571,6 +574,23 @@ class CudaServer:
             if st != 0:
                 self._err(st)
             return out[:n.value]
+
+    def poll_any(self, wait_ms: int = -1, capacity: int = 4096):
+        """The next finished request in completion order: (ticket, rows), or
+        None when none finished within wait_ms.  A request that failed raises
+        its error."""
+        tk = ctypes.c_uint64()
+        out = np.empty(capacity, dtype=abi.OVERLAP_DTYPE)
+        n = ctypes.c_size_t()
+        st = self._L.cuflye_poll_any(self._h, int(wait_ms), ctypes.byref(tk), out.ctypes.data,
+                                     capacity, ctypes.byref(n))
+        if st == PENDING:
+            return None
+        if st == ERR_CAPACITY:  # kept for poll on its ticket
+            return tk.value, self.poll(tk.value, 0, capacity=n.value)
+        if st != 0:
+            self._err(st)
+        return tk.value, out[:n.value]
 
     def stats(self) -> dict:
         a, b, c = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()

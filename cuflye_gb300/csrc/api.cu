@@ -740,6 +740,7 @@ struct PassState {
   const uint64_t* wmeta = nullptr;
   const uint8_t* wflags = nullptr;
   const uint32_t* wself = nullptr;
+  uint64_t fit_hits = 0;  // the hits the memory left could hold when the pass was cut
 };
 
 // Buffers sized by the hit count of a pass (reused by the next pass).
@@ -899,6 +900,7 @@ bool run_hits(cuflye_ctx* c, const Queries& Q, size_t q0, size_t q1, bool want_k
   const uint64_t fits = static_cast<uint64_t>(
       static_cast<double>(avail) / (static_cast<double>(bytes_per_hit) + c->other_per_hit));
   uint64_t hit_limit = fits;
+  ps.fit_hits = fits;
   if (c->pass_hit_cap) hit_limit = std::min(hit_limit, c->pass_hit_cap);
   // Under a caller's budget a pass keeps to the per-hit buffers an earlier
   // pass grew when they hold at least 90 % of what fits: growing them frees
@@ -1342,7 +1344,11 @@ void for_each_pass(cuflye_ctx* c, const Queries& Q, bool kmers, uint64_t bytes_p
       step = std::max<size_t>(ps.nq / 2, 1);
       continue;
     }
-    if (c->budget && ps.nhits) {
+    // Learn the body's other buffers per hit only from passes that came near
+    // what the memory left could hold: a small pass's buffers (some held at
+    // the size an earlier, larger pass grew them to), divided by its few
+    // hits, would make every later pass of the context tiny.
+    if (c->budget && ps.nhits && ps.nhits * 2 >= ps.fit_hits) {
       const double other = static_cast<double>(c->in_use - held_bytes(c));
       c->other_per_hit = std::max(c->other_per_hit, other / static_cast<double>(ps.nhits));
     }
@@ -2350,6 +2356,7 @@ struct cuflye_server {
   std::condition_variable cv_work, cv_done;
   std::deque<ServeRequest> pending;
   std::unordered_map<uint64_t, ServeResult> results;
+  std::deque<uint64_t> finished;  // tickets in completion order, for cuflye_poll_any
   uint64_t next_ticket = 1;
   bool stop = false;
   uint64_t batches = 0, batched_requests = 0;
@@ -2405,6 +2412,7 @@ void serve_worker(cuflye_server* s, cuflye_ctx* c) {
       for (const ServeRequest& req : batch) {
         ServeResult& res = s->results[req.ticket];
         res.done = true;
+        s->finished.push_back(req.ticket);
         res.status = st;
         res.err = msg;
         if (st == CUFLYE_OK) {
@@ -2538,6 +2546,45 @@ cuflye_status cuflye_poll(cuflye_server* s, uint64_t ticket, int wait_ms, cuflye
   if (res.rows.size() > out_cap) {
     s->err = "output capacity too small: need " + std::to_string(res.rows.size()) +
              " overlap rows";
+    return CUFLYE_ERR_CAPACITY;
+  }
+  if (!res.rows.empty()) std::memcpy(out, res.rows.data(), res.rows.size() * sizeof(res.rows[0]));
+  s->results.erase(it);
+  return CUFLYE_OK;
+}
+
+cuflye_status cuflye_poll_any(cuflye_server* s, int wait_ms, uint64_t* ticket,
+                              cuflye_overlap_range* out, size_t out_cap, size_t* n_out) {
+  if (!s || !ticket) return CUFLYE_ERR_INVALID;
+  *ticket = 0;
+  std::unique_lock<std::mutex> lk(s->mu);
+  // drop tickets that cuflye_poll consumed already
+  auto settle = [&] {
+    while (!s->finished.empty() && !s->results.count(s->finished.front())) s->finished.pop_front();
+    return !s->finished.empty();
+  };
+  if (!settle() && wait_ms != 0) {
+    if (wait_ms < 0)
+      s->cv_done.wait(lk, settle);
+    else
+      s->cv_done.wait_for(lk, std::chrono::milliseconds(wait_ms), settle);
+  }
+  if (!settle()) return CUFLYE_PENDING;
+  const uint64_t tk = s->finished.front();
+  s->finished.pop_front();
+  *ticket = tk;
+  auto it = s->results.find(tk);
+  ServeResult& res = it->second;
+  if (res.status != CUFLYE_OK) {
+    const cuflye_status st = res.status;
+    s->err = res.err;
+    s->results.erase(it);
+    return st;
+  }
+  if (n_out) *n_out = res.rows.size();
+  if (res.rows.size() > out_cap) {
+    s->err = "output capacity too small: need " + std::to_string(res.rows.size()) +
+             " overlap rows (ticket " + std::to_string(tk) + ", kept for cuflye_poll)";
     return CUFLYE_ERR_CAPACITY;
   }
   if (!res.rows.empty()) std::memcpy(out, res.rows.data(), res.rows.size() * sizeof(res.rows[0]));

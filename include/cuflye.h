@@ -460,6 +460,15 @@ cuflye_status cuflye_submit(cuflye_server* server, size_t n, const int64_t* quer
                             const int64_t* offsets, const char* bases, uint64_t* ticket);
 cuflye_status cuflye_poll(cuflye_server* server, uint64_t ticket, int wait_ms,
                           cuflye_overlap_range* out, size_t out_cap, size_t* n_out);
+/* The next finished request in completion order, for a caller with many in
+ * flight: waits up to wait_ms (negative: until one finishes, 0: no wait) and
+ * returns CUFLYE_PENDING with *ticket = 0, or the ticket with the request's
+ * error or rows (consumed as by cuflye_poll).  With too small a capacity it
+ * returns CUFLYE_ERR_CAPACITY with the ticket and the row count; the result
+ * is then kept for cuflye_poll on that ticket and not returned here again.
+ * Tickets that cuflye_poll consumed first are skipped. */
+cuflye_status cuflye_poll_any(cuflye_server* server, int wait_ms, uint64_t* ticket,
+                              cuflye_overlap_range* out, size_t out_cap, size_t* n_out);
 /* Batches run so far, requests they carried, requests waiting. */
 cuflye_status cuflye_server_stats(cuflye_server* server, uint64_t* batches, uint64_t* requests,
                                   uint64_t* pending);

@@ -98,3 +98,22 @@ def test_candidates_passes_do_not_change_records(built_lib, scale_case):
         cand2, filt2 = be.candidates(q)
     assert len(cand) > 0
     assert cand2.tobytes() == cand.tobytes() and filt2.tobytes() == filt.tobytes()
+
+
+def test_small_calls_do_not_shrink_later_passes(built_lib, scale_case):
+    """Under a budget, one-read calls before a large call leave its passes as
+    they are: the pass body's other buffers are learned per hit only from
+    passes where they take a real share of the budget."""
+    from cuflye_gb300.backend import CudaBackend, OverlapParams
+    wl = scale_case
+    p = OverlapParams.make(**wl.params)
+    with CudaBackend(device=0, memory_budget_bytes=16 << 30) as be:
+        be.build_index(wl.reads, wl.k, wl.min_freq, wl.max_freq)
+        whole = be.overlaps(wl.reads, p)
+        assert be.last_passes() == 1
+        for i in range(5):
+            be.overlaps(wl.reads.subset(np.arange(i, i + 1)), p)
+        again = be.overlaps(wl.reads, p)
+        assert be.last_passes() == 1
+        assert be.last_pass_stats()["retries"] == 0
+    assert again.tobytes() == whole.tobytes()

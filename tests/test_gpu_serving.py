@@ -78,3 +78,34 @@ def test_server_errors(gpu, golden_cases):
     gpu.build_index(reads, meta["k"], meta["min_freq"], meta["max_freq"])  # closed: fine
     with pytest.raises(CuflyeError):  # k of the params must match the index
         CudaServer(gpu, OverlapParams.make(**dict(meta["params"], kmer_size=meta["k"] + 2)))
+
+
+def test_poll_any_returns_each_request_once_in_completion_order(gpu, golden_cases):
+    """cuflye_poll_any hands back every finished request exactly once, with
+    the rows cuflye_overlaps gives it alone; a request whose rows do not fit
+    stays for cuflye_poll on its ticket; one that cuflye_poll consumed first
+    is skipped; with nothing in flight it reports pending."""
+    from cuflye_gb300.backend import CudaServer, OverlapParams
+    reads, meta, _ = golden_cases["ovl-d"]
+    gpu.build_index(reads, meta["k"], meta["min_freq"], meta["max_freq"])
+    params = OverlapParams.make(**meta["params"])
+    reqs = _split(reads, [2, 5, 1, 9, 3, 12, 4, 6])
+    direct = [overlap_tuples_gpu(gpu.overlaps(r, params)) for r in reqs]
+    with CudaServer(gpu, params, workers=2) as srv:
+        assert srv.poll_any(0) is None
+        tickets = [srv.submit(r) for r in reqs]
+        which = {tk: i for i, tk in enumerate(tickets)}
+        got = {}
+        while len(got) < len(reqs):
+            tk, rows = srv.poll_any(-1, capacity=1)  # small: some take the poll route
+            assert tk in which and tk not in got
+            got[tk] = overlap_tuples_gpu(rows)
+        assert [got[tk] for tk in tickets] == direct
+        assert srv.poll_any(0) is None
+        # consumed by poll first: poll_any skips it
+        t1 = srv.submit(reqs[0])
+        assert overlap_tuples_gpu(srv.poll(t1, -1)) == direct[0]
+        t2 = srv.submit(reqs[1])
+        tk, rows = srv.poll_any(-1)
+        assert tk == t2 and overlap_tuples_gpu(rows) == direct[1]
+        assert srv.poll_any(0) is None
