@@ -565,6 +565,11 @@ def run_ours(args, world, rank, local) -> None:
     # this rank's queries (all reads on one GPU; a length-balanced share
     # under torchrun), against the index of all reads
     mine = reads if world == 1 else reads.subset(shard_reads(np.diff(reads.offsets), world)[rank])
+    if args.query_sample > 0:
+        # profiling cases: the first reads only, against the index of all
+        mine = mine.subset(np.arange(min(args.query_sample, mine.n)))
+    if args.emission_mode >= 0:
+        gpu.set_sorted_emission(args.emission_mode)
     # pinned host inputs / outputs for the end-to-end leg
     seqs = Sequences(pinned_like(np.ascontiguousarray(mine.ids, dtype=np.int64)),
                      pinned_like(np.ascontiguousarray(mine.offsets, dtype=np.int64)),
@@ -692,6 +697,10 @@ def run_ours(args, world, rank, local) -> None:
                      if peak else "missing"},
         "clocks": clocks,
     }
+    if args.query_sample > 0:
+        line["config"]["query_sample"] = int(mine.n)
+    if args.emission_mode >= 0:
+        line["config"]["emission_mode"] = args.emission_mode
     if plain:
         line["plain"] = plain
         lat_ms = sorted(1000 * x for x in lat)
@@ -741,6 +750,12 @@ def main() -> int:
     ap.add_argument("--serve-workers", type=int, default=2)
     ap.add_argument("--serve-batch-bases", type=int, default=32_000_000,
                     help="most read bases one served batch takes")
+    ap.add_argument("--query-sample", type=int, default=0,
+                    help="time only this many reads (the first) as queries against the "
+                         "index of all reads, for profiling cases (0: all)")
+    ap.add_argument("--emission-mode", type=int, default=-1, choices=[-1, 0, 1, 2],
+                    help="cuflye_set_sorted_emission mode for the timed calls (-1: the "
+                         "library's default)")
     ap.add_argument("--autotune", type=int, default=1500,
                     help="reads in the autotuner's sample, run before the timed steps "
                          "(0: the default launch shape)")

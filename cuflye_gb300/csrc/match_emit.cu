@@ -399,8 +399,7 @@ __global__ void __launch_bounds__(kSeBlock, 3) match_dict_kernel(MatchEmitArgs a
 // ------------------------------------------------------------ emission
 
 struct EmitSmem {
-  uint32_t hkey[kHashSlots];
-  uint16_t hrank[kHashSlots];
+  unsigned long long hent[kHashSlots];  // rank << 32 | ext id (kNone: free)
   uint32_t cursor[kMatchDictCap];  // the group's next hit, counted from the query's first
   unsigned long long mask[kSeMaskWords][kMatchDictCap];  // batch windows that hit the group
   int32_t mnx[kMatchDictCap];      // least ext pos of the group's hits
@@ -434,8 +433,9 @@ __device__ __forceinline__ uint32_t block_exclusive(uint32_t v, uint32_t* ws) {
 __device__ __forceinline__ uint32_t rank_of(const EmitSmem& sm, uint32_t id, DeviceStatus* st) {
   uint32_t s = hash_slot(id);
   for (uint32_t probe = 0; probe < kHashSlots; ++probe) {
-    const uint32_t k = sm.hkey[s];
-    if (k == id) return sm.hrank[s];
+    const unsigned long long e = sm.hent[s];
+    const uint32_t k = static_cast<uint32_t>(e);
+    if (k == id) return static_cast<uint32_t>(e >> 32);
     if (k == kNone) break;
     s = (s + 1) & (kHashSlots - 1);
   }
@@ -470,7 +470,7 @@ __global__ void __launch_bounds__(kSeBlock, 2) match_emit_kernel(
     const uint64_t dbase = q_dbase[q];
     const bool flagged = q_tie[q] != 0;
     // dictionary -> hash of ext id to rank, and each group's first hit
-    for (uint32_t s = t; s < kHashSlots; s += kSeBlock) sm.hkey[s] = kNone;
+    for (uint32_t s = t; s < kHashSlots; s += kSeBlock) sm.hent[s] = kNone;
     __syncthreads();
     uint32_t c[kPer], sum = 0;
 #pragma unroll
@@ -485,10 +485,9 @@ __global__ void __launch_bounds__(kSeBlock, 2) match_emit_kernel(
         // slot is always found within the table
         uint32_t s = hash_slot(id);
         for (uint32_t probe = 0; probe < kHashSlots; ++probe) {
-          if (atomicCAS(&sm.hkey[s], kNone, id) == kNone) {
-            sm.hrank[s] = static_cast<uint16_t>(r);
+          if (atomicCAS(&sm.hent[s], static_cast<unsigned long long>(kNone),
+                        (static_cast<unsigned long long>(r) << 32) | id) == kNone)
             break;
-          }
           s = (s + 1) & (kHashSlots - 1);
         }
       }
