@@ -188,6 +188,8 @@ def load_library(path: Path | None = None) -> ctypes.CDLL:
     L.cuflye_submit.argtypes = [_vp, ctypes.c_size_t, _i64p, _i64p, ctypes.c_char_p, _u64p]
     L.cuflye_poll.restype = S
     L.cuflye_poll.argtypes = [_vp, ctypes.c_uint64, ctypes.c_int, _vp, ctypes.c_size_t, _szp]
+    L.cuflye_trim.restype = S
+    L.cuflye_trim.argtypes = [_vp]
     L.cuflye_poll_any.restype = S
     L.cuflye_poll_any.argtypes = [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_uint64), _vp,
                                   ctypes.c_size_t, _szp]
@@ -311,6 +313,11 @@ class CudaBackend:
         """Hits straight into KmerMatch order: 1 / True where windows are
         dense (the default), 2 for every pass, 0 / False never (emit + sort)."""
         self._check(self._L.cuflye_set_sorted_emission(self._h, int(mode)))
+
+    def trim(self) -> None:
+        """Returns the context's cached working buffers to the device (the
+        index stays)."""
+        self._check(self._L.cuflye_trim(self._h))
 
     def last_pass_stats(self) -> dict:
         """Passes of the last call, budget retries, and host ms in allocation."""

@@ -990,6 +990,111 @@ SortTasks sort_tasks(cuflye_ctx* c, const std::string& prefix, uint64_t nelems, 
                    c->shape.round_blocks_per_sm};
 }
 
+// The flagged queries' KmerMatch sort (their hits in generation order at
+// [qb[s], qe[s]), *ecount of them) in libstdc++ order.  Their equal keys
+// are few (a window whose bucket lists one target twice), and a range of
+// the introsort whose key interval holds none of them has distinct keys, so
+// its final order is its sorted order.  So the hits are radix-sorted in
+// place (the sorted order up to the order among equal keys), and the
+// introsort is emulated on a copy in generation order, pruned to the
+// ranges that may hold equal keys; the ranges it sorted are copied back.
+// Without the recorded keys (more than the list holds) the whole introsort
+// is emulated in place.
+void flagged_sort(cuflye_ctx* c, PassState& ps, const MatchEmitLists& L, uint64_t* qb,
+                  uint64_t* qe, uint32_t* ecount, uint64_t* alt_keys, uint32_t* alt_vals,
+                  uint32_t* lscr, uint32_t* rscr, uint32_t* lists, uint32_t* scounts) {
+  cudaStream_t st = c->stream;
+  const uint64_t H = ps.nhits;
+  const uint32_t nq = ps.nq;
+  uint32_t back[2] = {0, 0};
+  CUFLYE_CHECK(cudaMemcpyAsync(&back[0], ecount, 4, cudaMemcpyDeviceToHost, st));
+  CUFLYE_CHECK(cudaMemcpyAsync(&back[1], L.tie_count, 4, cudaMemcpyDeviceToHost, st));
+  sync(c);
+  const uint32_t E = back[0], T = back[1];
+  if (E == 0) return;
+  if (T > L.tie_cap) {
+    CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, qb, qe, nq, ecount, lists,
+                                    scounts, c->num_sms, st, sort_tasks(c, "s", H, nq)));
+    return;
+  }
+  std::vector<uint64_t> b(E), e(E), th(T), tk(T);
+  CUFLYE_CHECK(cudaMemcpyAsync(b.data(), qb, E * 8ull, cudaMemcpyDeviceToHost, st));
+  CUFLYE_CHECK(cudaMemcpyAsync(e.data(), qe, E * 8ull, cudaMemcpyDeviceToHost, st));
+  if (T) {
+    CUFLYE_CHECK(cudaMemcpyAsync(th.data(), L.tie_h0, T * 8ull, cudaMemcpyDeviceToHost, st));
+    CUFLYE_CHECK(cudaMemcpyAsync(tk.data(), L.tie_key, T * 8ull, cudaMemcpyDeviceToHost, st));
+  }
+  sync(c);
+  // segments in hit order, their places in the compact copy
+  std::vector<uint32_t> ord(E);
+  for (uint32_t i = 0; i < E; ++i) ord[i] = i;
+  std::sort(ord.begin(), ord.end(), [&](uint32_t x, uint32_t y) { return b[x] < b[y]; });
+  // host staging: begin, end, compact begin, compact end (4 E words), then
+  // the keys' offsets (E + 1) and the keys
+  std::vector<uint64_t> seg(4ull * E);
+  uint64_t F = 0;
+  for (uint32_t i = 0; i < E; ++i) {
+    seg[i] = b[ord[i]];
+    seg[E + i] = e[ord[i]];
+    seg[2ull * E + i] = F;
+    F += e[ord[i]] - b[ord[i]];
+    seg[3ull * E + i] = F;
+  }
+  std::vector<std::pair<uint32_t, uint64_t>> ties(T);
+  for (uint32_t i = 0; i < T; ++i) {
+    const uint32_t s = static_cast<uint32_t>(
+        std::upper_bound(seg.begin(), seg.begin() + E, th[i]) - seg.begin() - 1);
+    ties[i] = {s, tk[i]};
+  }
+  std::sort(ties.begin(), ties.end());
+  ties.erase(std::unique(ties.begin(), ties.end()), ties.end());
+  std::vector<uint32_t> poff(E + 1, 0);
+  std::vector<uint64_t> pkeys(ties.size());
+  for (size_t i = 0; i < ties.size(); ++i) {
+    ++poff[ties[i].first + 1];
+    pkeys[i] = ties[i].second;
+  }
+  for (uint32_t i = 0; i < E; ++i) poff[i + 1] += poff[i];
+  uint64_t* dseg = buf<uint64_t>(c, "f_seg", 4ull * E);
+  uint32_t* dpoff = buf<uint32_t>(c, "f_poff", E + 1);
+  uint64_t* dpkeys = buf<uint64_t>(c, "f_pkeys", std::max<size_t>(pkeys.size(), 1));
+  uint64_t* gk = buf<uint64_t>(c, "f_gk", F);
+  uint32_t* gv = buf<uint32_t>(c, "f_gv", F);
+  CUFLYE_CHECK(cudaMemcpyAsync(dseg, seg.data(), seg.size() * 8ull, cudaMemcpyHostToDevice, st));
+  CUFLYE_CHECK(cudaMemcpyAsync(dpoff, poff.data(), poff.size() * 4ull, cudaMemcpyHostToDevice, st));
+  if (!pkeys.empty())
+    CUFLYE_CHECK(cudaMemcpyAsync(dpkeys, pkeys.data(), pkeys.size() * 8ull,
+                                 cudaMemcpyHostToDevice, st));
+  const uint64_t* sb = dseg;
+  const uint64_t* se = dseg + E;
+  const uint64_t* cb = dseg + 2ull * E;
+  const uint64_t* ce = dseg + 3ull * E;
+  // the generation order, gathered
+  CUFLYE_CHECK(gather_ranges(ps.keys, ps.vals, sb, se, cb, E, gk, gv, c->num_sms, st));
+  // the sorted order in place: a stable radix sort by ext id of each
+  // flagged query's hits (in cur-pos order as generated)
+  uint32_t* ntiles = buf<uint32_t>(c, "m_ntiles", nq);
+  uint64_t* tile_off = buf<uint64_t>(c, "m_tileoff", nq + 1);
+  int id_bits = 0;
+  while (id_bits < 32 && ((2ull * c->idx.nslots - 1) >> id_bits) != 0) ++id_bits;
+  CUFLYE_CHECK(match_plan(ps.q_off, ps.q_tie, nq, ntiles, nullptr, nullptr, nullptr, st, true));
+  const uint64_t NT = scan_u32(c, ntiles, tile_off, nq, "m_scan");
+  MatchTile* tiles = buf<MatchTile>(c, "m_tiles", NT);
+  uint32_t* mcounts = buf<uint32_t>(c, "m_counts", 256 * NT);
+  CUFLYE_CHECK(match_tiles(ps.q_off, ntiles, tile_off, nq, tiles, st));
+  CUFLYE_CHECK(match_radix(ps.keys, ps.vals, alt_keys, alt_vals, tiles, static_cast<uint32_t>(NT),
+                           ps.q_off, ntiles, tile_off, nq, id_bits, mcounts, c->num_sms,
+                           c->shape.scatter_blocks_per_sm, st));
+  // the pruned introsort on the copy, and the ranges it sorted copied back
+  SortTasks t = sort_tasks(c, "f", F, E);
+  t.prune_keys = dpkeys;
+  t.prune_off = dpoff;
+  CUFLYE_CHECK(segmented_std_sort(gk, gv, lscr, rscr, cb, ce, E, nullptr, lists, scounts,
+                                  c->num_sms, st, t));
+  CUFLYE_CHECK(copy_sorted_ranges(gk, gv, cb, ce, sb, E, scounts, t, ps.keys, ps.vals, c->num_sms,
+                                  st));
+}
+
 // Sort + chaining of the pass's hits; returns the number of overlap rows left
 // on the device in "o_rows" (OverlapRow, query order, Flye emission order).
 uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp,
@@ -1037,7 +1142,7 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp,
     uint32_t* q_ng = buf<uint32_t>(c, "m_qng", nq);
     uint64_t* q_dbase = buf<uint64_t>(c, "m_qdbase", nq);
     uint64_t* q_goff = buf<uint64_t>(c, "m_qgoff", nq + 1);
-    uint32_t* mwords = buf<uint32_t>(c, "m_words", 4);  // overflow, counter
+    uint32_t* mwords = buf<uint32_t>(c, "m_words", 4);  // overflow, counter, tie count
     unsigned long long* dcur = buf<unsigned long long>(c, "m_dcur", 3);  // cursor, tallies
     CUFLYE_CHECK(cudaMemsetAsync(mwords, 0, 4 * sizeof(uint32_t), st));
     CUFLYE_CHECK(cudaMemsetAsync(dcur, 0, 3 * sizeof(unsigned long long), st));
@@ -1064,13 +1169,18 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp,
       CUFLYE_CHECK(cudaMemsetAsync(gcounts, 0, 4 * sizeof(uint32_t), st));
       CUFLYE_CHECK(cudaMemsetAsync(ecount, 0, sizeof(uint32_t), st));
       MatchEmitLists L{dp_list, ext_list, pf_list, gcounts, qb, qe, ecount, dcur + 1};
+      const uint32_t tie_cap = static_cast<uint32_t>(std::min<uint64_t>(H / 16 + 1024, 1u << 22));
+      L.tie_h0 = buf<uint64_t>(c, "f_tieh0", tie_cap);
+      L.tie_key = buf<uint64_t>(c, "f_tiekey", tie_cap);
+      L.tie_count = mwords + 2;
+      L.tie_cap = tie_cap;
+      CUFLYE_CHECK(cudaMemsetAsync(L.tie_count, 0, sizeof(uint32_t), st));
       CUFLYE_CHECK(match_emit(a, alt_keys, q_ng, q_dbase, q_goff, ps.q_tie, ps.qinfo, cp, ps.keys,
                               ps.vals, groups, L, mwords + 1, c->num_sms, st));
       CUFLYE_CHECK(cudaEventRecord(c->ev[1], st));
       // 1. the flagged queries' KmerMatch sort in libstdc++ order
       CUFLYE_CHECK(sort_stats_add(sstats, 0, 1, nullptr, nq, ecount, st));
-      CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, qb, qe, nq, ecount, lists,
-                                      scounts, c->num_sms, st, sort_tasks(c, "s", H, nq)));
+      flagged_sort(c, ps, L, qb, qe, ecount, alt_keys, alt_vals, lscr, rscr, lists, scounts);
       CUFLYE_CHECK(cudaEventRecord(c->ev[2], st));
       // 2. the prefilter of the groups the emission left open
       CUFLYE_CHECK(groups_prefilter_list(ps.keys, ps.vals, groups, pf_list, ps.qinfo, slot_len, cp,
@@ -2264,6 +2374,20 @@ cuflye_status cuflye_last_passes(const cuflye_ctx* c, uint64_t* passes) {
   if (!c || !passes) return CUFLYE_ERR_INVALID;
   *passes = c->passes;
   return CUFLYE_OK;
+}
+
+cuflye_status cuflye_trim(cuflye_ctx* c) {
+  CUFLYE_API_BEGIN(c)
+  sync(c);
+  std::vector<std::string> names;
+  for (const auto& kv : c->bufs) {
+    const std::string& n = kv.first;
+    const bool keep = n.compare(0, 3, "ix_") == 0 || n.compare(0, 3, "gr_") == 0 ||
+                      n.compare(0, 5, "logf_") == 0 || n == "status";
+    if (!keep) names.push_back(n);
+  }
+  for (const std::string& n : names) release(c, n);
+  CUFLYE_API_END(c)
 }
 
 cuflye_status cuflye_last_pass_stats(const cuflye_ctx* c, uint64_t* passes, uint64_t* retries,

@@ -62,11 +62,15 @@ struct PairsAoS {
 __global__ void match_plan_kernel(const uint64_t* __restrict__ q_off,
                                   const uint32_t* __restrict__ q_tie, uint32_t nq,
                                   uint32_t* __restrict__ ntiles, uint64_t* __restrict__ emu_begin,
-                                  uint64_t* __restrict__ emu_end, uint32_t* __restrict__ emu_count) {
+                                  uint64_t* __restrict__ emu_end, uint32_t* __restrict__ emu_count,
+                                  bool tile_flagged) {
   for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
     const uint64_t b = q_off[q], e = q_off[q + 1];
     uint32_t t = 0;
-    if (e - b > 1) {
+    if (tile_flagged) {
+      // the flagged queries only, all by radix tiles
+      if (e - b > 1 && q_tie[q]) t = static_cast<uint32_t>((e - b + kMatchTile - 1) / kMatchTile);
+    } else if (e - b > 1) {
       if (q_tie[q]) {
         const uint32_t s = atomicAdd(emu_count, 1u);
         emu_begin[s] = b;
@@ -579,12 +583,12 @@ void allow_smem(T* kernel, size_t bytes) {
 
 cudaError_t match_plan(const uint64_t* q_off, const uint32_t* q_tie, uint32_t nq, uint32_t* ntiles,
                        uint64_t* emu_begin, uint64_t* emu_end, uint32_t* emu_count,
-                       cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(emu_count, 0, 4, s);
+                       cudaStream_t s, bool tile_flagged) {
+  cudaError_t e = tile_flagged ? cudaSuccess : cudaMemsetAsync(emu_count, 0, 4, s);
   if (e != cudaSuccess || nq == 0) return e;
   count_launch();
   match_plan_kernel<<<(nq + 255) / 256, 256, 0, s>>>(q_off, q_tie, nq, ntiles, emu_begin, emu_end,
-                                                     emu_count);
+                                                     emu_count, tile_flagged);
   return cudaGetLastError();
 }
 

@@ -30,6 +30,7 @@ size_t segsort_smem_bytes();
 constexpr uint32_t kHeapPackCap = 57344;
 // Rounds of the global phase (partitions of ranges beyond shared memory).
 constexpr int kSortRounds = 64;
+constexpr size_t kRoundItemBytes = 40;  // one range of a global-phase round
 struct SortTasks {
   uint64_t* f;
   uint32_t* n;
@@ -40,6 +41,12 @@ struct SortTasks {
   void* round[2];         // two round lists of segsort_round_bytes(nelems) each
   uint32_t* round_counts;  // 2 * (kSortRounds + 1) words
   int round_per_sm = 0;    // blocks per SM of the global phase (1-2; 0: 2)
+  // Pruning (optional): segment s's keys that may repeat, sorted, are
+  // prune_keys[prune_off[s] .. prune_off[s + 1]).  A global-phase range whose
+  // key interval holds none of them has distinct keys, so any sort gives its
+  // final order: it is dropped (left as it is) and not listed as a task.
+  const uint64_t* prune_keys = nullptr;
+  const uint32_t* prune_off = nullptr;
 };
 uint32_t segsort_pair_reserve(uint64_t nelems);
 size_t segsort_round_bytes(uint64_t nelems);
@@ -51,6 +58,19 @@ cudaError_t segmented_std_sort(uint64_t* keys, uint32_t* vals, uint32_t* lscratc
                                uint32_t nseg, const uint32_t* nseg_dev, uint32_t* lists,
                                uint32_t* counts, int num_sms, cudaStream_t stream,
                                SortTasks tasks);
+// Copies the ranges [begin[s], end[s]) of (keys, vals) to (ck, cv) at cbeg[s]
+// (the flagged queries' generation order, gathered for a pruned sort).
+cudaError_t gather_ranges(const uint64_t* keys, const uint32_t* vals, const uint64_t* begin,
+                          const uint64_t* end, const uint64_t* cbeg, uint32_t nseg, uint64_t* ck,
+                          uint32_t* cv, int num_sms, cudaStream_t s);
+// After a pruned segmented_std_sort of (ck, cv) over the segments
+// [cbeg[s], cend[s]) with `counts` and `tasks`: copies every range it sorted
+// (segments of up to 4,096 elements whole, its tasks and its heap ranges) to
+// (keys, vals) at begin[s] + (offset within the segment); cbeg ascending.
+cudaError_t copy_sorted_ranges(const uint64_t* ck, const uint32_t* cv, const uint64_t* cbeg,
+                               const uint64_t* cend, const uint64_t* begin, uint32_t nseg,
+                               const uint32_t* counts, const SortTasks& tasks, uint64_t* keys,
+                               uint32_t* vals, int num_sms, cudaStream_t s);
 size_t radix_hist_words(uint64_t n);
 cudaError_t radix_sort_pairs(uint64_t* keys, uint64_t* vals, uint64_t* keys_alt,
                              uint64_t* vals_alt, uint64_t n, const int* digits, int ndigits,
@@ -202,9 +222,11 @@ struct MatchTile {
 
 // Per query with two or more hits: flagged queries (q_tie, keys may repeat)
 // are listed for the emulated sort; the others get ntiles[q] radix tiles.
+// tile_flagged: the flagged queries get the tiles (their sorted order up to
+// the order among equal keys) and nothing is listed.
 cudaError_t match_plan(const uint64_t* q_off, const uint32_t* q_tie, uint32_t nq, uint32_t* ntiles,
                        uint64_t* emu_begin, uint64_t* emu_end, uint32_t* emu_count,
-                       cudaStream_t s);
+                       cudaStream_t s, bool tile_flagged = false);
 // tile_off: exclusive scan of ntiles.
 cudaError_t match_tiles(const uint64_t* q_off, const uint32_t* ntiles, const uint64_t* tile_off,
                         uint32_t nq, MatchTile* tiles, cudaStream_t s);
@@ -300,6 +322,13 @@ struct MatchEmitLists {
   uint64_t* emu_end;
   uint32_t* emu_count;  // zeroed by the caller
   unsigned long long* tally;  // [0]: flagged queries' hits, [1]: hits of pf_list groups
+  // flagged queries' keys that may repeat (optional): (the query's first hit,
+  // key) of every hit whose window's bucket lists its target just before it;
+  // tie_count (zeroed by the caller) counts them all, tie_cap are stored
+  uint64_t* tie_h0 = nullptr;
+  uint64_t* tie_key = nullptr;
+  uint32_t* tie_count = nullptr;
+  uint32_t tie_cap = 0;
 };
 
 size_t match_dict_smem_bytes();

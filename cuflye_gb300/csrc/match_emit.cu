@@ -527,9 +527,24 @@ __global__ void __launch_bounds__(kSeBlock, 2) match_emit_kernel(
           const int32_t j = static_cast<int32_t>(t + u * kSeBlock);
           const uint64_t d = sm.b.hbase[wl] + static_cast<uint64_t>(j) -
                              (sm.b.self_j[wl] < j ? 1u : 0u);
+          const uint64_t key = (static_cast<uint64_t>(id) << 32) | (sm.b.prev[wl] & 0x7fffffffu);
           if (d >= eq.h0 && d < eq.h1) {  // always: the window's hits lie in the query's range
-            keys[d] = (static_cast<uint64_t>(id) << 32) | (sm.b.prev[wl] & 0x7fffffffu);
+            keys[d] = key;
             vals[d] = pos;
+          }
+          // equal keys come only from a bucket listing one target twice, at
+          // neighbouring entries: record the key when the entry before this
+          // one (in the bucket) has the same target
+          if (lists.tie_count &&
+              (j > static_cast<int32_t>(sm.b.cum[wl]) || (wl == 0 && e0 > 0))) {
+            const uint64_t before = __ldg(a.idx.pos + (sm.b.jbase[wl] + static_cast<uint64_t>(j) - 1u));
+            if ((before >> 32) == (x.sv[u] >> 32)) {
+              const uint32_t slot = atomicAdd(lists.tie_count, 1u);
+              if (slot < lists.tie_cap) {
+                lists.tie_h0[slot] = eq.h0;
+                lists.tie_key[slot] = key;
+              }
+            }
           }
         }
       } else {

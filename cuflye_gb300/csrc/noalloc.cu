@@ -51,7 +51,7 @@ constexpr size_t kOffSegs = align256(kOffCounts + 4 * 16);
 constexpr size_t kOffTf = align256(kOffSegs + 8 * (kMaxSegs + 1));
 constexpr size_t kOffTn = align256(kOffTf + 8 * kTaskCap);
 constexpr size_t kOffTd = align256(kOffTn + 4 * kTaskCap);
-constexpr size_t kRoundBytes = (kMaxElems / 4096 + 1) * 16;  // segsort_round_bytes(kMaxElems)
+constexpr size_t kRoundBytes = (kMaxElems / 4096 + 1) * kRoundItemBytes;  // segsort_round_bytes(kMaxElems)
 constexpr size_t kOffR0 = align256(kOffTd + 4 * kTaskCap);
 constexpr size_t kOffR1 = align256(kOffR0 + kRoundBytes);
 constexpr size_t kOffRc = align256(kOffR1 + kRoundBytes);

@@ -684,18 +684,49 @@ __global__ void __launch_bounds__(kBlock, 3) sort_cta(uint64_t* K, uint32_t* V,
 constexpr int kBigBlock = 512;
 constexpr int kBigPerSm = 2;
 
+// A range of a round: its elements [f, f + n), depth budget d, segment seg,
+// and the key interval [lo, hi] its elements lie in (the pivots above it).
 struct RoundItem {
   uint64_t f;
+  uint64_t lo, hi;
   uint32_t n;
   int d;
+  uint32_t seg;
+  uint32_t pad;
+};
+static_assert(sizeof(RoundItem) == kRoundItemBytes, "round item size");
+
+struct PruneLists {
+  const uint64_t* keys;
+  const uint32_t* off;
 };
 
+// Whether segment seg's list holds a key in [lo, hi] (always, without lists).
+__device__ __forceinline__ bool holds_listed_key(const PruneLists& pl, uint32_t seg, uint64_t lo,
+                                                 uint64_t hi) {
+  if (!pl.off) return true;
+  uint32_t a = pl.off[seg], b = pl.off[seg + 1];
+  while (a < b) {  // first key >= lo
+    const uint32_t m = (a + b) >> 1;
+    if (pl.keys[m] < lo)
+      a = m + 1;
+    else
+      b = m;
+  }
+  return a < pl.off[seg + 1] && pl.keys[a] <= hi;
+}
+
 // Where a child range of a global-phase partition goes.
-__device__ __forceinline__ void place_range(uint64_t f, uint32_t n, int d, RoundItem* out,
+__device__ __forceinline__ void place_range(const RoundItem& r, RoundItem* out,
                                             uint32_t* out_count, uint64_t* task_f,
                                             uint32_t* task_n, int* task_d, uint32_t* task_count,
                                             uint32_t* heap_count, uint32_t* pair_count,
-                                            uint32_t task_cap, uint32_t pair_reserve) {
+                                            uint32_t task_cap, uint32_t pair_reserve,
+                                            const PruneLists& pl) {
+  const uint64_t f = r.f;
+  const uint32_t n = r.n;
+  const int d = r.d;
+  if (n > 1 && !holds_listed_key(pl, r.seg, r.lo, r.hi)) return;  // distinct keys: dropped
   if (n <= kCap) {
     if (n > 1) {
       const uint32_t slot = atomicAdd(task_count, 1u);
@@ -714,7 +745,7 @@ __device__ __forceinline__ void place_range(uint64_t f, uint32_t n, int d, Round
     task_n[slot] = n;
     task_d[slot] = 0;
   } else {
-    out[atomicAdd(out_count, 1u)] = RoundItem{f, n, d};
+    out[atomicAdd(out_count, 1u)] = r;
   }
 }
 
@@ -726,7 +757,7 @@ __global__ void round_seed(const uint64_t* __restrict__ begin, const uint64_t* _
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
     const uint32_t s = list[i];
     const uint32_t n = static_cast<uint32_t>(end[s] - begin[s]);
-    out[i] = RoundItem{begin[s], n, isort::depth_limit(n)};
+    out[i] = RoundItem{begin[s], 0ull, ~0ull, n, isort::depth_limit(n), s, 0u};
   }
 }
 
@@ -735,7 +766,7 @@ __global__ void __launch_bounds__(kBigBlock, kBigPerSm)
                const RoundItem* __restrict__ in, const uint32_t* __restrict__ in_count,
                uint32_t* work, RoundItem* out, uint32_t* out_count, uint64_t* task_f,
                uint32_t* task_n, int* task_d, uint32_t* task_count, uint32_t* heap_count,
-               uint32_t* pair_count, uint32_t task_cap, uint32_t pair_reserve) {
+               uint32_t* pair_count, uint32_t task_cap, uint32_t pair_reserve, PruneLists pl) {
   __shared__ RoundScratch<kBigBlock, 8> rs;
   __shared__ uint32_t item;
   const uint32_t cnt = *in_count;
@@ -750,10 +781,15 @@ __global__ void __launch_bounds__(kBigBlock, kBigPerSm)
     const uint32_t cut =
         round_partition<kBigBlock, uint32_t>(K + r.f, V + r.f, Lg + r.f, Rg + r.f, 0, r.n, rs);
     if (threadIdx.x == 0) {
-      place_range(r.f, cut, r.d - 1, out, out_count, task_f, task_n, task_d, task_count,
-                  heap_count, pair_count, task_cap, pair_reserve);
-      place_range(r.f + cut, r.n - cut, r.d - 1, out, out_count, task_f, task_n, task_d,
-                  task_count, heap_count, pair_count, task_cap, pair_reserve);
+      // the pivot stays at the range's first slot: the left part holds keys
+      // <= it, the right part keys >= it
+      const uint64_t p = K[r.f];
+      const RoundItem left{r.f, r.lo, p, cut, r.d - 1, r.seg, 0u};
+      const RoundItem right{r.f + cut, p, r.hi, r.n - cut, r.d - 1, r.seg, 0u};
+      place_range(left, out, out_count, task_f, task_n, task_d, task_count, heap_count,
+                  pair_count, task_cap, pair_reserve, pl);
+      place_range(right, out, out_count, task_f, task_n, task_d, task_count, heap_count,
+                  pair_count, task_cap, pair_reserve, pl);
     }
     __syncthreads();
   }
@@ -1278,7 +1314,96 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kHeapBlock, 1)
 
 }  // namespace
 
+// One block per range: grid-stride over ranges, threads over elements.
+__global__ void gather_ranges_kernel(const uint64_t* __restrict__ keys,
+                                     const uint32_t* __restrict__ vals,
+                                     const uint64_t* __restrict__ begin,
+                                     const uint64_t* __restrict__ end,
+                                     const uint64_t* __restrict__ cbeg, uint32_t nseg,
+                                     uint64_t* __restrict__ ck, uint32_t* __restrict__ cv) {
+  for (uint32_t s = blockIdx.x; s < nseg; s += gridDim.x) {
+    const uint64_t b = begin[s], n = end[s] - b, c = cbeg[s];
+    for (uint64_t i = threadIdx.x; i < n; i += blockDim.x) {
+      ck[c + i] = keys[b + i];
+      cv[c + i] = vals[b + i];
+    }
+  }
+}
+
+// Sorted ranges of the pruned sort: items [0, nseg) are the segments (copied
+// when they have at most kCap elements), then the tasks, the block-pair heaps
+// and the own-block heaps.
+__global__ void copy_sorted_kernel(const uint64_t* __restrict__ ck, const uint32_t* __restrict__ cv,
+                                   const uint64_t* __restrict__ cbeg,
+                                   const uint64_t* __restrict__ cend,
+                                   const uint64_t* __restrict__ begin, uint32_t nseg,
+                                   const uint32_t* __restrict__ counts,
+                                   const uint64_t* __restrict__ task_f,
+                                   const uint32_t* __restrict__ task_n, uint32_t task_cap,
+                                   uint32_t pair_reserve, uint64_t* __restrict__ keys,
+                                   uint32_t* __restrict__ vals) {
+  const uint32_t ntask = counts[4], nheap = counts[5], npair = counts[7];
+  const uint64_t items = static_cast<uint64_t>(nseg) + ntask + npair + nheap;
+  for (uint64_t it = blockIdx.x; it < items; it += gridDim.x) {
+    uint64_t f = 0, n = 0;
+    if (it < nseg) {
+      f = cbeg[it];
+      n = cend[it] - f;
+      if (n > kCap) continue;  // the global phase's ranges come below
+    } else {
+      uint64_t j = it - nseg;
+      uint32_t slot;
+      if (j < ntask) {
+        slot = static_cast<uint32_t>(j);
+      } else if ((j -= ntask) < npair) {
+        slot = task_cap - 1u - static_cast<uint32_t>(j);
+      } else {
+        j -= npair;
+        slot = task_cap - 1u - pair_reserve - static_cast<uint32_t>(j);
+      }
+      f = task_f[slot];
+      n = task_n[slot];
+    }
+    // the segment holding f: the last s with cbeg[s] <= f
+    uint32_t lo = 0, hi = nseg;
+    while (hi - lo > 1) {
+      const uint32_t m = (lo + hi) >> 1;
+      if (cbeg[m] <= f)
+        lo = m;
+      else
+        hi = m;
+    }
+    const uint64_t dst = begin[lo] + (f - cbeg[lo]);
+    for (uint64_t i = threadIdx.x; i < n; i += blockDim.x) {
+      keys[dst + i] = ck[f + i];
+      vals[dst + i] = cv[f + i];
+    }
+  }
+}
+
 size_t segsort_smem_bytes() { return sizeof(CtaSmem); }
+
+cudaError_t gather_ranges(const uint64_t* keys, const uint32_t* vals, const uint64_t* begin,
+                          const uint64_t* end, const uint64_t* cbeg, uint32_t nseg, uint64_t* ck,
+                          uint32_t* cv, int num_sms, cudaStream_t s) {
+  if (nseg == 0) return cudaSuccess;
+  count_launch();
+  gather_ranges_kernel<<<std::min<uint32_t>(nseg, 8u * num_sms), 256, 0, s>>>(
+      keys, vals, begin, end, cbeg, nseg, ck, cv);
+  return cudaGetLastError();
+}
+
+cudaError_t copy_sorted_ranges(const uint64_t* ck, const uint32_t* cv, const uint64_t* cbeg,
+                               const uint64_t* cend, const uint64_t* begin, uint32_t nseg,
+                               const uint32_t* counts, const SortTasks& tasks, uint64_t* keys,
+                               uint32_t* vals, int num_sms, cudaStream_t s) {
+  if (nseg == 0) return cudaSuccess;
+  count_launch();
+  copy_sorted_kernel<<<8u * num_sms, 256, 0, s>>>(ck, cv, cbeg, cend, begin, nseg, counts, tasks.f,
+                                                  tasks.n, tasks.cap, tasks.pair_reserve, keys,
+                                                  vals);
+  return cudaGetLastError();
+}
 
 uint32_t segsort_pair_reserve(uint64_t nelems) {
   return static_cast<uint32_t>(nelems / kHeapPackCap + 1);
@@ -1350,7 +1475,7 @@ cudaError_t segmented_std_sort(uint64_t* keys, uint32_t* vals, uint32_t* lscratc
       sort_round<<<num_sms * round_blocks, kBigBlock, 0, stream>>>(
           keys, vals, lscratch, rscratch, rl[r & 1], r == 0 ? counts + 3 : rcount + r, rwork + r,
           rl[(r + 1) & 1], rcount + r + 1, tasks.f, tasks.n, tasks.d, counts + 4, counts + 5,
-          counts + 7, tasks.cap, tasks.pair_reserve);
+          counts + 7, tasks.cap, tasks.pair_reserve, PruneLists{tasks.prune_keys, tasks.prune_off});
       if (((r + 1) & r) == 0) {
         uint32_t next = 0;
         cudaError_t e = cudaMemcpyAsync(&next, rcount + r + 1, sizeof(next),

@@ -513,6 +513,13 @@ cuflye_status cuflye_last_passes(const cuflye_ctx* ctx, uint64_t* passes);
 cuflye_status cuflye_last_pass_stats(const cuflye_ctx* ctx, uint64_t* passes, uint64_t* retries,
                                      double* alloc_ms);
 
+/* Returns the context's cached working buffers to the device: everything a
+ * call allocates and keeps for the next one (hit arrays, sort scratch,
+ * per-group tables, rows), leaving the index, the graph and the logf table.
+ * The next call allocates what it needs again.  For a long-lived process
+ * that holds a context between large calls. */
+cuflye_status cuflye_trim(cuflye_ctx* ctx);
+
 /* Kernel launches issued by the library in this process so far. */
 cuflye_status cuflye_kernel_launches(uint64_t* total);
 

@@ -77,6 +77,12 @@ def test_config2_batched_repeats_sample_against_full_index(gpu, oracle_mod):
     ids = set(int(i) for i in sub.ids)
     in_batch = overlap_tuples_gpu(r for r in full if int(r["cur_id"]) in ids)
     assert in_batch == got
+    # the full call's working buffers go back to the device (the session's
+    # context otherwise keeps most of the GPU for the tests after this one)
+    held = gpu.memory_stats()[0]
+    gpu.trim()
+    assert gpu.memory_stats()[0] < held
+    assert overlap_tuples_gpu(gpu.overlaps(sub, p)) == got
 
 
 def _reads_over_duplicated_edges(wl, count):
