@@ -508,6 +508,7 @@ def scale_config(args, device: int) -> dict:
         ms, by = be.last_timing()
         passes = be.last_passes()
         pass_stats = be.last_pass_stats()
+        sort_paths = be.last_sort_stats()
         dev_peak = be.memory_stats()[1]
     ms = np.array(ms)
     by = np.array(by, dtype=np.float64)
@@ -521,6 +522,7 @@ def scale_config(args, device: int) -> dict:
         "index_build_s": round(build_s, 3), "index_key_ranges": ranges,
         "index_positions": stats["positions"], "passes": passes,
         "pass_retries": pass_stats["retries"], "host_alloc_ms": pass_stats["alloc_ms"],
+        "sort_paths": sort_paths,
         "batched_read_bases_per_s": bases / wall,
         "device_read_bases_per_s": bases / (float(ms[:5].sum()) / 1000.0),
         "stages_ms": {n: round(float(ms[i]), 3)

@@ -998,8 +998,8 @@ SortTasks sort_tasks(cuflye_ctx* c, const std::string& prefix, uint64_t nelems, 
 // place (the sorted order up to the order among equal keys), and the
 // introsort is emulated on a copy in generation order, pruned to the
 // ranges that may hold equal keys; the ranges it sorted are copied back.
-// Without the recorded keys (more than the list holds) the whole introsort
-// is emulated in place.
+// Without the recorded keys (more than the list holds), or with more than
+// one per 64 hits, the whole introsort is emulated in place.
 void flagged_sort(cuflye_ctx* c, PassState& ps, const MatchEmitLists& L, uint64_t* qb,
                   uint64_t* qe, uint32_t* ecount, uint64_t* alt_keys, uint32_t* alt_vals,
                   uint32_t* lscr, uint32_t* rscr, uint32_t* lists, uint32_t* scounts) {
@@ -1039,6 +1039,12 @@ void flagged_sort(cuflye_ctx* c, PassState& ps, const MatchEmitLists& L, uint64_
     seg[2ull * E + i] = F;
     F += e[ord[i]] - b[ord[i]];
     seg[3ull * E + i] = F;
+  }
+  if (static_cast<uint64_t>(T) * 64u > F) {
+    // equal keys everywhere: the pruning would keep most ranges
+    CUFLYE_CHECK(segmented_std_sort(ps.keys, ps.vals, lscr, rscr, qb, qe, nq, ecount, lists,
+                                    scounts, c->num_sms, st, sort_tasks(c, "s", H, nq)));
+    return;
   }
   std::vector<std::pair<uint32_t, uint64_t>> ties(T);
   for (uint32_t i = 0; i < T; ++i) {
@@ -1169,11 +1175,10 @@ uint64_t run_chain(cuflye_ctx* c, PassState& ps, const ChainParams& cp,
       CUFLYE_CHECK(cudaMemsetAsync(gcounts, 0, 4 * sizeof(uint32_t), st));
       CUFLYE_CHECK(cudaMemsetAsync(ecount, 0, sizeof(uint32_t), st));
       MatchEmitLists L{dp_list, ext_list, pf_list, gcounts, qb, qe, ecount, dcur + 1};
-      const uint32_t tie_cap = static_cast<uint32_t>(std::min<uint64_t>(H / 16 + 1024, 1u << 22));
-      L.tie_h0 = buf<uint64_t>(c, "f_tieh0", tie_cap);
-      L.tie_key = buf<uint64_t>(c, "f_tiekey", tie_cap);
+      L.tie_cap = static_cast<uint32_t>(std::min<uint64_t>(H / 16 + 1024, 1u << 22));
+      L.tie_h0 = buf<uint64_t>(c, "f_tieh0", L.tie_cap);
+      L.tie_key = buf<uint64_t>(c, "f_tiekey", L.tie_cap);
       L.tie_count = mwords + 2;
-      L.tie_cap = tie_cap;
       CUFLYE_CHECK(cudaMemsetAsync(L.tie_count, 0, sizeof(uint32_t), st));
       CUFLYE_CHECK(match_emit(a, alt_keys, q_ng, q_dbase, q_goff, ps.q_tie, ps.qinfo, cp, ps.keys,
                               ps.vals, groups, L, mwords + 1, c->num_sms, st));
