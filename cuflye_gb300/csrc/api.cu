@@ -95,6 +95,7 @@ struct cuflye_ctx {
   cuflye_ctx* lender = nullptr;  // the context whose index this one borrows (cuflye_open_shared)
   int sorted_emission = 1;  // see cuflye_set_sorted_emission
   double other_per_hit = 0;  // a pass body's buffers beyond the per-hit ones, per hit
+  std::map<std::string, uint64_t> pass_need;  // bytes each buffer was asked for in this pass
   uint64_t pass_retries = 0;   // passes of the last call run again on half their queries
   uint64_t pass_hit_cap = 0;   // hits a pass may take after a retry in this call (0: no cap)
   double alloc_ms = 0;         // host time of the last call in cudaMalloc / cudaFree
@@ -109,6 +110,8 @@ constexpr int kSortStats = 7;
 template <typename T>
 T* buf(cuflye_ctx* c, const std::string& name, uint64_t count) {
   const size_t bytes = std::max<size_t>(static_cast<size_t>(count) * sizeof(T), 16);
+  uint64_t& need = c->pass_need[name];
+  need = std::max<uint64_t>(need, bytes);
   DevBuf& b = c->bufs[name];
   if (b.cap >= bytes) return static_cast<T*>(b.p);
   // grow by half, or under a budget that has no room for that, by an eighth
@@ -281,6 +284,8 @@ struct BuiltIndex {
   uint64_t cap = 0;
   uint64_t* pos = nullptr;
   uint64_t npos = 0, nsolid = 0, nrep = 0;
+  uint32_t* self_at = nullptr;  // one-range builds, when memory allows
+  uint64_t* win_off = nullptr;
 };
 
 // Scratch of one key range's build.
@@ -360,8 +365,27 @@ BuiltIndex build_one_range(cuflye_ctx* c, const WindowSet& w, const std::vector<
   if (r.npos >= (1ull << 40)) throw Error(CUFLYE_ERR_UNSUPPORTED, "index larger than 2^40 entries");
   BuiltIndex bi;
   bi.pos = buf<uint64_t>(c, "ix_pos", r.npos);
+  // each indexed window's own bucket entry (4 bytes a window), when memory
+  // allows: hit counting then finds a query's own entry with one load
+  uint32_t* self_at = nullptr;
+  uint64_t* win_off = nullptr;
+  try {
+    self_at = buf<uint32_t>(c, "ix_selfat", w.nwin);
+    win_off = buf<uint64_t>(c, "ix_winoff", static_cast<uint64_t>(w.nslots) + 1);
+  } catch (const Error& e) {
+    if (e.code != CUFLYE_ERR_BUDGET) throw;
+    release(c, "ix_selfat");
+    release(c, "ix_winoff");
+    self_at = nullptr;
+    win_off = nullptr;
+  }
+  if (win_off)
+    CUFLYE_CHECK(cudaMemcpyAsync(win_off, w.win_off, (static_cast<uint64_t>(w.nslots) + 1) * 8,
+                                 cudaMemcpyDeviceToDevice, st));
   CUFLYE_CHECK(index_copy_positions(r.vals, r.run_id, r.run_start, r.cls, r.kept_off, w.nwin,
-                                    bi.pos, st));
+                                    bi.pos, st, self_at, win_off, w.slot_len, w.k));
+  bi.self_at = self_at;
+  bi.win_off = win_off;
   bi.cap = 16;
   while (bi.cap < 2 * r.nruns) bi.cap <<= 1;
   bi.table = buf<TableEntry>(c, "ix_table", bi.cap);
@@ -552,6 +576,10 @@ void build_index(cuflye_ctx* c, int k, size_t n, const int64_t* ids, const int64
   // the previous index's arrays go first (has_index is false from here on)
   release(c, "ix_pos");
   release(c, "ix_table");
+  release(c, "ix_selfat");
+  release(c, "ix_winoff");
+  c->idx.self_at = nullptr;
+  c->idx.win_off = nullptr;
   // bases packed in chunks of 256 MiB (a multiple of 32 bases: chunks start on
   // word boundaries; each chunk's trailing pad word is overwritten by the next)
   uint64_t* words = buf<uint64_t>(c, "ib_words", (nbases + 31) / 32 + 2);
@@ -598,6 +626,8 @@ void build_index(cuflye_ctx* c, int k, size_t n, const int64_t* ids, const int64
       release_build_scratch(c);
       release(c, "ix_pos");
       release(c, "ix_table");
+      release(c, "ix_selfat");
+      release(c, "ix_winoff");
       ranges = true;
     }
   }
@@ -613,6 +643,8 @@ void build_index(cuflye_ctx* c, int k, size_t n, const int64_t* ids, const int64
   c->idx.slot_len = d_len;
   c->idx.slot_signed = d_signed;
   c->idx.nslots = static_cast<uint32_t>(n);
+  c->idx.self_at = bi.self_at;
+  c->idx.win_off = bi.win_off;
   c->idx.nkeys = bi.nsolid + bi.nrep;
   c->idx.nrep = bi.nrep;
   c->has_index = true;
@@ -699,6 +731,10 @@ void build_index_entries(cuflye_ctx* c, int k, size_t n, const int64_t* tids, co
     release(c, t);
   c->idx.k = k;
   c->idx.transform = false;
+  release(c, "ix_selfat");
+  release(c, "ix_winoff");
+  c->idx.self_at = nullptr;
+  c->idx.win_off = nullptr;
   c->idx.table = table;
   c->idx.cap = cap;
   c->idx.pos = pos;
@@ -948,9 +984,12 @@ bool run_hits(cuflye_ctx* c, const Queries& Q, size_t q0, size_t q1, bool want_k
   // pass has queries for every SM (it runs a block per query); a pass of
   // sparse hits (reads against a genome or a graph) or of a few queries (the
   // one-read path) is cheaper to emit and sort.
+  // A call whose passes overflowed the dictionary twice (queries hitting
+  // more targets than it holds) emits the rest in generation order.
   ps.emitted = !(fused && (c->sorted_emission == 2 ||
                            (ps.nhits >= kSortedEmissionMinHitsPerWindow * ps.nwin &&
-                            ps.nq >= 2ull * static_cast<uint64_t>(c->num_sms))));
+                            ps.nq >= 2ull * static_cast<uint64_t>(c->num_sms) &&
+                            c->emission_fallbacks < 2)));
   if (ps.emitted) emit_generation_order(c, ps);
   return true;
 }
@@ -1442,6 +1481,7 @@ void for_each_pass(cuflye_ctx* c, const Queries& Q, bool kmers, uint64_t bytes_p
   while (q0 < Q.n) {
     size_t q1 = run_end(c, Q, q0, std::min(Q.n, q0 + step), bytes_per_hit, hpw);
     PassState ps;
+    c->pass_need.clear();
     CUFLYE_CHECK(cudaEventRecord(c->ev[0], c->stream));
     run_hits(c, Q, q0, q1, kmers, bytes_per_hit, ps);
     q1 = q0 + ps.nq;
@@ -1459,13 +1499,20 @@ void for_each_pass(cuflye_ctx* c, const Queries& Q, bool kmers, uint64_t bytes_p
       step = std::max<size_t>(ps.nq / 2, 1);
       continue;
     }
-    // Learn the body's other buffers per hit only from passes that came near
-    // what the memory left could hold: a small pass's buffers (some held at
-    // the size an earlier, larger pass grew them to), divided by its few
-    // hits, would make every later pass of the context tiny.
-    if (c->budget && ps.nhits && ps.nhits * 2 >= ps.fit_hits) {
-      const double other = static_cast<double>(c->in_use - held_bytes(c));
-      c->other_per_hit = std::max(c->other_per_hit, other / static_cast<double>(ps.nhits));
+    // Learn the body's other buffers per hit from the ones this pass used
+    // (at the size they are held), and only from passes of at least a 64th
+    // of what the memory left could hold: a small pass's tables (held at the
+    // size an earlier, larger pass grew them to), divided by its few hits,
+    // would make every later pass of the context tiny.
+    if (c->budget && ps.nhits && ps.nhits * 64 >= ps.fit_hits) {
+      uint64_t other = 0;
+      for (const auto& kv : c->pass_need) {
+        if (kept_buffer(kv.first)) continue;
+        auto it = c->bufs.find(kv.first);
+        if (it != c->bufs.end()) other += it->second.cap;
+      }
+      c->other_per_hit =
+          std::max(c->other_per_hit, static_cast<double>(other) / static_cast<double>(ps.nhits));
     }
     ++c->passes;
     q0 = q1;

@@ -82,17 +82,37 @@ __global__ void count_kernel(DeviceIndex idx, QueryBatch q, uint32_t* __restrict
       const uint64_t off = meta & kOffsetMask;
       uint32_t self_hits = 0;
       if (idx.transform) {
-        // built buckets are sorted by (stored id, stored position), entries unique
-        uint32_t lo = 0, hi = c;
-        while (lo < hi) {
-          const uint32_t mid = (lo + hi) >> 1;
-          if (__ldg(idx.pos + off + mid) < want)
-            lo = mid + 1;
-          else
-            hi = mid;
+        // built buckets are sorted by (stored id, stored position), entries
+        // unique.  A query that is an indexed target finds its own entry
+        // where the index recorded it (checked: a query sequence that
+        // differs from the indexed one searches as any other)
+        bool known = false;
+        uint32_t at = 0;
+        if (idx.self_at && !(qdi & 1)) {
+          const uint32_t slot = static_cast<uint32_t>(qdi) >> 1;
+          const uint64_t w0 = idx.win_off[slot];
+          if (w0 + p < idx.win_off[slot + 1]) {
+            const uint32_t g = idx.self_at[w0 + p];
+            if (g < c && __ldg(idx.pos + off + g) == want) {
+              known = true;
+              at = g;
+            }
+          }
         }
-        self_hits = (lo < c && __ldg(idx.pos + off + lo) == want) ? 1u : 0u;
-        if (self_hits && wself) wself[w] = lo;
+        if (!known) {
+          uint32_t lo = 0, hi = c;
+          while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (__ldg(idx.pos + off + mid) < want)
+              lo = mid + 1;
+            else
+              hi = mid;
+          }
+          known = lo < c && __ldg(idx.pos + off + lo) == want;
+          at = lo;
+        }
+        self_hits = known ? 1u : 0u;
+        if (self_hits && wself) wself[w] = at;
       } else {
         // explicit entries keep input order and may repeat
         for (uint32_t e = 0; e < c; ++e) self_hits += __ldg(idx.pos + off + e) == want;

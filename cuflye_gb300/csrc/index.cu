@@ -175,7 +175,9 @@ __global__ void copy_positions_kernel(const uint64_t* __restrict__ vals,
                                       const uint64_t* __restrict__ run_start,
                                       const uint8_t* __restrict__ cls,
                                       const uint64_t* __restrict__ kept_off, uint64_t n,
-                                      uint64_t* __restrict__ pos) {
+                                      uint64_t* __restrict__ pos, uint32_t* __restrict__ self_at,
+                                      const uint64_t* __restrict__ win_off,
+                                      const int32_t* __restrict__ slot_len, int k) {
   const uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= n) return;
   // flags_scan holds the exclusive scan of run-start flags: the run of
@@ -184,7 +186,17 @@ __global__ void copy_positions_kernel(const uint64_t* __restrict__ vals,
   if (r >= 1 && run_start[r] > i) r -= 1;
   while (run_start[r] > i) --r;
   if (cls[r] != 1) return;
-  pos[kept_off[r] + (i - run_start[r])] = vals[i];
+  const uint64_t v = vals[i];
+  pos[kept_off[r] + (i - run_start[r])] = v;
+  if (self_at) {
+    // the window this entry came from: its forward position in its target
+    const uint32_t sid = static_cast<uint32_t>(v >> 32);
+    const uint32_t slot = sid >> 1;
+    const int64_t sp = static_cast<int64_t>(v & 0xffffffffu);
+    const int64_t p = (sid & 1u) ? static_cast<int64_t>(slot_len[slot]) - sp - k : sp;
+    const uint64_t w = win_off[slot] + static_cast<uint64_t>(p);
+    if (p >= 0 && w < win_off[slot + 1]) self_at[w] = static_cast<uint32_t>(i - run_start[r]);
+  }
 }
 
 __device__ bool table_insert(TableEntry* table, uint64_t cap, uint64_t key, uint64_t meta,
@@ -364,11 +376,12 @@ cudaError_t index_classify_runs(const uint64_t* run_start, uint64_t nruns, uint3
 cudaError_t index_copy_positions(const uint64_t* vals, const uint64_t* run_id,
                                  const uint64_t* run_start, const uint8_t* cls,
                                  const uint64_t* kept_off, uint64_t n, uint64_t* pos,
-                                 cudaStream_t s) {
+                                 cudaStream_t s, uint32_t* self_at, const uint64_t* win_off,
+                                 const int32_t* slot_len, int k) {
   if (n == 0) return cudaSuccess;
   count_launch();
   copy_positions_kernel<<<grid(n, 256), 256, 0, s>>>(vals, run_id, run_start, cls, kept_off, n,
-                                                     pos);
+                                                     pos, self_at, win_off, slot_len, k);
   return cudaGetLastError();
 }
 

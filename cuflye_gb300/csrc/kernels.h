@@ -92,6 +92,11 @@ struct DeviceIndex {
   int64_t* slot_signed = nullptr;  // signed id per dense slot
   uint32_t nslots = 0;
   uint64_t nkeys = 0, nrep = 0;
+  // optional (one-range builds): per window of the indexed targets (slot
+  // order, win_off per slot), the index of its own entry in its k-mer's
+  // bucket when that k-mer is solid (other windows: any value)
+  uint32_t* self_at = nullptr;
+  uint64_t* win_off = nullptr;
 };
 
 // Window enumeration over packed targets: keys = standard forms, vals =
@@ -125,7 +130,9 @@ cudaError_t index_classify_runs(const uint64_t* run_start, uint64_t nruns, uint3
 cudaError_t index_copy_positions(const uint64_t* vals, const uint64_t* run_id,
                                  const uint64_t* run_start, const uint8_t* cls,
                                  const uint64_t* kept_off, uint64_t n, uint64_t* pos,
-                                 cudaStream_t s);
+                                 cudaStream_t s, uint32_t* self_at = nullptr,
+                                 const uint64_t* win_off = nullptr,
+                                 const int32_t* slot_len = nullptr, int k = 0);
 // Table insert of every solid and repetitive run, a solid run's positions
 // at pos_base + kept_off of the position array.  Solid buckets that list
 // one stored id twice get kDupIdsBit (sorted_ids: runs are in (id, position)
