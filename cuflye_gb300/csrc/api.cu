@@ -1111,11 +1111,10 @@ void flagged_sort(cuflye_ctx* c, PassState& ps, const MatchEmitLists& L, uint64_
     CUFLYE_CHECK(cudaMemcpyAsync(dpkeys, pkeys.data(), pkeys.size() * 8ull,
                                  cudaMemcpyHostToDevice, st));
   const uint64_t* sb = dseg;
-  const uint64_t* se = dseg + E;
   const uint64_t* cb = dseg + 2ull * E;
   const uint64_t* ce = dseg + 3ull * E;
   // the generation order, gathered
-  CUFLYE_CHECK(gather_ranges(ps.keys, ps.vals, sb, se, cb, E, gk, gv, c->num_sms, st));
+  CUFLYE_CHECK(gather_ranges(ps.keys, ps.vals, sb, cb, E, F, gk, gv, c->num_sms, st));
   // the sorted order in place: a stable radix sort by ext id of each
   // flagged query's hits (in cur-pos order as generated)
   uint32_t* ntiles = buf<uint32_t>(c, "m_ntiles", nq);
@@ -1449,13 +1448,6 @@ bool kept_buffer(const std::string& name) {
   for (const char* nm : kPerWindowBuffers)
     if (name == nm) return true;
   return false;
-}
-
-uint64_t held_bytes(cuflye_ctx* c) {
-  uint64_t b = 0;
-  for (const auto& kv : c->bufs)
-    if (kept_buffer(kv.first)) b += kv.second.cap;
-  return b;
 }
 
 // Frees every buffer of the pass body (its tables, lists and rows).

@@ -58,10 +58,11 @@ cudaError_t segmented_std_sort(uint64_t* keys, uint32_t* vals, uint32_t* lscratc
                                uint32_t nseg, const uint32_t* nseg_dev, uint32_t* lists,
                                uint32_t* counts, int num_sms, cudaStream_t stream,
                                SortTasks tasks);
-// Copies the ranges [begin[s], end[s]) of (keys, vals) to (ck, cv) at cbeg[s]
+// Copies the ranges of (keys, vals) starting at begin[s] to (ck, cv) at
+// cbeg[s], where cbeg ascends and the ranges fill [0, total) end to end
 // (the flagged queries' generation order, gathered for a pruned sort).
 cudaError_t gather_ranges(const uint64_t* keys, const uint32_t* vals, const uint64_t* begin,
-                          const uint64_t* end, const uint64_t* cbeg, uint32_t nseg, uint64_t* ck,
+                          const uint64_t* cbeg, uint32_t nseg, uint64_t total, uint64_t* ck,
                           uint32_t* cv, int num_sms, cudaStream_t s);
 // After a pruned segmented_std_sort of (ck, cv) over the segments
 // [cbeg[s], cend[s]) with `counts` and `tasks`: copies every range it sorted

@@ -1314,18 +1314,35 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kHeapBlock, 1)
 
 }  // namespace
 
-// One block per range: grid-stride over ranges, threads over elements.
+// Blocks over fixed chunks of the compact copy (its ranges ascending in
+// cbeg, end to end): each element finds its range by a search of cbeg.
+constexpr uint32_t kGatherChunk = 4096;
+
 __global__ void gather_ranges_kernel(const uint64_t* __restrict__ keys,
                                      const uint32_t* __restrict__ vals,
                                      const uint64_t* __restrict__ begin,
-                                     const uint64_t* __restrict__ end,
                                      const uint64_t* __restrict__ cbeg, uint32_t nseg,
-                                     uint64_t* __restrict__ ck, uint32_t* __restrict__ cv) {
-  for (uint32_t s = blockIdx.x; s < nseg; s += gridDim.x) {
-    const uint64_t b = begin[s], n = end[s] - b, c = cbeg[s];
-    for (uint64_t i = threadIdx.x; i < n; i += blockDim.x) {
-      ck[c + i] = keys[b + i];
-      cv[c + i] = vals[b + i];
+                                     uint64_t total, uint64_t* __restrict__ ck,
+                                     uint32_t* __restrict__ cv) {
+  const uint64_t nchunk = (total + kGatherChunk - 1) / kGatherChunk;
+  for (uint64_t ch = blockIdx.x; ch < nchunk; ch += gridDim.x) {
+    const uint64_t c0 = ch * kGatherChunk;
+    // the range holding the chunk's first element
+    uint32_t lo = 0, hi = nseg;
+    while (hi - lo > 1) {
+      const uint32_t m = (lo + hi) >> 1;
+      if (cbeg[m] <= c0)
+        lo = m;
+      else
+        hi = m;
+    }
+    const uint64_t c1 = c0 + kGatherChunk < total ? c0 + kGatherChunk : total;
+    for (uint64_t c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
+      uint32_t s = lo;
+      while (s + 1 < nseg && cbeg[s + 1] <= c) ++s;
+      const uint64_t src = begin[s] + (c - cbeg[s]);
+      ck[c] = keys[src];
+      cv[c] = vals[src];
     }
   }
 }
@@ -1384,12 +1401,13 @@ __global__ void copy_sorted_kernel(const uint64_t* __restrict__ ck, const uint32
 size_t segsort_smem_bytes() { return sizeof(CtaSmem); }
 
 cudaError_t gather_ranges(const uint64_t* keys, const uint32_t* vals, const uint64_t* begin,
-                          const uint64_t* end, const uint64_t* cbeg, uint32_t nseg, uint64_t* ck,
+                          const uint64_t* cbeg, uint32_t nseg, uint64_t total, uint64_t* ck,
                           uint32_t* cv, int num_sms, cudaStream_t s) {
-  if (nseg == 0) return cudaSuccess;
+  if (nseg == 0 || total == 0) return cudaSuccess;
   count_launch();
-  gather_ranges_kernel<<<std::min<uint32_t>(nseg, 8u * num_sms), 256, 0, s>>>(
-      keys, vals, begin, end, cbeg, nseg, ck, cv);
+  const uint64_t nchunk = (total + kGatherChunk - 1) / kGatherChunk;
+  gather_ranges_kernel<<<static_cast<unsigned>(std::min<uint64_t>(nchunk, 16ull * num_sms)), 512,
+                         0, s>>>(keys, vals, begin, cbeg, nseg, total, ck, cv);
   return cudaGetLastError();
 }
 
