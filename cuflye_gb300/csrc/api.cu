@@ -81,6 +81,9 @@ struct cuflye_ctx {
   size_t queries_per_pass = 0;
   // timing
   cudaEvent_t ev[8]{};
+  // the segmented sort's side stream and its fork / rounds-done / join events
+  cudaStream_t side = nullptr;
+  cudaEvent_t side_ev[3]{};
   double stage_ms[7]{};
   uint64_t stage_bytes[7]{};
   uint64_t sort_stats[8]{};  // see cuflye_last_sort_stats ([7]: emission fallbacks)
@@ -1018,15 +1021,20 @@ ChainParams to_chain_params(const cuflye_overlap_params* p) {
 SortTasks sort_tasks(cuflye_ctx* c, const std::string& prefix, uint64_t nelems, uint32_t nseg) {
   const uint64_t w = segsort_task_words(nelems, nseg);
   const size_t rb = segsort_round_bytes(nelems);
-  return SortTasks{buf<uint64_t>(c, prefix + "_tf", w),
-                   buf<uint32_t>(c, prefix + "_tn", w),
-                   buf<int>(c, prefix + "_td", w),
-                   static_cast<uint32_t>(w),
-                   segsort_pair_reserve(nelems),
-                   nelems,
-                   {buf<uint8_t>(c, prefix + "_r0", rb), buf<uint8_t>(c, prefix + "_r1", rb)},
-                   buf<uint32_t>(c, prefix + "_rc", 2 * (kSortRounds + 1)),
-                   c->shape.round_blocks_per_sm};
+  SortTasks t{buf<uint64_t>(c, prefix + "_tf", w),
+              buf<uint32_t>(c, prefix + "_tn", w),
+              buf<int>(c, prefix + "_td", w),
+              static_cast<uint32_t>(w),
+              segsort_pair_reserve(nelems),
+              nelems,
+              {buf<uint8_t>(c, prefix + "_r0", rb), buf<uint8_t>(c, prefix + "_r1", rb)},
+              buf<uint32_t>(c, prefix + "_rc", 2 * (kSortRounds + 1)),
+              c->shape.round_blocks_per_sm};
+  t.side = c->side;
+  t.fork = c->side_ev[0];
+  t.rounds_done = c->side_ev[1];
+  t.join = c->side_ev[2];
+  return t;
 }
 
 // The flagged queries' KmerMatch sort (their hits in generation order at
@@ -1612,6 +1620,8 @@ cuflye_status cuflye_open(int device, uint64_t memory_budget_bytes, cuflye_ctx**
     CUFLYE_CHECK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     CUFLYE_CHECK(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device));
     for (auto& e : c->ev) CUFLYE_CHECK(cudaEventCreate(&e));
+    CUFLYE_CHECK(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+    for (auto& e : c->side_ev) CUFLYE_CHECK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     c->status = buf<DeviceStatus>(c, "status", 1);
     CUFLYE_CHECK(cudaMemset(c->status, 0, sizeof(DeviceStatus)));
     load_logf_table(c);
@@ -1700,8 +1710,12 @@ void cuflye_close(cuflye_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (auto& kv : c->bufs)
     if (kv.second.p) cudaFree(kv.second.p);
+  if (c->side) cudaStreamSynchronize(c->side);
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
+  for (auto& e : c->side_ev)
+    if (e) cudaEventDestroy(e);
+  if (c->side) cudaStreamDestroy(c->side);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }

@@ -1459,19 +1459,26 @@ cudaError_t segmented_std_sort(uint64_t* keys, uint32_t* vals, uint32_t* lscratc
     if (e != cudaSuccess) return e;
   }
   if (nseg == 0) return cudaSuccess;
+  const bool split = tasks.side && tasks.fork && tasks.rounds_done && tasks.join;
+  cudaStream_t side = split ? tasks.side : stream;
   cudaMemsetAsync(counts, 0, 9 * sizeof(uint32_t), stream);
   count_launch();
   classify_segments<<<(nseg + 255) / 256, 256, 0, stream>>>(begin, end, nseg, nseg_dev, lists,
                                                             counts);
+  if (split) {
+    cudaError_t e = cudaEventRecord(tasks.fork, stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(side, tasks.fork, 0);
+    if (e != cudaSuccess) return e;
+  }
   count_launch();
-  sort_tiny<<<num_sms * 4, 128, 0, stream>>>(keys, vals, begin, end, lists, counts);
+  sort_tiny<<<num_sms * 4, 128, 0, side>>>(keys, vals, begin, end, lists, counts);
   count_launch();
-  sort_warp<<<num_sms, kWarpSegWarps * 32, sizeof(WarpSlice) * kWarpSegWarps, stream>>>(
+  sort_warp<<<num_sms, kWarpSegWarps * 32, sizeof(WarpSlice) * kWarpSegWarps, side>>>(
       keys, vals, begin, end, lists + nseg, counts);
   count_launch();
-  sort_cta<<<num_sms * 3, kBlock, sizeof(CtaSmem), stream>>>(keys, vals, begin, end,
-                                                         lists + 2 * static_cast<size_t>(nseg),
-                                                         counts);
+  sort_cta<<<num_sms * 3, kBlock, sizeof(CtaSmem), side>>>(keys, vals, begin, end,
+                                                       lists + 2 * static_cast<size_t>(nseg),
+                                                       counts);
   if (tasks.nelems > kCap) {
     // global phase in rounds; the host looks at the next round's list after
     // rounds 0, 1, 3, 7, ... and stops when it is empty (every range's budget
@@ -1504,13 +1511,24 @@ cudaError_t segmented_std_sort(uint64_t* keys, uint32_t* vals, uint32_t* lscratc
       }
     }
   }
+  if (split) {
+    cudaError_t e = cudaEventRecord(tasks.rounds_done, stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(side, tasks.rounds_done, 0);
+    if (e != cudaSuccess) return e;
+  }
+  // the heap ranges first: their serial pops are the longest chains
+  count_launch();
+  sort_heaps<<<(num_sms + 1) / 2 * 2, kHeapBlock, kHeapSmem, side>>>(
+      keys, vals, lscratch, rscratch, tasks.f, tasks.n, counts + 5, counts + 6, counts + 7,
+      counts + 8, tasks.cap, tasks.pair_reserve);
   count_launch();
   sort_tasks<<<num_sms * 3, kBlock, sizeof(CtaSmem), stream>>>(keys, vals, tasks.f, tasks.n, tasks.d,
                                                            counts + 4);
-  count_launch();
-  sort_heaps<<<(num_sms + 1) / 2 * 2, kHeapBlock, kHeapSmem, stream>>>(
-      keys, vals, lscratch, rscratch, tasks.f, tasks.n, counts + 5, counts + 6, counts + 7,
-      counts + 8, tasks.cap, tasks.pair_reserve);
+  if (split) {
+    cudaError_t e = cudaEventRecord(tasks.join, side);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(stream, tasks.join, 0);
+    if (e != cudaSuccess) return e;
+  }
   return cudaGetLastError();
 }
 
