@@ -1134,13 +1134,21 @@ void flagged_sort(cuflye_ctx* c, PassState& ps, const MatchEmitLists& L, uint64_
   MatchTile* tiles = buf<MatchTile>(c, "m_tiles", NT);
   uint32_t* mcounts = buf<uint32_t>(c, "m_counts", 256 * NT);
   CUFLYE_CHECK(match_tiles(ps.q_off, ntiles, tile_off, nq, tiles, st));
-  CUFLYE_CHECK(match_radix(ps.keys, ps.vals, alt_keys, alt_vals, tiles, static_cast<uint32_t>(NT),
-                           ps.q_off, ntiles, tile_off, nq, id_bits, mcounts, c->num_sms,
-                           c->shape.scatter_blocks_per_sm, st));
-  // the pruned introsort on the copy, and the ranges it sorted copied back
   SortTasks t = sort_tasks(c, "f", F, E);
   t.prune_keys = dpkeys;
   t.prune_off = dpoff;
+  // The radix sort (in place, with the second buffer) and the emulation (on
+  // the copy) touch disjoint buffers: the radix sort runs on the side stream
+  // beside the emulation's global phase, and the emulation's side-stream
+  // work queues behind it, so the emulation's join also waits for it.  Every
+  // buffer is allocated before the fork: an allocation may fail, and a pass
+  // that is run again must find no work of the failed one still running.
+  CUFLYE_CHECK(cudaEventRecord(c->side_ev[0], st));
+  CUFLYE_CHECK(cudaStreamWaitEvent(c->side, c->side_ev[0], 0));
+  CUFLYE_CHECK(match_radix(ps.keys, ps.vals, alt_keys, alt_vals, tiles, static_cast<uint32_t>(NT),
+                           ps.q_off, ntiles, tile_off, nq, id_bits, mcounts, c->num_sms,
+                           c->shape.scatter_blocks_per_sm, c->side));
+  // the pruned introsort on the copy, and the ranges it sorted copied back
   CUFLYE_CHECK(segmented_std_sort(gk, gv, lscr, rscr, cb, ce, E, nullptr, lists, scounts,
                                   c->num_sms, st, t));
   CUFLYE_CHECK(copy_sorted_ranges(gk, gv, cb, ce, sb, E, scounts, t, ps.keys, ps.vals, c->num_sms,
