@@ -81,9 +81,9 @@ struct cuflye_ctx {
   size_t queries_per_pass = 0;
   // timing
   cudaEvent_t ev[8]{};
-  // the segmented sort's side stream and its fork / rounds-done / join events
-  cudaStream_t side = nullptr;
-  cudaEvent_t side_ev[3]{};
+  // the segmented sort's side streams and its fork / rounds-done / join events
+  cudaStream_t side = nullptr, side2 = nullptr;
+  cudaEvent_t side_ev[4]{};
   double stage_ms[7]{};
   uint64_t stage_bytes[7]{};
   uint64_t sort_stats[8]{};  // see cuflye_last_sort_stats ([7]: emission fallbacks)
@@ -1031,9 +1031,11 @@ SortTasks sort_tasks(cuflye_ctx* c, const std::string& prefix, uint64_t nelems, 
               buf<uint32_t>(c, prefix + "_rc", 2 * (kSortRounds + 1)),
               c->shape.round_blocks_per_sm};
   t.side = c->side;
+  t.side2 = c->side2;
   t.fork = c->side_ev[0];
   t.rounds_done = c->side_ev[1];
   t.join = c->side_ev[2];
+  t.join2 = c->side_ev[3];
   return t;
 }
 
@@ -1629,6 +1631,7 @@ cuflye_status cuflye_open(int device, uint64_t memory_budget_bytes, cuflye_ctx**
     CUFLYE_CHECK(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device));
     for (auto& e : c->ev) CUFLYE_CHECK(cudaEventCreate(&e));
     CUFLYE_CHECK(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+    CUFLYE_CHECK(cudaStreamCreateWithFlags(&c->side2, cudaStreamNonBlocking));
     for (auto& e : c->side_ev) CUFLYE_CHECK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     c->status = buf<DeviceStatus>(c, "status", 1);
     CUFLYE_CHECK(cudaMemset(c->status, 0, sizeof(DeviceStatus)));
@@ -1719,11 +1722,13 @@ void cuflye_close(cuflye_ctx* c) {
   for (auto& kv : c->bufs)
     if (kv.second.p) cudaFree(kv.second.p);
   if (c->side) cudaStreamSynchronize(c->side);
+  if (c->side2) cudaStreamSynchronize(c->side2);
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
   for (auto& e : c->side_ev)
     if (e) cudaEventDestroy(e);
   if (c->side) cudaStreamDestroy(c->side);
+  if (c->side2) cudaStreamDestroy(c->side2);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }

@@ -47,15 +47,16 @@ struct SortTasks {
   // final order: it is dropped (left as it is) and not listed as a task.
   const uint64_t* prune_keys = nullptr;
   const uint32_t* prune_off = nullptr;
-  // Side stream (optional): the whole-segment sorts (tiny, warp and CTA
-  // segments) run on it beside the global phase, and the heap ranges beside
-  // the final tasks.  They all sort disjoint element ranges, and each ends
-  // with the serial chain of its slowest range, so their tails overlap
-  // instead of adding up.  fork, rounds_done and join order the side stream
-  // against the call's stream; the call returns with the call's stream
-  // waiting for the side stream.  Null: everything on the call's stream.
-  cudaStream_t side = nullptr;
-  cudaEvent_t fork = nullptr, rounds_done = nullptr, join = nullptr;
+  // Side streams (optional): the whole-segment sorts (tiny, warp and CTA
+  // segments) run on `side` beside the global phase, and the heap ranges on
+  // `side2` beside the final tasks once the global phase is done.  They all
+  // sort disjoint element ranges, and each ends with the serial chain of its
+  // slowest range, so their tails overlap instead of adding up.  fork and
+  // rounds_done order the side streams after the call's stream; the call
+  // returns with its stream waiting for both (join, join2).  Null:
+  // everything on the call's stream.
+  cudaStream_t side = nullptr, side2 = nullptr;
+  cudaEvent_t fork = nullptr, rounds_done = nullptr, join = nullptr, join2 = nullptr;
 };
 uint32_t segsort_pair_reserve(uint64_t nelems);
 size_t segsort_round_bytes(uint64_t nelems);

@@ -800,12 +800,22 @@ __global__ void __launch_bounds__(kBlock, 3) sort_tasks(uint64_t* K, uint32_t* V
                                                      const uint64_t* __restrict__ task_f,
                                                      const uint32_t* __restrict__ task_n,
                                                      const int* __restrict__ task_d,
-                                                     const uint32_t* __restrict__ task_count) {
+                                                     const uint32_t* __restrict__ task_count,
+                                                     uint32_t* work) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   CtaSmem& sm = *reinterpret_cast<CtaSmem*>(smem_raw);
+  __shared__ uint32_t item;
   const uint32_t cnt = *task_count;
-  for (uint32_t i = blockIdx.x; i < cnt; i += gridDim.x)
+  // blocks claim tasks from a counter: a task with equal keys runs the whole
+  // emulation and costs far more than one the radix check finishes
+  for (;;) {
+    if (threadIdx.x == 0) item = atomicAdd(work, 1u);
+    __syncthreads();
+    const uint32_t i = item;
+    __syncthreads();
+    if (i >= cnt) break;
     if (task_n[i] <= kCap) cta_load_sort_store(K, V, task_f[i], task_n[i], task_d[i], sm);
+  }
 }
 
 // Heapsorts the tasks longer than kCap (ranges whose introsort depth ran out
@@ -1459,9 +1469,11 @@ cudaError_t segmented_std_sort(uint64_t* keys, uint32_t* vals, uint32_t* lscratc
     if (e != cudaSuccess) return e;
   }
   if (nseg == 0) return cudaSuccess;
-  const bool split = tasks.side && tasks.fork && tasks.rounds_done && tasks.join;
+  const bool split = tasks.side && tasks.side2 && tasks.fork && tasks.rounds_done && tasks.join &&
+                     tasks.join2;
   cudaStream_t side = split ? tasks.side : stream;
-  cudaMemsetAsync(counts, 0, 9 * sizeof(uint32_t), stream);
+  cudaStream_t side2 = split ? tasks.side2 : stream;
+  cudaMemsetAsync(counts, 0, 10 * sizeof(uint32_t), stream);
   count_launch();
   classify_segments<<<(nseg + 255) / 256, 256, 0, stream>>>(begin, end, nseg, nseg_dev, lists,
                                                             counts);
@@ -1513,20 +1525,22 @@ cudaError_t segmented_std_sort(uint64_t* keys, uint32_t* vals, uint32_t* lscratc
   }
   if (split) {
     cudaError_t e = cudaEventRecord(tasks.rounds_done, stream);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(side, tasks.rounds_done, 0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(side2, tasks.rounds_done, 0);
     if (e != cudaSuccess) return e;
   }
   // the heap ranges first: their serial pops are the longest chains
   count_launch();
-  sort_heaps<<<(num_sms + 1) / 2 * 2, kHeapBlock, kHeapSmem, side>>>(
+  sort_heaps<<<(num_sms + 1) / 2 * 2, kHeapBlock, kHeapSmem, side2>>>(
       keys, vals, lscratch, rscratch, tasks.f, tasks.n, counts + 5, counts + 6, counts + 7,
       counts + 8, tasks.cap, tasks.pair_reserve);
   count_launch();
   sort_tasks<<<num_sms * 3, kBlock, sizeof(CtaSmem), stream>>>(keys, vals, tasks.f, tasks.n, tasks.d,
-                                                           counts + 4);
+                                                           counts + 4, counts + 9);
   if (split) {
     cudaError_t e = cudaEventRecord(tasks.join, side);
+    if (e == cudaSuccess) e = cudaEventRecord(tasks.join2, side2);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(stream, tasks.join, 0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(stream, tasks.join2, 0);
     if (e != cudaSuccess) return e;
   }
   return cudaGetLastError();
