@@ -477,7 +477,8 @@ void cuflye_server_close(cuflye_server* server);
 
 /* --------------------------------------------------------------------------
  * Timing of the last call's device work (CUDA events on the context's
- * stream), in milliseconds, by stage: 0 hit generation, 1 KmerMatch sort,
+ * stream; the work its sorts run on the context's two side streams is joined
+ * into that stream before each sort returns), in milliseconds, by stage: 0 hit generation, 1 KmerMatch sort,
  * 2 group prefilter + ext re-sort, 3 chaining DP, 4 score sort + backtrack +
  * row compaction, 5 output conversion + device-to-host copy, 6 host-to-device
  * copy of the queries.  Stages 0-4 run on inputs already in device memory.
